@@ -1,0 +1,179 @@
+"""fortkernels_gb300 -- GB300 (sm_103a) GPP and FF self-energy kernels.
+
+Python face of the C ABI in include/fk_abi.h.  The two entry points mirror
+the reference mini-apps' hot paths and take their arrays in the reference
+layouts:
+
+* :func:`gppKer`   -- the GPP sum of BGW-Kernels/gppKer.cpp:303-439
+                      (outputs achtemp[3], asxtemp[3], acht_n1_loc, achstemp)
+* :func:`ffKernel` -- the FF kernels of FFKer_cori/ffKernel.cpp:480-503
+                      (outputs achsDtemp, asxDtemp, achDtemp, achDtemp_cor,
+                      ach2Dtemp, schDt_matrix)
+
+Arrays may be numpy arrays (host memory; staged by the library) or torch
+CUDA tensors (device memory; used in place).  All compute runs in the CUDA
+library; nothing here computes results on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native
+from ._native import (FK_FF_PHYSICS, FK_FF_SCHDT_GEMM, FK_FF_SPLIT_ACHD, FK_FP64, FK_GPP_ACHSTEMP,
+                      FK_GPP_ROOT_QUIRKS, FK_MIXED, FKError)
+
+__all__ = ["Context", "gppKer", "ffKernel", "FKError", "FK_FP64", "FK_MIXED", "FK_GPP_ROOT_QUIRKS",
+           "FK_GPP_ACHSTEMP", "FK_FF_SCHDT_GEMM", "FK_FF_PHYSICS", "FK_FF_SPLIT_ACHD", "precision_code"]
+
+
+def precision_code(p) -> int:
+    if p in (FK_FP64, "fp64", "FP64", None):
+        return FK_FP64
+    if p in (FK_MIXED, "mixed", "MIXED"):
+        return FK_MIXED
+    raise ValueError(f"unknown precision {p!r}")
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def _arg(x, kind: str, n: int, name: str):
+    """(pointer, keepalive) for an input array of n elements of `kind`
+    ('c128', 'f64', 'i32').  numpy arrays are converted to the exact dtype and
+    made contiguous; torch tensors must already be contiguous with that dtype."""
+    if _is_torch(x):
+        import torch
+        want = {"c128": torch.complex128, "f64": torch.float64, "i32": torch.int32}[kind]
+        if x.dtype != want or not x.is_contiguous() or x.numel() < n:
+            raise ValueError(f"{name}: need a contiguous {want} tensor with >= {n} elements")
+        return ctypes.c_void_p(x.data_ptr()), x
+    dt = {"c128": np.complex128, "f64": np.float64, "i32": np.int32}[kind]
+    a = np.ascontiguousarray(x, dtype=dt)
+    if a.size < n:
+        raise ValueError(f"{name}: need >= {n} elements, got {a.size}")
+    return ctypes.c_void_p(a.ctypes.data), a
+
+
+class Context:
+    """A CUDA context handle of the library (one device, one stream)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _native.load()
+        h = ctypes.c_void_p()
+        self._check(self.lib.fk_create(device, ctypes.byref(h)), None)
+        self.h = h
+        self.device = device
+
+    def _check(self, st: int, h):
+        if st != _native.FK_OK:
+            detail = self.lib.fk_last_error(h).decode() if h is not None else ""
+            raise FKError(st, f"{self.lib.fk_strerror(st).decode()}: {detail}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fk_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr: int | None):
+        self._check(self.lib.fk_set_stream(self.h, ctypes.c_void_p(stream_ptr or 0)), self.h)
+
+    def synchronize(self):
+        self._check(self.lib.fk_synchronize(self.h), self.h)
+
+    def reserve(self, nbytes: int):
+        self._check(self.lib.fk_reserve(self.h, ctypes.c_size_t(nbytes)), self.h)
+
+    def set_profiling(self, on: bool):
+        self._check(self.lib.fk_set_profiling(self.h, int(bool(on))), self.h)
+
+    def last_timings(self):
+        ms = (ctypes.c_float * 4)()
+        self._check(self.lib.fk_last_timings(self.h, ms), self.h)
+        return list(ms)
+
+    def last_launches(self) -> int:
+        return int(self.lib.fk_last_launches(self.h))
+
+    # ------------------------------------------------------------------ GPP
+    def gpp(self, p: dict, precision="fp64", flags: int = 0, out=None) -> dict:
+        """GPP sum on the input dict (keys as in fortkernels_gb300.inputs)."""
+        nb, nv, nc, ng = int(p["number_bands"]), int(p["nvband"]), int(p["ncouls"]), int(p["ngpown"])
+        keep = []
+
+        def a(key, kind, n):
+            ptr, k = _arg(p[key], kind, n, key)
+            keep.append(k)
+            return ptr
+
+        args = [a("aqsmtemp", "c128", nb * nc), a("aqsntemp", "c128", nb * nc),
+                a("I_eps_array", "c128", ng * nc), a("wtilde_array", "c128", ng * nc),
+                a("vcoul", "f64", nc), a("inv_igp_index", "i32", ng), a("indinv", "i32", nc),
+                a("wx_array", "f64", 3)]
+        if out is None:
+            out = {"achtemp": np.zeros(3, np.complex128), "asxtemp": np.zeros(3, np.complex128),
+                   "acht_n1_loc": np.zeros(nb, np.complex128), "achstemp": np.zeros(1, np.complex128)}
+        optr = [ctypes.c_void_p(_data_ptr(out[k])) if out.get(k) is not None else None
+                for k in ("achtemp", "asxtemp", "acht_n1_loc", "achstemp")]
+        st = self.lib.fk_gpp(self.h, nb, nv, nc, ng, *args, precision_code(precision), flags, *optr)
+        self._check(st, self.h)
+        return out
+
+    # ------------------------------------------------------------------- FF
+    def ff(self, p: dict, precision="fp64", flags: int = 0, out=None) -> dict:
+        nb, nv, nc, ng = int(p["number_bands"]), int(p["nvband"]), int(p["ncouls"]), int(p["ngpown"])
+        nf, ne = int(p["nFreq"]), int(p["nfreqeval"])
+        keep = []
+
+        def a(key, kind, n):
+            ptr, k = _arg(p[key], kind, n, key)
+            keep.append(k)
+            return ptr
+
+        args = [a("aqsmtemp", "c128", nb * nc), a("aqsntemp", "c128", nb * nc),
+                a("I_epsR_array", "c128", nf * ng * nc), a("I_epsA_array", "c128", nf * ng * nc),
+                a("vcoul", "f64", nc), a("inv_igp_index", "i32", ng), a("indinv", "i32", nc),
+                a("ekq", "f64", nb), a("dFreqGrid", "f64", nf), a("dFreqBrd", "c128", nf), a("pref", "f64", nf)]
+        if out is None:
+            out = {"achsDtemp": np.zeros(1, np.complex128), "asxDtemp": np.zeros(ne, np.complex128),
+                   "achDtemp": np.zeros(ne, np.complex128), "achDtemp_cor": np.zeros(ne, np.complex128),
+                   "ach2Dtemp": np.zeros(ne, np.complex128), "schDt_matrix": np.zeros((nb, nf), np.complex128)}
+        optr = [ctypes.c_void_p(_data_ptr(out[k])) if out.get(k) is not None else None
+                for k in ("achsDtemp", "asxDtemp", "achDtemp", "achDtemp_cor", "ach2Dtemp", "schDt_matrix")]
+        st = self.lib.fk_ff(self.h, nb, nv, nc, ng, nf, ne, *args, float(p["pref_zb"]), float(p["freqevalmin"]),
+                            float(p["freqevalstep"]), float(p.get("occ", 1.0)), precision_code(precision), flags,
+                            *optr)
+        self._check(st, self.h)
+        return out
+
+
+def _data_ptr(x) -> int:
+    return x.data_ptr() if _is_torch(x) else x.ctypes.data
+
+
+_default_ctx = None
+
+
+def _ctx() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def gppKer(p: dict, precision="fp64", flags: int = 0) -> dict:
+    """GPP self-energy sum (BGW-Kernels/gppKer.cpp:303-439) on device 0."""
+    return _ctx().gpp(p, precision, flags)
+
+
+def ffKernel(p: dict, precision="fp64", flags: int = 0) -> dict:
+    """FF full-frequency kernels (FFKer_cori/ffKernel.cpp:480-503) on device 0."""
+    return _ctx().ff(p, precision, flags)

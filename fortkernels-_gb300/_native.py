@@ -1,0 +1,69 @@
+"""ctypes binding of libfk_gb300.so (the C ABI of include/fk_abi.h).
+
+The library is the only compute path: if it cannot be loaded, every call
+raises.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfk_gb300.so")
+
+FK_OK, FK_EINVAL, FK_ENOMEM, FK_ECUDA, FK_ETIMEOUT, FK_EBUSY, FK_ENOTSUP = range(7)
+FK_FP64, FK_MIXED = 0, 1
+FK_GPP_ROOT_QUIRKS = 0x1
+FK_GPP_ACHSTEMP = 0x2
+FK_FF_SCHDT_GEMM = 0x1
+FK_FF_PHYSICS = 0x2
+FK_FF_SPLIT_ACHD = 0x4
+
+# Every symbol include/fk_abi.h declares.
+SYMBOLS = ("fk_create", "fk_destroy", "fk_set_stream", "fk_synchronize", "fk_reserve", "fk_strerror",
+           "fk_last_error", "fk_version", "fk_gpp", "fk_ff", "fk_set_profiling", "fk_last_timings",
+           "fk_last_launches")
+
+
+class FKError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(msg)
+        self.status = status
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libfk_gb300.so; raise if it is missing (no fallback path exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FKError(FK_ECUDA, f"{path} is missing: build it with __graft_entry__.build() "
+                                "(the CUDA library is the only compute path)")
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    I, D, U = ctypes.c_int, ctypes.c_double, ctypes.c_uint
+    L.fk_create.argtypes = [I, ctypes.POINTER(P)]
+    L.fk_destroy.argtypes = [P]
+    L.fk_set_stream.argtypes = [P, P]
+    L.fk_synchronize.argtypes = [P]
+    L.fk_reserve.argtypes = [P, ctypes.c_size_t]
+    L.fk_strerror.argtypes = [I]
+    L.fk_strerror.restype = ctypes.c_char_p
+    L.fk_last_error.argtypes = [P]
+    L.fk_last_error.restype = ctypes.c_char_p
+    L.fk_version.argtypes = []
+    L.fk_version.restype = ctypes.c_char_p
+    L.fk_gpp.argtypes = [P, I, I, I, I] + [P] * 8 + [I, U] + [P] * 4
+    L.fk_ff.argtypes = [P] + [I] * 6 + [P] * 11 + [D] * 4 + [I, U] + [P] * 6
+    L.fk_set_profiling.argtypes = [P, I]
+    L.fk_last_timings.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
+    L.fk_last_launches.argtypes = [P]
+    for name in SYMBOLS:
+        f = getattr(L, name)
+        if name not in ("fk_strerror", "fk_last_error", "fk_version"):
+            f.restype = ctypes.c_int
+    _lib = L
+    return L

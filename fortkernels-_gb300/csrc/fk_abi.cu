@@ -1,0 +1,349 @@
+// fk_abi.cu -- implementation of the C ABI declared in include/fk_abi.h:
+// contexts, argument checks, host/device residency of the caller's arrays,
+// input staging, workspace management and output delivery.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "fk_internal.h"
+
+struct fk_ctx : public fk::Ctx {};
+
+namespace fk {
+
+fk_status fail(Ctx& c, fk_status s, const std::string& msg) {
+    c.err = msg;
+    return s;
+}
+
+fk_status cuda_fail(Ctx& c, cudaError_t e, const char* where) {
+    c.err = std::string(where) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return e == cudaErrorMemoryAllocation ? FK_ENOMEM : FK_ECUDA;
+}
+
+void phase_mark(Ctx& c, int i) {
+    if (c.profiling && i >= 0 && i < 5) cudaEventRecord(c.ev[i], c.stream);
+}
+
+void phase_close(Ctx& c, int nphases) {
+    if (!c.profiling) return;
+    if (cudaEventSynchronize(c.ev[nphases]) != cudaSuccess) return;
+    for (int i = 0; i < nphases && i < 4; ++i) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, c.ev[i], c.ev[i + 1]) == cudaSuccess) c.timings[i] = ms;
+    }
+}
+
+namespace {
+
+// Restores the caller's current device when a call returns.
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = false;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        ok = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+bool is_device_ptr(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // clear the sticky-free error of a failed query
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+bool capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &st) != cudaSuccess) return false;
+    return st != cudaStreamCaptureStatusNone;
+}
+
+fk_status ensure_workspace(Ctx& c, size_t need) {
+    if (c.ws.cap >= need) return FK_OK;
+    if (capturing(c.stream))
+        return fail(c, FK_ENOMEM, "workspace must grow, which is not allowed during stream capture: call fk_reserve first");
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "workspace: synchronize");
+    if (c.ws.base) cudaFree(c.ws.base);
+    c.ws.base = nullptr;
+    c.ws.cap = 0;
+    size_t cap = need + need / 4 + (1u << 20);
+    e = cudaMalloc(&c.ws.base, cap);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_fail(c, e, "workspace: cudaMalloc");
+    }
+    c.ws.cap = cap;
+    return FK_OK;
+}
+
+// An input array: used in place when it is device memory, staged otherwise.
+struct In {
+    const void* user;
+    size_t bytes;
+    bool dev;
+    const void* d;
+};
+
+size_t staged_bytes(const std::vector<In*>& v) {
+    size_t s = 0;
+    for (auto* i : v)
+        if (!i->dev) s += (i->bytes + 255) & ~size_t(255);
+    return s;
+}
+
+fk_status stage(Ctx& c, const std::vector<In*>& v) {
+    for (auto* i : v) {
+        if (i->dev || !i->user) {
+            i->d = i->user;
+            continue;
+        }
+        void* d = c.ws.take(i->bytes);
+        if (!d) return fail(c, FK_ENOMEM, "workspace: staging");
+        cudaError_t e = cudaMemcpyAsync(d, i->user, i->bytes, cudaMemcpyHostToDevice, c.stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "staging copy");
+        i->d = d;
+    }
+    return FK_OK;
+}
+
+// Copies out[off..off+n) to a caller pointer (host or device).
+fk_status deliver(Ctx& c, void* dst, const double2* out, size_t off, size_t n, bool& host_out) {
+    if (!dst || n == 0) return FK_OK;
+    if (!is_device_ptr(dst)) host_out = true;
+    cudaError_t e = cudaMemcpyAsync(dst, out + off, n * sizeof(double2), cudaMemcpyDefault, c.stream);
+    return e == cudaSuccess ? FK_OK : cuda_fail(c, e, "output copy");
+}
+
+}  // namespace
+}  // namespace fk
+
+using fk::Ctx;
+
+extern "C" {
+
+const char* fk_version(void) { return "fk_gb300 1.0 sm_103a"; }
+
+const char* fk_strerror(fk_status s) {
+    switch (s) {
+        case FK_OK: return "ok";
+        case FK_EINVAL: return "invalid argument";
+        case FK_ENOMEM: return "out of memory";
+        case FK_ECUDA: return "CUDA error";
+        case FK_ETIMEOUT: return "device wait timed out";
+        case FK_EBUSY: return "busy: request not admitted";
+        case FK_ENOTSUP: return "not supported";
+    }
+    return "unknown status";
+}
+
+const char* fk_last_error(fk_ctx_t ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+fk_status fk_create(int device, fk_ctx_t* out) {
+    if (!out) return FK_EINVAL;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+        cudaGetLastError();
+        return FK_ECUDA;
+    }
+    fk_ctx* c = new (std::nothrow) fk_ctx();
+    if (!c) return FK_ENOMEM;
+    c->device = device;
+    fk::DeviceGuard g(device);
+    if (!g.ok || cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return FK_ECUDA;
+    }
+    c->stream = c->own_stream;
+    for (auto& e : c->ev)
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            cudaGetLastError();
+            delete c;
+            return FK_ECUDA;
+        }
+    *out = c;
+    return FK_OK;
+}
+
+fk_status fk_destroy(fk_ctx_t c) {
+    if (!c) return FK_EINVAL;
+    {
+        fk::DeviceGuard g(c->device);
+        if (c->stream) cudaStreamSynchronize(c->stream);
+        if (c->ws.base) cudaFree(c->ws.base);
+        if (c->pinned) cudaFreeHost(c->pinned);
+        for (auto& e : c->ev)
+            if (e) cudaEventDestroy(e);
+        if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    }
+    delete c;
+    return FK_OK;
+}
+
+fk_status fk_set_stream(fk_ctx_t c, void* stream) {
+    if (!c) return FK_EINVAL;
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return FK_OK;
+}
+
+fk_status fk_synchronize(fk_ctx_t c) {
+    if (!c) return FK_EINVAL;
+    fk::DeviceGuard g(c->device);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? FK_OK : fk::cuda_fail(*c, e, "synchronize");
+}
+
+fk_status fk_reserve(fk_ctx_t c, size_t bytes) {
+    if (!c) return FK_EINVAL;
+    fk::DeviceGuard g(c->device);
+    return fk::ensure_workspace(*c, bytes);
+}
+
+fk_status fk_set_profiling(fk_ctx_t c, int enable) {
+    if (!c) return FK_EINVAL;
+    c->profiling = enable != 0;
+    return FK_OK;
+}
+
+fk_status fk_last_timings(fk_ctx_t c, float ms[4]) {
+    if (!c || !ms) return FK_EINVAL;
+    for (int i = 0; i < 4; ++i) ms[i] = c->timings[i];
+    return FK_OK;
+}
+
+int fk_last_launches(fk_ctx_t c) { return c ? c->launches : -1; }
+
+fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsmtemp, const fk_c128* aqsntemp,
+                 const fk_c128* I_eps_array, const fk_c128* wtilde_array, const double* vcoul,
+                 const int* inv_igp_index, const int* indinv, const double* wx_array, fk_precision precision,
+                 unsigned flags, fk_c128* achtemp, fk_c128* asxtemp, fk_c128* acht_n1_loc, fk_c128* achstemp) {
+    if (!c) return FK_EINVAL;
+    Ctx& x = *c;
+    if (nb <= 0 || nc <= 0 || ng <= 0 || nv < 0 || nv > nb)
+        return fk::fail(x, FK_EINVAL, "gpp: need number_bands, ncouls, ngpown > 0 and 0 <= nvband <= number_bands");
+    if (!aqsmtemp || !aqsntemp || !I_eps_array || !wtilde_array || !vcoul || !inv_igp_index || !indinv ||
+        !wx_array || !achtemp || !asxtemp)
+        return fk::fail(x, FK_EINVAL, "gpp: null required pointer");
+    if (precision != FK_FP64 && precision != FK_MIXED) return fk::fail(x, FK_EINVAL, "gpp: bad precision");
+    if (flags & ~(FK_GPP_ROOT_QUIRKS | FK_GPP_ACHSTEMP)) return fk::fail(x, FK_EINVAL, "gpp: unknown flag");
+    if ((flags & FK_GPP_ROOT_QUIRKS) && ng > nc)
+        return fk::fail(x, FK_EINVAL, "gpp: FK_GPP_ROOT_QUIRKS indexes I_eps[my_igp*ngpown+ig] and needs ngpown <= ncouls");
+    if (ng > 65535) return fk::fail(x, FK_ENOTSUP, "gpp: ngpown > 65535");
+    fk::DeviceGuard g(x.device);
+    if (!g.ok) return fk::fail(x, FK_ECUDA, "gpp: cannot select device");
+
+    const size_t band = (size_t)nb * nc * sizeof(double2), col = (size_t)ng * nc * sizeof(double2);
+    fk::In aqm{aqsmtemp, band}, aqn{aqsntemp, band}, eps{I_eps_array, col}, wt{wtilde_array, col},
+        vc{vcoul, (size_t)nc * sizeof(double)}, inv{inv_igp_index, (size_t)ng * sizeof(int)},
+        ind{indinv, (size_t)nc * sizeof(int)}, wx{wx_array, 3 * sizeof(double)};
+    std::vector<fk::In*> ins{&aqm, &aqn, &eps, &wt, &vc, &inv, &ind, &wx};
+    for (auto* i : ins) i->dev = fk::is_device_ptr(i->user);
+
+    fk::GppDev r{};
+    r.nb = nb; r.nv = nv; r.nc = nc; r.ng = ng; r.prec = precision; r.flags = flags;
+    const size_t outn = 7 + (size_t)nb;
+    const size_t need = fk::staged_bytes(ins) + fk::gpp_workspace(x, r) + outn * sizeof(double2) + 4096;
+    fk_status s = fk::ensure_workspace(x, need);
+    if (s != FK_OK) return s;
+    x.ws.reset();
+    double2* out = (double2*)x.ws.take(outn * sizeof(double2));
+    fk::phase_mark(x, 0);
+    if ((s = fk::stage(x, ins)) != FK_OK) return s;
+    r.aqsm = (const double2*)aqm.d; r.aqsn = (const double2*)aqn.d;
+    r.eps = (const double2*)eps.d; r.wt = (const double2*)wt.d;
+    r.vcoul = (const double*)vc.d; r.inv = (const int*)inv.d; r.indinv = (const int*)ind.d;
+    r.wx = (const double*)wx.d; r.out = out;
+    if ((s = fk::gpp_run(x, r)) != FK_OK) return s;
+    bool host_out = false;
+    if ((s = fk::deliver(x, achtemp, out, 0, 3, host_out)) != FK_OK) return s;
+    if ((s = fk::deliver(x, asxtemp, out, 3, 3, host_out)) != FK_OK) return s;
+    if ((s = fk::deliver(x, achstemp, out, 6, 1, host_out)) != FK_OK) return s;
+    if ((s = fk::deliver(x, acht_n1_loc, out, 7, nb, host_out)) != FK_OK) return s;
+    if (host_out || x.profiling) {
+        cudaError_t e = cudaStreamSynchronize(x.stream);
+        if (e != cudaSuccess) return fk::cuda_fail(x, e, "gpp: synchronize");
+        fk::phase_close(x, 4);
+    }
+    return FK_OK;
+}
+
+fk_status fk_ff(fk_ctx_t c, int nb, int nv, int nc, int ng, int nf, int ne, const fk_c128* aqsmtemp,
+                const fk_c128* aqsntemp, const fk_c128* I_epsR_array, const fk_c128* I_epsA_array,
+                const double* vcoul, const int* inv_igp_index, const int* indinv, const double* ekq,
+                const double* dFreqGrid, const fk_c128* dFreqBrd, const double* pref, double pref_zb,
+                double freqevalmin, double freqevalstep, double occ, fk_precision precision, unsigned flags,
+                fk_c128* achsDtemp, fk_c128* asxDtemp, fk_c128* achDtemp, fk_c128* achDtemp_cor,
+                fk_c128* ach2Dtemp, fk_c128* schDt_matrix) {
+    if (!c) return FK_EINVAL;
+    Ctx& x = *c;
+    if (nb <= 0 || nc <= 0 || ng <= 0 || nv < 0 || nv > nb || nf < 2 || ne < 1)
+        return fk::fail(x, FK_EINVAL, "ff: need sizes > 0, nFreq >= 2, 0 <= nvband <= number_bands");
+    if (ng > nc) return fk::fail(x, FK_EINVAL, "ff: ngpown cannot be greater than ncouls");
+    if (!aqsmtemp || !aqsntemp || !I_epsR_array || !I_epsA_array || !vcoul || !inv_igp_index || !indinv || !ekq ||
+        !dFreqGrid || !dFreqBrd || !pref || !achsDtemp || !asxDtemp || !achDtemp_cor)
+        return fk::fail(x, FK_EINVAL, "ff: null required pointer");
+    if (precision != FK_FP64 && precision != FK_MIXED) return fk::fail(x, FK_EINVAL, "ff: bad precision");
+    if (flags & ~(FK_FF_SCHDT_GEMM | FK_FF_PHYSICS | FK_FF_SPLIT_ACHD)) return fk::fail(x, FK_EINVAL, "ff: unknown flag");
+    fk::DeviceGuard g(x.device);
+    if (!g.ok) return fk::fail(x, FK_ECUDA, "ff: cannot select device");
+
+    const size_t band = (size_t)nb * nc * sizeof(double2), planes = (size_t)nf * ng * nc * sizeof(double2);
+    fk::In aqm{aqsmtemp, band}, aqn{aqsntemp, band}, er{I_epsR_array, planes}, ea{I_epsA_array, planes},
+        vc{vcoul, (size_t)nc * sizeof(double)}, inv{inv_igp_index, (size_t)ng * sizeof(int)},
+        ind{indinv, (size_t)nc * sizeof(int)}, ek{ekq, (size_t)nb * sizeof(double)},
+        gr{dFreqGrid, (size_t)nf * sizeof(double)}, br{dFreqBrd, (size_t)nf * sizeof(double2)},
+        pr{pref, (size_t)nf * sizeof(double)};
+    std::vector<fk::In*> ins{&aqm, &aqn, &er, &ea, &vc, &inv, &ind, &ek, &gr, &br, &pr};
+    for (auto* i : ins) i->dev = fk::is_device_ptr(i->user);
+
+    fk::FfDev r{};
+    r.nb = nb; r.nv = nv; r.nc = nc; r.ng = ng; r.nf = nf; r.ne = ne;
+    r.pref_zb = pref_zb; r.fmin = freqevalmin; r.fstep = freqevalstep; r.occ = occ;
+    r.prec = precision; r.flags = flags;
+    r.ekq = ekq; r.grid = dFreqGrid;  // host or device; only read by the planner
+    const size_t wsb = fk::ff_workspace(x, r);
+    if (wsb == (size_t)-1) return fk::fail(x, FK_ECUDA, "ff: reading ekq/dFreqGrid");
+    const size_t outn = 1 + 4 * (size_t)ne + (size_t)nb * nf;
+    const size_t need = fk::staged_bytes(ins) + wsb + outn * sizeof(double2) + 4096;
+    fk_status s = fk::ensure_workspace(x, need);
+    if (s != FK_OK) return s;
+    x.ws.reset();
+    double2* out = (double2*)x.ws.take(outn * sizeof(double2));
+    fk::phase_mark(x, 0);
+    if ((s = fk::stage(x, ins)) != FK_OK) return s;
+    r.aqsm = (const double2*)aqm.d; r.aqsn = (const double2*)aqn.d;
+    r.epsR = (const double2*)er.d; r.epsA = (const double2*)ea.d; r.brd = (const double2*)br.d;
+    r.vcoul = (const double*)vc.d; r.ekq = (const double*)ek.d; r.grid = (const double*)gr.d;
+    r.pref = (const double*)pr.d; r.inv = (const int*)inv.d; r.indinv = (const int*)ind.d; r.out = out;
+    if ((s = fk::ff_run(x, r)) != FK_OK) return s;
+    bool host_out = false;
+    if ((s = fk::deliver(x, achsDtemp, out, 0, 1, host_out)) != FK_OK) return s;
+    if ((s = fk::deliver(x, asxDtemp, out, 1, ne, host_out)) != FK_OK) return s;
+    if ((s = fk::deliver(x, achDtemp, out, 1 + ne, ne, host_out)) != FK_OK) return s;
+    if ((s = fk::deliver(x, achDtemp_cor, out, 1 + 2 * (size_t)ne, ne, host_out)) != FK_OK) return s;
+    if ((s = fk::deliver(x, ach2Dtemp, out, 1 + 3 * (size_t)ne, ne, host_out)) != FK_OK) return s;
+    if ((s = fk::deliver(x, schDt_matrix, out, 1 + 4 * (size_t)ne, (size_t)nb * nf, host_out)) != FK_OK) return s;
+    if (host_out || x.profiling) {
+        cudaError_t e = cudaStreamSynchronize(x.stream);
+        if (e != cudaSuccess) return fk::cuda_fail(x, e, "ff: synchronize");
+        fk::phase_close(x, 4);
+    }
+    return FK_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,348 @@
+// fk_ff.cu -- FF full-frequency self-energy on sm_103a.
+//
+// Reference: the kernel sequence of FFKer_cori/ffKernel.cpp:480-503.  Every
+// band sum there is a contraction over ig of aqsntemp[n1][ig] with a
+// frequency plane of I_epsR / I_epsA, weighted by conj(aqsmtemp[n1][igp]) (and
+// vcoul[igp]) and summed over igp:
+//   achsDtemp_Kernel (:107-131)         plane 1 of I_epsR, all bands
+//   asxDtemp_Kernel  (:133-153)         planes ifreq, ifreq+1 of I_epsR, n1 < nvband
+//   achDtemp_cor_Kernel (:212-300)      planes ifreq, ifreq+1 of I_epsR - I_epsA
+//   schDt_matrix (.back1 :402-418)      every plane of I_epsR, no vcoul
+// so the library runs one batched complex contraction per eps array over the
+// planes that are needed (fk_gemm.cuh, EPI_FF), producing per (n1, plane)
+//   RW = sum_igp vcoul*conj(aqsm)*S,   RS = sum_igp conj(aqsm)*S,
+// and then evaluates the reference's scalar epilogues (compute_fact,
+// calculate_schDt_lin3, achDtemp_Kernel's frequency sums) in FP64.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "fk_gemm.cuh"
+#include "fk_internal.h"
+
+namespace fk {
+namespace {
+
+__global__ void ff_igp_kernel(int ng, int nc, const int* inv, const int* indinv, int* igp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    int ind = inv[i];
+    int g = (ind >= 0 && ind < nc) ? indinv[ind] : -1;
+    igp[i] = (g >= 0 && g < nc) ? g : -1;
+}
+
+// Sum the (KS x NT) partial slots of each (batch, n1, group) and scatter into
+// the per-plane tables RW/RS [nb][nf].
+__global__ void ff_rows_kernel(int nb, int nf, int batches, int slots_per_batch, const int* planes,
+                               const double2* P, double2* RW, double2* RS) {
+    const int n1 = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (n1 >= nb || b >= batches) return;
+    double2 s0 = make_double2(0.0, 0.0), s1 = s0;
+    for (int s = 0; s < slots_per_batch; ++s) {
+        const double2* q = P + (((long)b * slots_per_batch + s) * nb + n1) * 2;
+        s0 = cadd(s0, q[0]);
+        s1 = cadd(s1, q[1]);
+    }
+    const int f = planes[b];
+    RW[(long)n1 * nf + f] = s0;
+    if (RS) RS[(long)n1 * nf + f] = s1;
+}
+
+struct FactRow {
+    int ifq_a, ifq_c, kind;  // kind: 0 none, 1 schDttt_corKernel1, 2 schDttt_corKernel2
+    double fa1, fa2, fc1, fc2;
+};
+
+struct EpiArgs {
+    int nb, nv, nf, ne;
+    const double2 *RW, *RS, *AW;  // [nb][nf]
+    const FactRow* fact;
+    const double *ekq, *grid, *pref;
+    const double2* brd;
+    double pref_zb, fmin, fstep, fminI, fstepI, occ;
+    unsigned flags;
+    double2* SD;   // [ne][nb] achDtemp per band
+    double2* out;  // [achs | asx ne | achD ne | cor ne | a2 ne | schDt nb*nf]
+};
+
+// schDt value used by achDtemp_Kernel: RS when the band x G x G' contraction
+// is requested, zero otherwise (FFKer_cori/ffKernel.cpp:421-422).
+FK_DEV double2 schdt_of(const EpiArgs& a, int n1, int f) {
+    return (a.flags & FK_FF_SCHDT_GEMM) ? a.RS[(long)n1 * a.nf + f] : make_double2(0.0, 0.0);
+}
+
+// GPUComplex_divide(a, b), FFKer_cori/Complex.h:201-211.
+FK_DEV double2 gc_div(double2 a, double2 b) {
+    double2 bc = cconj(b);
+    double2 num = cmul(a, bc), den = cmul(b, bc);
+    return make_double2(__ddiv_rn(num.x, den.x), __ddiv_rn(num.y, den.x));
+}
+
+// achDtemp_Kernel's schDi sum over ifreq for one (iw, n1), ffKernel.cpp:199-206.
+__global__ void ff_schdi_kernel(EpiArgs a) {
+    const int n1 = blockIdx.x * blockDim.x + threadIdx.x, iw = blockIdx.y;
+    if (n1 >= a.nb) return;
+    double2 s = make_double2(0.0, 0.0);
+    const double wx = a.fmin - a.ekq[n1] + (iw - 1) * a.fstep;
+    for (int f = 0; f < a.nf; ++f) {
+        const double2 coh = make_double2(__dsub_rn(a.grid[f], a.brd[f].x), 0.0 - a.brd[f].y);
+        const double2 num = cmul(make_double2(0.0, a.pref[f]), schdt_of(a, n1, f));
+        const double2 q = gc_div(num, make_double2(__dsub_rn(wx, coh.x), 0 - coh.y));
+        s = cadd(s, make_double2(0.0 - q.x, 0.0 - q.y));
+    }
+    a.SD[(long)iw * a.nb + n1] = s;
+}
+
+FK_DEV void bsum(double2& v, double2* sm) {
+    for (int off = 16; off > 0; off >>= 1) {
+        v.x += __shfl_down_sync(0xffffffffu, v.x, off);
+        v.y += __shfl_down_sync(0xffffffffu, v.y, off);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sm[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s = cadd(s, sm[w]);
+        v = s;
+    }
+}
+
+// One block per output iw (blockIdx.x < ne) plus one block for the
+// iw-independent scalars (blockIdx.x == ne).
+__global__ void ff_epilogue_kernel(EpiArgs a) {
+    __shared__ double2 sm[32];
+    const int tid = threadIdx.x, iw = blockIdx.x;
+    // iw-independent sums, computed redundantly per block (tiny)
+    double2 achs = make_double2(0, 0), asx = achs, cor = achs;
+    for (int n1 = tid; n1 < a.nb; n1 += blockDim.x) {
+        achs = cadd(achs, a.RW[(long)n1 * a.nf + 1]);
+        const FactRow fr = a.fact[n1];
+        if (n1 < a.nv) {
+            double2 v = cadd(cscale(a.RW[(long)n1 * a.nf + fr.ifq_a], fr.fa1),
+                             cscale(a.RW[(long)n1 * a.nf + fr.ifq_a + 1], fr.fa2));
+            asx = cadd(asx, cscale(v, a.occ));
+        }
+        if (fr.kind) {
+            const double2 d0 = csub(a.RW[(long)n1 * a.nf + fr.ifq_c], a.AW[(long)n1 * a.nf + fr.ifq_c]);
+            const double2 d1 = csub(a.RW[(long)n1 * a.nf + fr.ifq_c + 1], a.AW[(long)n1 * a.nf + fr.ifq_c + 1]);
+            double2 v = cadd(cscale(d0, fr.fc1), cscale(d1, fr.fc2));
+            if (fr.kind == 2) v = cscale(v, -0.5);
+            cor = cadd(cor, v);
+        }
+    }
+    bsum(achs, sm);
+    bsum(asx, sm);
+    bsum(cor, sm);
+    if (iw == a.ne) {
+        if (tid == 0) a.out[0] = cscale(achs, -0.5);
+        // schDt_matrix output
+        for (long i = tid; i < (long)a.nb * a.nf; i += blockDim.x)
+            a.out[1 + 4L * a.ne + i] = (a.flags & FK_FF_SCHDT_GEMM) ? a.RS[i] : make_double2(0.0, 0.0);
+        return;
+    }
+    double2 achd = make_double2(0, 0);
+    for (int n1 = tid; n1 < a.nb; n1 += blockDim.x) achd = cadd(achd, a.SD[(long)iw * a.nb + n1]);
+    bsum(achd, sm);
+    if (tid == 0) {
+        // sch2Di after achDtemp_Kernel holds the value of its last (n1, ifreq)
+        // iteration, which achDtemp_cor_Kernel adds once per band (:191-192, :241).
+        double2 last = make_double2(0.0, 0.0);
+        const int n1 = a.nb - 1, f = a.nf - 1;
+        if (f >= 1) {
+            const double right = a.grid[f], left = a.grid[f - 1];
+            const double2 R = schdt_of(a, n1, f), L = schdt_of(a, n1, f - 1);
+            const double2 avg = cscale(cadd(R, L), 0.5);
+            const double ew = a.fminI - a.ekq[n1] + (double)(iw - 1) * a.fstepI;
+            double intfact = __ddiv_rn(__dsub_rn(ew, right), __dsub_rn(ew, left));
+            if (intfact < 0.0001) intfact = 0.0001;
+            if (intfact > 10000) intfact = 10000;
+            intfact = -log(intfact);
+            last = csub(make_double2(0.0, 0.0), cscale(cmul(make_double2(0.0, a.pref_zb), avg), intfact));
+        }
+        const int ne = a.ne;
+        double2 asx_iw = asx;
+        if (!(a.flags & FK_FF_SPLIT_ACHD)) asx_iw = cadd(asx_iw, achd);  // ffKernel.cpp:495
+        a.out[1 + iw] = asx_iw;
+        a.out[1 + ne + iw] = (a.flags & FK_FF_SPLIT_ACHD) ? achd : make_double2(0.0, 0.0);
+        a.out[1 + 2 * ne + iw] = cor;
+        a.out[1 + 3 * ne + iw] = cscale(last, (double)a.nb);
+    }
+}
+
+// compute_fact, FFKer_cori/ffKernel.cpp:30-78 (host copy; the oracle holds
+// the same restatement).
+void compute_fact(double wx, int nFreq, const double* g, double& fact1, double& fact2, int& ifreq, int loop,
+                  bool flag_occ) {
+    if (loop == 1 && wx > 0.00) {
+        for (int k = 0; k < nFreq - 1; ++k)
+            if (wx > g[k] && wx < g[k + 1]) ifreq = k;
+        if (ifreq == 0) ifreq = nFreq - 2;
+        fact1 = (g[ifreq + 1] - wx) / (g[ifreq + 1] - g[ifreq]);
+        fact2 = (wx - g[ifreq]) / (g[ifreq + 1] - g[ifreq]);
+    } else if (loop == 1) {
+        for (int k = 0; k < nFreq - 1; ++k)
+            if (-wx > g[k] && -wx < g[k + 1]) ifreq = k;
+        if (ifreq == 0) ifreq = nFreq - 2;
+        fact1 = (g[ifreq + 1] + wx) / (g[ifreq + 1] - g[ifreq]);
+        fact2 = (-g[ifreq] - wx) / (g[ifreq + 1] - g[ifreq]);
+    }
+    if (loop == 2 && wx > 0.00) {
+        for (int k = 0; k < nFreq - 1; ++k)
+            if (wx > g[k] && wx < g[k + 1]) ifreq = k;
+        if (ifreq == -1) ifreq = nFreq - 2;
+        fact1 = -0.5 * (g[ifreq + 1] - wx) / (g[ifreq + 1] - g[ifreq]);
+        fact2 = -0.5 * (wx - g[ifreq]) / (g[ifreq + 1] - g[ifreq]);
+    } else if (loop == 2 && flag_occ) {
+        wx = -wx;
+        ifreq = 0;
+        for (int k = 0; k < nFreq - 1; ++k)
+            if (wx > g[k] && wx < g[k + 1]) ifreq = k;
+        if (ifreq == 0) ifreq = nFreq - 2;
+        fact1 = (g[ifreq + 1] - wx) / (g[ifreq + 1] - g[ifreq]);
+        fact2 = (wx - g[ifreq]) / (g[ifreq + 1] - g[ifreq]);
+    }
+}
+
+struct FfPlan {
+    std::vector<FactRow> fact;
+    std::vector<int> planesR, planesA;
+    int MT, NT, KS, kchunk;
+    bool mixed;
+    size_t bytes;
+};
+
+FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double* grid_h) {
+    FfPlan p;
+    p.mixed = r.prec == FK_MIXED;
+    p.fact.resize(r.nb);
+    std::vector<char> needR(r.nf, 0), needA(r.nf, 0);
+    needR[1] = 1;
+    const bool all = (r.flags & FK_FF_SCHDT_GEMM) != 0;
+    for (int n1 = 0; n1 < r.nb; ++n1) {
+        FactRow fr{0, 0, 0, 0.0, 0.0, 0.0, 0.0};
+        const double wx = r.fmin - ekq_h[n1] + r.fstep;
+        if (n1 < r.nv) {
+            compute_fact(wx, r.nf, grid_h, fr.fa1, fr.fa2, fr.ifq_a, 1, false);
+            needR[fr.ifq_a] = needR[fr.ifq_a + 1] = 1;
+        }
+        const bool occ = n1 < r.nv;
+        compute_fact(wx, r.nf, grid_h, fr.fc1, fr.fc2, fr.ifq_c, 2, occ);
+        if (wx > 0) fr.kind = occ ? 0 : 1;
+        else fr.kind = occ ? 2 : 0;
+        if (fr.kind) needR[fr.ifq_c] = needR[fr.ifq_c + 1] = needA[fr.ifq_c] = needA[fr.ifq_c + 1] = 1;
+        p.fact[n1] = fr;
+    }
+    for (int f = 0; f < r.nf; ++f) {
+        if (all || needR[f]) p.planesR.push_back(f);
+        if (needA[f]) p.planesA.push_back(f);
+    }
+    const int BM = p.mixed ? f32::BM : d64::BM, BN = p.mixed ? f32::BN : d64::BN;
+    p.MT = ceil_div(r.nb, BM);
+    p.NT = ceil_div(r.ng, BN);
+    const int per_sm = p.mixed ? 4 : 2;
+    const int tiles = p.MT * p.NT * std::max<int>(1, (int)p.planesR.size());
+    p.KS = std::max(1, std::min((c.sms * per_sm + tiles - 1) / tiles, std::max(1, r.nc / 256)));
+    p.kchunk = ((r.nc + p.KS - 1) / p.KS + 15) / 16 * 16;
+    p.KS = (r.nc + p.kchunk - 1) / p.kchunk;
+    const size_t slots = (size_t)p.KS * p.NT;
+    p.bytes = (slots * (p.planesR.size() + p.planesA.size()) * r.nb * 2 + 3 * (size_t)r.nb * r.nf +
+               (size_t)r.ne * r.nb) * sizeof(double2) +
+              r.nb * sizeof(FactRow) + (p.planesR.size() + p.planesA.size()) * sizeof(int) + r.ng * sizeof(int) +
+              16 * 256;
+    return p;
+}
+
+}  // namespace
+
+size_t ff_workspace(const Ctx& c, const FfDev& r) {
+    std::vector<double> ekq(r.nb), grid(r.nf);
+    if (cudaMemcpy(ekq.data(), r.ekq, r.nb * sizeof(double), cudaMemcpyDefault) != cudaSuccess ||
+        cudaMemcpy(grid.data(), r.grid, r.nf * sizeof(double), cudaMemcpyDefault) != cudaSuccess)
+        return (size_t)-1;
+    return make_plan(c, r, ekq.data(), grid.data()).bytes;
+}
+
+fk_status ff_run(Ctx& c, const FfDev& r) {
+    std::vector<double> ekq(r.nb), grid(r.nf);
+    cudaError_t e = cudaMemcpyAsync(ekq.data(), r.ekq, r.nb * sizeof(double), cudaMemcpyDefault, c.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(grid.data(), r.grid, r.nf * sizeof(double), cudaMemcpyDefault, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "ff: reading ekq/dFreqGrid");
+    const FfPlan p = make_plan(c, r, ekq.data(), grid.data());
+    cudaStream_t st = c.stream;
+    const int nR = (int)p.planesR.size(), nA = (int)p.planesA.size();
+    const size_t slots = (size_t)p.KS * p.NT;
+    int* igp = (int*)c.ws.take(r.ng * sizeof(int));
+    int* planes = (int*)c.ws.take((nR + nA) * sizeof(int));
+    FactRow* fact = (FactRow*)c.ws.take(r.nb * sizeof(FactRow));
+    double2* PR = (double2*)c.ws.take(slots * std::max(nR, 1) * r.nb * 2 * sizeof(double2));
+    double2* PA = nA ? (double2*)c.ws.take(slots * nA * r.nb * 2 * sizeof(double2)) : nullptr;
+    double2* tabs = (double2*)c.ws.take(3 * (size_t)r.nb * r.nf * sizeof(double2));
+    double2* SD = (double2*)c.ws.take((size_t)r.ne * r.nb * sizeof(double2));
+    if (!igp || !planes || !fact || !PR || (nA && !PA) || !tabs || !SD)
+        return fail(c, FK_ENOMEM, "workspace too small for FF request");
+    double2 *RW = tabs, *RS = tabs + (size_t)r.nb * r.nf, *AW = tabs + 2 * (size_t)r.nb * r.nf;
+    // host tables -> device (pageable source; the copy completes before return of the call's sync)
+    std::vector<int> pl(p.planesR);
+    pl.insert(pl.end(), p.planesA.begin(), p.planesA.end());
+    e = cudaMemcpyAsync(planes, pl.data(), pl.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fact, p.fact.data(), r.nb * sizeof(FactRow), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(tabs, 0, 3 * (size_t)r.nb * r.nf * sizeof(double2), st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "ff: tables");
+    c.launches = 0;
+
+    phase_mark(c, 1);
+    ff_igp_kernel<<<ceil_div(r.ng, 128), 128, 0, st>>>(r.ng, r.nc, r.inv, r.indinv, igp);
+    ++c.launches;
+    phase_mark(c, 2);
+    auto contract = [&](const double2* eps, const int* pls, int nb_, double2* P) {
+        ContractArgs a{};
+        a.A = r.aqsn; a.lda = r.nc; a.m0 = 0; a.M = r.nb;
+        a.B = eps; a.ldb = r.nc; a.bstride = (long)r.ng * r.nc; a.N = r.ng; a.K = r.nc;
+        a.KS = p.KS; a.kchunk = p.kchunk; a.batches = nb_; a.batch_plane = pls;
+        a.aqsm = r.aqsm; a.ldm = r.nc; a.vcoul = r.vcoul; a.igp = igp; a.wscale = 1.0; a.G = 2; a.P = P;
+        dim3 grid(p.MT, p.NT * p.KS * nb_);
+        if (p.mixed) {
+            auto k = f32::contract_kernel<EPI_FF, double2>;
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f32::SMEM);
+            k<<<grid, f32::THREADS, f32::SMEM, st>>>(a);
+        } else {
+            auto k = d64::contract_kernel<EPI_FF>;
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d64::SMEM);
+            k<<<grid, d64::THREADS, d64::SMEM, st>>>(a);
+        }
+        ++c.launches;
+    };
+    if (nR) contract(r.epsR, planes, nR, PR);
+    if (nA) contract(r.epsA, planes + nR, nA, PA);
+    phase_mark(c, 3);
+    if (nR) {
+        ff_rows_kernel<<<dim3(ceil_div(r.nb, 128), nR), 128, 0, st>>>(r.nb, r.nf, nR, (int)slots, planes, PR, RW, RS);
+        ++c.launches;
+    }
+    if (nA) {
+        ff_rows_kernel<<<dim3(ceil_div(r.nb, 128), nA), 128, 0, st>>>(r.nb, r.nf, nA, (int)slots, planes + nR, PA, AW,
+                                                                     nullptr);
+        ++c.launches;
+    }
+    EpiArgs ea{};
+    ea.nb = r.nb; ea.nv = r.nv; ea.nf = r.nf; ea.ne = r.ne;
+    ea.RW = RW; ea.RS = RS; ea.AW = AW; ea.fact = fact;
+    ea.ekq = r.ekq; ea.grid = r.grid; ea.pref = r.pref; ea.brd = r.brd;
+    ea.pref_zb = r.pref_zb; ea.fmin = r.fmin; ea.fstep = r.fstep; ea.occ = r.occ; ea.flags = r.flags;
+    const bool phys = (r.flags & FK_FF_PHYSICS) != 0;
+    ea.fminI = phys ? r.fmin : (double)(int)r.fmin;
+    ea.fstepI = phys ? r.fstep : (double)(int)r.fstep;
+    ea.SD = SD; ea.out = r.out;
+    ff_schdi_kernel<<<dim3(ceil_div(r.nb, 128), r.ne), 128, 0, st>>>(ea);
+    ff_epilogue_kernel<<<r.ne + 1, 256, 0, st>>>(ea);
+    c.launches += 2;
+    phase_mark(c, 4);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "ff kernels");
+    return FK_OK;
+}
+
+}  // namespace fk

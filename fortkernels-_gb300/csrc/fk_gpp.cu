@@ -1,0 +1,467 @@
+// fk_gpp.cu -- GPP self-energy sum on sm_103a.
+//
+// Reference: the n1 x my_igp x ig x iw loop nest of BGW-Kernels/gppKer.cpp:
+// 303-439 (ssxt_scht_solver :19-65, flagOCC_solver :130-159, noflag block
+// :349-413, accumulation :416-439).
+//
+// Structure.  Every factor of a GPP term except the band pair product
+//     conj(aqsmtemp[n1][igp]) * aqsntemp[n1][ig]
+// depends only on (my_igp, ig, iw).  The kernels therefore
+//   1. build, once per (my_igp, ig), the three branch-resolved factors
+//      D[my_igp*3+iw][ig] = mask(wdiffr > limittwo && delwr < limitone)
+//                           * delw * I_eps                     (prep kernel),
+//      and contract the flagOCC bands (n1 < nvband: sch and ssx) right there;
+//   2. contract the noflag bands as a complex GEMM, aqsntemp x D^T, whose
+//      epilogue applies 0.5*vcoul[igp]*conj(aqsmtemp[n1][igp]) and reduces
+//      each row to its three iw sums (fk_gemm.cuh);
+//   3. add all partials in a fixed order (finalize kernels).
+// FP64 path: every branch quantity follows the reference's expression
+// sequence with round-to-nearest FP64 operations (no contraction), so each
+// branch is taken exactly as in the reference's C++; the contraction runs on
+// FP64 DMMA.  Mixed path: the branch quantities are evaluated in FP32 from an
+// FP64 wdiff and re-evaluated with the exact FP64 sequence whenever a test
+// value lies within a relative guard band of its threshold, so branch
+// decisions remain those of the FP64 sequence; the bulk products run in FP32
+// with compensated accumulation.
+#include <algorithm>
+
+#include "fk_gemm.cuh"
+#include "fk_internal.h"
+
+namespace fk {
+namespace {
+
+constexpr int PREP_THREADS = 256;
+constexpr int PREP_EPT = 2;
+constexpr int PREP_TILE = PREP_THREADS * PREP_EPT;
+constexpr int NVC = 2;  // flag bands contracted per prep pass
+constexpr double TO1 = 1e-6;
+constexpr float GUARD = 1e-5f;  // relative guard band of the FP32 branch tests
+
+__global__ void igp_map_kernel(int ng, int nc, const int* inv, const int* indinv, int* igp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ng) igp[i] = gpp_igp_of(i, nc, inv, indinv);
+}
+
+struct PrepArgs {
+    int nb, nv, nc, ng;
+    const double2 *aqsn, *eps, *wt;
+    const double* wx;
+    const int* igp;
+    void* D;     // [3*ng][nc]: double2 (FP64) or float2 (mixed); nullptr = not needed
+    double2* F;  // [nch][nv][ng][3][2]  (sch, ssx) flag-band sums over the chunk
+    int nch;
+    int n1base;  // first flag band handled by this pass
+};
+
+// ---------------------------------------------------------------- FP64 exact
+struct Branch64 {
+    double2 delw;
+    bool A, B;
+};
+// ssxt_scht_solver's branch quantities, BGW-Kernels/gppKer.cpp:30-38.
+FK_DEV Branch64 branch64(double wxt, double2 wt) {
+    const double limitone = 1.0 / (TO1 * 4.0);
+    const double limittwo = 0.5 * 0.5;
+    double2 wdiff = make_double2(__dsub_rn(wxt, wt.x), -wt.y);
+    double rden = __ddiv_rn(1.0, cnorm2(wdiff));
+    Branch64 b;
+    b.delw = cscale(cmul(wt, cconj(wdiff)), rden);
+    double delwr = cnorm2(b.delw);
+    double wdiffr = cnorm2(wdiff);
+    b.A = (wdiffr > limittwo) && (delwr < limitone);
+    b.B = delwr > TO1;
+    return b;
+}
+// ssx of ssxt_scht_solver, BGW-Kernels/gppKer.cpp:38-58.
+FK_DEV double2 ssx64(const Branch64& b, double wxt, double2 wt2, double2 Omega2) {
+    if (b.A) {
+        double w2 = __dmul_rn(wxt, wxt);
+        double rd = __ddiv_rn(1.0, __dmul_rn(w2, w2));
+        double2 t = make_double2(__dsub_rn(__dmul_rn(Omega2.x, w2), __dmul_rn(Omega2.y, -0.0)),
+                                 __dadd_rn(__dmul_rn(Omega2.x, -0.0), __dmul_rn(Omega2.y, w2)));
+        return cscale(t, rd);
+    }
+    if (b.B) {
+        double2 c = cmul(cscale(wt2, 4.0), make_double2(__dadd_rn(b.delw.x, 0.5), b.delw.y));
+        double rd = __ddiv_rn(1.0, cnorm2(c));
+        double2 negO = make_double2(-Omega2.x, -Omega2.y);
+        return cmul(cscale(cmul(negO, cconj(c)), rd), b.delw);
+    }
+    return make_double2(0.0, 0.0);
+}
+
+// Fixed-order block sum of NV values per thread; thread v < NV of the block
+// receives the total of value v.  Deterministic: shuffle tree, then warps in order.
+template <int NV>
+FK_DEV void block_sum(double2 (&v)[NV], double2* sm /* [8][NV] */) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            v[i].x += __shfl_down_sync(0xffffffffu, v[i].x, off);
+            v[i].y += __shfl_down_sync(0xffffffffu, v[i].y, off);
+        }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < NV; ++i) sm[warp * NV + i] = v[i];
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s = cadd(s, sm[w * NV + threadIdx.x]);
+        v[threadIdx.x] = s;
+    }
+}
+
+template <int Q>  // Q = 1: root gppKer.cpp semantics
+__global__ void __launch_bounds__(PREP_THREADS) prep64_kernel(PrepArgs p) {
+    __shared__ double2 sm[8 * NVC * 6];
+    const int my_igp = blockIdx.y, ch = blockIdx.x, tid = threadIdx.x;
+    const int igp = p.igp[my_igp];
+    const int nflag = min(NVC, p.nv - p.n1base);
+    double2 acc[NVC * 6];
+#pragma unroll
+    for (int i = 0; i < NVC * 6; ++i) acc[i] = make_double2(0.0, 0.0);
+    const double2* wrow = p.wt + (long)my_igp * p.nc;
+    const double2* erow = p.eps + (long)my_igp * p.nc;
+    double2* D = reinterpret_cast<double2*>(p.D);
+    for (int e = 0; e < PREP_EPT; ++e) {
+        const int ig = ch * PREP_TILE + e * PREP_THREADS + tid;
+        if (ig >= p.nc) continue;
+        const double2 wt = wrow[ig], ep = erow[ig];
+        double2 wt2 = make_double2(0, 0), Om = make_double2(0, 0), eq = ep;
+        if (nflag > 0) {
+            wt2 = cmul(wt, wt);
+            Om = cmul(wt2, ep);
+            if (Q) eq = p.eps[(long)my_igp * p.ng + ig];  // gppKer.cpp:139
+        }
+#pragma unroll
+        for (int iw = 0; iw < 3; ++iw) {
+            const double wxt = p.wx[iw];
+            Branch64 b = branch64(wxt, wt);
+            if (D) {
+                double2 dv = (igp >= 0 && (Q || b.A)) ? cmul(b.delw, ep) : make_double2(0.0, 0.0);
+                D[((long)my_igp * 3 + iw) * p.nc + ig] = dv;
+            }
+            if (nflag > 0 && igp >= 0) {
+                double2 sch = b.A ? cmul(b.delw, eq) : make_double2(0.0, 0.0);
+                double2 ssx = ssx64(b, wxt, wt2, Om);
+#pragma unroll
+                for (int j = 0; j < NVC; ++j)
+                    if (j < nflag) {
+                        double2 an = p.aqsn[(long)(p.n1base + j) * p.nc + ig];
+                        cfma(acc[(j * 3 + iw) * 2 + 0], an, sch);
+                        cfma(acc[(j * 3 + iw) * 2 + 1], an, ssx);
+                    }
+            }
+        }
+    }
+    if (nflag <= 0) return;
+    block_sum<NVC * 6>(acc, sm);
+    if (tid < nflag * 6) {
+        int j = tid / 6, r = tid % 6;
+        p.F[(((long)ch * p.nv + p.n1base + j) * p.ng + my_igp) * 6 + r] = acc[tid];
+    }
+}
+
+// ------------------------------------------------------------ mixed (guarded)
+template <int Q>
+__global__ void __launch_bounds__(PREP_THREADS) prep_mixed_kernel(PrepArgs p) {
+    __shared__ double2 sm[8 * NVC * 6];
+    const int my_igp = blockIdx.y, ch = blockIdx.x, tid = threadIdx.x;
+    const int igp = p.igp[my_igp];
+    const int nflag = min(NVC, p.nv - p.n1base);
+    float2 acc[NVC * 6];
+#pragma unroll
+    for (int i = 0; i < NVC * 6; ++i) acc[i] = make_float2(0.f, 0.f);
+    const float limitone = 250000.0f, limittwo = 0.25f, to1 = 1e-6f;
+    const double2* wrow = p.wt + (long)my_igp * p.nc;
+    const double2* erow = p.eps + (long)my_igp * p.nc;
+    float2* D = reinterpret_cast<float2*>(p.D);
+    float wxf[3], iw2[3];
+#pragma unroll
+    for (int iw = 0; iw < 3; ++iw) {
+        wxf[iw] = f64_to_f32_bits(p.wx[iw]);
+        iw2[iw] = 1.0f / (wxf[iw] * wxf[iw]);
+    }
+    for (int e = 0; e < PREP_EPT; ++e) {
+        const int ig = ch * PREP_TILE + e * PREP_THREADS + tid;
+        if (ig >= p.nc) continue;
+        const double2 wt64 = wrow[ig], ep64 = erow[ig];
+        const float2 wt = c64_to_f32(wt64), ep = c64_to_f32(ep64);
+        float2 wt2 = make_float2(0.f, 0.f), Om = wt2, eq = ep;
+        if (nflag > 0) {
+            wt2 = cmulf(wt, wt);
+            Om = cmulf(wt2, ep);
+            if (Q) eq = c64_to_f32(p.eps[(long)my_igp * p.ng + ig]);
+        }
+#pragma unroll
+        for (int iw = 0; iw < 3; ++iw) {
+            const double wxt = p.wx[iw];
+            // wdiff from an FP64 subtraction: keeps full relative accuracy next to the pole
+            const float wdr = f64_to_f32_bits(__dsub_rn(wxt, wt64.x)), wdi = -wt.y;
+            const float wdiffr = wdr * wdr + wdi * wdi;
+            const float rden = __frcp_rn(wdiffr);
+            float2 delw = cmulf(wt, make_float2(wdr, -wdi));
+            delw.x *= rden;
+            delw.y *= rden;
+            const float delwr = delw.x * delw.x + delw.y * delw.y;
+            bool A, B;
+            float2 dv, sch, ssx;
+            const bool amb = !(wdiffr > 1e-30f) || !(delwr < 1e30f) ||
+                             fabsf(wdiffr - limittwo) <= limittwo * GUARD ||
+                             fabsf(delwr - limitone) <= limitone * GUARD || fabsf(delwr - to1) <= to1 * GUARD;
+            if (amb) {
+                // exact FP64 sequence for this element (rare)
+                Branch64 b = branch64(wxt, wt64);
+                A = b.A;
+                B = b.B;
+                dv = c64_to_f32(cmul(b.delw, ep64));
+                sch = A ? c64_to_f32(cmul(b.delw, Q ? p.eps[(long)my_igp * p.ng + ig] : ep64)) : make_float2(0.f, 0.f);
+                if (nflag > 0) {
+                    double2 wt2d = cmul(wt64, wt64);
+                    ssx = c64_to_f32(ssx64(b, wxt, wt2d, cmul(wt2d, ep64)));
+                } else {
+                    ssx = make_float2(0.f, 0.f);
+                }
+            } else {
+                A = (wdiffr > limittwo) && (delwr < limitone);
+                B = delwr > to1;
+                dv = cmulf(delw, ep);
+                sch = A ? cmulf(delw, eq) : make_float2(0.f, 0.f);
+                if (A) {
+                    ssx = make_float2(Om.x * iw2[iw], Om.y * iw2[iw]);
+                } else if (B) {
+                    float2 c = cmulf(make_float2(4.f * wt2.x, 4.f * wt2.y), make_float2(delw.x + 0.5f, delw.y));
+                    float rd = __frcp_rn(c.x * c.x + c.y * c.y);
+                    float2 t = cmulf(make_float2(-Om.x, -Om.y), make_float2(c.x, -c.y));
+                    ssx = cmulf(make_float2(t.x * rd, t.y * rd), delw);
+                } else {
+                    ssx = make_float2(0.f, 0.f);
+                }
+            }
+            if (D) D[((long)my_igp * 3 + iw) * p.nc + ig] = (igp >= 0 && (Q || A)) ? dv : make_float2(0.f, 0.f);
+            if (nflag > 0 && igp >= 0) {
+#pragma unroll
+                for (int j = 0; j < NVC; ++j)
+                    if (j < nflag) {
+                        float2 an = c64_to_f32(p.aqsn[(long)(p.n1base + j) * p.nc + ig]);
+                        cfmaf(acc[(j * 3 + iw) * 2 + 0], an, sch);
+                        cfmaf(acc[(j * 3 + iw) * 2 + 1], an, ssx);
+                    }
+            }
+        }
+    }
+    if (nflag <= 0) return;
+    double2 accd[NVC * 6];
+#pragma unroll
+    for (int i = 0; i < NVC * 6; ++i) accd[i] = make_double2((double)acc[i].x, (double)acc[i].y);
+    block_sum<NVC * 6>(accd, sm);
+    if (tid < nflag * 6) {
+        int j = tid / 6, r = tid % 6;
+        p.F[(((long)ch * p.nv + p.n1base + j) * p.ng + my_igp) * 6 + r] = accd[tid];
+    }
+}
+
+// ------------------------------------------------------------------ finalize
+// Flag bands: sum the chunk partials, apply the reference's weights
+// (sch: 0.5*vcoul*conj(aqsm), BGW-Kernels/gppKer.cpp:346,421; ssx:
+// occ*vcoul*conj(aqsm), :419).  FW[n1][my_igp][6].
+__global__ void flag_weights_kernel(int nv, int ng, int nc, int nch, const double2* F, const double2* aqsm,
+                                    const double* vcoul, const int* igp, double2* FW) {
+    const int my_igp = blockIdx.x * blockDim.x + threadIdx.x, n1 = blockIdx.y;
+    if (my_igp >= ng) return;
+    const int g = igp[my_igp];
+    double2 s[6];
+    for (int r = 0; r < 6; ++r) s[r] = make_double2(0.0, 0.0);
+    for (int ch = 0; ch < nch; ++ch)
+        for (int r = 0; r < 6; ++r) s[r] = cadd(s[r], F[(((long)ch * nv + n1) * ng + my_igp) * 6 + r]);
+    double2* o = FW + ((long)n1 * ng + my_igp) * 6;
+    if (g < 0) {
+        for (int r = 0; r < 6; ++r) o[r] = make_double2(0.0, 0.0);
+        return;
+    }
+    const double2 cm = cconj(aqsm[(long)n1 * nc + g]);
+    const double v = vcoul[g], occ = 1.0;
+    for (int iw = 0; iw < 3; ++iw) {
+        o[iw * 2 + 0] = cscale(cmul(cm, s[iw * 2 + 0]), 0.5 * v);
+        o[iw * 2 + 1] = cscale(cmul(cm, s[iw * 2 + 1]), occ * v);
+    }
+}
+
+// Per-band sums.  rows[n1][8] = {sch iw0..2, ssx iw0..2, stat, 0}.
+__global__ void row_sums_kernel(int nb, int nv, int ng, int nslots, const double2* P, int nslots_s,
+                                const double2* S, const double2* FW, double2* rows) {
+    __shared__ double2 sm[8 * 7];
+    const int n1 = blockIdx.x, tid = threadIdx.x;
+    double2 v[7];
+    for (int i = 0; i < 7; ++i) v[i] = make_double2(0.0, 0.0);
+    if (n1 >= nv) {
+        const int M = nb - nv, m = n1 - nv;
+        for (int s = tid; s < nslots; s += blockDim.x)
+            for (int iw = 0; iw < 3; ++iw) v[iw] = cadd(v[iw], P[((long)s * M + m) * 3 + iw]);
+    } else {
+        for (int h = tid; h < ng; h += blockDim.x) {
+            const double2* o = FW + ((long)n1 * ng + h) * 6;
+            for (int iw = 0; iw < 3; ++iw) {
+                v[iw] = cadd(v[iw], o[iw * 2]);
+                v[3 + iw] = cadd(v[3 + iw], o[iw * 2 + 1]);
+            }
+        }
+    }
+    if (S)
+        for (int s = tid; s < nslots_s; s += blockDim.x) v[6] = cadd(v[6], S[(long)s * nb + n1]);
+    block_sum<7>(v, sm);
+    if (tid < 7) rows[(long)n1 * 8 + tid] = v[tid];
+}
+
+// Totals over bands; out = [achtemp 3 | asxtemp 3 | achstemp | acht_n1_loc nb].
+__global__ void totals_kernel(int nb, const double2* rows, double2* out) {
+    __shared__ double2 sm[8 * 7];
+    const int tid = threadIdx.x;
+    double2 v[7];
+    for (int i = 0; i < 7; ++i) v[i] = make_double2(0.0, 0.0);
+    for (int n1 = tid; n1 < nb; n1 += blockDim.x) {
+        for (int i = 0; i < 7; ++i) v[i] = cadd(v[i], rows[(long)n1 * 8 + i]);
+        out[7 + n1] = rows[(long)n1 * 8 + 2];  // acht_n1_loc, BGW-Kernels/gppKer.cpp:424
+    }
+    block_sum<7>(v, sm);
+    if (tid < 7) out[tid] = v[tid];
+}
+
+struct Plan {
+    int nch, passes;
+    int MT, NT, KS, kchunk;      // main contraction
+    int MTs, NTs, KSs, kchunks;  // static remainder contraction
+    bool mixed;
+    size_t bytesD, bytesF, bytesP, bytesS, bytesFW, bytesRows, bytesIgp;
+};
+
+void pick_split(int tiles, int K, int target, int& KS, int& kchunk) {
+    KS = std::max(1, std::min((target + tiles - 1) / tiles, std::max(1, K / 256)));
+    kchunk = ((K + KS - 1) / KS + 15) / 16 * 16;
+    KS = (K + kchunk - 1) / kchunk;
+}
+
+Plan make_plan(const Ctx& c, const GppDev& r) {
+    Plan p{};
+    p.mixed = r.prec == FK_MIXED;
+    p.nch = ceil_div(r.nc, PREP_TILE);
+    p.passes = std::max(1, ceil_div(r.nv, NVC));
+    const int M = r.nb - r.nv, N = 3 * r.ng;
+    const int BM = p.mixed ? f32::BM : d64::BM, BN = p.mixed ? f32::BN : d64::BN;
+    const int per_sm = p.mixed ? 4 : 2;
+    p.MT = ceil_div(std::max(M, 1), BM);
+    p.NT = ceil_div(N, BN);
+    pick_split(p.MT * p.NT, r.nc, c.sms * per_sm, p.KS, p.kchunk);
+    p.MTs = ceil_div(r.nb, BM);
+    p.NTs = ceil_div(r.ng, BN);
+    pick_split(p.MTs * p.NTs, r.nc, c.sms * per_sm, p.KSs, p.kchunks);
+    p.bytesD = M > 0 ? (size_t)N * r.nc * (p.mixed ? sizeof(float2) : sizeof(double2)) : 0;
+    p.bytesF = (size_t)p.nch * std::max(r.nv, 1) * r.ng * 6 * sizeof(double2);
+    p.bytesP = M > 0 ? (size_t)p.KS * p.NT * M * 3 * sizeof(double2) : 0;
+    p.bytesS = (r.flags & FK_GPP_ACHSTEMP) ? (size_t)p.KSs * p.NTs * r.nb * sizeof(double2) : 0;
+    p.bytesFW = (size_t)std::max(r.nv, 1) * r.ng * 6 * sizeof(double2);
+    p.bytesRows = (size_t)r.nb * 8 * sizeof(double2);
+    p.bytesIgp = (size_t)r.ng * sizeof(int);
+    return p;
+}
+
+template <class K>
+cudaError_t set_smem(K kernel, size_t bytes) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+}  // namespace
+
+size_t gpp_workspace(const Ctx& c, const GppDev& r) {
+    Plan p = make_plan(c, r);
+    return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesFW + p.bytesRows + p.bytesIgp + 8 * 256;
+}
+
+fk_status gpp_run(Ctx& c, const GppDev& r) {
+    const Plan p = make_plan(c, r);
+    cudaStream_t st = c.stream;
+    int* igp = (int*)c.ws.take(p.bytesIgp);
+    void* D = p.bytesD ? c.ws.take(p.bytesD) : nullptr;
+    double2* F = (double2*)c.ws.take(p.bytesF);
+    double2* P = p.bytesP ? (double2*)c.ws.take(p.bytesP) : nullptr;
+    double2* S = p.bytesS ? (double2*)c.ws.take(p.bytesS) : nullptr;
+    double2* FW = (double2*)c.ws.take(p.bytesFW);
+    double2* rows = (double2*)c.ws.take(p.bytesRows);
+    if (!igp || !F || !FW || !rows || (p.bytesD && !D) || (p.bytesP && !P) || (p.bytesS && !S))
+        return fail(c, FK_ENOMEM, "workspace too small for GPP request");
+    const bool Q = (r.flags & FK_GPP_ROOT_QUIRKS) != 0;
+    const int M = r.nb - r.nv;
+    c.launches = 0;
+
+    phase_mark(c, 1);
+    igp_map_kernel<<<ceil_div(r.ng, 128), 128, 0, st>>>(r.ng, r.nc, r.inv, r.indinv, igp);
+    ++c.launches;
+    for (int pass = 0; pass < p.passes; ++pass) {
+        PrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, pass == 0 ? D : nullptr, F, p.nch,
+                   pass * NVC};
+        dim3 grid(p.nch, r.ng);
+        if (p.mixed) {
+            if (Q) prep_mixed_kernel<1><<<grid, PREP_THREADS, 0, st>>>(a);
+            else prep_mixed_kernel<0><<<grid, PREP_THREADS, 0, st>>>(a);
+        } else {
+            if (Q) prep64_kernel<1><<<grid, PREP_THREADS, 0, st>>>(a);
+            else prep64_kernel<0><<<grid, PREP_THREADS, 0, st>>>(a);
+        }
+        ++c.launches;
+    }
+    phase_mark(c, 2);
+    if (M > 0) {
+        ContractArgs a{};
+        a.A = r.aqsn; a.lda = r.nc; a.m0 = r.nv; a.M = M;
+        a.B = D; a.ldb = r.nc; a.bstride = 0; a.N = 3 * r.ng; a.K = r.nc;
+        a.KS = p.KS; a.kchunk = p.kchunk; a.batches = 1; a.batch_plane = nullptr;
+        a.aqsm = r.aqsm; a.ldm = r.nc; a.vcoul = r.vcoul; a.igp = igp; a.wscale = 0.5; a.G = 3; a.P = P;
+        dim3 grid(p.MT, p.NT * p.KS);
+        if (p.mixed) {
+            auto k = f32::contract_kernel<EPI_GPP, float2>;
+            set_smem(k, f32::SMEM);
+            k<<<grid, f32::THREADS, f32::SMEM, st>>>(a);
+        } else {
+            auto k = d64::contract_kernel<EPI_GPP>;
+            set_smem(k, d64::SMEM);
+            k<<<grid, d64::THREADS, d64::SMEM, st>>>(a);
+        }
+        ++c.launches;
+    }
+    if (S) {
+        ContractArgs a{};
+        a.A = r.aqsn; a.lda = r.nc; a.m0 = 0; a.M = r.nb;
+        a.B = r.eps; a.ldb = r.nc; a.bstride = 0; a.N = r.ng; a.K = r.nc;
+        a.KS = p.KSs; a.kchunk = p.kchunks; a.batches = 1; a.batch_plane = nullptr;
+        a.aqsm = r.aqsm; a.ldm = r.nc; a.vcoul = r.vcoul; a.igp = igp; a.wscale = -0.5; a.G = 1; a.P = S;
+        dim3 grid(p.MTs, p.NTs * p.KSs);
+        if (p.mixed) {
+            auto k = f32::contract_kernel<EPI_STAT, double2>;
+            set_smem(k, f32::SMEM);
+            k<<<grid, f32::THREADS, f32::SMEM, st>>>(a);
+        } else {
+            auto k = d64::contract_kernel<EPI_STAT>;
+            set_smem(k, d64::SMEM);
+            k<<<grid, d64::THREADS, d64::SMEM, st>>>(a);
+        }
+        ++c.launches;
+    }
+    phase_mark(c, 3);
+    if (r.nv > 0) {
+        flag_weights_kernel<<<dim3(ceil_div(r.ng, 128), r.nv), 128, 0, st>>>(r.nv, r.ng, r.nc, p.nch, F, r.aqsm,
+                                                                             r.vcoul, igp, FW);
+        ++c.launches;
+    }
+    row_sums_kernel<<<r.nb, 256, 0, st>>>(r.nb, r.nv, r.ng, p.KS * p.NT, P, p.KSs * p.NTs, S, FW, rows);
+    totals_kernel<<<1, 256, 0, st>>>(r.nb, rows, r.out);
+    c.launches += 2;
+    phase_mark(c, 4);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "gpp kernels");
+    return FK_OK;
+}
+
+}  // namespace fk

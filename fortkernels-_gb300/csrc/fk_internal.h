@@ -1,0 +1,78 @@
+// fk_internal.h -- host-side declarations shared by the C ABI and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/fk_abi.h"
+
+namespace fk {
+
+// Device workspace: a bump allocator over one grow-only cudaMalloc block.
+struct Workspace {
+    void* base = nullptr;
+    size_t cap = 0, used = 0;
+    void reset() { used = 0; }
+    void* take(size_t bytes) {  // 256-byte aligned; nullptr when it does not fit
+        size_t off = (used + 255) & ~size_t(255);
+        if (off + bytes > cap) return nullptr;
+        used = off + bytes;
+        return (char*)base + off;
+    }
+};
+
+struct Ctx {
+    int device = 0;
+    int sms = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    Workspace ws;
+    void* pinned = nullptr;      // pinned host staging for small outputs
+    size_t pinned_cap = 0;
+    std::string err;
+    bool profiling = false;
+    cudaEvent_t ev[5] = {};
+    float timings[4] = {0, 0, 0, 0};
+    int launches = 0;
+};
+
+// Set the context's last error and return the status.
+fk_status fail(Ctx& c, fk_status s, const std::string& msg);
+fk_status cuda_fail(Ctx& c, cudaError_t e, const char* where);
+
+// Resolved GPP request: every pointer is device memory.
+struct GppDev {
+    int nb, nv, nc, ng;
+    const double2 *aqsm, *aqsn, *eps, *wt;
+    const double* vcoul;
+    const int *inv, *indinv;
+    const double* wx;  // device [3]
+    fk_precision prec;
+    unsigned flags;
+    double2* out;      // device [3 achtemp | 3 asxtemp | 1 achstemp | nb acht_n1_loc]
+};
+// Bytes of workspace gpp_run needs for this request (excluding staged inputs).
+size_t gpp_workspace(const Ctx& c, const GppDev& r);
+fk_status gpp_run(Ctx& c, const GppDev& r);
+
+struct FfDev {
+    int nb, nv, nc, ng, nf, ne;
+    const double2 *aqsm, *aqsn, *epsR, *epsA, *brd;
+    const double *vcoul, *ekq, *grid, *pref;
+    const int *inv, *indinv;
+    double pref_zb, fmin, fstep, occ;
+    fk_precision prec;
+    unsigned flags;
+    // outputs (device): [achsDtemp | asx[ne] | achD[ne] | cor[ne] | a2[ne] | schDt[nb*nf]]
+    double2* out;
+};
+size_t ff_workspace(const Ctx& c, const FfDev& r);
+fk_status ff_run(Ctx& c, const FfDev& r);
+
+// Phase timing helpers (no-ops unless profiling is on).
+void phase_mark(Ctx& c, int i);
+void phase_close(Ctx& c, int nphases);
+
+}  // namespace fk

@@ -69,12 +69,15 @@ def gpp_synthetic(number_bands: int, nvband: int, ncouls: int, ngpown: int, seed
            "reference" inv_igp_index[i] = (i+1)*ncouls/ngpown (clamped by the kernel)
     wx:    "baseline"  e_lk-dw, e_lk, e_lk+dw with e_lk=10, dw=1
            "reference" e_lk - e_n1kq + dw*(iw-1) = {3,4,5}
+           "stress"    {0.4, 3, 5}: a frequency below 0.5 makes the third branch
+                       (neither sch nor ssx, |delw|^2 <= 1e-6) reachable
     """
     rng = np.random.default_rng(seed)
     aqsm = _cu(rng, (number_bands, ncouls))
     aqsn = _cu(rng, (number_bands, ncouls))
     eps = _cu(rng, (ngpown, ncouls))
-    wxa = np.array([9.0, 10.0, 11.0]) if wx == "baseline" else gpp_wx()
+    wxa = {"baseline": np.array([9.0, 10.0, 11.0]), "reference": gpp_wx(),
+           "stress": np.array([0.4, 3.0, 5.0])}[wx]
     if dist == "uniform":
         wt = rng.uniform(0.5, 2.0, (ngpown, ncouls)) + 1j * rng.uniform(-0.05, 0.05, (ngpown, ncouls))
     elif dist == "branch":

@@ -1,0 +1,163 @@
+/*
+ * fk_abi.h -- C ABI of the GB300 (sm_103a) GPP / FF self-energy library.
+ *
+ * The reference mini-apps have no library boundary: each hot path is a loop
+ * nest inside a driver main() that fills its own arrays.  Every entry point
+ * below replaces one of those loop nests with a call that takes the same
+ * arrays in the same layouts:
+ *
+ *   fk_gpp  <- the n1 x my_igp x ig x iw nest of BGW-Kernels/gppKer.cpp:303-439
+ *              (flagOCC_solver :130-159 + ssxt_scht_solver :19-65 for n1 < nvband,
+ *              the cache-blocked noflag block :349-413 otherwise), and its
+ *              repo-root variant gppKer.cpp:266-345 (FK_GPP_ROOT_QUIRKS).
+ *   fk_ff   <- the kernel sequence of FFKer_cori/ffKernel.cpp:480-503
+ *              (achsDtemp_Kernel :107-131, asxDtemp_Kernel :133-153,
+ *              achDtemp_Kernel :155-210, achDtemp_cor_Kernel :212-246) plus the
+ *              band x G x G' contraction of ffkernel.deslippe.best.f90.back1:402-418.
+ *
+ * Conventions
+ *   - Complex numbers are fk_c128 = {double re, im}, bit-compatible with
+ *     std::complex<double> and with the reference's GPUComplex.
+ *   - Arrays are row-major exactly as in the reference:
+ *       aqsmtemp/aqsntemp [number_bands][ncouls]
+ *       I_eps_array/wtilde_array [ngpown][ncouls]
+ *       I_epsR_array/I_epsA_array [nFreq][ngpown][ncouls]
+ *   - Every array pointer may be host memory or device memory of the
+ *     context's GPU; the library detects which.  Host inputs are staged to the
+ *     device; host outputs are copied back and the call returns after the
+ *     stream has finished.  When every output pointer is device memory the
+ *     call only enqueues work on the context's stream and returns at once.
+ *   - The caller owns all buffers; no pointer is kept after a call returns.
+ *   - Errors are reported by status code only; nothing aborts or throws.
+ *   - A context is bound to one device and one stream and is not thread-safe:
+ *     use one context per host thread.
+ *   - There is no CPU fallback: without a usable GPU every compute call
+ *     returns FK_ECUDA.
+ */
+#ifndef FK_ABI_H
+#define FK_ABI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fk_ctx* fk_ctx_t;
+
+typedef enum {
+    FK_OK = 0,
+    FK_EINVAL = 1,    /* bad sizes, null required pointer, bad flags          */
+    FK_ENOMEM = 2,    /* device or pinned-host allocation failed              */
+    FK_ECUDA = 3,     /* a CUDA call failed (no device, launch error, ...)    */
+    FK_ETIMEOUT = 4,  /* a bounded device-side wait gave up                   */
+    FK_EBUSY = 5,     /* admission refused (serving: over the memory budget)  */
+    FK_ENOTSUP = 6    /* valid request this build does not support           */
+} fk_status;
+
+typedef enum {
+    FK_FP64 = 0,   /* plain path: FP64 everywhere; matches the reference C++ to 1e-12 */
+    FK_MIXED = 1   /* branch tests and near-pole divisions in FP64, bulk
+                      contractions in reduced precision with FP32 accumulation
+                      and FP64 block reductions; <= 1e-6 relative to FP64 */
+} fk_precision;
+
+typedef struct { double re, im; } fk_c128;
+
+/* ---------------------------------------------------------------- context */
+
+/* Create a context on CUDA device `device` with its own non-blocking stream. */
+fk_status fk_create(int device, fk_ctx_t* out);
+fk_status fk_destroy(fk_ctx_t ctx);
+/* Use `stream` (a cudaStream_t of the context's device) for later calls;
+ * NULL restores the context's own stream. */
+fk_status fk_set_stream(fk_ctx_t ctx, void* stream);
+/* Wait for all work enqueued by the context. */
+fk_status fk_synchronize(fk_ctx_t ctx);
+/* Grow the device workspace to at least `bytes` now (e.g. before capturing
+ * a CUDA graph, during which the library must not allocate). */
+fk_status fk_reserve(fk_ctx_t ctx, size_t bytes);
+/* Static description of a status code, and the last detailed message. */
+const char* fk_strerror(fk_status s);
+const char* fk_last_error(fk_ctx_t ctx);
+/* Library version string, e.g. "fk_gb300 1.0 sm_103a". */
+const char* fk_version(void);
+
+/* ------------------------------------------------------------------- GPP */
+
+/* Flags for fk_gpp */
+#define FK_GPP_ROOT_QUIRKS 0x1u /* semantics of the repo-root gppKer.cpp: every noflag
+                                   term is summed (no |wdiff|/|delw| mask, gppKer.cpp:336)
+                                   and flagOCC's sch uses I_eps[my_igp*ngpown+ig]
+                                   (gppKer.cpp:139) */
+#define FK_GPP_ACHSTEMP    0x2u /* also compute the static-CH remainder achstemp
+                                   (gppkernel.deslippe.09.30.2014.f90:195-229) */
+
+/*
+ * GPP self-energy sum (BGW-Kernels/gppKer.cpp:303-439).
+ *
+ *   inv_igp_index[ngpown], indinv[ncouls] (int32): column map
+ *       igp = indinv[inv_igp_index[my_igp]], with inv_igp_index == ncouls
+ *       mapped to igp = ncouls-1 (BGW-Kernels/gppKer.cpp:322-325); entries that
+ *       map outside [0, ncouls) are skipped as the reference skips them (:328).
+ *   wx_array[3]: the evaluation frequencies (the reference computes
+ *       e_lk - e_n1kq + dw*(iw-1), clamped away from 0, :310-314).
+ *   Outputs: achtemp[3], asxtemp[3]; acht_n1_loc[number_bands] and achstemp[1]
+ *       may be NULL.
+ */
+fk_status fk_gpp(fk_ctx_t ctx, int number_bands, int nvband, int ncouls, int ngpown,
+                 const fk_c128* aqsmtemp, const fk_c128* aqsntemp,
+                 const fk_c128* I_eps_array, const fk_c128* wtilde_array,
+                 const double* vcoul, const int* inv_igp_index, const int* indinv,
+                 const double* wx_array, fk_precision precision, unsigned flags,
+                 fk_c128* achtemp, fk_c128* asxtemp, fk_c128* acht_n1_loc, fk_c128* achstemp);
+
+/* -------------------------------------------------------------------- FF */
+
+/* Flags for fk_ff */
+#define FK_FF_SCHDT_GEMM  0x1u /* schDt_matrix[n1][f] = sum_igp conj(aqsm[n1][igp]) *
+                                  sum_ig I_epsR[f][my_igp][ig]*aqsn[n1][ig]
+                                  (ffkernel.deslippe.best.f90.back1:402-418); without it
+                                  schDt_matrix is zero as in FFKer_cori/ffKernel.cpp:421-422 */
+#define FK_FF_PHYSICS     0x2u /* calculate_schDt_lin3 gets freqevalmin/freqevalstep as
+                                  doubles; the reference C++ truncates them to int
+                                  (FFKer_cori/ffKernel.cpp:10) */
+#define FK_FF_SPLIT_ACHD  0x4u /* return achDtemp separately; the reference main passes
+                                  asxDtemp as achDtemp_Kernel's output (ffKernel.cpp:495),
+                                  so by default the sum lands in asxDtemp */
+
+/*
+ * FF full-frequency kernels (FFKer_cori/ffKernel.cpp:480-503).
+ *   ekq[number_bands], dFreqGrid[nFreq], pref[nFreq] (float64),
+ *   dFreqBrd[nFreq] (complex), vcoul[ncouls], inv_igp_index[ngpown], indinv[ncouls].
+ *   Outputs: achsDtemp[1], asxDtemp[nfreqeval], achDtemp_cor[nfreqeval];
+ *   achDtemp[nfreqeval], ach2Dtemp[nfreqeval] and schDt_matrix[number_bands][nFreq]
+ *   may be NULL.  Requires nFreq >= 2 and ngpown <= ncouls (ffKernel.cpp:320).
+ */
+fk_status fk_ff(fk_ctx_t ctx, int number_bands, int nvband, int ncouls, int ngpown,
+                int nFreq, int nfreqeval,
+                const fk_c128* aqsmtemp, const fk_c128* aqsntemp,
+                const fk_c128* I_epsR_array, const fk_c128* I_epsA_array,
+                const double* vcoul, const int* inv_igp_index, const int* indinv,
+                const double* ekq, const double* dFreqGrid, const fk_c128* dFreqBrd,
+                const double* pref, double pref_zb, double freqevalmin, double freqevalstep,
+                double occ, fk_precision precision, unsigned flags,
+                fk_c128* achsDtemp, fk_c128* asxDtemp, fk_c128* achDtemp,
+                fk_c128* achDtemp_cor, fk_c128* ach2Dtemp, fk_c128* schDt_matrix);
+
+/* ------------------------------------------------------------ measurement */
+
+/* Kernel-level timing of the most recent fk_gpp/fk_ff call, measured with
+ * CUDA events on the launch stream when enabled with fk_set_profiling(ctx,1).
+ * Phases: 0 = input staging, 1 = prep / branch kernel, 2 = contraction
+ * (the dominant kernel), 3 = reduction + epilogue.  Milliseconds. */
+fk_status fk_set_profiling(fk_ctx_t ctx, int enable);
+fk_status fk_last_timings(fk_ctx_t ctx, float ms[4]);
+/* Number of kernels the most recent call launched. */
+int fk_last_launches(fk_ctx_t ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FK_ABI_H */

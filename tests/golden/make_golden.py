@@ -1,0 +1,85 @@
+"""Regenerate the golden fixtures of tests/golden/ from the reference.
+
+Needs the reference tree (its drivers and harnesses are compiled into
+oracle/_ref/ by `make -C oracle ref`).  It runs:
+  * the unmodified reference drivers (BGW-Kernels/gppKer.cpp, repo-root
+    gppKer.cpp, gppKer_orig.cpp, FFKer_cori/ffKernel.cpp) with their own
+    constant inputs, recording what they print;
+  * the harnesses that call the reference's own solver functions
+    (oracle/ref_harness_gpp.cpp, oracle/ref_harness_ff.cpp) on small seeded
+    random inputs, stored together with the inputs.
+The oracle and the CUDA library are then checked against these files on any
+machine, without the reference.
+
+usage: python tests/golden/make_golden.py [--big]
+  --big also runs gppKer 512 2 32768 20 (about two minutes on 8 cores).
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+import __graft_entry__  # noqa: E402
+
+inputs = __graft_entry__.load_package().inputs
+
+GPP_SIZES = [(64, 2, 512, 4), (32, 2, 1000, 8), (128, 4, 777, 7), (512, 2, 2048, 32), (40, 0, 600, 6),
+             (24, 24, 256, 4)]
+FF_SIZES = [(16, 3, 300, 40, 6, 7), (64, 2, 512, 64, 15, 10), (512, 2, 4096, 512, 15, 10)]
+
+
+def cx(z):
+    return [z.real, z.imag]
+
+
+def main(big: bool):
+    oracle.build()
+    out = {"gppKer_bgw": [], "gppKer_root": [], "gppKer_orig": [], "ffKernel": []}
+    sizes = GPP_SIZES + ([(512, 2, 32768, 20)] if big else [])
+    for s in sizes:
+        r = oracle.run_ref_driver("gppKer_bgw", s)
+        out["gppKer_bgw"].append({"args": list(s), "achtemp": [cx(r[f"achtemp[{i}]"]) for i in range(3)],
+                                  "seconds": r.get("seconds")})
+        if s[0] <= 128:
+            r = oracle.run_ref_driver("gppKer_root", s, threads=1)
+            out["gppKer_root"].append({"args": list(s), "achtemp": [cx(r[f"achtemp[{i}]"]) for i in range(3)],
+                                       "achstemp_printed": cx(r["achstemp"])})
+    r = oracle.run_ref_driver("gppKer_orig", (512, 2, 2048, 32))
+    out["gppKer_orig"].append({"args": [512, 2, 2048, 32], "achtemp": [cx(r[f"achtemp[{i}]"]) for i in range(3)]})
+    for s in FF_SIZES:
+        r = oracle.run_ref_driver("ffKernel", s)
+        out["ffKernel"].append({"args": list(s), "achsDtemp": cx(r["achsDtemp"]), "asxDtemp0": cx(r["asxDtemp"]),
+                                "achDtemp_cor0": cx(r["achDtemp_cor"])})
+    with open(os.path.join(HERE, "reference_drivers.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+    # per-(n1, my_igp, iw) values of the reference solver functions
+    for name, kw in (("gpp_pairs_branch", dict(dist="branch")), ("gpp_pairs_uniform", dict(dist="uniform"))):
+        p = inputs.gpp_synthetic(7, 3, 300, 5, seed=11, index="reference", wx="reference", **kw)
+        inv, nc = p["inv_igp_index"], p["ncouls"]
+        igp = np.array([nc - 1 if i == nc else p["indinv"][i] for i in inv], np.int32)
+        h = oracle.ref_gpp_pairs(p, igp)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), sch=h["sch"], ssx=h["ssx"],
+                            **{k: np.asarray(v) for k, v in p.items()})
+    p = inputs.ff_synthetic(9, 3, 96, 12, 4, 5, seed=5)
+    # schDt_matrix from the band x G x G' contraction, fed to the reference's
+    # own achDtemp_Kernel (the reference C++ leaves it zero)
+    schdt = oracle.ff(p, flags=oracle.ORC_FF_SCHDT_GEMM)["schDt_matrix"]
+    h = oracle.ref_ff(p, schDt=schdt)
+    np.savez_compressed(os.path.join(HERE, "ff_harness.npz"), ref_achsDtemp=h["achsDtemp"],
+                        ref_asxDtemp=h["asxDtemp"], ref_achDtemp_cor=h["achDtemp_cor"], ref_ach2Dtemp=h["ach2Dtemp"],
+                        ref_schDt=schdt, **{k: np.asarray(v) for k, v in p.items()})
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main("--big" in sys.argv)

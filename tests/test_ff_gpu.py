@@ -1,0 +1,87 @@
+"""GPU parity tests of the FF path (fk_ff through the C ABI) against the oracle.
+
+Tolerances: FP64 <= 1e-12 relative to the oracle; mixed <= 1e-6 relative to FP64.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+TOL64, TOLMX = 1e-12, 1e-6
+KEYS = ("achsDtemp", "asxDtemp", "achDtemp", "achDtemp_cor", "ach2Dtemp", "schDt_matrix")
+
+
+def check(res, ref, tol, keys=KEYS):
+    errs = {}
+    for k in keys:
+        a, b = np.atleast_1d(res[k]), np.atleast_1d(ref[k])
+        if np.max(np.abs(b)) == 0:
+            errs[k] = float(np.max(np.abs(a)))
+        else:
+            errs[k] = rel(a, b)
+    assert all(e <= tol for e in errs.values()), errs
+    return errs
+
+
+FLAGS = [0, 1, 2, 4, 7]
+CASES = [(40, 2, 640, 48, 6, 5), (17, 3, 1001, 33, 4, 3), (64, 0, 512, 64, 15, 10), (9, 9, 300, 20, 2, 1)]
+
+
+@pytest.mark.parametrize("flags", FLAGS)
+@pytest.mark.parametrize("case", CASES, ids=lambda c: "x".join(map(str, c)))
+def test_ff_fp64_matches_oracle(ctx, fk, orc, case, flags):
+    p = fk.inputs.ff_synthetic(*case, seed=sum(case))
+    ref = orc.ff(p, flags=flags)
+    check(ctx.ff(p, "fp64", flags), ref, TOL64)
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: "x".join(map(str, c)))
+def test_ff_mixed_within_1e6(ctx, fk, case):
+    p = fk.inputs.ff_synthetic(*case, seed=sum(case))
+    f = fk.FK_FF_SCHDT_GEMM | fk.FK_FF_SPLIT_ACHD
+    check(ctx.ff(p, "mixed", f), ctx.ff(p, "fp64", f), TOLMX)
+
+
+def test_ff_matches_reference_kernels_with_schdt(ctx, fk):
+    z = np.load(os.path.join(GOLD, "ff_harness.npz"))
+    p = {k: z[k] for k in z.files if not k.startswith("ref_")}
+    for k in ("number_bands", "nvband", "ncouls", "ngpown", "nFreq", "nfreqeval"):
+        p[k] = int(p[k])
+    r = ctx.ff(p, "fp64", fk.FK_FF_SCHDT_GEMM)
+    assert rel(r["schDt_matrix"], z["ref_schDt"]) <= TOL64
+    for k in ("achsDtemp", "asxDtemp", "achDtemp_cor", "ach2Dtemp"):
+        assert rel(np.atleast_1d(r[k]), np.atleast_1d(z["ref_" + k])) <= TOL64, k
+
+
+def test_ff_matches_reference_driver_prints(ctx, fk):
+    with open(os.path.join(GOLD, "reference_drivers.json")) as f:
+        entries = json.load(f)["ffKernel"]
+    for e in entries:
+        r = ctx.ff(fk.inputs.ff_reference_init(*e["args"]), "fp64")
+        assert abs(r["achsDtemp"][0] - complex(*e["achsDtemp"])) <= TOL64 * abs(complex(*e["achsDtemp"]))
+        assert abs(r["asxDtemp"][0] - complex(*e["asxDtemp0"])) <= TOL64 * abs(complex(*e["asxDtemp0"]))
+        assert abs(r["achDtemp_cor"][0] - complex(*e["achDtemp_cor0"])) <= TOL64 * abs(complex(*e["achDtemp_cor0"]))
+
+
+def test_ff_bitwise_deterministic(ctx, fk):
+    p = fk.inputs.ff_synthetic(64, 2, 1024, 96, 8, 6, seed=3)
+    a = ctx.ff(p, "mixed", fk.FK_FF_SCHDT_GEMM)
+    b = ctx.ff(p, "mixed", fk.FK_FF_SCHDT_GEMM)
+    for k in KEYS:
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+def test_ff_rejects_bad_arguments(ctx, fk):
+    p = fk.inputs.ff_synthetic(8, 2, 64, 8, 4, 2, seed=1)
+    with pytest.raises(fk.FKError):
+        ctx.ff(dict(p, nFreq=1))
+    q = dict(p, ngpown=65, I_epsR_array=np.zeros(4 * 65 * 64, np.complex128),
+             I_epsA_array=np.zeros(4 * 65 * 64, np.complex128), inv_igp_index=np.arange(65, dtype=np.int32))
+    with pytest.raises(fk.FKError) as e:
+        ctx.ff(q)  # ngpown > ncouls, rejected as in FFKer_cori/ffKernel.cpp:320
+    assert e.value.status == 1

@@ -1,0 +1,147 @@
+"""CPU tests: the oracle pinned against the reference's own outputs.
+
+* reference_drivers.json: values printed by the unmodified reference drivers
+  (constant inputs of their main()), generated by tests/golden/make_golden.py;
+* gpp_pairs_*.npz / ff_harness.npz: per-(n1, igp, iw) values and FF outputs of
+  the reference's own solver functions on seeded random inputs.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def drivers():
+    with open(os.path.join(GOLD, "reference_drivers.json")) as f:
+        return json.load(f)
+
+
+def cx(v):
+    return np.array([complex(*z) for z in v]) if isinstance(v[0], list) else complex(*v)
+
+
+@pytest.mark.parametrize("entry", [e for e in drivers()["gppKer_bgw"] if e["args"][2] <= 4096],
+                         ids=lambda e: "x".join(map(str, e["args"])))
+def test_gpp_oracle_matches_bgw_driver(fk, orc, entry):
+    p = fk.inputs.gpp_reference_init(*entry["args"])
+    o = orc.gpp(p)
+    # the driver prints 15 significant digits and sums in a schedule-dependent order
+    assert rel(o["achtemp"], cx(entry["achtemp"])) < 1e-13
+
+
+@pytest.mark.parametrize("entry", drivers()["gppKer_root"], ids=lambda e: "x".join(map(str, e["args"])))
+def test_gpp_oracle_matches_root_driver_quirks(fk, orc, entry):
+    p = fk.inputs.gpp_reference_init(*entry["args"])
+    o = orc.gpp(p, flags=orc.ORC_GPP_ROOT_QUIRKS)
+    # gppKer.cpp sums whole rows sequentially; its own rounding is ~1e-13
+    assert rel(o["achtemp"], cx(entry["achtemp"])) < 1e-12
+
+
+def test_gpp_negative_control_igblk_off_by_one(fk, orc):
+    # gppKer_orig.cpp drops one ig per 512-block (igend = igbeg+igblk-1); the
+    # oracle must NOT reproduce it.
+    e = drivers()["gppKer_orig"][0]
+    o = orc.gpp(fk.inputs.gpp_reference_init(*e["args"]))
+    assert rel(o["achtemp"], cx(e["achtemp"])) > 1e-5
+
+
+@pytest.mark.parametrize("name", ["gpp_pairs_branch", "gpp_pairs_uniform"])
+def test_gpp_oracle_bitexact_vs_reference_solvers(orc, name):
+    z = np.load(os.path.join(GOLD, name + ".npz"))
+    p = {k: z[k] for k in z.files}
+    for k in ("number_bands", "nvband", "ncouls", "ngpown"):
+        p[k] = int(p[k])
+    o = orc.gpp(p, per_pair=True)
+    np.testing.assert_array_equal(o["sch"], z["sch"])
+    np.testing.assert_array_equal(o["ssx"], z["ssx"])
+
+
+def branch_counts(p):
+    """Count which branch of ssxt_scht_solver each (igp, ig, iw) takes."""
+    wt = p["wtilde_array"]
+    counts = {"A": 0, "B": 0, "none": 0, "near_limittwo": 0, "pole": 0}
+    for wx in p["wx_array"]:
+        wd = wx - wt
+        wdr = np.abs(wd) ** 2
+        delw = wt * np.conj(wd) / wdr
+        dr = np.abs(delw) ** 2
+        A = (wdr > 0.25) & (dr < 2.5e5)
+        B = ~A & (dr > 1e-6)
+        counts["A"] += int(A.sum())
+        counts["B"] += int(B.sum())
+        counts["none"] += int((~A & ~B).sum())
+        counts["near_limittwo"] += int((np.abs(wdr - 0.25) < 0.05).sum())
+        counts["pole"] += int((dr >= 2.5e5).sum())
+    return counts
+
+
+def test_branch_stress_inputs_take_every_branch(fk):
+    p = fk.inputs.gpp_synthetic(4, 2, 4096, 8, seed=3, dist="branch", index="reference", wx="stress")
+    c = branch_counts(p)
+    assert all(v > 0 for v in c.values()), c
+
+
+def test_ff_oracle_matches_ffkernel_driver(fk, orc):
+    for e in drivers()["ffKernel"]:
+        if e["args"][0] * e["args"][2] * e["args"][3] > 64 * 512 * 64:
+            continue
+        o = orc.ff(fk.inputs.ff_reference_init(*e["args"]))
+        assert abs(o["achsDtemp"] - cx(e["achsDtemp"])) <= 1e-13 * abs(cx(e["achsDtemp"]))
+        assert abs(o["asxDtemp"][0] - cx(e["asxDtemp0"])) <= 1e-13 * abs(cx(e["asxDtemp0"]))
+        assert abs(o["achDtemp_cor"][0] - cx(e["achDtemp_cor0"])) <= 1e-13 * abs(cx(e["achDtemp_cor0"]))
+
+
+def test_ff_oracle_matches_reference_kernels_with_schdt(orc):
+    z = np.load(os.path.join(GOLD, "ff_harness.npz"))
+    p = {k: z[k] for k in z.files if not k.startswith("ref_")}
+    for k in ("number_bands", "nvband", "ncouls", "ngpown", "nFreq", "nfreqeval"):
+        p[k] = int(p[k])
+    o = orc.ff(p, flags=orc.ORC_FF_SCHDT_GEMM)
+    np.testing.assert_allclose(o["schDt_matrix"], z["ref_schDt"], rtol=0, atol=0)
+    assert rel(o["achsDtemp"], z["ref_achsDtemp"]) < 1e-14
+    assert rel(o["asxDtemp"], z["ref_asxDtemp"]) < 1e-14
+    assert rel(o["achDtemp_cor"], z["ref_achDtemp_cor"]) < 1e-14
+    assert rel(o["ach2Dtemp"], z["ref_ach2Dtemp"]) < 1e-14
+
+
+def test_compute_fact_quirks(orc):
+    g = np.array([0.0, 2.0, 4.0, 6.0, 8.0])
+    # loop 1, bracket [2,4] -> ifreq 1
+    f1, f2, i = orc.compute_fact(3.0, g, 1, False)
+    assert i == 1 and f1 == pytest.approx(0.5) and f2 == pytest.approx(0.5)
+    # loop 1, bracket [0,2] (ifreq 0) is remapped to the last interval
+    f1, f2, i = orc.compute_fact(1.0, g, 1, False)
+    assert i == 3 and f1 == pytest.approx((8 - 1) / 2) and f2 == pytest.approx((1 - 6) / 2)
+    # loop 2, wx > 0: factors carry -0.5
+    f1, f2, i = orc.compute_fact(5.0, g, 2, False)
+    assert i == 2 and f1 == pytest.approx(-0.25) and f2 == pytest.approx(-0.25)
+    # loop 2, wx <= 0 and unoccupied: nothing is computed
+    f1, f2, i = orc.compute_fact(-5.0, g, 2, False)
+    assert (f1, f2, i) == (0.0, 0.0, 0)
+    # loop 2, wx <= 0 and occupied: mirrored bracket
+    f1, f2, i = orc.compute_fact(-5.0, g, 2, True)
+    assert i == 2 and f1 == pytest.approx(0.5) and f2 == pytest.approx(0.5)
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(__file__), "..", "oracle", "_ref",
+                                                    "ref_harness_gpp")), reason="reference harness not built")
+def test_gpp_oracle_bitexact_live_harness(fk, orc):
+    p = fk.inputs.gpp_synthetic(9, 4, 700, 6, seed=21, dist="branch", index="baseline", wx="reference")
+    o = orc.gpp(p, per_pair=True)
+    igp = p["indinv"][p["inv_igp_index"]]
+    h = orc.ref_gpp_pairs(p, igp)
+    np.testing.assert_array_equal(o["sch"], h["sch"])
+    np.testing.assert_array_equal(o["ssx"], h["ssx"])
+
+
+def test_gpp_oracle_thread_count_independent(fk, orc):
+    p = fk.inputs.gpp_synthetic(16, 2, 600, 6, seed=4, dist="branch")
+    a = orc.gpp(p, nthreads=1)
+    b = orc.gpp(p, nthreads=3)
+    np.testing.assert_array_equal(a["achtemp"], b["achtemp"])
+    np.testing.assert_array_equal(a["asxtemp"], b["asxtemp"])
