@@ -1,0 +1,370 @@
+"""Benchmark: GPP / FF self-energy terms/s on GB300 (one JSON line on rank 0).
+
+Default workload: the GPP sum at full mini-app size, number_bands=512,
+nvband=2, ncouls=32768, ngpown=20 (synthetic inputs with the benchmark value
+distributions), mixed precision, with the FP64 path measured beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload gpp|gpp1638|ff] [--precision mixed|fp64]
+
+A step is one call of the hot path over one set of inputs.  `value` is the
+device throughput with inputs resident in HBM (CUDA events on the library's
+stream); `e2e` repeats the step through the C ABI with pinned HOST buffers,
+so the host->device staging and the device->host read of the outputs are
+inside the timed region.  Under torchrun every rank runs its own replica
+(the path has no exchange step), and the slowest rank's time is used.
+`--impl reference` times the CPU restatement of the reference loop nest
+(oracle/, OpenMP on all host cores) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # BASELINE config 1: GPP at full mini-app size
+    "gpp": dict(kind="gpp", nb=512, nv=2, nc=32768, ng=20),
+    # the reference's canonical run `gppKer 512 2 32768 20` (ngpown = 32768/20)
+    "gpp1638": dict(kind="gpp", nb=512, nv=2, nc=32768, ng=1638),
+    # BASELINE config 2: FF full-frequency contraction
+    "ff": dict(kind="ff", nb=512, nv=2, nc=4096, ng=512, nf=15, ne=10),
+}
+
+
+def terms(w):
+    if w["kind"] == "gpp":
+        return w["nb"] * w["ng"] * w["nc"] * 3
+    return w["nb"] * w["ng"] * w["nc"] * w["nf"]
+
+
+def algorithmic(w):
+    """(bytes, flops) of the dominant contraction kernel per launch."""
+    if w["kind"] == "gpp":
+        M, N, K = w["nb"] - w["nv"], 3 * w["ng"], w["nc"]
+        return 16 * M * K + 8 * N * K, 8 * M * N * K
+    return 16 * w["nb"] * w["nc"] + 16 * w["nf"] * w["ng"] * w["nc"], 8 * w["nf"] * w["nb"] * w["ng"] * w["nc"]
+
+
+def make_inputs(fk, w, seed=2024):
+    if w["kind"] == "gpp":
+        return fk.inputs.gpp_synthetic(w["nb"], w["nv"], w["nc"], w["ng"], seed=seed, dist="uniform",
+                                       index="baseline", wx="baseline")
+    return fk.inputs.ff_synthetic(w["nb"], w["nv"], w["nc"], w["ng"], w["nf"], w["ne"], seed=seed)
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if r and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) > 1 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 3 + i and r[3 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(a, w):
+    """CPU restatement of the reference loop nest (oracle/) on all host cores."""
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    import __graft_entry__
+    fk = __graft_entry__.load_package()
+    cores = os.cpu_count() or 1
+    p = make_inputs(fk, w)
+    call = (lambda: oracle.gpp(p, nthreads=cores)) if w["kind"] == "gpp" else \
+        (lambda: oracle.ff(p, flags=oracle.ORC_FF_SCHDT_GEMM, nthreads=cores))
+    for _ in range(a.warmup):
+        call()
+    times = []
+    for _ in range(a.steps):
+        t0 = time.perf_counter()
+        call()
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    val = terms(w) * a.steps / tot
+    sample = f"full workload per step ({terms(w):.3g} terms), OpenMP {cores} threads"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "terms/s", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * tot / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(a, w),
+        "cpu_baseline": {"value": val, "unit": "terms/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": "terms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "latency_ms": {"p50": 1e3 * statistics.median(times), "p99": 1e3 * float(np.percentile(times, 99))},
+    }), flush=True)
+
+
+METRIC = "GPP/FF self-energy terms/s + p99 latency, mixed vs FP64 at <=1e-6 rel err"
+
+
+def workload_config(a, w):
+    c = {"workload": ("GPP self-energy sum, number_bands=%d nvband=%d ncouls=%d ngpown=%d" %
+                      (w["nb"], w["nv"], w["nc"], w["ng"])) if w["kind"] == "gpp" else
+         ("FF full-frequency contraction, number_bands=%d nvband=%d ncouls=%d ngpown=%d nFreq=%d nfreqeval=%d"
+          % (w["nb"], w["nv"], w["nc"], w["ng"], w["nf"], w["ne"])),
+         "precision": a.precision, "parallelism": f"replicas x{a.gpus}",
+         "l2": "inputs larger than L2 (aqsntemp %.0f MB)" % (16 * w["nb"] * w["nc"] / 1e6)}
+    return c
+
+
+def timed(torch, stream, fn, steps, warmup, per_step=False):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    evs[0].record(stream)
+    for i in range(steps):
+        fn()
+        if per_step:
+            evs[i + 1].record(stream)
+    if not per_step:
+        evs[steps].record(stream)
+    torch.cuda.synchronize()
+    if per_step:
+        return [evs[i].elapsed_time(evs[i + 1]) for i in range(steps)]
+    return [evs[0].elapsed_time(evs[steps]) / steps] * steps
+
+
+def rel(a, b):
+    a, b = np.atleast_1d(np.asarray(a)), np.atleast_1d(np.asarray(b))
+    d = float(np.max(np.abs(b)))
+    return float(np.max(np.abs(a - b))) / d if d > 0 else float(np.max(np.abs(a)))
+
+
+def run_ours(a, w):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import __graft_entry__
+    fk = __graft_entry__.load_package()
+    ctx = fk.Context(local)
+    stream = torch.cuda.Stream(local)
+    ctx.set_stream(stream.cuda_stream)
+    p = make_inputs(fk, w, seed=2024 + rank)
+    keys_c = [k for k, v in p.items() if isinstance(v, np.ndarray)]
+    d = dict(p)
+    for k in keys_c:
+        d[k] = torch.from_numpy(np.ascontiguousarray(p[k])).to(f"cuda:{local}")
+    if w["kind"] == "gpp":
+        outs = {k: torch.zeros(n, dtype=torch.complex128, device=f"cuda:{local}")
+                for k, n in (("achtemp", 3), ("asxtemp", 3), ("acht_n1_loc", w["nb"]))}
+        outs["achstemp"] = None
+        call = lambda prec: ctx.gpp(d, prec, 0, out=outs)
+        host_call = lambda prec, hp: ctx.gpp(hp, prec, 0)
+        flags = 0
+    else:
+        flags = fk.FK_FF_SCHDT_GEMM | fk.FK_FF_SPLIT_ACHD
+        outs = {"achsDtemp": torch.zeros(1, dtype=torch.complex128, device=f"cuda:{local}"),
+                "asxDtemp": torch.zeros(w["ne"], dtype=torch.complex128, device=f"cuda:{local}"),
+                "achDtemp": torch.zeros(w["ne"], dtype=torch.complex128, device=f"cuda:{local}"),
+                "achDtemp_cor": torch.zeros(w["ne"], dtype=torch.complex128, device=f"cuda:{local}"),
+                "ach2Dtemp": torch.zeros(w["ne"], dtype=torch.complex128, device=f"cuda:{local}"),
+                "schDt_matrix": torch.zeros((w["nb"], w["nf"]), dtype=torch.complex128, device=f"cuda:{local}")}
+        call = lambda prec: ctx.ff(d, prec, flags, out=outs)
+        host_call = lambda prec, hp: ctx.ff(hp, prec, flags)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # accuracy of the mixed path against FP64 (stated for every output)
+    def fetch(r):
+        torch.cuda.synchronize()
+        return {k: (v.cpu().numpy().copy() if v is not None else None) for k, v in r.items()}
+
+    ref64 = fetch(call("fp64"))
+    resm = fetch(call("mixed"))
+    errs = {k: rel(resm[k], ref64[k]) for k in ref64 if ref64[k] is not None and np.max(np.abs(ref64[k])) > 0}
+
+    prec = a.precision
+    other = "fp64" if prec == "mixed" else "mixed"
+    barrier()
+    with ClockSampler(local) as clk:
+        barrier()
+        per = timed(torch, stream, lambda: call(prec), a.steps, a.warmup, per_step=False)
+        barrier()
+    ms = per[0]
+    if world > 1:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    launches = ctx.last_launches()
+    # per-step latency distribution (events around each call)
+    lat = timed(torch, stream, lambda: call(prec), a.steps, 1, per_step=True)
+    # the other precision, for the mixed-vs-FP64 ratio
+    k_other = max(3, min(a.steps, 10))
+    ms_other = statistics.mean(timed(torch, stream, lambda: call(other), k_other, 1, per_step=True))
+    # dominant-kernel duration from the library's events on its stream
+    ctx.set_profiling(True)
+    ph = []
+    for _ in range(max(3, min(a.steps, 10))):
+        call(prec)
+        ph.append(ctx.last_timings())
+    ctx.set_profiling(False)
+    phase = [statistics.mean(x[i] for x in ph) for i in range(4)]
+    # end to end through the C ABI with pinned host buffers
+    hp = dict(p)
+    h2d = 0
+    for k in keys_c:
+        t = torch.from_numpy(np.ascontiguousarray(p[k])).pin_memory()
+        hp[k] = t
+        h2d += t.numel() * t.element_size()
+    d2h = sum(v.numel() * v.element_size() for v in outs.values() if v is not None)
+    for _ in range(max(1, a.warmup)):
+        host_call(prec, hp)
+    barrier()
+    t0 = time.perf_counter()
+    ke = max(3, min(a.steps, 10))
+    for _ in range(ke):
+        host_call(prec, hp)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / ke
+    if world > 1:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu:
+        cpu = cpu_baseline(fk, w, p)
+    if rank == 0:
+        peaks = {}
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                peaks = json.load(f)
+        except OSError:
+            pass
+        hbm = peaks.get("hbm_gbs", 6800.0)
+        byts, flops = algorithmic(w)
+        kms = phase[2]
+        achieved = byts / (kms * 1e-3) / 1e9 if kms > 0 else None
+        T = terms(w)
+        line = {
+            "metric": METRIC, "value": world * T / (ms * 1e-3), "unit": "terms/s", "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 in / fp32 bulk + fp64 branch/reductions" if prec == "mixed" else "f64",
+            "data": "synthetic (seeded, benchmark value distributions)", "config": workload_config(a, w),
+            "precision": prec,
+            "fp64_value" if prec == "mixed" else "mixed_value": world * T / (ms_other * 1e-3),
+            "mixed_vs_fp64": (ms_other / ms) if prec == "mixed" else (ms / ms_other),
+            "rel_err_mixed_vs_fp64": errs,
+            "latency_ms": {"p50": statistics.median(lat), "p99": float(np.percentile(lat, 99))},
+            "phase_ms": {"staging": phase[0], "prep": phase[1], "contraction": phase[2], "reduction": phase[3]},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                         "kernel": "contraction", "algorithmic_bytes": byts, "algorithmic_flops": flops,
+                         "achieved_tflops": flops / (kms * 1e-3) / 1e12 if kms > 0 else None,
+                         "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
+            "e2e": {"value": world * T / e2e_s, "unit": "terms/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+            "gpu_launches": launches * a.steps,
+            "clocks": clk.summary(),
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(fk, w, p):
+    """Oracle (CPU restatement of the reference loop nest) on the host cores,
+    on a bounded sample of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    cores = os.cpu_count() or 1
+    if w["kind"] == "gpp":
+        t0 = time.perf_counter()
+        oracle.gpp(p, nthreads=cores)
+        dt = time.perf_counter() - t0
+        return {"value": terms(w) / dt, "unit": "terms/s", "cores": cores, "kind": "port",
+                "sample": f"one full call ({terms(w):.3g} terms)"}
+    q = dict(p)
+    nbs = 64
+    for k in ("aqsmtemp", "aqsntemp"):
+        q[k] = p[k][:nbs]
+    q["ekq"] = p["ekq"][:nbs]
+    q["number_bands"] = nbs
+    t0 = time.perf_counter()
+    oracle.ff(q, flags=oracle.ORC_FF_SCHDT_GEMM, nthreads=cores)
+    dt = time.perf_counter() - t0
+    tq = nbs * w["ng"] * w["nc"] * w["nf"]
+    return {"value": tq / dt, "unit": "terms/s", "cores": cores, "kind": "port",
+            "sample": f"first {nbs} of {w['nb']} bands ({tq:.3g} terms)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="gpp", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    a = ap.parse_args()
+    a.warmup = max(a.warmup, 3)
+    w = WORKLOADS[a.workload]
+    if a.impl == "reference":
+        run_reference(a, w)
+    else:
+        run_ours(a, w)
+
+
+if __name__ == "__main__":
+    main()

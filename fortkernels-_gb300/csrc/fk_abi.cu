@@ -127,6 +127,21 @@ fk_status deliver(Ctx& c, void* dst, const double2* out, size_t off, size_t n, b
     return e == cudaSuccess ? FK_OK : cuda_fail(c, e, "output copy");
 }
 
+// After a synchronize: a nonzero error word means a bounded device-side wait
+// of the tensor-core kernels gave up.
+fk_status check_errword(Ctx& c) {
+    int w = 0;
+    cudaError_t e = cudaMemcpy(&w, c.errword, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "reading the device error word");
+    if (w != 0) {
+        cudaMemset(c.errword, 0, sizeof(int));
+        char buf[96];
+        std::snprintf(buf, sizeof buf, "a device-side wait timed out (code 0x%x)", w);
+        return fail(c, FK_ETIMEOUT, buf);
+    }
+    return FK_OK;
+}
+
 }  // namespace
 }  // namespace fk
 
@@ -170,6 +185,12 @@ fk_status fk_create(int device, fk_ctx_t* out) {
         return FK_ECUDA;
     }
     c->stream = c->own_stream;
+    if (cudaMalloc(&c->errword, 256) != cudaSuccess || cudaMemset(c->errword, 0, 256) != cudaSuccess) {
+        cudaGetLastError();
+        cudaStreamDestroy(c->own_stream);
+        delete c;
+        return FK_ECUDA;
+    }
     for (auto& e : c->ev)
         if (cudaEventCreate(&e) != cudaSuccess) {
             cudaGetLastError();
@@ -186,6 +207,7 @@ fk_status fk_destroy(fk_ctx_t c) {
         fk::DeviceGuard g(c->device);
         if (c->stream) cudaStreamSynchronize(c->stream);
         if (c->ws.base) cudaFree(c->ws.base);
+        if (c->errword) cudaFree(c->errword);
         if (c->pinned) cudaFreeHost(c->pinned);
         for (auto& e : c->ev)
             if (e) cudaEventDestroy(e);
@@ -205,7 +227,8 @@ fk_status fk_synchronize(fk_ctx_t c) {
     if (!c) return FK_EINVAL;
     fk::DeviceGuard g(c->device);
     cudaError_t e = cudaStreamSynchronize(c->stream);
-    return e == cudaSuccess ? FK_OK : fk::cuda_fail(*c, e, "synchronize");
+    if (e != cudaSuccess) return fk::cuda_fail(*c, e, "synchronize");
+    return fk::check_errword(*c);
 }
 
 fk_status fk_reserve(fk_ctx_t c, size_t bytes) {
@@ -278,6 +301,7 @@ fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsm
         cudaError_t e = cudaStreamSynchronize(x.stream);
         if (e != cudaSuccess) return fk::cuda_fail(x, e, "gpp: synchronize");
         fk::phase_close(x, 4);
+        if ((s = fk::check_errword(x)) != FK_OK) return s;
     }
     return FK_OK;
 }
@@ -342,6 +366,7 @@ fk_status fk_ff(fk_ctx_t c, int nb, int nv, int nc, int ng, int nf, int ne, cons
         cudaError_t e = cudaStreamSynchronize(x.stream);
         if (e != cudaSuccess) return fk::cuda_fail(x, e, "ff: synchronize");
         fk::phase_close(x, 4);
+        if ((s = fk::check_errword(x)) != FK_OK) return s;
     }
     return FK_OK;
 }

@@ -19,6 +19,7 @@
 
 #include "fk_gemm.cuh"
 #include "fk_internal.h"
+#include "fk_tc_contract.cuh"
 
 namespace fk {
 namespace {
@@ -209,9 +210,27 @@ struct FfPlan {
     std::vector<FactRow> fact;
     std::vector<int> planesR, planesA;
     int MT, NT, KS, kchunk;
+    int BN, kstages;              // tensor-core path (mixed)
     bool mixed;
-    size_t bytes;
+    size_t bytes, bytesImgR, bytesImgA, bytesW;
 };
+
+// k-slices for the persistent tensor-core kernel (see fk_gpp.cu)
+void ff_pick_split_tc(long tiles, int K, int sms, int& KS, int& kchunk) {
+    const int kmax = std::max(1, K / 256);
+    int best = 1;
+    double best_cost = 1e30;
+    for (int ks = 1; ks <= std::min(kmax, 64); ++ks) {
+        const long units = tiles * ks;
+        const long waves = (units + sms - 1) / sms;
+        const double eff = (double)units / (double)(waves * sms);
+        const double cost = (1.0 / eff) * (1.0 + 0.002 * ks);
+        if (cost < best_cost - 1e-9) { best_cost = cost; best = ks; }
+        if (eff > 0.92 && units >= sms) break;
+    }
+    kchunk = ((K + best - 1) / best + tcx::BK - 1) / tcx::BK * tcx::BK;
+    KS = (K + kchunk - 1) / kchunk;
+}
 
 FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double* grid_h) {
     FfPlan p;
@@ -238,19 +257,33 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
         if (all || needR[f]) p.planesR.push_back(f);
         if (needA[f]) p.planesA.push_back(f);
     }
-    const int BM = p.mixed ? f32::BM : d64::BM, BN = p.mixed ? f32::BN : d64::BN;
-    p.MT = ceil_div(r.nb, BM);
-    p.NT = ceil_div(r.ng, BN);
-    const int per_sm = p.mixed ? 4 : 2;
-    const int tiles = p.MT * p.NT * std::max<int>(1, (int)p.planesR.size());
-    p.KS = std::max(1, std::min((c.sms * per_sm + tiles - 1) / tiles, std::max(1, r.nc / 256)));
-    p.kchunk = ((r.nc + p.KS - 1) / p.KS + 15) / 16 * 16;
-    p.KS = (r.nc + p.kchunk - 1) / p.kchunk;
+    const int nplanes = std::max<int>(1, (int)p.planesR.size());
+    p.bytesImgR = p.bytesImgA = p.bytesW = 0;
+    if (p.mixed) {
+        p.BN = 64;
+        p.kstages = ceil_div(r.nc, tcx::BK);
+        p.MT = ceil_div(r.nb, tcx::BM);
+        p.NT = ceil_div(r.ng, p.BN);
+        ff_pick_split_tc((long)p.MT * p.NT * nplanes, r.nc, c.sms, p.KS, p.kchunk);
+        const size_t bb = tcx::Cfg<64>::B_BYTES;
+        p.bytesImgR = p.planesR.size() * (size_t)p.NT * p.kstages * bb;
+        p.bytesImgA = p.planesA.size() * (size_t)p.NT * p.kstages * bb;
+        p.bytesW = 2 * (size_t)r.nb * r.ng * sizeof(float2);
+    } else {
+        p.BN = d64::BN;
+        p.kstages = 0;
+        p.MT = ceil_div(r.nb, d64::BM);
+        p.NT = ceil_div(r.ng, d64::BN);
+        const int tiles = p.MT * p.NT * nplanes;
+        p.KS = std::max(1, std::min((c.sms * 2 + tiles - 1) / tiles, std::max(1, r.nc / 256)));
+        p.kchunk = ((r.nc + p.KS - 1) / p.KS + 15) / 16 * 16;
+        p.KS = (r.nc + p.kchunk - 1) / p.kchunk;
+    }
     const size_t slots = (size_t)p.KS * p.NT;
     p.bytes = (slots * (p.planesR.size() + p.planesA.size()) * r.nb * 2 + 3 * (size_t)r.nb * r.nf +
                (size_t)r.ne * r.nb) * sizeof(double2) +
               r.nb * sizeof(FactRow) + (p.planesR.size() + p.planesA.size()) * sizeof(int) + r.ng * sizeof(int) +
-              16 * 256;
+              p.bytesImgR + p.bytesImgA + p.bytesW + 20 * 256;
     return p;
 }
 
@@ -281,7 +314,11 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
     double2* PA = nA ? (double2*)c.ws.take(slots * nA * r.nb * 2 * sizeof(double2)) : nullptr;
     double2* tabs = (double2*)c.ws.take(3 * (size_t)r.nb * r.nf * sizeof(double2));
     double2* SD = (double2*)c.ws.take((size_t)r.ne * r.nb * sizeof(double2));
-    if (!igp || !planes || !fact || !PR || (nA && !PA) || !tabs || !SD)
+    uint8_t* imgR = p.bytesImgR ? (uint8_t*)c.ws.take(p.bytesImgR) : nullptr;
+    uint8_t* imgA = p.bytesImgA ? (uint8_t*)c.ws.take(p.bytesImgA) : nullptr;
+    float2* W = p.bytesW ? (float2*)c.ws.take(p.bytesW) : nullptr;
+    if (!igp || !planes || !fact || !PR || (nA && !PA) || !tabs || !SD || (p.bytesImgR && !imgR) ||
+        (p.bytesImgA && !imgA) || (p.bytesW && !W))
         return fail(c, FK_ENOMEM, "workspace too small for FF request");
     double2 *RW = tabs, *RS = tabs + (size_t)r.nb * r.nf, *AW = tabs + 2 * (size_t)r.nb * r.nf;
     // host tables -> device (pageable source; the copy completes before return of the call's sync)
@@ -297,26 +334,46 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
     ff_igp_kernel<<<ceil_div(r.ng, 128), 128, 0, st>>>(r.ng, r.nc, r.inv, r.indinv, igp);
     ++c.launches;
     phase_mark(c, 2);
-    auto contract = [&](const double2* eps, const int* pls, int nb_, double2* P) {
+    if (p.mixed) {
+        tcx::weight_table_kernel<<<dim3(ceil_div(r.ng, 128), r.nb), 128, 0, st>>>(r.nb, 0, r.ng, r.aqsm, r.nc, r.vcoul,
+                                                                                igp, 1.0, W, W + (size_t)r.nb * r.ng);
+        ++c.launches;
+        cudaMemsetAsync(c.errword, 0, sizeof(int), st);
+    }
+    auto contract = [&](const double2* eps, const int* pls, int nb_, double2* P, uint8_t* img, size_t img_bytes) {
         ContractArgs a{};
         a.A = r.aqsn; a.lda = r.nc; a.m0 = 0; a.M = r.nb;
         a.B = eps; a.ldb = r.nc; a.bstride = (long)r.ng * r.nc; a.N = r.ng; a.K = r.nc;
         a.KS = p.KS; a.kchunk = p.kchunk; a.batches = nb_; a.batch_plane = pls;
         a.aqsm = r.aqsm; a.ldm = r.nc; a.vcoul = r.vcoul; a.igp = igp; a.wscale = 1.0; a.G = 2; a.P = P;
-        dim3 grid(p.MT, p.NT * p.KS * nb_);
         if (p.mixed) {
-            auto k = f32::contract_kernel<EPI_FF, double2>;
-            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f32::SMEM);
-            k<<<grid, f32::THREADS, f32::SMEM, st>>>(a);
+            // pre-split B planes (bf16 x 3), then the tensor-core contraction
+            cudaMemsetAsync(img, 0, img_bytes, st);
+            dim3 gconv(ceil_div(r.nc, 256), r.ng, nb_);
+            tcx::bimg_convert_kernel<64><<<gconv, 256, 0, st>>>(eps, a.bstride, r.ng, r.nc, pls, p.kstages, img);
+            tcx::TcArgs t{};
+            t.c = a;
+            t.c.batch_plane = nullptr;  // the image is indexed by batch position
+            t.Bimg = img;
+            t.W1 = W; t.W2 = W + (size_t)r.nb * r.ng; t.ldw = r.ng;
+            t.kstages_total = p.kstages;
+            t.MT = p.MT; t.NT = p.NT; t.units = p.MT * p.NT * p.KS * nb_;
+            t.err = c.errword;
+            const int grid1 = std::min(t.units, c.sms);
+            auto k = tcx::tc_contract_kernel<EPI_FF, 64>;
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcx::Cfg<64>::SMEM);
+            k<<<grid1, tcx::THREADS, tcx::Cfg<64>::SMEM, st>>>(t);
+            c.launches += 2;
         } else {
+            dim3 grid(p.MT, p.NT * p.KS * nb_);
             auto k = d64::contract_kernel<EPI_FF>;
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d64::SMEM);
             k<<<grid, d64::THREADS, d64::SMEM, st>>>(a);
+            ++c.launches;
         }
-        ++c.launches;
     };
-    if (nR) contract(r.epsR, planes, nR, PR);
-    if (nA) contract(r.epsA, planes + nR, nA, PA);
+    if (nR) contract(r.epsR, planes, nR, PR, imgR, p.bytesImgR);
+    if (nA) contract(r.epsA, planes + nR, nA, PA, imgA, p.bytesImgA);
     phase_mark(c, 3);
     if (nR) {
         ff_rows_kernel<<<dim3(ceil_div(r.nb, 128), nR), 128, 0, st>>>(r.nb, r.nf, nR, (int)slots, planes, PR, RW, RS);

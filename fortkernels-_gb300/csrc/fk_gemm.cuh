@@ -105,8 +105,9 @@ constexpr size_t SMEM = (size_t)STAGES * (BM + BN) * LDS * sizeof(double2);
 static_assert(SMEM >= (size_t)BM * 8 * GMAX * sizeof(double2), "reduction partials must fit in the pipeline buffers");
 
 FK_DEV void dmma(double& c0, double& c1, double a, double b) {
-    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
-                 : "+d"(c0), "+d"(c1) : "d"(a), "d"(b));
+    // not volatile: the scheduler may interleave independent accumulators
+    asm("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+        : "+d"(c0), "+d"(c1) : "d"(a), "d"(b));
 }
 FK_DEV void cp_async16(void* smem, const void* gmem, bool pred) {
     unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -177,15 +178,25 @@ __global__ void __launch_bounds__(THREADS) contract_kernel(ContractArgs a) {
             for (int i = 0; i < 4; ++i) af[i] = as[(wm * 32 + i * 8 + (lane >> 2)) * LDS + kk + (lane & 3)];
 #pragma unroll
             for (int j = 0; j < 2; ++j) bf[j] = bs[(wn * 16 + j * 8 + (lane >> 2)) * LDS + kk + (lane & 3)];
+            double nbi[2] = {-bf[0].y, -bf[1].y};
+            // four passes over the 8 accumulator tiles: consecutive updates of
+            // one accumulator are 8 independent DMMAs apart
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
-                for (int j = 0; j < 2; ++j) {
-                    dmma(cr[i][j][0], cr[i][j][1], af[i].x, bf[j].x);
-                    dmma(cr[i][j][0], cr[i][j][1], af[i].y, -bf[j].y);
-                    dmma(ci[i][j][0], ci[i][j][1], af[i].x, bf[j].y);
-                    dmma(ci[i][j][0], ci[i][j][1], af[i].y, bf[j].x);
-                }
+                for (int j = 0; j < 2; ++j) dmma(cr[i][j][0], cr[i][j][1], af[i].x, bf[j].x);
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) dmma(ci[i][j][0], ci[i][j][1], af[i].x, bf[j].y);
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) dmma(cr[i][j][0], cr[i][j][1], af[i].y, nbi[j]);
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) dmma(ci[i][j][0], ci[i][j][1], af[i].y, bf[j].x);
         }
     }
     cp_wait<0>();
@@ -215,10 +226,10 @@ __global__ void __launch_bounds__(THREADS) contract_kernel(ContractArgs a) {
 // ================================================== FP32 SIMT (mixed, v1)
 // CTA tile 64 x 64 complex, 256 threads, 4 x 4 complex per thread, k-step
 // 16.  FP64 inputs are rounded to FP32 with the integer conversion; products
-// accumulate in FP32 for FLUSH k-values, then into a float-float (hi, lo)
-// accumulator (TwoSum), so the FP32 rounding error grows with FLUSH, not K.
+// accumulate in FP32 for one 16-value k-step, then into a float-float (hi, lo)
+// accumulator (TwoSum), so the FP32 rounding error does not grow with K.
 namespace f32 {
-constexpr int BM = 64, BN = 64, BK = 16, THREADS = 256, FLUSH_TILES = 4;
+constexpr int BM = 64, BN = 64, BK = 16, THREADS = 256, FLUSH_TILES = 1;
 constexpr int LDA = BM + 1, LDB = BN + 1;
 constexpr size_t SMEM_PIPE = (size_t)2 * BK * (LDA + LDB) * sizeof(float2);
 constexpr size_t SMEM_RED = (size_t)BM * 16 * GMAX * sizeof(double2);

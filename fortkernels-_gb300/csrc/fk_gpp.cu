@@ -27,13 +27,16 @@
 
 #include "fk_gemm.cuh"
 #include "fk_internal.h"
+#include "fk_tc_contract.cuh"
 
 namespace fk {
 namespace {
 
 constexpr int PREP_THREADS = 256;
-constexpr int PREP_EPT = 2;
+constexpr int PREP_EPT = 2;  // elements per thread, FP64 prep
 constexpr int PREP_TILE = PREP_THREADS * PREP_EPT;
+constexpr int PREPM_EPT = 8;  // elements per thread, mixed prep
+constexpr int PREPM_TILE = PREP_THREADS * PREPM_EPT;
 constexpr int NVC = 2;  // flag bands contracted per prep pass
 constexpr double TO1 = 1e-6;
 constexpr float GUARD = 1e-5f;  // relative guard band of the FP32 branch tests
@@ -48,7 +51,8 @@ struct PrepArgs {
     const double2 *aqsn, *eps, *wt;
     const double* wx;
     const int* igp;
-    void* D;     // [3*ng][nc]: double2 (FP64) or float2 (mixed); nullptr = not needed
+    void* D;     // FP64: [3*ng][nc] double2; mixed: pre-split B image (fk_tc_contract.cuh); nullptr = not needed
+    int kstages; // mixed: k-stages per n-tile in the image
     double2* F;  // [nch][nv][ng][3][2]  (sch, ssx) flag-band sums over the chunk
     int nch;
     int n1base;  // first flag band handled by this pass
@@ -114,6 +118,44 @@ FK_DEV void block_sum(double2 (&v)[NV], double2* sm /* [8][NV] */) {
     }
 }
 
+// Fixed-order block sum of FP32 values carried as float-float pairs (TwoSum
+// at every level), finished in FP64 across warps: FP32 instructions only in
+// the shuffle tree (the FP64 pipe of GB300 is narrow).
+template <int NV>
+FK_DEV void block_sum_ff(float2 (&v)[NV], double2* sm /* [8][NV] */, double2 (&out)[NV]) {
+    float2 lo[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) lo[i] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            const float hx = __shfl_down_sync(0xffffffffu, v[i].x, off), hy = __shfl_down_sync(0xffffffffu, v[i].y, off);
+            const float lx = __shfl_down_sync(0xffffffffu, lo[i].x, off), ly = __shfl_down_sync(0xffffffffu, lo[i].y, off);
+            ff32 a{v[i].x, lo[i].x + lx}, b{v[i].y, lo[i].y + ly};
+            ff_add(a, hx);
+            ff_add(b, hy);
+            v[i] = make_float2(a.hi, b.hi);
+            lo[i] = make_float2(a.lo, b.lo);
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < NV; ++i)
+            sm[warp * NV + i] = make_double2((double)v[i].x + (double)lo[i].x, (double)v[i].y + (double)lo[i].y);
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) out[i] = make_double2(0.0, 0.0);
+    if (threadIdx.x < NV) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s = cadd(s, sm[w * NV + threadIdx.x]);
+#pragma unroll
+        for (int i = 0; i < NV; ++i)
+            if (i == (int)threadIdx.x) out[i] = s;
+    }
+}
+
 template <int Q>  // Q = 1: root gppKer.cpp semantics
 __global__ void __launch_bounds__(PREP_THREADS) prep64_kernel(PrepArgs p) {
     __shared__ double2 sm[8 * NVC * 6];
@@ -166,7 +208,9 @@ __global__ void __launch_bounds__(PREP_THREADS) prep64_kernel(PrepArgs p) {
 }
 
 // ------------------------------------------------------------ mixed (guarded)
-template <int Q>
+// Writes D straight into the pre-split BF16 image consumed by the tensor-core
+// contraction (column j = my_igp*3 + iw lives in n-tile j / BN).
+template <int Q, int BN>
 __global__ void __launch_bounds__(PREP_THREADS) prep_mixed_kernel(PrepArgs p) {
     __shared__ double2 sm[8 * NVC * 6];
     const int my_igp = blockIdx.y, ch = blockIdx.x, tid = threadIdx.x;
@@ -178,15 +222,15 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_mixed_kernel(PrepArgs p) {
     const float limitone = 250000.0f, limittwo = 0.25f, to1 = 1e-6f;
     const double2* wrow = p.wt + (long)my_igp * p.nc;
     const double2* erow = p.eps + (long)my_igp * p.nc;
-    float2* D = reinterpret_cast<float2*>(p.D);
+    uint8_t* D = reinterpret_cast<uint8_t*>(p.D);
     float wxf[3], iw2[3];
 #pragma unroll
     for (int iw = 0; iw < 3; ++iw) {
         wxf[iw] = f64_to_f32_bits(p.wx[iw]);
         iw2[iw] = 1.0f / (wxf[iw] * wxf[iw]);
     }
-    for (int e = 0; e < PREP_EPT; ++e) {
-        const int ig = ch * PREP_TILE + e * PREP_THREADS + tid;
+    for (int e = 0; e < PREPM_EPT; ++e) {
+        const int ig = ch * PREPM_TILE + e * PREP_THREADS + tid;
         if (ig >= p.nc) continue;
         const double2 wt64 = wrow[ig], ep64 = erow[ig];
         const float2 wt = c64_to_f32(wt64), ep = c64_to_f32(ep64);
@@ -241,7 +285,11 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_mixed_kernel(PrepArgs p) {
                     ssx = make_float2(0.f, 0.f);
                 }
             }
-            if (D) D[((long)my_igp * 3 + iw) * p.nc + ig] = (igp >= 0 && (Q || A)) ? dv : make_float2(0.f, 0.f);
+            if (D && igp >= 0 && (Q || A)) {
+                const int j = my_igp * 3 + iw;
+                tcx::bimg_store<BN>(D + (long)(j / BN) * p.kstages * tcx::Cfg<BN>::B_BYTES, p.kstages, j % BN, ig,
+                                    dv.x, dv.y);
+            }
             if (nflag > 0 && igp >= 0) {
 #pragma unroll
                 for (int j = 0; j < NVC; ++j)
@@ -255,28 +303,45 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_mixed_kernel(PrepArgs p) {
     }
     if (nflag <= 0) return;
     double2 accd[NVC * 6];
-#pragma unroll
-    for (int i = 0; i < NVC * 6; ++i) accd[i] = make_double2((double)acc[i].x, (double)acc[i].y);
-    block_sum<NVC * 6>(accd, sm);
+    block_sum_ff<NVC * 6>(acc, sm, accd);
     if (tid < nflag * 6) {
         int j = tid / 6, r = tid % 6;
-        p.F[(((long)ch * p.nv + p.n1base + j) * p.ng + my_igp) * 6 + r] = accd[tid];
+#pragma unroll
+        for (int i = 0; i < NVC * 6; ++i)
+            if (i == tid) p.F[(((long)ch * p.nv + p.n1base + j) * p.ng + my_igp) * 6 + r] = accd[i];
     }
 }
 
 // ------------------------------------------------------------------ finalize
-// Flag bands: sum the chunk partials, apply the reference's weights
-// (sch: 0.5*vcoul*conj(aqsm), BGW-Kernels/gppKer.cpp:346,421; ssx:
-// occ*vcoul*conj(aqsm), :419).  FW[n1][my_igp][6].
+// Warp-level fixed-order sum of NV double2 values (shuffle tree).
+template <int NV>
+FK_DEV void warp_sum(double2 (&v)[NV]) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            v[i].x += __shfl_down_sync(0xffffffffu, v[i].x, off);
+            v[i].y += __shfl_down_sync(0xffffffffu, v[i].y, off);
+        }
+}
+
+// Flag bands: one warp per (n1, my_igp) sums the chunk partials and applies
+// the reference's weights (sch: 0.5*vcoul*conj(aqsm), BGW-Kernels/gppKer.cpp:
+// 346,421; ssx: occ*vcoul*conj(aqsm), :419).  FW[n1][my_igp][6].
 __global__ void flag_weights_kernel(int nv, int ng, int nc, int nch, const double2* F, const double2* aqsm,
                                     const double* vcoul, const int* igp, double2* FW) {
-    const int my_igp = blockIdx.x * blockDim.x + threadIdx.x, n1 = blockIdx.y;
-    if (my_igp >= ng) return;
-    const int g = igp[my_igp];
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (wid >= nv * ng) return;
+    const int n1 = wid / ng, my_igp = wid % ng;
     double2 s[6];
+#pragma unroll
     for (int r = 0; r < 6; ++r) s[r] = make_double2(0.0, 0.0);
-    for (int ch = 0; ch < nch; ++ch)
+    for (int ch = lane; ch < nch; ch += 32)
+#pragma unroll
         for (int r = 0; r < 6; ++r) s[r] = cadd(s[r], F[(((long)ch * nv + n1) * ng + my_igp) * 6 + r]);
+    warp_sum<6>(s);
+    if (lane != 0) return;
+    const int g = igp[my_igp];
     double2* o = FW + ((long)n1 * ng + my_igp) * 6;
     if (g < 0) {
         for (int r = 0; r < 6; ++r) o[r] = make_double2(0.0, 0.0);
@@ -290,53 +355,93 @@ __global__ void flag_weights_kernel(int nv, int ng, int nc, int nch, const doubl
     }
 }
 
-// Per-band sums.  rows[n1][8] = {sch iw0..2, ssx iw0..2, stat, 0}.
-__global__ void row_sums_kernel(int nb, int nv, int ng, int nslots, const double2* P, int nslots_s,
-                                const double2* S, const double2* FW, double2* rows) {
-    __shared__ double2 sm[8 * 7];
-    const int n1 = blockIdx.x, tid = threadIdx.x;
-    double2 v[7];
-    for (int i = 0; i < 7; ++i) v[i] = make_double2(0.0, 0.0);
-    if (n1 >= nv) {
-        const int M = nb - nv, m = n1 - nv;
-        for (int s = tid; s < nslots; s += blockDim.x)
-            for (int iw = 0; iw < 3; ++iw) v[iw] = cadd(v[iw], P[((long)s * M + m) * 3 + iw]);
-    } else {
-        for (int h = tid; h < ng; h += blockDim.x) {
-            const double2* o = FW + ((long)n1 * ng + h) * 6;
-            for (int iw = 0; iw < 3; ++iw) {
-                v[iw] = cadd(v[iw], o[iw * 2]);
-                v[3 + iw] = cadd(v[3 + iw], o[iw * 2 + 1]);
+// Per-band sums, one warp per band: rows[n1][8] = {sch iw0..2, ssx iw0..2,
+// stat, 0}.  The last block to finish adds the bands in order and writes
+// out = [achtemp 3 | asxtemp 3 | achstemp | acht_n1_loc nb].
+__global__ void rows_totals_kernel(int nb, int nv, int ng, int nslots, const double2* P, int nslots_s,
+                                   const double2* S, const double2* FW, double2* rows, unsigned* counter,
+                                   double2* out) {
+    const int lane = threadIdx.x & 31;
+    const int n1 = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (n1 < nb) {
+        double2 v[7];
+#pragma unroll
+        for (int i = 0; i < 7; ++i) v[i] = make_double2(0.0, 0.0);
+        if (n1 >= nv) {
+            const int M = nb - nv, m = n1 - nv;
+            for (int s = lane; s < nslots; s += 32)
+#pragma unroll
+                for (int iw = 0; iw < 3; ++iw) v[iw] = cadd(v[iw], P[((long)s * M + m) * 3 + iw]);
+        } else {
+            for (int h = lane; h < ng; h += 32) {
+                const double2* o = FW + ((long)n1 * ng + h) * 6;
+#pragma unroll
+                for (int iw = 0; iw < 3; ++iw) {
+                    v[iw] = cadd(v[iw], o[iw * 2]);
+                    v[3 + iw] = cadd(v[3 + iw], o[iw * 2 + 1]);
+                }
             }
         }
+        if (S)
+            for (int s = lane; s < nslots_s; s += 32) v[6] = cadd(v[6], S[(long)s * nb + n1]);
+        warp_sum<7>(v);
+        if (lane == 0)
+#pragma unroll
+            for (int i = 0; i < 7; ++i) rows[(long)n1 * 8 + i] = v[i];
     }
-    if (S)
-        for (int s = tid; s < nslots_s; s += blockDim.x) v[6] = cadd(v[6], S[(long)s * nb + n1]);
-    block_sum<7>(v, sm);
-    if (tid < 7) rows[(long)n1 * 8 + tid] = v[tid];
-}
-
-// Totals over bands; out = [achtemp 3 | asxtemp 3 | achstemp | acht_n1_loc nb].
-__global__ void totals_kernel(int nb, const double2* rows, double2* out) {
-    __shared__ double2 sm[8 * 7];
-    const int tid = threadIdx.x;
-    double2 v[7];
-    for (int i = 0; i < 7; ++i) v[i] = make_double2(0.0, 0.0);
-    for (int n1 = tid; n1 < nb; n1 += blockDim.x) {
-        for (int i = 0; i < 7; ++i) v[i] = cadd(v[i], rows[(long)n1 * 8 + i]);
-        out[7 + n1] = rows[(long)n1 * 8 + 2];  // acht_n1_loc, BGW-Kernels/gppKer.cpp:424
+    // last block: totals in band order
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x < 32) {
+        double2 t[7];
+#pragma unroll
+        for (int i = 0; i < 7; ++i) t[i] = make_double2(0.0, 0.0);
+        for (int r = lane; r < nb; r += 32) {
+#pragma unroll
+            for (int i = 0; i < 7; ++i) t[i] = cadd(t[i], rows[(long)r * 8 + i]);
+        }
+        warp_sum<7>(t);
+        if (lane == 0) {
+#pragma unroll
+            for (int i = 0; i < 7; ++i) out[i] = t[i];
+            *counter = 0u;
+        }
     }
-    block_sum<7>(v, sm);
-    if (tid < 7) out[tid] = v[tid];
+    for (int r = threadIdx.x; r < nb; r += blockDim.x) out[7 + r] = rows[(long)r * 8 + 2];  // acht_n1_loc
 }
 
 struct Plan {
     int nch, passes;
+    int BN, kstages, units;      // tensor-core contraction (mixed)
     int MT, NT, KS, kchunk;      // main contraction
     int MTs, NTs, KSs, kchunks;  // static remainder contraction
     bool mixed;
-    size_t bytesD, bytesF, bytesP, bytesS, bytesFW, bytesRows, bytesIgp;
+    size_t bytesD, bytesF, bytesP, bytesS, bytesFW, bytesRows, bytesIgp, bytesW;
 };
+
+// k-slice count for the persistent tensor-core kernel: the fewest slices
+// whose unit count fills the SMs evenly (tail waste <= 8%), with slices of at
+// least 256 k-values.
+void pick_split_tc(int tiles, int K, int sms, int& KS, int& kchunk) {
+    const int kmax = std::max(1, K / 256);
+    int best = 1;
+    double best_cost = 1e30;
+    for (int ks = 1; ks <= std::min(kmax, 256); ++ks) {
+        const long units = (long)tiles * ks;
+        const long waves = (units + sms - 1) / sms;
+        const double eff = (double)units / (double)(waves * sms);
+        const double cost = (1.0 / eff) * (1.0 + 0.002 * ks);  // mild preference for fewer slices
+        if (cost < best_cost - 1e-9) { best_cost = cost; best = ks; }
+        if (eff > 0.92 && units >= sms) break;
+    }
+    kchunk = ((K + best - 1) / best + tcx::BK - 1) / tcx::BK * tcx::BK;
+    KS = (K + kchunk - 1) / kchunk;
+}
 
 void pick_split(int tiles, int K, int target, int& KS, int& kchunk) {
     KS = std::max(1, std::min((target + tiles - 1) / tiles, std::max(1, K / 256)));
@@ -347,24 +452,36 @@ void pick_split(int tiles, int K, int target, int& KS, int& kchunk) {
 Plan make_plan(const Ctx& c, const GppDev& r) {
     Plan p{};
     p.mixed = r.prec == FK_MIXED;
-    p.nch = ceil_div(r.nc, PREP_TILE);
+    p.nch = ceil_div(r.nc, r.prec == FK_MIXED ? PREPM_TILE : PREP_TILE);
     p.passes = std::max(1, ceil_div(r.nv, NVC));
     const int M = r.nb - r.nv, N = 3 * r.ng;
-    const int BM = p.mixed ? f32::BM : d64::BM, BN = p.mixed ? f32::BN : d64::BN;
+    if (p.mixed) {
+        p.BN = 64;
+        p.kstages = ceil_div(r.nc, tcx::BK);
+        p.MT = ceil_div(std::max(M, 1), tcx::BM);
+        p.NT = ceil_div(N, p.BN);
+        pick_split_tc(p.MT * p.NT, r.nc, c.sms, p.KS, p.kchunk);
+        p.units = p.MT * p.NT * p.KS;
+    } else {
+        p.MT = ceil_div(std::max(M, 1), d64::BM);
+        p.NT = ceil_div(N, d64::BN);
+        pick_split(p.MT * p.NT, r.nc, c.sms * 2, p.KS, p.kchunk);
+    }
     const int per_sm = p.mixed ? 4 : 2;
-    p.MT = ceil_div(std::max(M, 1), BM);
-    p.NT = ceil_div(N, BN);
-    pick_split(p.MT * p.NT, r.nc, c.sms * per_sm, p.KS, p.kchunk);
+    const int BM = p.mixed ? f32::BM : d64::BM, BN = p.mixed ? f32::BN : d64::BN;
     p.MTs = ceil_div(r.nb, BM);
     p.NTs = ceil_div(r.ng, BN);
     pick_split(p.MTs * p.NTs, r.nc, c.sms * per_sm, p.KSs, p.kchunks);
-    p.bytesD = M > 0 ? (size_t)N * r.nc * (p.mixed ? sizeof(float2) : sizeof(double2)) : 0;
+    p.bytesD = M <= 0 ? 0
+               : p.mixed ? (size_t)p.NT * p.kstages * tcx::Cfg<64>::B_BYTES
+                         : (size_t)N * r.nc * sizeof(double2);
+    p.bytesW = (p.mixed && M > 0) ? (size_t)M * r.ng * sizeof(float2) : 0;
     p.bytesF = (size_t)p.nch * std::max(r.nv, 1) * r.ng * 6 * sizeof(double2);
     p.bytesP = M > 0 ? (size_t)p.KS * p.NT * M * 3 * sizeof(double2) : 0;
     p.bytesS = (r.flags & FK_GPP_ACHSTEMP) ? (size_t)p.KSs * p.NTs * r.nb * sizeof(double2) : 0;
     p.bytesFW = (size_t)std::max(r.nv, 1) * r.ng * 6 * sizeof(double2);
     p.bytesRows = (size_t)r.nb * 8 * sizeof(double2);
-    p.bytesIgp = (size_t)r.ng * sizeof(int);
+    p.bytesIgp = (size_t)r.ng * sizeof(int) + 256;  // + the totals counter
     return p;
 }
 
@@ -377,21 +494,27 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 
 size_t gpp_workspace(const Ctx& c, const GppDev& r) {
     Plan p = make_plan(c, r);
-    return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesFW + p.bytesRows + p.bytesIgp + 8 * 256;
+    return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesFW + p.bytesRows + p.bytesIgp + p.bytesW + 10 * 256;
 }
 
 fk_status gpp_run(Ctx& c, const GppDev& r) {
     const Plan p = make_plan(c, r);
     cudaStream_t st = c.stream;
     int* igp = (int*)c.ws.take(p.bytesIgp);
+    unsigned* counter = (unsigned*)((char*)igp + (p.bytesIgp - 256));
     void* D = p.bytesD ? c.ws.take(p.bytesD) : nullptr;
     double2* F = (double2*)c.ws.take(p.bytesF);
     double2* P = p.bytesP ? (double2*)c.ws.take(p.bytesP) : nullptr;
     double2* S = p.bytesS ? (double2*)c.ws.take(p.bytesS) : nullptr;
     double2* FW = (double2*)c.ws.take(p.bytesFW);
     double2* rows = (double2*)c.ws.take(p.bytesRows);
-    if (!igp || !F || !FW || !rows || (p.bytesD && !D) || (p.bytesP && !P) || (p.bytesS && !S))
+    float2* W = p.bytesW ? (float2*)c.ws.take(p.bytesW) : nullptr;
+    if (!igp || !F || !FW || !rows || (p.bytesD && !D) || (p.bytesP && !P) || (p.bytesS && !S) || (p.bytesW && !W))
         return fail(c, FK_ENOMEM, "workspace too small for GPP request");
+    if (p.mixed && D) {
+        cudaError_t e = cudaMemsetAsync(D, 0, p.bytesD, st);  // padding rows and k >= ncouls stay zero
+        if (e != cudaSuccess) return cuda_fail(c, e, "gpp: image clear");
+    }
     const bool Q = (r.flags & FK_GPP_ROOT_QUIRKS) != 0;
     const int M = r.nb - r.nv;
     c.launches = 0;
@@ -400,12 +523,12 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
     igp_map_kernel<<<ceil_div(r.ng, 128), 128, 0, st>>>(r.ng, r.nc, r.inv, r.indinv, igp);
     ++c.launches;
     for (int pass = 0; pass < p.passes; ++pass) {
-        PrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, pass == 0 ? D : nullptr, F, p.nch,
-                   pass * NVC};
+        PrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, pass == 0 ? D : nullptr, p.kstages,
+                   F, p.nch, pass * NVC};
         dim3 grid(p.nch, r.ng);
         if (p.mixed) {
-            if (Q) prep_mixed_kernel<1><<<grid, PREP_THREADS, 0, st>>>(a);
-            else prep_mixed_kernel<0><<<grid, PREP_THREADS, 0, st>>>(a);
+            if (Q) prep_mixed_kernel<1, 64><<<grid, PREP_THREADS, 0, st>>>(a);
+            else prep_mixed_kernel<0, 64><<<grid, PREP_THREADS, 0, st>>>(a);
         } else {
             if (Q) prep64_kernel<1><<<grid, PREP_THREADS, 0, st>>>(a);
             else prep64_kernel<0><<<grid, PREP_THREADS, 0, st>>>(a);
@@ -421,9 +544,21 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
         a.aqsm = r.aqsm; a.ldm = r.nc; a.vcoul = r.vcoul; a.igp = igp; a.wscale = 0.5; a.G = 3; a.P = P;
         dim3 grid(p.MT, p.NT * p.KS);
         if (p.mixed) {
-            auto k = f32::contract_kernel<EPI_GPP, float2>;
-            set_smem(k, f32::SMEM);
-            k<<<grid, f32::THREADS, f32::SMEM, st>>>(a);
+            tcx::weight_table_kernel<<<dim3(ceil_div(r.ng, 128), M), 128, 0, st>>>(M, r.nv, r.ng, r.aqsm, r.nc, r.vcoul,
+                                                                                igp, 0.5, W, nullptr);
+            tcx::TcArgs t{};
+            t.c = a;
+            t.Bimg = (const uint8_t*)D;
+            t.W1 = W; t.W2 = nullptr; t.ldw = r.ng;
+            t.kstages_total = p.kstages;
+            t.MT = p.MT; t.NT = p.NT; t.units = p.units;
+            t.err = c.errword;
+            cudaMemsetAsync(c.errword, 0, sizeof(int), st);
+            const int grid1 = std::min(p.units, c.sms);
+            auto k = tcx::tc_contract_kernel<EPI_GPP, 64>;
+            set_smem(k, tcx::Cfg<64>::SMEM);
+            k<<<grid1, tcx::THREADS, tcx::Cfg<64>::SMEM, st>>>(t);
+            c.launches += 1;
         } else {
             auto k = d64::contract_kernel<EPI_GPP>;
             set_smem(k, d64::SMEM);
@@ -451,13 +586,14 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
     }
     phase_mark(c, 3);
     if (r.nv > 0) {
-        flag_weights_kernel<<<dim3(ceil_div(r.ng, 128), r.nv), 128, 0, st>>>(r.nv, r.ng, r.nc, p.nch, F, r.aqsm,
+        flag_weights_kernel<<<ceil_div(r.nv * r.ng * 32, 256), 256, 0, st>>>(r.nv, r.ng, r.nc, p.nch, F, r.aqsm,
                                                                              r.vcoul, igp, FW);
         ++c.launches;
     }
-    row_sums_kernel<<<r.nb, 256, 0, st>>>(r.nb, r.nv, r.ng, p.KS * p.NT, P, p.KSs * p.NTs, S, FW, rows);
-    totals_kernel<<<1, 256, 0, st>>>(r.nb, rows, r.out);
-    c.launches += 2;
+    cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
+    rows_totals_kernel<<<ceil_div(r.nb, 8), 256, 0, st>>>(r.nb, r.nv, r.ng, p.KS * p.NT, P, p.KSs * p.NTs, S, FW,
+                                                          rows, counter, r.out);
+    c.launches += 1;
     phase_mark(c, 4);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "gpp kernels");

@@ -36,6 +36,7 @@ struct Ctx {
     cudaEvent_t ev[5] = {};
     float timings[4] = {0, 0, 0, 0};
     int launches = 0;
+    int* errword = nullptr;      // device error word of the tensor-core kernels (bounded waits)
 };
 
 // Set the context's last error and return the status.

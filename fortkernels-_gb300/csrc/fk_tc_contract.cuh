@@ -1,0 +1,427 @@
+// fk_tc_contract.cuh -- tensor-core (tcgen05) form of the band x G
+// contraction with the fused weighted row reduction of fk_gemm.cuh.
+//
+//   S[m][n] = sum_k A[m][k] * B[n][k]        (complex; A = aqsntemp, FP64 in HBM)
+//   P[slot][m][g] = sum_n w(m, n) * S[m][n]  (FP64 partials, fixed order)
+//
+// Precision scheme (mixed path): every FP64 operand is rounded to FP32 with
+// integer instructions and split exactly into three BF16 pieces
+// x = x_h + x_m + x_l.  A complex product uses the six piece products whose
+// order is at least 2^-16 (hh, hm, mh, hl, lh, mm).  Tensor-core FP32
+// accumulation truncates, so its error grows with the number of MMA results
+// added into one accumulator: the hh products go to their own (re, im)
+// accumulators, which receive 2 MMA results per 16 k-values, the five
+// smaller piece products to separate correction accumulators (2^-8 smaller,
+// so their truncation is negligible), and all four are drained into the
+// FP64 epilogue every CHUNK_STAGES*32 k-values.
+//
+// CTA organisation (one persistent CTA per SM, 448 threads):
+//   warp 0      TMEM allocation, MMA issue (one lane)
+//   warp 1      bulk copies of the pre-split B tiles (one lane)
+//   warps 4..7  epilogue: TMEM lanes 0..127 = tile rows, weighted sums
+//   warps 2,3,8..13  converters: FP64 A rows -> swizzled BF16 pieces in smem
+// Work units are (m-tile, n-tile, k-slice, batch); CTA i takes units
+// i, i + gridDim.x, ...  Every wait is bounded; on timeout the CTA records
+// an error code and unwinds without further waits of unbounded length.
+#pragma once
+#include <cuda_bf16.h>
+
+#include "fk_gemm.cuh"
+#include "fk_tc.cuh"
+
+namespace fk {
+namespace tcx {
+
+constexpr int BM = 128;
+constexpr int BK = 32;            // complex k-values per stage (64 B of bf16 per row)
+constexpr int NSPLIT = 3;         // bf16 pieces per real value
+constexpr int NSUB = 2 * NSPLIT;  // sub-tiles per operand: re h/m/l, im h/m/l
+constexpr int THREADS = 448;
+constexpr int NCONV = 8;          // converter warps
+constexpr long long WAIT_LIMIT = 4000000000LL;  // ~2 s at 2 GHz
+
+template <int BN>
+struct Cfg {
+    static_assert(BN == 64, "four accumulators x two buffers fill the 512 TMEM columns at BN = 64");
+    static constexpr int STAGES = 3;
+    static constexpr int CHUNK_STAGES = 2;  // k-values per TMEM accumulation = 64
+    static constexpr uint32_t A_BYTES = NSUB * BM * 64;
+    static constexpr uint32_t B_BYTES = NSUB * BN * 64;
+    static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+    static constexpr uint32_t ACC_COLS = 4 * BN;       // main re, main im, corr re, corr im
+    static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;  // double buffered
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+};
+
+struct TcArgs {
+    ContractArgs c;       // shapes, partial buffer (same meaning as fk_gemm.cuh)
+    const uint8_t* Bimg;  // pre-split B tiles: [plane][nt][kstage][NSUB][BN rows][64 B]
+    const float2* W1;     // epilogue weights [M][ldw] (GPP: 0.5 vcoul conj(aqsm); FF: vcoul conj(aqsm))
+    const float2* W2;     // FF only: conj(aqsm) [M][ldw]
+    int ldw;
+    int kstages_total;    // k-stages per (plane, nt) in Bimg = ceil(K/32)
+    int MT, NT, units;
+    int* err;             // device error word (nonzero: a wait timed out)
+};
+
+// Split an FP32 value into three BF16 pieces (exact: 8+8+8 significand bits).
+__device__ __forceinline__ void split3(float f, uint16_t& h, uint16_t& m, uint16_t& l) {
+    const uint32_t fb = __float_as_uint(f);
+    const uint32_t hb = fb & 0xFFFF0000u;
+    const float r1 = f - __uint_as_float(hb);
+    const uint32_t mb = __float_as_uint(r1) & 0xFFFF0000u;
+    const float r2 = r1 - __uint_as_float(mb);
+    h = (uint16_t)(hb >> 16);
+    m = (uint16_t)(mb >> 16);
+    l = (uint16_t)(__float_as_uint(r2) >> 16);  // r2 has at most 8 significant bits: exact
+}
+
+// B image element writer shared by the prep/conversion kernels: value x of
+// row n (within its n-tile) at k-value k of a (plane, nt) image.
+template <int BN>
+__device__ __forceinline__ void bimg_store(uint8_t* img_nt, int kstage_total_unused, int n_in_tile, int k,
+                                           float re, float im) {
+    (void)kstage_total_unused;
+    uint8_t* st = img_nt + (long)(k / BK) * Cfg<BN>::B_BYTES;
+    const uint32_t off = tc::sw64_offset(n_in_tile, k % BK);
+    uint16_t h, m, l;
+    split3(re, h, m, l);
+    *(uint16_t*)(st + 0 * BN * 64 + off) = h;
+    *(uint16_t*)(st + 1 * BN * 64 + off) = m;
+    *(uint16_t*)(st + 2 * BN * 64 + off) = l;
+    split3(im, h, m, l);
+    *(uint16_t*)(st + 3 * BN * 64 + off) = h;
+    *(uint16_t*)(st + 4 * BN * 64 + off) = m;
+    *(uint16_t*)(st + 5 * BN * 64 + off) = l;
+}
+
+template <int EPI, int BN>
+__global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(TcArgs t) {
+    using C = Cfg<BN>;
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    // 1024-aligned operand area
+    uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* bars = (uint64_t*)(base + C::STAGES * C::STAGE_BYTES);
+    uint64_t* fullA = bars;
+    uint64_t* fullB = bars + C::STAGES;
+    uint64_t* empty = bars + 2 * C::STAGES;
+    uint64_t* accFull = bars + 3 * C::STAGES;
+    uint64_t* accEmpty = accFull + 2;
+    uint64_t* done = accEmpty + 2;
+    uint32_t* tslot = (uint32_t*)(done + 1);
+    __shared__ int s_abort_flag;
+    volatile int& s_abort = s_abort_flag;
+
+    const ContractArgs& a = t.c;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int NTu = t.NT;
+
+    if (tid == 0) {
+        for (int s = 0; s < C::STAGES; ++s) {
+            tc::mbar_init(&fullA[s], NCONV);
+            tc::mbar_init(&fullB[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&accFull[b], 1);
+            tc::mbar_init(&accEmpty[b], 4);
+        }
+        tc::mbar_init(done, 1);
+        tc::fence_barrier_init();
+        s_abort = 0;
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tslot, C::TMEM_COLS);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    auto unit_coords = [&](int u, int& mt, int& nt, int& ks, int& batch) {
+        mt = u % t.MT;
+        int r = u / t.MT;
+        nt = r % NTu;
+        r /= NTu;
+        ks = r % a.KS;
+        batch = r / a.KS;
+    };
+    auto krange = [&](int ks, int& k0, int& k1) {
+        k0 = ks * a.kchunk;
+        k1 = min(a.K, k0 + a.kchunk);
+    };
+    auto fail = [&](int code) {
+        atomicOr(t.err, code);
+        s_abort = 1;
+    };
+
+    if (warp == 0) {
+        // ------------------------------------------------------------ MMA
+        if (lane == 0) {
+            int g = 0, chunk = 0;
+            bool ok = true;
+            const uint32_t idp = tc::idesc_bf16(BM, BN, false), idn = tc::idesc_bf16(BM, BN, true);
+            for (int u = blockIdx.x; u < t.units && ok; u += gridDim.x) {
+                int mt, nt, ks, batch, k0, k1;
+                unit_coords(u, mt, nt, ks, batch);
+                krange(ks, k0, k1);
+                const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
+                for (int st0 = 0; st0 < nst && ok; st0 += C::CHUNK_STAGES, ++chunk) {
+                    const int b = chunk & 1;
+                    if (!tc::mbar_wait(&accEmpty[b], ((chunk >> 1) & 1) ^ 1, WAIT_LIMIT)) { fail(1); ok = false; break; }
+                    tc::tc_fence_after();
+                    const uint32_t dR = tmem + (uint32_t)(b * C::ACC_COLS), dI = dR + BN;
+                    const uint32_t cR = dR + 2 * BN, cI = dR + 3 * BN;
+                    const int st1 = min(nst, st0 + C::CHUNK_STAGES);
+                    for (int st = st0; st < st1; ++st, ++g) {
+                        const int s = g % C::STAGES;
+                        const uint32_t par = (g / C::STAGES) & 1;
+                        if (!tc::mbar_wait(&fullA[s], par, WAIT_LIMIT) || !tc::mbar_wait(&fullB[s], par, WAIT_LIMIT)) {
+                            fail(2);
+                            ok = false;
+                            break;
+                        }
+                        tc::tc_fence_after();
+                        const uint32_t sa = tc::smem_u32(base + s * C::STAGE_BYTES);
+                        const uint32_t sb = sa + C::A_BYTES;
+#pragma unroll
+                        for (int kk = 0; kk < 2; ++kk) {
+                            // sub-tile descriptors at k offset kk*16 (32 bytes)
+                            auto ad = [&](int sub) { return tc::sdesc_sw64(sa + sub * BM * 64) + 2 * kk; };
+                            auto bd = [&](int sub) { return tc::sdesc_sw64(sb + sub * BN * 64) + 2 * kk; };
+                            const uint32_t acc0 = (st > st0 || kk > 0) ? 1u : 0u;
+                            // correction pieces (ia, ib): mm, lh, hl, mh, hm
+                            const int PA[5] = {1, 2, 0, 1, 0};
+                            const int PB[5] = {1, 0, 2, 0, 1};
+#pragma unroll
+                            for (int q = 0; q < 5; ++q) {
+                                const uint32_t first = (q == 0) ? acc0 : 1u;
+                                tc::mma_bf16(cR, ad(PA[q]), bd(PB[q]), idp, first);       // Ar*Br
+                                tc::mma_bf16(cR, ad(3 + PA[q]), bd(3 + PB[q]), idn, 1u);  // -Ai*Bi
+                                tc::mma_bf16(cI, ad(PA[q]), bd(3 + PB[q]), idp, first);   // Ar*Bi
+                                tc::mma_bf16(cI, ad(3 + PA[q]), bd(PB[q]), idp, 1u);      // Ai*Br
+                            }
+                            // main hh products
+                            tc::mma_bf16(dR, ad(0), bd(0), idp, acc0);
+                            tc::mma_bf16(dR, ad(3), bd(3), idn, 1u);
+                            tc::mma_bf16(dI, ad(0), bd(3), idp, acc0);
+                            tc::mma_bf16(dI, ad(3), bd(0), idp, 1u);
+                        }
+                        tc::mma_commit(&empty[s]);
+                    }
+                    if (!ok) break;
+                    tc::mma_commit(&accFull[b]);
+                }
+            }
+            // drain: every issued MMA has completed before TMEM is released
+            tc::mma_commit(done);
+            if (!tc::mbar_wait(done, 0, WAIT_LIMIT)) fail(4);
+        }
+    } else if (warp == 1) {
+        // -------------------------------------------------- B bulk copies
+        if (lane == 0) {
+            int g = 0;
+            bool ok = true;
+            for (int u = blockIdx.x; u < t.units && ok; u += gridDim.x) {
+                int mt, nt, ks, batch, k0, k1;
+                unit_coords(u, mt, nt, ks, batch);
+                krange(ks, k0, k1);
+                const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
+                const int plane = a.batch_plane ? a.batch_plane[batch] : batch;
+                for (int st = 0; st < nst; ++st, ++g) {
+                    const int s = g % C::STAGES;
+                    if (!tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, WAIT_LIMIT) || s_abort) {
+                        fail(8);
+                        ok = false;
+                        break;
+                    }
+                    const long kst = (long)(k0 / BK) + st;
+                    const uint8_t* src =
+                        t.Bimg + (((long)plane * NTu + nt) * t.kstages_total + kst) * (long)C::B_BYTES;
+                    tc::mbar_arrive_expect_tx(&fullB[s], C::B_BYTES);
+                    tc::bulk_g2s(base + s * C::STAGE_BYTES + C::A_BYTES, src, C::B_BYTES, &fullB[s]);
+                }
+            }
+        }
+    } else if (warp >= 4 && warp < 8) {
+        // ------------------------------------------------------- epilogue
+        const int q4 = warp - 4;  // TMEM lane quarter
+        const int row = q4 * 32 + lane;
+        int chunk = 0;
+        bool ok = true;
+        for (int u = blockIdx.x; u < t.units && ok; u += gridDim.x) {
+            int mt, nt, ks, batch, k0, k1;
+            unit_coords(u, mt, nt, ks, batch);
+            krange(ks, k0, k1);
+            const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
+            const int m = mt * BM + row;
+            const float2* wrow1 = t.W1 + (long)min(m, a.M - 1) * t.ldw;
+            const float2* wrow2 = EPI == EPI_FF ? t.W2 + (long)min(m, a.M - 1) * t.ldw : nullptr;
+            double2 acc[GMAX] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+            for (int st0 = 0; st0 < nst; st0 += C::CHUNK_STAGES, ++chunk) {
+                const int b = chunk & 1;
+                if (!tc::mbar_wait(&accFull[b], (chunk >> 1) & 1, WAIT_LIMIT) || s_abort) {
+                    fail(16);
+                    ok = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * C::ACC_COLS);
+                float2 gsum[GMAX] = {make_float2(0, 0), make_float2(0, 0), make_float2(0, 0)};
+#pragma unroll 1
+                for (int c0 = 0; c0 < BN; c0 += 16) {
+                    float vr[16], vi[16], wr[16], wi[16];
+                    tc::tmem_ld16(tl + c0, vr);
+                    tc::tmem_ld16(tl + BN + c0, vi);
+                    tc::tmem_ld16(tl + 2 * BN + c0, wr);
+                    tc::tmem_ld16(tl + 3 * BN + c0, wi);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        vr[j] += wr[j];
+                        vi[j] += wi[j];
+                    }
+                    if (m < a.M) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const int n = nt * BN + c0 + j;
+                            if (n >= a.N) continue;
+                            const float2 s = make_float2(vr[j], vi[j]);
+                            if (EPI == EPI_GPP) {
+                                cfmaf(gsum[n % 3], wrow1[n / 3], s);
+                            } else {
+                                const float2 t1 = cmulf(wrow1[n], s), t2 = cmulf(wrow2[n], s);
+                                gsum[0].x += t1.x;
+                                gsum[0].y += t1.y;
+                                gsum[1].x += t2.x;
+                                gsum[1].y += t2.y;
+                            }
+                        }
+                    }
+                    if (EPI == EPI_FF && (c0 & 31) == 16) {
+                        // keep FP32 column sums short: fold every 32 columns into FP64
+                        for (int gg = 0; gg < 2; ++gg) {
+                            acc[gg].x += (double)gsum[gg].x;
+                            acc[gg].y += (double)gsum[gg].y;
+                            gsum[gg] = make_float2(0.f, 0.f);
+                        }
+                    }
+                }
+                tc::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&accEmpty[b]);
+                for (int gg = 0; gg < GMAX; ++gg) {
+                    acc[gg].x += (double)gsum[gg].x;
+                    acc[gg].y += (double)gsum[gg].y;
+                }
+            }
+            if (!ok) break;
+            if (m < a.M) {
+                const int slot = (batch * a.KS + ks) * NTu + nt;
+                for (int gg = 0; gg < a.G; ++gg) a.P[((long)slot * a.M + m) * a.G + gg] = acc[gg];
+            }
+        }
+    } else {
+        // ----------------------------------------------------- converters
+        const int cw = warp < 4 ? warp - 2 : warp - 6;  // 0..7
+        const int ct = cw * 32 + lane;                   // 0..255
+        const int r = ct >> 1, half = ct & 1;
+        int g = 0;
+        bool ok = true;
+        for (int u = blockIdx.x; u < t.units && ok; u += gridDim.x) {
+            int mt, nt, ks, batch, k0, k1;
+            unit_coords(u, mt, nt, ks, batch);
+            krange(ks, k0, k1);
+            const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
+            const int m = mt * BM + r;
+            const double2* arow = a.A + (long)(a.m0 + min(m, a.M - 1)) * a.lda;
+            for (int st = 0; st < nst; ++st, ++g) {
+                const int s = g % C::STAGES;
+                const int kb = k0 + st * BK + half * 16;
+                // issue the loads before waiting for the slot
+                double2 v[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int k = kb + j;
+                    v[j] = (m < a.M && k < k1) ? __ldg(arow + k) : make_double2(0.0, 0.0);
+                }
+                if (!tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, WAIT_LIMIT) || s_abort) {
+                    fail(32);
+                    ok = false;
+                    break;
+                }
+                uint8_t* sa = base + s * C::STAGE_BYTES;
+                uint32_t pk[NSUB][8];
+#pragma unroll
+                for (int j = 0; j < 16; j += 2) {
+                    uint16_t h0, m0, l0, h1, m1, l1, H0, M0, L0, H1, M1, L1;
+                    split3(f64_to_f32_bits(v[j].x), h0, m0, l0);
+                    split3(f64_to_f32_bits(v[j + 1].x), h1, m1, l1);
+                    split3(f64_to_f32_bits(v[j].y), H0, M0, L0);
+                    split3(f64_to_f32_bits(v[j + 1].y), H1, M1, L1);
+                    pk[0][j >> 1] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+                    pk[1][j >> 1] = (uint32_t)m0 | ((uint32_t)m1 << 16);
+                    pk[2][j >> 1] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+                    pk[3][j >> 1] = (uint32_t)H0 | ((uint32_t)H1 << 16);
+                    pk[4][j >> 1] = (uint32_t)M0 | ((uint32_t)M1 << 16);
+                    pk[5][j >> 1] = (uint32_t)L0 | ((uint32_t)L1 << 16);
+                }
+#pragma unroll
+                for (int sub = 0; sub < NSUB; ++sub) {
+                    uint8_t* tile = sa + sub * BM * 64;
+#pragma unroll
+                    for (int c8 = 0; c8 < 2; ++c8) {
+                        const uint32_t off = tc::sw64_offset(r, half * 16 + c8 * 8);
+                        *reinterpret_cast<uint4*>(tile + off) =
+                            make_uint4(pk[sub][c8 * 4 + 0], pk[sub][c8 * 4 + 1], pk[sub][c8 * 4 + 2], pk[sub][c8 * 4 + 3]);
+                    }
+                }
+                tc::fence_proxy_async_smem();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&fullA[s]);
+            }
+        }
+    }
+
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        __syncwarp();
+        tc::tmem_dealloc(tmem, C::TMEM_COLS);
+    }
+}
+
+// Epilogue weight tables in FP32: W1[m][h] = wscale*vcoul[igp]*conj(aqsm[m0+m][igp])
+// (vcoul omitted when with_vcoul == 0), W2[m][h] = conj(aqsm[m0+m][igp]).
+static __global__ void weight_table_kernel(int M, int m0, int ncols, const double2* aqsm, long ldm, const double* vcoul,
+                                    const int* igp, double wscale, float2* W1, float2* W2) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
+    if (h >= ncols || m >= M) return;
+    const int g = igp[h];
+    float2 w1 = make_float2(0.f, 0.f), w2 = w1;
+    if (g >= 0) {
+        const double2 am = aqsm[(long)(m0 + m) * ldm + g];
+        const double s = wscale * vcoul[g];
+        w1 = make_float2(f64_to_f32_bits(am.x * s), f64_to_f32_bits(-am.y * s));
+        w2 = make_float2(f64_to_f32_bits(am.x), f64_to_f32_bits(-am.y));
+    }
+    W1[(long)m * ncols + h] = w1;
+    if (W2) W2[(long)m * ncols + h] = w2;
+}
+
+// FP64 planes [plane][rows][K] -> pre-split B images [plane][nt][kstage][NSUB][BN][64 B].
+template <int BN>
+__global__ void bimg_convert_kernel(const double2* src, long plane_stride, int rows, int K, const int* planes,
+                                    int kstages, uint8_t* img) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x, n = blockIdx.y, b = blockIdx.z;
+    if (k >= K) return;
+    const int f = planes ? planes[b] : b;
+    const double2 v = src[(long)f * plane_stride + (long)n * K + k];
+    const int NT = (rows + BN - 1) / BN;
+    uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * (long)Cfg<BN>::B_BYTES;
+    bimg_store<BN>(img_nt, kstages, n % BN, k, f64_to_f32_bits(v.x), f64_to_f32_bits(v.y));
+}
+
+}  // namespace tcx
+}  // namespace fk

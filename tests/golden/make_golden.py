@@ -41,6 +41,28 @@ def cx(z):
     return [z.real, z.imag]
 
 
+def exact_constant_gpp(nb, nv, nc, npg):
+    """Closed form of achtemp for the drivers' constant inputs (every array
+    0.5+0.5i, vcoul = 1, wx = {3,4,5}): all (n1, igp, ig) terms are equal and
+    take the first branch, so achtemp[iw] = nb*ngpown*0.5*nc*t(iw) exactly
+    (rational arithmetic)."""
+    from fractions import Fraction as F
+    h = F(1, 2)
+
+    def mul(a, b):
+        return (a[0] * b[0] - a[1] * b[1], a[0] * b[1] + a[1] * b[0])
+
+    ng = nc // npg
+    out = []
+    for wx in (F(3), F(4), F(5)):
+        wd = (wx - h, -h)
+        r = wd[0] ** 2 + wd[1] ** 2
+        d = mul((h, h), (wd[0], -wd[1]))
+        t = mul(mul(mul((h, -h), (h, h)), (d[0] / r, d[1] / r)), (h, h))
+        out.append([float(t[0] * h * nc * nb * ng), float(t[1] * h * nc * nb * ng)])
+    return out
+
+
 def main(big: bool):
     oracle.build()
     out = {"gppKer_bgw": [], "gppKer_root": [], "gppKer_orig": [], "ffKernel": []}
@@ -48,10 +70,11 @@ def main(big: bool):
     for s in sizes:
         r = oracle.run_ref_driver("gppKer_bgw", s)
         out["gppKer_bgw"].append({"args": list(s), "achtemp": [cx(r[f"achtemp[{i}]"]) for i in range(3)],
-                                  "seconds": r.get("seconds")})
+                                  "achtemp_exact": exact_constant_gpp(*s), "seconds": r.get("seconds")})
         if s[0] <= 128:
             r = oracle.run_ref_driver("gppKer_root", s, threads=1)
             out["gppKer_root"].append({"args": list(s), "achtemp": [cx(r[f"achtemp[{i}]"]) for i in range(3)],
+                                       "achtemp_exact": exact_constant_gpp(*s),
                                        "achstemp_printed": cx(r["achstemp"])})
     r = oracle.run_ref_driver("gppKer_orig", (512, 2, 2048, 32))
     out["gppKer_orig"].append({"args": [512, 2, 2048, 32], "achtemp": [cx(r[f"achtemp[{i}]"]) for i in range(3)]})

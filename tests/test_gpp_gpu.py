@@ -10,7 +10,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import rel
+from conftest import gpp_scales, rel, scaled_err
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
@@ -43,19 +43,29 @@ def test_gpp_fp64_matches_oracle(ctx, fk, orc, case):
     check(ctx.gpp(p, "fp64"), ref, TOL64)
 
 
+def check_mixed(res, ref, scales, tol=TOLMX):
+    errs = {k: scaled_err(res[k], ref[k], scales[k]) for k in scales}
+    assert all(e <= tol for e in errs.values()), errs
+    return errs
+
+
 @pytest.mark.parametrize("case", CASES, ids=lambda c: "x".join(map(str, c[:4])) + "-" + c[4])
 def test_gpp_mixed_within_1e6(ctx, fk, orc, case):
     nb, nv, nc, ng, dist, index, wx = case
     p = fk.inputs.gpp_synthetic(nb, nv, nc, ng, seed=nb + nc, dist=dist, index=index, wx=wx)
     ref = ctx.gpp(p, "fp64")
-    check(ctx.gpp(p, "mixed"), ref, TOLMX)
+    check_mixed(ctx.gpp(p, "mixed"), ref, gpp_scales(p, orc))
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_gpp_root_quirks(ctx, fk, orc, prec):
     p = fk.inputs.gpp_synthetic(40, 3, 900, 9, seed=7, dist="branch", index="reference", wx="stress")
     ref = orc.gpp(p, flags=orc.ORC_GPP_ROOT_QUIRKS)
-    check(ctx.gpp(p, prec, fk.FK_GPP_ROOT_QUIRKS), ref, TOL64 if prec == "fp64" else TOLMX)
+    res = ctx.gpp(p, prec, fk.FK_GPP_ROOT_QUIRKS)
+    if prec == "fp64":
+        check(res, ref, TOL64)
+    else:
+        check_mixed(res, ref, gpp_scales(p, orc, orc.ORC_GPP_ROOT_QUIRKS))
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
@@ -63,8 +73,12 @@ def test_gpp_static_remainder(ctx, fk, orc, prec):
     p = fk.inputs.gpp_synthetic(48, 2, 1024, 16, seed=8, dist="uniform")
     ref = orc.gpp(p, flags=orc.ORC_GPP_ACHSTEMP)
     r = ctx.gpp(p, prec, fk.FK_GPP_ACHSTEMP)
-    assert rel(r["achstemp"], [ref["achstemp"]]) <= (TOL64 if prec == "fp64" else TOLMX)
-    check(r, ref, TOL64 if prec == "fp64" else TOLMX)
+    if prec == "fp64":
+        assert rel(r["achstemp"], [ref["achstemp"]]) <= TOL64
+        check(r, ref, TOL64)
+    else:
+        assert rel(r["achstemp"], [ref["achstemp"]]) <= TOLMX
+        check_mixed(r, ref, gpp_scales(p, orc))
 
 
 def golden(name):
@@ -72,19 +86,26 @@ def golden(name):
         return json.load(f)[name]
 
 
+def driver_check(res, entry, tol):
+    """The driver's printed value carries its own summation error; the exact
+    closed form of its constant inputs is the tight target."""
+    exact = np.array([complex(*z) for z in entry["achtemp_exact"]])
+    printed = np.array([complex(*z) for z in entry["achtemp"]])
+    assert rel(res, exact) <= tol
+    assert rel(res, printed) <= tol + rel(printed, exact)
+
+
 @pytest.mark.parametrize("entry", golden("gppKer_bgw"), ids=lambda e: "x".join(map(str, e["args"])))
 def test_gpp_matches_reference_driver_prints(ctx, fk, entry):
     p = fk.inputs.gpp_reference_init(*entry["args"])
-    want = np.array([complex(*z) for z in entry["achtemp"]])
-    assert rel(ctx.gpp(p, "fp64")["achtemp"], want) <= TOL64
-    assert rel(ctx.gpp(p, "mixed")["achtemp"], want) <= TOLMX
+    driver_check(ctx.gpp(p, "fp64")["achtemp"], entry, TOL64)
+    driver_check(ctx.gpp(p, "mixed")["achtemp"], entry, TOLMX)
 
 
 @pytest.mark.parametrize("entry", golden("gppKer_root"), ids=lambda e: "x".join(map(str, e["args"])))
 def test_gpp_matches_root_driver_prints(ctx, fk, entry):
     p = fk.inputs.gpp_reference_init(*entry["args"])
-    want = np.array([complex(*z) for z in entry["achtemp"]])
-    assert rel(ctx.gpp(p, "fp64", fk.FK_GPP_ROOT_QUIRKS)["achtemp"], want) <= TOL64
+    driver_check(ctx.gpp(p, "fp64", fk.FK_GPP_ROOT_QUIRKS)["achtemp"], entry, TOL64)
 
 
 def test_gpp_skips_unmapped_columns(ctx, fk, orc):
@@ -143,7 +164,7 @@ def test_gpp_full_size_benchmark_config(ctx, fk, orc):
     p = fk.inputs.gpp_synthetic(512, 2, 32768, 20, seed=2024, dist="uniform")
     r64 = ctx.gpp(p, "fp64")
     check(r64, orc.gpp(p), TOL64)
-    check(ctx.gpp(p, "mixed"), r64, TOLMX)
+    check(ctx.gpp(p, "mixed"), r64, TOLMX)   # plain relative error at the benchmark size
 
 
 def test_gpp_full_size_reference_run(ctx, fk):
@@ -153,6 +174,5 @@ def test_gpp_full_size_reference_run(ctx, fk):
     if not e:
         pytest.skip("full-size golden vector not generated")
     p = fk.inputs.gpp_reference_init(*e[0]["args"])
-    want = np.array([complex(*z) for z in e[0]["achtemp"]])
-    assert rel(ctx.gpp(p, "fp64")["achtemp"], want) <= TOL64
-    assert rel(ctx.gpp(p, "mixed")["achtemp"], want) <= TOLMX
+    driver_check(ctx.gpp(p, "fp64")["achtemp"], e[0], TOL64)
+    driver_check(ctx.gpp(p, "mixed")["achtemp"], e[0], TOLMX)
