@@ -70,8 +70,26 @@ bool capturing(cudaStream_t s) {
     return st != cudaStreamCaptureStatusNone;
 }
 
+void drop_graphs(Ctx& c) {
+    for (auto& kv : c.graphs)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    c.graphs.clear();
+}
+
+// FNV-1a over a word sequence (graph cache key).
+uint64_t fnv(const uint64_t* w, size_t n) {
+    uint64_t h = 1469598103934665603ull;
+    for (size_t i = 0; i < n; ++i)
+        for (int b = 0; b < 8; ++b) {
+            h ^= (w[i] >> (8 * b)) & 0xFF;
+            h *= 1099511628211ull;
+        }
+    return h;
+}
+
 fk_status ensure_workspace(Ctx& c, size_t need) {
     if (c.ws.cap >= need) return FK_OK;
+    drop_graphs(c);  // captured graphs refer to the old workspace
     if (capturing(c.stream))
         return fail(c, FK_ENOMEM, "workspace must grow, which is not allowed during stream capture: call fk_reserve first");
     cudaError_t e = cudaStreamSynchronize(c.stream);
@@ -125,6 +143,24 @@ fk_status deliver(Ctx& c, void* dst, const double2* out, size_t off, size_t n, b
     if (!is_device_ptr(dst)) host_out = true;
     cudaError_t e = cudaMemcpyAsync(dst, out + off, n * sizeof(double2), cudaMemcpyDefault, c.stream);
     return e == cudaSuccess ? FK_OK : cuda_fail(c, e, "output copy");
+}
+
+// Pinned host buffer of at least `bytes`, safe to overwrite (its previous
+// contents have been copied out).
+void* pinned_buffer(Ctx& c, size_t bytes) {
+    if (c.pinned_ev) cudaEventSynchronize(c.pinned_ev);
+    if (c.pinned_cap < bytes) {
+        if (c.pinned) cudaFreeHost(c.pinned);
+        c.pinned = nullptr;
+        c.pinned_cap = 0;
+        size_t cap = bytes + bytes / 4 + 4096;
+        if (cudaHostAlloc(&c.pinned, cap, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        c.pinned_cap = cap;
+    }
+    return c.pinned;
 }
 
 // After a synchronize: a nonzero error word means a bounded device-side wait
@@ -191,6 +227,11 @@ fk_status fk_create(int device, fk_ctx_t* out) {
         delete c;
         return FK_ECUDA;
     }
+    if (cudaEventCreateWithFlags(&c->pinned_ev, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return FK_ECUDA;
+    }
     for (auto& e : c->ev)
         if (cudaEventCreate(&e) != cudaSuccess) {
             cudaGetLastError();
@@ -206,9 +247,11 @@ fk_status fk_destroy(fk_ctx_t c) {
     {
         fk::DeviceGuard g(c->device);
         if (c->stream) cudaStreamSynchronize(c->stream);
+        fk::drop_graphs(*c);
         if (c->ws.base) cudaFree(c->ws.base);
         if (c->errword) cudaFree(c->errword);
         if (c->pinned) cudaFreeHost(c->pinned);
+        if (c->pinned_ev) cudaEventDestroy(c->pinned_ev);
         for (auto& e : c->ev)
             if (e) cudaEventDestroy(e);
         if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -279,31 +322,115 @@ fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsm
 
     fk::GppDev r{};
     r.nb = nb; r.nv = nv; r.nc = nc; r.ng = ng; r.prec = precision; r.flags = flags;
+    r.ldm = nc;
+    r.aqsm_compact = false;
+    // Host aqsmtemp: the sum reads only its ngpown columns igp(my_igp)
+    // (BGW-Kernels/gppKer.cpp:322-325), so when those are few, gather them on
+    // the host and stage nb x ngpown values instead of nb x ncouls.
+    if (!aqm.dev && (long)ng * 128 <= (long)nc) {
+        std::vector<int> invh(ng), indh(nc);
+        const int* ip = inv_igp_index;
+        const int* dp = indinv;
+        bool ok = true;
+        if (inv.dev) { ok = ok && cudaMemcpy(invh.data(), inv_igp_index, ng * sizeof(int), cudaMemcpyDefault) == cudaSuccess; ip = invh.data(); }
+        if (ind.dev) { ok = ok && cudaMemcpy(indh.data(), indinv, nc * sizeof(int), cudaMemcpyDefault) == cudaSuccess; dp = indh.data(); }
+        fk_c128* buf = ok ? (fk_c128*)fk::pinned_buffer(x, band / nc * ng) : nullptr;
+        if (buf) {
+            for (int h = 0; h < ng; ++h) {
+                const int ind_ = ip[h];
+                int g = -1;
+                if (ind_ == nc) g = nc - 1;
+                else if (ind_ >= 0 && ind_ < nc) g = dp[ind_];
+                if (g >= nc) g = -1;
+                for (int n1 = 0; n1 < nb; ++n1)
+                    buf[(size_t)n1 * ng + h] = g >= 0 ? aqsmtemp[(size_t)n1 * nc + g] : fk_c128{0.0, 0.0};
+            }
+            aqm.user = buf;
+            aqm.bytes = (size_t)nb * ng * sizeof(double2);
+            r.ldm = ng;
+            r.aqsm_compact = true;
+        } else {
+            cudaGetLastError();
+        }
+    }
     const size_t outn = 7 + (size_t)nb;
     const size_t need = fk::staged_bytes(ins) + fk::gpp_workspace(x, r) + outn * sizeof(double2) + 4096;
     fk_status s = fk::ensure_workspace(x, need);
     if (s != FK_OK) return s;
-    x.ws.reset();
-    double2* out = (double2*)x.ws.take(outn * sizeof(double2));
-    fk::phase_mark(x, 0);
-    if ((s = fk::stage(x, ins)) != FK_OK) return s;
-    r.aqsm = (const double2*)aqm.d; r.aqsn = (const double2*)aqn.d;
-    r.eps = (const double2*)eps.d; r.wt = (const double2*)wt.d;
-    r.vcoul = (const double*)vc.d; r.inv = (const int*)inv.d; r.indinv = (const int*)ind.d;
-    r.wx = (const double*)wx.d; r.out = out;
-    if ((s = fk::gpp_run(x, r)) != FK_OK) return s;
-    bool host_out = false;
-    if ((s = fk::deliver(x, achtemp, out, 0, 3, host_out)) != FK_OK) return s;
-    if ((s = fk::deliver(x, asxtemp, out, 3, 3, host_out)) != FK_OK) return s;
-    if ((s = fk::deliver(x, achstemp, out, 6, 1, host_out)) != FK_OK) return s;
-    if ((s = fk::deliver(x, acht_n1_loc, out, 7, nb, host_out)) != FK_OK) return s;
-    if (host_out || x.profiling) {
-        cudaError_t e = cudaStreamSynchronize(x.stream);
-        if (e != cudaSuccess) return fk::cuda_fail(x, e, "gpp: synchronize");
-        fk::phase_close(x, 4);
-        if ((s = fk::check_errword(x)) != FK_OK) return s;
+
+    // Repeated calls whose arrays are all device memory replay a captured
+    // CUDA graph of the whole sequence (one launch instead of ~12).
+    bool all_dev = !x.profiling && x.use_graphs;
+    for (auto* i : ins) all_dev = all_dev && i->dev;
+    const void* outs[4] = {achtemp, asxtemp, acht_n1_loc, achstemp};
+    for (auto* o : outs) all_dev = all_dev && (o == nullptr || fk::is_device_ptr(o));
+    uint64_t key = 0;
+    fk::Ctx::GraphEntry* ge = nullptr;
+    if (all_dev) {
+        uint64_t w[24] = {(uint64_t)nb, (uint64_t)nv, (uint64_t)nc, (uint64_t)ng, (uint64_t)precision, flags,
+                          (uint64_t)(uintptr_t)x.stream, (uint64_t)(uintptr_t)x.ws.base};
+        int n = 8;
+        for (auto* i : ins) w[n++] = (uint64_t)(uintptr_t)i->user;
+        for (auto* o : outs) w[n++] = (uint64_t)(uintptr_t)o;
+        key = fk::fnv(w, n);
+        ge = &x.graphs[key];
+        if (ge->exec) {
+            cudaError_t e = cudaGraphLaunch(ge->exec, x.stream);
+            if (e != cudaSuccess) return fk::cuda_fail(x, e, "gpp: graph launch");
+            return FK_OK;
+        }
     }
-    return FK_OK;
+    const bool capture = ge && ge->seen >= 1 && x.graphs.size() <= 64;
+    if (ge) ++ge->seen;
+    if (capture) {
+        cudaError_t e = cudaStreamBeginCapture(x.stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return fk::cuda_fail(x, e, "gpp: begin capture");
+    }
+    auto enqueue = [&]() -> fk_status {
+        x.ws.reset();
+        double2* out = (double2*)x.ws.take(outn * sizeof(double2));
+        fk::phase_mark(x, 0);
+        fk_status st = fk::stage(x, ins);
+        if (st != FK_OK) return st;
+        if (r.aqsm_compact) cudaEventRecord(x.pinned_ev, x.stream);
+        r.aqsm = (const double2*)aqm.d; r.aqsn = (const double2*)aqn.d;
+        r.eps = (const double2*)eps.d; r.wt = (const double2*)wt.d;
+        r.vcoul = (const double*)vc.d; r.inv = (const int*)inv.d; r.indinv = (const int*)ind.d;
+        r.wx = (const double*)wx.d; r.out = out;
+        if ((st = fk::gpp_run(x, r)) != FK_OK) return st;
+        bool host_out = false;
+        if ((st = fk::deliver(x, achtemp, out, 0, 3, host_out)) != FK_OK) return st;
+        if ((st = fk::deliver(x, asxtemp, out, 3, 3, host_out)) != FK_OK) return st;
+        if ((st = fk::deliver(x, achstemp, out, 6, 1, host_out)) != FK_OK) return st;
+        if ((st = fk::deliver(x, acht_n1_loc, out, 7, nb, host_out)) != FK_OK) return st;
+        if (host_out || x.profiling) {
+            cudaError_t e = cudaStreamSynchronize(x.stream);
+            if (e != cudaSuccess) return fk::cuda_fail(x, e, "gpp: synchronize");
+            fk::phase_close(x, 4);
+            if ((st = fk::check_errword(x)) != FK_OK) return st;
+        }
+        return FK_OK;
+    };
+    s = enqueue();
+    if (capture) {
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(x.stream, &graph);
+        cudaError_t ei = cudaErrorUnknown;
+        if (s == FK_OK && e == cudaSuccess && graph) ei = cudaGraphInstantiate(&ge->exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (ei == cudaSuccess) {
+            e = cudaGraphLaunch(ge->exec, x.stream);
+            if (e != cudaSuccess) return fk::cuda_fail(x, e, "gpp: graph launch");
+            return FK_OK;
+        }
+        // The sequence could not be captured: never try again for this key and
+        // run it directly (the captured work, if any, was discarded).
+        cudaGetLastError();
+        ge->exec = nullptr;
+        ge->seen = -(1 << 30);
+        s = enqueue();
+    }
+    return s;
 }
 
 fk_status fk_ff(fk_ctx_t c, int nb, int nv, int nc, int ng, int nf, int ne, const fk_c128* aqsmtemp,

@@ -212,7 +212,7 @@ struct FfPlan {
     int MT, NT, KS, kchunk;
     int BN, kstages;              // tensor-core path (mixed)
     bool mixed;
-    size_t bytes, bytesImgR, bytesImgA, bytesW;
+    size_t bytes, bytesImgR, bytesImgA, bytesW, bytesAimg;
 };
 
 // k-slices for the persistent tensor-core kernel (see fk_gpp.cu)
@@ -258,7 +258,7 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
         if (needA[f]) p.planesA.push_back(f);
     }
     const int nplanes = std::max<int>(1, (int)p.planesR.size());
-    p.bytesImgR = p.bytesImgA = p.bytesW = 0;
+    p.bytesImgR = p.bytesImgA = p.bytesW = p.bytesAimg = 0;
     if (p.mixed) {
         p.BN = 64;
         p.kstages = ceil_div(r.nc, tcx::BK);
@@ -268,7 +268,8 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
         const size_t bb = tcx::Cfg<64>::B_BYTES;
         p.bytesImgR = p.planesR.size() * (size_t)p.NT * p.kstages * bb;
         p.bytesImgA = p.planesA.size() * (size_t)p.NT * p.kstages * bb;
-        p.bytesW = 2 * (size_t)r.nb * r.ng * sizeof(float2);
+        p.bytesW = 2 * (size_t)r.nb * r.ng * sizeof(float2) + (size_t)r.ng * sizeof(float) + 256;
+        p.bytesAimg = (size_t)p.MT * p.kstages * tcx::Cfg<64>::A_BYTES;
     } else {
         p.BN = d64::BN;
         p.kstages = 0;
@@ -283,7 +284,7 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
     p.bytes = (slots * (p.planesR.size() + p.planesA.size()) * r.nb * 2 + 3 * (size_t)r.nb * r.nf +
                (size_t)r.ne * r.nb) * sizeof(double2) +
               r.nb * sizeof(FactRow) + (p.planesR.size() + p.planesA.size()) * sizeof(int) + r.ng * sizeof(int) +
-              p.bytesImgR + p.bytesImgA + p.bytesW + 20 * 256;
+              p.bytesImgR + p.bytesImgA + p.bytesW + p.bytesAimg + 20 * 256;
     return p;
 }
 
@@ -317,8 +318,9 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
     uint8_t* imgR = p.bytesImgR ? (uint8_t*)c.ws.take(p.bytesImgR) : nullptr;
     uint8_t* imgA = p.bytesImgA ? (uint8_t*)c.ws.take(p.bytesImgA) : nullptr;
     float2* W = p.bytesW ? (float2*)c.ws.take(p.bytesW) : nullptr;
+    uint8_t* Aimg = p.bytesAimg ? (uint8_t*)c.ws.take(p.bytesAimg) : nullptr;
     if (!igp || !planes || !fact || !PR || (nA && !PA) || !tabs || !SD || (p.bytesImgR && !imgR) ||
-        (p.bytesImgA && !imgA) || (p.bytesW && !W))
+        (p.bytesImgA && !imgA) || (p.bytesW && !W) || (p.bytesAimg && !Aimg))
         return fail(c, FK_ENOMEM, "workspace too small for FF request");
     double2 *RW = tabs, *RS = tabs + (size_t)r.nb * r.nf, *AW = tabs + 2 * (size_t)r.nb * r.nf;
     // host tables -> device (pageable source; the copy completes before return of the call's sync)
@@ -335,9 +337,13 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
     ++c.launches;
     phase_mark(c, 2);
     if (p.mixed) {
-        tcx::weight_table_kernel<<<dim3(ceil_div(r.ng, 128), r.nb), 128, 0, st>>>(r.nb, 0, r.ng, r.aqsm, r.nc, r.vcoul,
-                                                                                igp, 1.0, W, W + (size_t)r.nb * r.ng);
-        ++c.launches;
+        tcx::weight_table_kernel<<<dim3(ceil_div(r.nb, 128), r.ng), 128, 0, st>>>(r.nb, 0, r.ng, r.aqsm, r.nc, r.vcoul,
+                                                                                igp, igp, 1.0, W, W + (size_t)r.nb * r.ng,
+                                                                                (float*)(W + 2 * (size_t)r.nb * r.ng));
+        // aqsntemp is reused by every (plane, n-tile): split it to BF16 pieces once
+        cudaMemsetAsync(Aimg, 0, p.bytesAimg, st);
+        tcx::aimg_convert_kernel<<<dim3(ceil_div(r.nc, 256), r.nb), 256, 0, st>>>(r.aqsn, r.nb, r.nc, p.kstages, Aimg);
+        c.launches += 2;
         cudaMemsetAsync(c.errword, 0, sizeof(int), st);
     }
     auto contract = [&](const double2* eps, const int* pls, int nb_, double2* P, uint8_t* img, size_t img_bytes) {
@@ -345,7 +351,7 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
         a.A = r.aqsn; a.lda = r.nc; a.m0 = 0; a.M = r.nb;
         a.B = eps; a.ldb = r.nc; a.bstride = (long)r.ng * r.nc; a.N = r.ng; a.K = r.nc;
         a.KS = p.KS; a.kchunk = p.kchunk; a.batches = nb_; a.batch_plane = pls;
-        a.aqsm = r.aqsm; a.ldm = r.nc; a.vcoul = r.vcoul; a.igp = igp; a.wscale = 1.0; a.G = 2; a.P = P;
+        a.aqsm = r.aqsm; a.ldm = r.nc; a.vcoul = r.vcoul; a.igp = igp; a.acol = igp; a.wscale = 1.0; a.G = 2; a.P = P;
         if (p.mixed) {
             // pre-split B planes (bf16 x 3), then the tensor-core contraction
             cudaMemsetAsync(img, 0, img_bytes, st);
@@ -355,14 +361,16 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
             t.c = a;
             t.c.batch_plane = nullptr;  // the image is indexed by batch position
             t.Bimg = img;
-            t.W1 = W; t.W2 = W + (size_t)r.nb * r.ng; t.ldw = r.ng;
+            t.W1 = W; t.W2 = W + (size_t)r.nb * r.ng; t.ldw = r.nb; t.Aimg = Aimg; t.gpp_cols = 0;
+            t.vcol = (const float*)(W + 2 * (size_t)r.nb * r.ng);
             t.kstages_total = p.kstages;
             t.MT = p.MT; t.NT = p.NT; t.units = p.MT * p.NT * p.KS * nb_;
             t.err = c.errword;
             const int grid1 = std::min(t.units, c.sms);
-            auto k = tcx::tc_contract_kernel<EPI_FF, 64>;
-            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcx::Cfg<64>::SMEM);
-            k<<<grid1, tcx::THREADS, tcx::Cfg<64>::SMEM, st>>>(t);
+            auto k = tcx::tc_contract_kernel<EPI_FF, 64, true>;
+            constexpr size_t smem = tcx::Cfg<64, true>::SMEM;
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k<<<grid1, tcx::THREADS, smem, st>>>(t);
             c.launches += 2;
         } else {
             dim3 grid(p.MT, p.NT * p.KS * nb_);

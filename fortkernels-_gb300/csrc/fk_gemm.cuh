@@ -43,7 +43,8 @@ struct ContractArgs {
     const double2* aqsm;    // [nb][ncouls]
     long ldm;
     const double* vcoul;
-    const int* igp;         // column h -> igp (-1: skipped)
+    const int* igp;         // column h -> igp (-1: skipped); indexes vcoul
+    const int* acol;        // column h -> column of the aqsm array passed (igp, or h when compacted)
     double wscale;
     int G;                  // groups per row in P
     double2* P;             // [slots][M][G]
@@ -55,7 +56,7 @@ __host__ __device__ inline int ceil_div(int a, int b) { return (a + b - 1) / b; 
 FK_DEV double2 epi_weight(const ContractArgs& a, int m, int h) {
     int g = a.igp[h];
     if (g < 0) return make_double2(0.0, 0.0);
-    double2 am = a.aqsm[(long)(a.m0 + m) * a.ldm + g];
+    double2 am = a.aqsm[(long)(a.m0 + m) * a.ldm + a.acol[h]];
     double s = a.wscale * a.vcoul[g];
     return make_double2(am.x * s, -am.y * s);
 }
@@ -70,7 +71,7 @@ FK_DEV void epi_accum(const ContractArgs& a, int m, int n, double2 c, double2* g
     } else if (EPI == EPI_FF) {
         int ig = a.igp[n];
         if (ig < 0) return;
-        double2 am = a.aqsm[(long)(a.m0 + m) * a.ldm + ig];
+        double2 am = a.aqsm[(long)(a.m0 + m) * a.ldm + a.acol[n]];
         double2 t = cmul(cconj(am), c);
         gs[0] = cadd(gs[0], cscale(t, a.vcoul[ig]));
         gs[1] = cadd(gs[1], t);

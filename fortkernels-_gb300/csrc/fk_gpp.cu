@@ -40,10 +40,14 @@ constexpr int PREPM_TILE = PREP_THREADS * PREPM_EPT;
 constexpr int NVC = 2;  // flag bands contracted per prep pass
 constexpr double TO1 = 1e-6;
 constexpr float GUARD = 1e-5f;  // relative guard band of the FP32 branch tests
+constexpr int GPP_COLS = 21;    // igp columns per 64-wide tensor-core n-tile (63 used)
 
-__global__ void igp_map_kernel(int ng, int nc, const int* inv, const int* indinv, int* igp) {
+__global__ void igp_map_kernel(int ng, int nc, const int* inv, const int* indinv, int compact, int* igp, int* acol) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < ng) igp[i] = gpp_igp_of(i, nc, inv, indinv);
+    if (i >= ng) return;
+    const int g = gpp_igp_of(i, nc, inv, indinv);
+    igp[i] = g;
+    acol[i] = g < 0 ? -1 : (compact ? i : g);
 }
 
 struct PrepArgs {
@@ -286,9 +290,9 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_mixed_kernel(PrepArgs p) {
                 }
             }
             if (D && igp >= 0 && (Q || A)) {
-                const int j = my_igp * 3 + iw;
-                tcx::bimg_store<BN>(D + (long)(j / BN) * p.kstages * tcx::Cfg<BN>::B_BYTES, p.kstages, j % BN, ig,
-                                    dv.x, dv.y);
+                // n-tile my_igp / GPP_COLS holds complete (igp, iw) triples
+                const int nt = my_igp / GPP_COLS, row = (my_igp % GPP_COLS) * 3 + iw;
+                tcx::bimg_store<BN>(D + (long)nt * p.kstages * tcx::Cfg<BN>::B_BYTES, p.kstages, row, ig, dv.x, dv.y);
             }
             if (nflag > 0 && igp >= 0) {
 #pragma unroll
@@ -328,8 +332,8 @@ FK_DEV void warp_sum(double2 (&v)[NV]) {
 // Flag bands: one warp per (n1, my_igp) sums the chunk partials and applies
 // the reference's weights (sch: 0.5*vcoul*conj(aqsm), BGW-Kernels/gppKer.cpp:
 // 346,421; ssx: occ*vcoul*conj(aqsm), :419).  FW[n1][my_igp][6].
-__global__ void flag_weights_kernel(int nv, int ng, int nc, int nch, const double2* F, const double2* aqsm,
-                                    const double* vcoul, const int* igp, double2* FW) {
+__global__ void flag_weights_kernel(int nv, int ng, long ldm, int nch, const double2* F, const double2* aqsm,
+                                    const double* vcoul, const int* igp, const int* acol, double2* FW) {
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (wid >= nv * ng) return;
     const int n1 = wid / ng, my_igp = wid % ng;
@@ -347,7 +351,7 @@ __global__ void flag_weights_kernel(int nv, int ng, int nc, int nch, const doubl
         for (int r = 0; r < 6; ++r) o[r] = make_double2(0.0, 0.0);
         return;
     }
-    const double2 cm = cconj(aqsm[(long)n1 * nc + g]);
+    const double2 cm = cconj(aqsm[(long)n1 * ldm + acol[my_igp]]);
     const double v = vcoul[g], occ = 1.0;
     for (int iw = 0; iw < 3; ++iw) {
         o[iw * 2 + 0] = cscale(cmul(cm, s[iw * 2 + 0]), 0.5 * v);
@@ -459,7 +463,7 @@ Plan make_plan(const Ctx& c, const GppDev& r) {
         p.BN = 64;
         p.kstages = ceil_div(r.nc, tcx::BK);
         p.MT = ceil_div(std::max(M, 1), tcx::BM);
-        p.NT = ceil_div(N, p.BN);
+        p.NT = ceil_div(r.ng, GPP_COLS);
         pick_split_tc(p.MT * p.NT, r.nc, c.sms, p.KS, p.kchunk);
         p.units = p.MT * p.NT * p.KS;
     } else {
@@ -481,7 +485,7 @@ Plan make_plan(const Ctx& c, const GppDev& r) {
     p.bytesS = (r.flags & FK_GPP_ACHSTEMP) ? (size_t)p.KSs * p.NTs * r.nb * sizeof(double2) : 0;
     p.bytesFW = (size_t)std::max(r.nv, 1) * r.ng * 6 * sizeof(double2);
     p.bytesRows = (size_t)r.nb * 8 * sizeof(double2);
-    p.bytesIgp = (size_t)r.ng * sizeof(int) + 256;  // + the totals counter
+    p.bytesIgp = 2 * (size_t)r.ng * sizeof(int) + 256;  // igp, acol, the totals counter
     return p;
 }
 
@@ -501,6 +505,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
     const Plan p = make_plan(c, r);
     cudaStream_t st = c.stream;
     int* igp = (int*)c.ws.take(p.bytesIgp);
+    int* acol = igp + r.ng;
     unsigned* counter = (unsigned*)((char*)igp + (p.bytesIgp - 256));
     void* D = p.bytesD ? c.ws.take(p.bytesD) : nullptr;
     double2* F = (double2*)c.ws.take(p.bytesF);
@@ -520,7 +525,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
     c.launches = 0;
 
     phase_mark(c, 1);
-    igp_map_kernel<<<ceil_div(r.ng, 128), 128, 0, st>>>(r.ng, r.nc, r.inv, r.indinv, igp);
+    igp_map_kernel<<<ceil_div(r.ng, 128), 128, 0, st>>>(r.ng, r.nc, r.inv, r.indinv, r.aqsm_compact ? 1 : 0, igp, acol);
     ++c.launches;
     for (int pass = 0; pass < p.passes; ++pass) {
         PrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, pass == 0 ? D : nullptr, p.kstages,
@@ -541,21 +546,21 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
         a.A = r.aqsn; a.lda = r.nc; a.m0 = r.nv; a.M = M;
         a.B = D; a.ldb = r.nc; a.bstride = 0; a.N = 3 * r.ng; a.K = r.nc;
         a.KS = p.KS; a.kchunk = p.kchunk; a.batches = 1; a.batch_plane = nullptr;
-        a.aqsm = r.aqsm; a.ldm = r.nc; a.vcoul = r.vcoul; a.igp = igp; a.wscale = 0.5; a.G = 3; a.P = P;
+        a.aqsm = r.aqsm; a.ldm = r.ldm; a.vcoul = r.vcoul; a.igp = igp; a.acol = acol; a.wscale = 0.5; a.G = 3; a.P = P;
         dim3 grid(p.MT, p.NT * p.KS);
         if (p.mixed) {
-            tcx::weight_table_kernel<<<dim3(ceil_div(r.ng, 128), M), 128, 0, st>>>(M, r.nv, r.ng, r.aqsm, r.nc, r.vcoul,
-                                                                                igp, 0.5, W, nullptr);
+            tcx::weight_table_kernel<<<dim3(ceil_div(M, 128), r.ng), 128, 0, st>>>(M, r.nv, r.ng, r.aqsm, r.ldm, r.vcoul,
+                                                                                igp, acol, 0.5, W, nullptr, nullptr);
             tcx::TcArgs t{};
             t.c = a;
             t.Bimg = (const uint8_t*)D;
-            t.W1 = W; t.W2 = nullptr; t.ldw = r.ng;
+            t.W1 = W; t.W2 = nullptr; t.ldw = M; t.gpp_cols = GPP_COLS; t.Aimg = nullptr; t.vcol = nullptr;
             t.kstages_total = p.kstages;
             t.MT = p.MT; t.NT = p.NT; t.units = p.units;
             t.err = c.errword;
             cudaMemsetAsync(c.errword, 0, sizeof(int), st);
             const int grid1 = std::min(p.units, c.sms);
-            auto k = tcx::tc_contract_kernel<EPI_GPP, 64>;
+            auto k = tcx::tc_contract_kernel<EPI_GPP, 64, false>;
             set_smem(k, tcx::Cfg<64>::SMEM);
             k<<<grid1, tcx::THREADS, tcx::Cfg<64>::SMEM, st>>>(t);
             c.launches += 1;
@@ -571,7 +576,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
         a.A = r.aqsn; a.lda = r.nc; a.m0 = 0; a.M = r.nb;
         a.B = r.eps; a.ldb = r.nc; a.bstride = 0; a.N = r.ng; a.K = r.nc;
         a.KS = p.KSs; a.kchunk = p.kchunks; a.batches = 1; a.batch_plane = nullptr;
-        a.aqsm = r.aqsm; a.ldm = r.nc; a.vcoul = r.vcoul; a.igp = igp; a.wscale = -0.5; a.G = 1; a.P = S;
+        a.aqsm = r.aqsm; a.ldm = r.ldm; a.vcoul = r.vcoul; a.igp = igp; a.acol = acol; a.wscale = -0.5; a.G = 1; a.P = S;
         dim3 grid(p.MTs, p.NTs * p.KSs);
         if (p.mixed) {
             auto k = f32::contract_kernel<EPI_STAT, double2>;
@@ -586,8 +591,8 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
     }
     phase_mark(c, 3);
     if (r.nv > 0) {
-        flag_weights_kernel<<<ceil_div(r.nv * r.ng * 32, 256), 256, 0, st>>>(r.nv, r.ng, r.nc, p.nch, F, r.aqsm,
-                                                                             r.vcoul, igp, FW);
+        flag_weights_kernel<<<ceil_div(r.nv * r.ng * 32, 256), 256, 0, st>>>(r.nv, r.ng, r.ldm, p.nch, F, r.aqsm,
+                                                                             r.vcoul, igp, acol, FW);
         ++c.launches;
     }
     cudaMemsetAsync(counter, 0, sizeof(unsigned), st);

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <unordered_map>
 
 #include "../../include/fk_abi.h"
 
@@ -29,14 +30,22 @@ struct Ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     Workspace ws;
-    void* pinned = nullptr;      // pinned host staging for small outputs
+    void* pinned = nullptr;      // pinned host staging (column gathers)
     size_t pinned_cap = 0;
+    cudaEvent_t pinned_ev = nullptr;  // last copy out of `pinned`
     std::string err;
     bool profiling = false;
     cudaEvent_t ev[5] = {};
     float timings[4] = {0, 0, 0, 0};
     int launches = 0;
     int* errword = nullptr;      // device error word of the tensor-core kernels (bounded waits)
+    // Graphs of repeated fully device-resident calls: key -> (times seen, executable graph).
+    struct GraphEntry {
+        int seen = 0;
+        cudaGraphExec_t exec = nullptr;
+    };
+    std::unordered_map<uint64_t, GraphEntry> graphs;
+    bool use_graphs = true;
 };
 
 // Set the context's last error and return the status.
@@ -47,6 +56,8 @@ fk_status cuda_fail(Ctx& c, cudaError_t e, const char* where);
 struct GppDev {
     int nb, nv, nc, ng;
     const double2 *aqsm, *aqsn, *eps, *wt;
+    long ldm;           // row stride of aqsm: ncouls, or ngpown when only the igp columns were staged
+    bool aqsm_compact;  // aqsm holds column igp(my_igp) at position my_igp
     const double* vcoul;
     const int *inv, *indinv;
     const double* wx;  // device [3]

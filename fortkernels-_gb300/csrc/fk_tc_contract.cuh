@@ -40,25 +40,31 @@ constexpr int THREADS = 448;
 constexpr int NCONV = 8;          // converter warps
 constexpr long long WAIT_LIMIT = 4000000000LL;  // ~2 s at 2 GHz
 
-template <int BN>
+template <int BN, bool WSMEM = false>
 struct Cfg {
     static_assert(BN == 64, "four accumulators x two buffers fill the 512 TMEM columns at BN = 64");
-    static constexpr int STAGES = 3;
+    // WSMEM (FF): the per-unit weight tile conj(aqsm)[BN][BM] lives in shared
+    // memory, which leaves room for two operand stages.
+    static constexpr int STAGES = WSMEM ? 2 : 3;
     static constexpr int CHUNK_STAGES = 2;  // k-values per TMEM accumulation = 64
     static constexpr uint32_t A_BYTES = NSUB * BM * 64;
     static constexpr uint32_t B_BYTES = NSUB * BN * 64;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
     static constexpr uint32_t ACC_COLS = 4 * BN;       // main re, main im, corr re, corr im
     static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;  // double buffered
-    static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+    static constexpr uint32_t W_BYTES = WSMEM ? (uint32_t)(BN * BM * sizeof(float2) + 4 * BN * sizeof(float)) : 0u;
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + W_BYTES + 1024 + 256;
 };
 
 struct TcArgs {
     ContractArgs c;       // shapes, partial buffer (same meaning as fk_gemm.cuh)
     const uint8_t* Bimg;  // pre-split B tiles: [plane][nt][kstage][NSUB][BN rows][64 B]
-    const float2* W1;     // epilogue weights [M][ldw] (GPP: 0.5 vcoul conj(aqsm); FF: vcoul conj(aqsm))
-    const float2* W2;     // FF only: conj(aqsm) [M][ldw]
-    int ldw;
+    const uint8_t* Aimg;  // pre-split A tiles [mt][kstage][NSUB][BM rows][64 B] (AIMG kernels only)
+    const float2* W1;     // epilogue weights, column-major [h][ldw] (GPP: 0.5 vcoul conj(aqsm); FF: vcoul conj(aqsm))
+    const float2* W2;     // FF only: conj(aqsm), [h][ldw]
+    int ldw;              // = M (rows are contiguous, so a warp's 32 rows load coalesced)
+    const float* vcol;    // FF: vcoul[igp(n)] per column n (FP32)
+    int gpp_cols;         // GPP: igp columns per n-tile (21: complete (igp, iw) triples)
     int kstages_total;    // k-stages per (plane, nt) in Bimg = ceil(K/32)
     int MT, NT, units;
     int* err;             // device error word (nonzero: a wait timed out)
@@ -76,32 +82,39 @@ __device__ __forceinline__ void split3(float f, uint16_t& h, uint16_t& m, uint16
     l = (uint16_t)(__float_as_uint(r2) >> 16);  // r2 has at most 8 significant bits: exact
 }
 
-// B image element writer shared by the prep/conversion kernels: value x of
-// row n (within its n-tile) at k-value k of a (plane, nt) image.
+// Image element writer shared by the prep/conversion kernels: complex value
+// (re, im) of row `row` (within its ROWS-row tile) at k-value k of a tile
+// column whose k-stages are ROWS*NSUB*64 bytes apart.
+template <int ROWS>
+__device__ __forceinline__ void img_store(uint8_t* img_tile, int row, int k, float re, float im) {
+    uint8_t* st = img_tile + (long)(k / BK) * (ROWS * NSUB * 64);
+    const uint32_t off = tc::sw64_offset(row, k % BK);
+    uint16_t h, m, l;
+    split3(re, h, m, l);
+    *(uint16_t*)(st + 0 * ROWS * 64 + off) = h;
+    *(uint16_t*)(st + 1 * ROWS * 64 + off) = m;
+    *(uint16_t*)(st + 2 * ROWS * 64 + off) = l;
+    split3(im, h, m, l);
+    *(uint16_t*)(st + 3 * ROWS * 64 + off) = h;
+    *(uint16_t*)(st + 4 * ROWS * 64 + off) = m;
+    *(uint16_t*)(st + 5 * ROWS * 64 + off) = l;
+}
 template <int BN>
 __device__ __forceinline__ void bimg_store(uint8_t* img_nt, int kstage_total_unused, int n_in_tile, int k,
                                            float re, float im) {
     (void)kstage_total_unused;
-    uint8_t* st = img_nt + (long)(k / BK) * Cfg<BN>::B_BYTES;
-    const uint32_t off = tc::sw64_offset(n_in_tile, k % BK);
-    uint16_t h, m, l;
-    split3(re, h, m, l);
-    *(uint16_t*)(st + 0 * BN * 64 + off) = h;
-    *(uint16_t*)(st + 1 * BN * 64 + off) = m;
-    *(uint16_t*)(st + 2 * BN * 64 + off) = l;
-    split3(im, h, m, l);
-    *(uint16_t*)(st + 3 * BN * 64 + off) = h;
-    *(uint16_t*)(st + 4 * BN * 64 + off) = m;
-    *(uint16_t*)(st + 5 * BN * 64 + off) = l;
+    img_store<BN>(img_nt, n_in_tile, k, re, im);
 }
 
-template <int EPI, int BN>
+template <int EPI, int BN, bool AIMG>
 __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(TcArgs t) {
-    using C = Cfg<BN>;
+    using C = Cfg<BN, EPI == EPI_FF>;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-aligned operand area
     uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t* bars = (uint64_t*)(base + C::STAGES * C::STAGE_BYTES);
+    float2* sW = (float2*)(base + C::STAGES * C::STAGE_BYTES);  // FF: [BN][BM] conj(aqsm)
+    float* sV = (float*)(sW + BN * BM);                           // FF: vcoul[BN], one copy per epilogue warp
+    uint64_t* bars = (uint64_t*)(base + C::STAGES * C::STAGE_BYTES + C::W_BYTES);
     uint64_t* fullA = bars;
     uint64_t* fullB = bars + C::STAGES;
     uint64_t* empty = bars + 2 * C::STAGES;
@@ -118,7 +131,7 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(TcArgs t) {
 
     if (tid == 0) {
         for (int s = 0; s < C::STAGES; ++s) {
-            tc::mbar_init(&fullA[s], NCONV);
+            tc::mbar_init(&fullA[s], AIMG ? 1 : NCONV);
             tc::mbar_init(&fullB[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
@@ -241,23 +254,54 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(TcArgs t) {
                         t.Bimg + (((long)plane * NTu + nt) * t.kstages_total + kst) * (long)C::B_BYTES;
                     tc::mbar_arrive_expect_tx(&fullB[s], C::B_BYTES);
                     tc::bulk_g2s(base + s * C::STAGE_BYTES + C::A_BYTES, src, C::B_BYTES, &fullB[s]);
+                    if (AIMG) {
+                        const uint8_t* asrc = t.Aimg + ((long)mt * t.kstages_total + kst) * (long)C::A_BYTES;
+                        tc::mbar_arrive_expect_tx(&fullA[s], C::A_BYTES);
+                        tc::bulk_g2s(base + s * C::STAGE_BYTES, asrc, C::A_BYTES, &fullA[s]);
+                    }
                 }
             }
         }
     } else if (warp >= 4 && warp < 8) {
         // ------------------------------------------------------- epilogue
+        // Weights are fetched once per unit: GPP into registers (a 64-wide
+        // tile holds complete (igp, iw) triples of GPP_COLS igp), FF into a
+        // column-major shared-memory tile.  Columns are fully unrolled so every
+        // register index is a compile-time constant.
         const int q4 = warp - 4;  // TMEM lane quarter
         const int row = q4 * 32 + lane;
         int chunk = 0;
         bool ok = true;
+        constexpr int GC = BN / 3;  // 21 igp per GPP tile
         for (int u = blockIdx.x; u < t.units && ok; u += gridDim.x) {
             int mt, nt, ks, batch, k0, k1;
             unit_coords(u, mt, nt, ks, batch);
             krange(ks, k0, k1);
             const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
             const int m = mt * BM + row;
-            const float2* wrow1 = t.W1 + (long)min(m, a.M - 1) * t.ldw;
-            const float2* wrow2 = EPI == EPI_FF ? t.W2 + (long)min(m, a.M - 1) * t.ldw : nullptr;
+            const int mc = min(m, a.M - 1);
+            float2 wreg[EPI == EPI_GPP ? GC : 1];
+            if (EPI == EPI_GPP) {
+#pragma unroll
+                for (int i = 0; i < GC; ++i) {
+                    const int h = nt * t.gpp_cols + i;
+                    wreg[i] = (i < t.gpp_cols && h < a.N / 3) ? t.W1[(long)h * t.ldw + mc] : make_float2(0.f, 0.f);
+                }
+            } else {
+                // each thread stages its own row of conj(aqsm) (only it reads
+                // that row, so no barrier is needed); each warp its own vcoul copy
+                __syncwarp();
+#pragma unroll 4
+                for (int c = 0; c < BN; ++c) {
+                    const int n = nt * BN + c;
+                    sW[c * BM + row] = (n < a.N && m < a.M) ? t.W2[(long)n * t.ldw + m] : make_float2(0.f, 0.f);
+                }
+                for (int c = lane; c < BN; c += 32) {
+                    const int n = nt * BN + c;
+                    sV[q4 * BN + c] = n < a.N ? t.vcol[n] : 0.f;
+                }
+                __syncwarp();
+            }
             double2 acc[GMAX] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
             for (int st0 = 0; st0 < nst; st0 += C::CHUNK_STAGES, ++chunk) {
                 const int b = chunk & 1;
@@ -269,7 +313,7 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(TcArgs t) {
                 tc::tc_fence_after();
                 const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * C::ACC_COLS);
                 float2 gsum[GMAX] = {make_float2(0, 0), make_float2(0, 0), make_float2(0, 0)};
-#pragma unroll 1
+#pragma unroll
                 for (int c0 = 0; c0 < BN; c0 += 16) {
                     float vr[16], vi[16], wr[16], wi[16];
                     tc::tmem_ld16(tl + c0, vr);
@@ -279,24 +323,19 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(TcArgs t) {
                     tc::tmem_ld_wait();
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
-                        vr[j] += wr[j];
-                        vi[j] += wi[j];
-                    }
-                    if (m < a.M) {
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) {
-                            const int n = nt * BN + c0 + j;
-                            if (n >= a.N) continue;
-                            const float2 s = make_float2(vr[j], vi[j]);
-                            if (EPI == EPI_GPP) {
-                                cfmaf(gsum[n % 3], wrow1[n / 3], s);
-                            } else {
-                                const float2 t1 = cmulf(wrow1[n], s), t2 = cmulf(wrow2[n], s);
-                                gsum[0].x += t1.x;
-                                gsum[0].y += t1.y;
-                                gsum[1].x += t2.x;
-                                gsum[1].y += t2.y;
-                            }
+                        const int c = c0 + j;
+                        const float2 sv = make_float2(vr[j] + wr[j], vi[j] + wi[j]);
+                        if (EPI == EPI_GPP) {
+                            // tile column c = 3*(igp offset) + iw; column 63 is padding
+                            if (c < 3 * GC) cfmaf(gsum[c % 3], wreg[c / 3], sv);
+                        } else {
+                            const float2 w2 = sW[c * BM + row];
+                            const float2 t2 = cmulf(w2, sv);
+                            const float v = sV[q4 * BN + c];
+                            gsum[0].x = fmaf(v, t2.x, gsum[0].x);
+                            gsum[0].y = fmaf(v, t2.y, gsum[0].y);
+                            gsum[1].x += t2.x;
+                            gsum[1].y += t2.y;
                         }
                     }
                     if (EPI == EPI_FF && (c0 & 31) == 16) {
@@ -311,9 +350,12 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(TcArgs t) {
                 tc::tc_fence_before();
                 __syncwarp();
                 if (lane == 0) tc::mbar_arrive(&accEmpty[b]);
-                for (int gg = 0; gg < GMAX; ++gg) {
-                    acc[gg].x += (double)gsum[gg].x;
-                    acc[gg].y += (double)gsum[gg].y;
+                if (EPI == EPI_GPP) {
+#pragma unroll
+                    for (int gg = 0; gg < 3; ++gg) {
+                        acc[gg].x += (double)gsum[gg].x;
+                        acc[gg].y += (double)gsum[gg].y;
+                    }
                 }
             }
             if (!ok) break;
@@ -324,62 +366,84 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(TcArgs t) {
         }
     } else {
         // ----------------------------------------------------- converters
-        const int cw = warp < 4 ? warp - 2 : warp - 6;  // 0..7
-        const int ct = cw * 32 + lane;                   // 0..255
-        const int r = ct >> 1, half = ct & 1;
-        int g = 0;
-        bool ok = true;
-        for (int u = blockIdx.x; u < t.units && ok; u += gridDim.x) {
-            int mt, nt, ks, batch, k0, k1;
-            unit_coords(u, mt, nt, ks, batch);
-            krange(ks, k0, k1);
-            const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
-            const int m = mt * BM + r;
-            const double2* arow = a.A + (long)(a.m0 + min(m, a.M - 1)) * a.lda;
-            for (int st = 0; st < nst; ++st, ++g) {
-                const int s = g % C::STAGES;
-                const int kb = k0 + st * BK + half * 16;
-                // issue the loads before waiting for the slot
-                double2 v[16];
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int k = kb + j;
-                    v[j] = (m < a.M && k < k1) ? __ldg(arow + k) : make_double2(0.0, 0.0);
+        // warp cw converts rows cw*16 .. cw*16+15 of each stage; lane = k, so
+        // every load instruction reads 512 contiguous bytes of one row.  The
+        // rows are handled in two halves and the loads of the next half are in
+        // flight while the current half is converted (software pipelining
+        // across stages), so HBM latency is not exposed once per stage.
+        if (!AIMG) {
+            const int cw = warp < 4 ? warp - 2 : warp - 6;  // 0..7
+            constexpr int RPW = BM / NCONV;                  // rows per converter warp
+            constexpr int HALF = RPW / 2;
+            // flattened (unit, stage) sequence of this CTA
+            struct Pos {
+                int u, st, nst, k0, k1, mt;
+            };
+            auto first = [&](Pos& p, int u) -> bool {
+                for (; u < t.units; u += gridDim.x) {
+                    int nt, ks, batch;
+                    unit_coords(u, p.mt, nt, ks, batch);
+                    krange(ks, p.k0, p.k1);
+                    p.nst = p.k1 > p.k0 ? (p.k1 - p.k0 + BK - 1) / BK : 0;
+                    if (p.nst > 0) {
+                        p.u = u;
+                        p.st = 0;
+                        return true;
+                    }
                 }
+                return false;
+            };
+            auto advance = [&](Pos& p) -> bool {
+                if (++p.st < p.nst) return true;
+                return first(p, p.u + gridDim.x);
+            };
+            auto load_half = [&](const Pos& p, int h, double2 (&v)[HALF]) {
+                const int k = p.k0 + p.st * BK + lane;
+#pragma unroll
+                for (int i = 0; i < HALF; ++i) {
+                    const int m = p.mt * BM + cw * RPW + h * HALF + i;
+                    v[i] = (m < a.M && k < p.k1) ? __ldg(a.A + (long)(a.m0 + m) * a.lda + k) : make_double2(0.0, 0.0);
+                }
+            };
+            auto store_half = [&](uint8_t* sa, int h, const double2 (&v)[HALF]) {
+#pragma unroll
+                for (int i = 0; i < HALF; ++i) {
+                    const uint32_t off = tc::sw64_offset(cw * RPW + h * HALF + i, lane);
+                    uint16_t hh, mm, ll;
+                    split3(f64_to_f32_bits(v[i].x), hh, mm, ll);
+                    *(uint16_t*)(sa + 0 * BM * 64 + off) = hh;
+                    *(uint16_t*)(sa + 1 * BM * 64 + off) = mm;
+                    *(uint16_t*)(sa + 2 * BM * 64 + off) = ll;
+                    split3(f64_to_f32_bits(v[i].y), hh, mm, ll);
+                    *(uint16_t*)(sa + 3 * BM * 64 + off) = hh;
+                    *(uint16_t*)(sa + 4 * BM * 64 + off) = mm;
+                    *(uint16_t*)(sa + 5 * BM * 64 + off) = ll;
+                }
+            };
+            Pos cur;
+            bool have = first(cur, blockIdx.x);
+            double2 va[HALF], vb[HALF];
+            if (have) load_half(cur, 0, va);
+            int g = 0;
+            while (have) {
+                const int s = g % C::STAGES;
+                load_half(cur, 1, vb);
                 if (!tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, WAIT_LIMIT) || s_abort) {
                     fail(32);
-                    ok = false;
                     break;
                 }
                 uint8_t* sa = base + s * C::STAGE_BYTES;
-                uint32_t pk[NSUB][8];
-#pragma unroll
-                for (int j = 0; j < 16; j += 2) {
-                    uint16_t h0, m0, l0, h1, m1, l1, H0, M0, L0, H1, M1, L1;
-                    split3(f64_to_f32_bits(v[j].x), h0, m0, l0);
-                    split3(f64_to_f32_bits(v[j + 1].x), h1, m1, l1);
-                    split3(f64_to_f32_bits(v[j].y), H0, M0, L0);
-                    split3(f64_to_f32_bits(v[j + 1].y), H1, M1, L1);
-                    pk[0][j >> 1] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-                    pk[1][j >> 1] = (uint32_t)m0 | ((uint32_t)m1 << 16);
-                    pk[2][j >> 1] = (uint32_t)l0 | ((uint32_t)l1 << 16);
-                    pk[3][j >> 1] = (uint32_t)H0 | ((uint32_t)H1 << 16);
-                    pk[4][j >> 1] = (uint32_t)M0 | ((uint32_t)M1 << 16);
-                    pk[5][j >> 1] = (uint32_t)L0 | ((uint32_t)L1 << 16);
-                }
-#pragma unroll
-                for (int sub = 0; sub < NSUB; ++sub) {
-                    uint8_t* tile = sa + sub * BM * 64;
-#pragma unroll
-                    for (int c8 = 0; c8 < 2; ++c8) {
-                        const uint32_t off = tc::sw64_offset(r, half * 16 + c8 * 8);
-                        *reinterpret_cast<uint4*>(tile + off) =
-                            make_uint4(pk[sub][c8 * 4 + 0], pk[sub][c8 * 4 + 1], pk[sub][c8 * 4 + 2], pk[sub][c8 * 4 + 3]);
-                    }
-                }
+                store_half(sa, 0, va);
+                Pos nxt = cur;
+                const bool more = advance(nxt);
+                if (more) load_half(nxt, 0, va);
+                store_half(sa, 1, vb);
                 tc::fence_proxy_async_smem();
                 __syncwarp();
                 if (lane == 0) tc::mbar_arrive(&fullA[s]);
+                cur = nxt;
+                have = more;
+                ++g;
             }
         }
     }
@@ -392,22 +456,24 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(TcArgs t) {
     }
 }
 
-// Epilogue weight tables in FP32: W1[m][h] = wscale*vcoul[igp]*conj(aqsm[m0+m][igp])
-// (vcoul omitted when with_vcoul == 0), W2[m][h] = conj(aqsm[m0+m][igp]).
+// Epilogue weight tables in FP32, column-major (row m contiguous):
+// W1[h][m] = wscale*vcoul[igp]*conj(aqsm[m0+m][igp]), W2[h][m] = conj(aqsm[m0+m][igp]).
 static __global__ void weight_table_kernel(int M, int m0, int ncols, const double2* aqsm, long ldm, const double* vcoul,
-                                    const int* igp, double wscale, float2* W1, float2* W2) {
-    const int h = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
+                                    const int* igp, const int* acol, double wscale, float2* W1, float2* W2,
+                                    float* vcol) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x, h = blockIdx.y;
     if (h >= ncols || m >= M) return;
     const int g = igp[h];
     float2 w1 = make_float2(0.f, 0.f), w2 = w1;
     if (g >= 0) {
-        const double2 am = aqsm[(long)(m0 + m) * ldm + g];
+        const double2 am = aqsm[(long)(m0 + m) * ldm + acol[h]];
         const double s = wscale * vcoul[g];
         w1 = make_float2(f64_to_f32_bits(am.x * s), f64_to_f32_bits(-am.y * s));
         w2 = make_float2(f64_to_f32_bits(am.x), f64_to_f32_bits(-am.y));
     }
-    W1[(long)m * ncols + h] = w1;
-    if (W2) W2[(long)m * ncols + h] = w2;
+    W1[(long)h * M + m] = w1;
+    if (W2) W2[(long)h * M + m] = w2;
+    if (vcol && m == 0) vcol[h] = g >= 0 ? f64_to_f32_bits(vcoul[g]) : 0.f;
 }
 
 // FP64 planes [plane][rows][K] -> pre-split B images [plane][nt][kstage][NSUB][BN][64 B].
@@ -421,6 +487,15 @@ __global__ void bimg_convert_kernel(const double2* src, long plane_stride, int r
     const int NT = (rows + BN - 1) / BN;
     uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * (long)Cfg<BN>::B_BYTES;
     bimg_store<BN>(img_nt, kstages, n % BN, k, f64_to_f32_bits(v.x), f64_to_f32_bits(v.y));
+}
+
+// FP64 rows [rows][K] -> pre-split A image [mt][kstage][NSUB][BM][64 B].
+static __global__ void aimg_convert_kernel(const double2* src, int rows, int K, int kstages, uint8_t* img) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
+    if (k >= K || m >= rows) return;
+    const double2 v = src[(long)m * K + k];
+    uint8_t* tile = img + ((long)(m / BM) * kstages) * (long)(BM * NSUB * 64);
+    img_store<BM>(tile, m % BM, k, f64_to_f32_bits(v.x), f64_to_f32_bits(v.y));
 }
 
 }  // namespace tcx

@@ -176,3 +176,33 @@ def test_gpp_full_size_reference_run(ctx, fk):
     p = fk.inputs.gpp_reference_init(*e[0]["args"])
     driver_check(ctx.gpp(p, "fp64")["achtemp"], e[0], TOL64)
     driver_check(ctx.gpp(p, "mixed")["achtemp"], e[0], TOLMX)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_gpp_graph_replay_tracks_new_data(ctx, fk, prec):
+    """Repeated device-resident calls are replayed from a captured CUDA graph;
+    the replay must read the current contents of the (same) buffers."""
+    import torch
+    p = fk.inputs.gpp_synthetic(96, 2, 2000, 10, seed=12, dist="branch", wx="stress")
+    d = dict(p)
+    for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array"):
+        d[k] = torch.from_numpy(np.ascontiguousarray(p[k])).cuda()
+    for k in ("vcoul", "wx_array"):
+        d[k] = torch.from_numpy(np.ascontiguousarray(p[k], np.float64)).cuda()
+    for k in ("inv_igp_index", "indinv"):
+        d[k] = torch.from_numpy(np.ascontiguousarray(p[k], np.int32)).cuda()
+    out = {"achtemp": torch.zeros(3, dtype=torch.complex128, device="cuda"),
+           "asxtemp": torch.zeros(3, dtype=torch.complex128, device="cuda"),
+           "acht_n1_loc": torch.zeros(96, dtype=torch.complex128, device="cuda"), "achstemp": None}
+    res = []
+    for _ in range(4):  # eager, captured, replayed, replayed
+        ctx.gpp(d, prec, out=out)
+        ctx.synchronize()
+        res.append(out["achtemp"].cpu().numpy().copy())
+    for r in res[1:]:
+        np.testing.assert_array_equal(r, res[0])
+    d["aqsntemp"].mul_(2.0)  # every term is linear in aqsntemp; x2 is exact
+    torch.cuda.synchronize()
+    ctx.gpp(d, prec, out=out)
+    ctx.synchronize()
+    np.testing.assert_array_equal(out["achtemp"].cpu().numpy(), 2.0 * res[0])
