@@ -212,6 +212,24 @@ __global__ void __launch_bounds__(PREP_THREADS) prep64_kernel(PrepArgs p) {
 }
 
 // ------------------------------------------------------------ mixed (guarded)
+// Exact FP64 re-evaluation of one (igp, ig, iw) element whose FP32 branch
+// quantities fell inside a guard band.  Kept out of line so that the compiler
+// does not if-convert it into the common path (it is rare; inlined and
+// predicated it would run on GB300's narrow FP64 pipe for every element).
+__device__ __noinline__ void exact_element(double wxt, double2 wt64, double2 ep64, double2 eq64, int need_ssx,
+                                           bool* A, bool* B, float2* dv, float2* sch, float2* ssx) {
+    Branch64 b = branch64(wxt, wt64);
+    *A = b.A;
+    *B = b.B;
+    *dv = c64_to_f32(cmul(b.delw, ep64));
+    *sch = b.A ? c64_to_f32(cmul(b.delw, eq64)) : make_float2(0.f, 0.f);
+    if (need_ssx) {
+        const double2 wt2d = cmul(wt64, wt64);
+        *ssx = c64_to_f32(ssx64(b, wxt, wt2d, cmul(wt2d, ep64)));
+    } else {
+        *ssx = make_float2(0.f, 0.f);
+    }
+}
 // Writes D straight into the pre-split BF16 image consumed by the tensor-core
 // contraction (column j = my_igp*3 + iw lives in n-tile j / BN).
 template <int Q, int BN>
@@ -260,19 +278,10 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_mixed_kernel(PrepArgs p) {
             const bool amb = !(wdiffr > 1e-30f) || !(delwr < 1e30f) ||
                              fabsf(wdiffr - limittwo) <= limittwo * GUARD ||
                              fabsf(delwr - limitone) <= limitone * GUARD || fabsf(delwr - to1) <= to1 * GUARD;
-            if (amb) {
+            if (__any_sync(__activemask(), amb) && amb) {
                 // exact FP64 sequence for this element (rare)
-                Branch64 b = branch64(wxt, wt64);
-                A = b.A;
-                B = b.B;
-                dv = c64_to_f32(cmul(b.delw, ep64));
-                sch = A ? c64_to_f32(cmul(b.delw, Q ? p.eps[(long)my_igp * p.ng + ig] : ep64)) : make_float2(0.f, 0.f);
-                if (nflag > 0) {
-                    double2 wt2d = cmul(wt64, wt64);
-                    ssx = c64_to_f32(ssx64(b, wxt, wt2d, cmul(wt2d, ep64)));
-                } else {
-                    ssx = make_float2(0.f, 0.f);
-                }
+                exact_element(wxt, wt64, ep64, Q ? p.eps[(long)my_igp * p.ng + ig] : ep64, nflag > 0, &A, &B, &dv,
+                              &sch, &ssx);
             } else {
                 A = (wdiffr > limittwo) && (delwr < limitone);
                 B = delwr > to1;
@@ -329,71 +338,53 @@ FK_DEV void warp_sum(double2 (&v)[NV]) {
         }
 }
 
-// Flag bands: one warp per (n1, my_igp) sums the chunk partials and applies
-// the reference's weights (sch: 0.5*vcoul*conj(aqsm), BGW-Kernels/gppKer.cpp:
-// 346,421; ssx: occ*vcoul*conj(aqsm), :419).  FW[n1][my_igp][6].
+// Flag bands: one thread per (n1, my_igp, iw, kind) sums its chunk partials in
+// order and applies the reference's weight (sch: 0.5*vcoul*conj(aqsm),
+// BGW-Kernels/gppKer.cpp:346,421; ssx: occ*vcoul*conj(aqsm), :419).
+// FW[n1][my_igp][6].
 __global__ void flag_weights_kernel(int nv, int ng, long ldm, int nch, const double2* F, const double2* aqsm,
                                     const double* vcoul, const int* igp, const int* acol, double2* FW) {
-    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (wid >= nv * ng) return;
-    const int n1 = wid / ng, my_igp = wid % ng;
-    double2 s[6];
-#pragma unroll
-    for (int r = 0; r < 6; ++r) s[r] = make_double2(0.0, 0.0);
-    for (int ch = lane; ch < nch; ch += 32)
-#pragma unroll
-        for (int r = 0; r < 6; ++r) s[r] = cadd(s[r], F[(((long)ch * nv + n1) * ng + my_igp) * 6 + r]);
-    warp_sum<6>(s);
-    if (lane != 0) return;
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long)nv * ng * 6) return;
+    const int r = (int)(t % 6);
+    const int my_igp = (int)((t / 6) % ng), n1 = (int)(t / (6L * ng));
+    double2 s = make_double2(0.0, 0.0);
+    for (int ch = 0; ch < nch; ++ch) s = cadd(s, F[(((long)ch * nv + n1) * ng + my_igp) * 6 + r]);
     const int g = igp[my_igp];
-    double2* o = FW + ((long)n1 * ng + my_igp) * 6;
-    if (g < 0) {
-        for (int r = 0; r < 6; ++r) o[r] = make_double2(0.0, 0.0);
-        return;
+    double2 o = make_double2(0.0, 0.0);
+    if (g >= 0) {
+        const double2 cm = cconj(aqsm[(long)n1 * ldm + acol[my_igp]]);
+        const double v = vcoul[g], occ = 1.0;
+        o = cscale(cmul(cm, s), (r & 1) ? occ * v : 0.5 * v);
     }
-    const double2 cm = cconj(aqsm[(long)n1 * ldm + acol[my_igp]]);
-    const double v = vcoul[g], occ = 1.0;
-    for (int iw = 0; iw < 3; ++iw) {
-        o[iw * 2 + 0] = cscale(cmul(cm, s[iw * 2 + 0]), 0.5 * v);
-        o[iw * 2 + 1] = cscale(cmul(cm, s[iw * 2 + 1]), occ * v);
-    }
+    FW[((long)n1 * ng + my_igp) * 6 + r] = o;
 }
 
-// Per-band sums, one warp per band: rows[n1][8] = {sch iw0..2, ssx iw0..2,
-// stat, 0}.  The last block to finish adds the bands in order and writes
+// Per-band sums: one thread per (band, complex component c of 7) adds its
+// partials in a fixed order.  rows[n1][8] = {sch iw0..2, ssx iw0..2, stat, 0}.
+// The last block to finish adds the bands in order and writes
 // out = [achtemp 3 | asxtemp 3 | achstemp | acht_n1_loc nb].
 __global__ void rows_totals_kernel(int nb, int nv, int ng, int nslots, const double2* P, int nslots_s,
                                    const double2* S, const double2* FW, double2* rows, unsigned* counter,
                                    double2* out) {
-    const int lane = threadIdx.x & 31;
-    const int n1 = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (n1 < nb) {
-        double2 v[7];
-#pragma unroll
-        for (int i = 0; i < 7; ++i) v[i] = make_double2(0.0, 0.0);
-        if (n1 >= nv) {
-            const int M = nb - nv, m = n1 - nv;
-            for (int s = lane; s < nslots; s += 32)
-#pragma unroll
-                for (int iw = 0; iw < 3; ++iw) v[iw] = cadd(v[iw], P[((long)s * M + m) * 3 + iw]);
-        } else {
-            for (int h = lane; h < ng; h += 32) {
-                const double2* o = FW + ((long)n1 * ng + h) * 6;
-#pragma unroll
-                for (int iw = 0; iw < 3; ++iw) {
-                    v[iw] = cadd(v[iw], o[iw * 2]);
-                    v[3 + iw] = cadd(v[3 + iw], o[iw * 2 + 1]);
-                }
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < (long)nb * 7) {
+        const int n1 = (int)(t / 7), c = (int)(t % 7);
+        double2 v = make_double2(0.0, 0.0);
+        if (c == 6) {
+            if (S)
+                for (int s = 0; s < nslots_s; ++s) v = cadd(v, S[(long)s * nb + n1]);
+        } else if (n1 >= nv) {
+            if (c < 3) {
+                const int M = nb - nv, m = n1 - nv;
+                for (int s = 0; s < nslots; ++s) v = cadd(v, P[((long)s * M + m) * 3 + c]);
             }
+        } else {
+            const int iw = c % 3, kind = c / 3;  // kind 0: sch, 1: ssx
+            for (int h = 0; h < ng; ++h) v = cadd(v, FW[((long)n1 * ng + h) * 6 + iw * 2 + kind]);
         }
-        if (S)
-            for (int s = lane; s < nslots_s; s += 32) v[6] = cadd(v[6], S[(long)s * nb + n1]);
-        warp_sum<7>(v);
-        if (lane == 0)
-#pragma unroll
-            for (int i = 0; i < 7; ++i) rows[(long)n1 * 8 + i] = v[i];
+        rows[(long)n1 * 8 + c] = v;
     }
-    // last block: totals in band order
     __shared__ bool last;
     __threadfence();
     __syncthreads();
@@ -401,21 +392,19 @@ __global__ void rows_totals_kernel(int nb, int nv, int ng, int nslots, const dou
     __syncthreads();
     if (!last) return;
     __threadfence();
-    if (threadIdx.x < 32) {
-        double2 t[7];
-#pragma unroll
-        for (int i = 0; i < 7; ++i) t[i] = make_double2(0.0, 0.0);
-        for (int r = lane; r < nb; r += 32) {
-#pragma unroll
-            for (int i = 0; i < 7; ++i) t[i] = cadd(t[i], rows[(long)r * 8 + i]);
+    // component c is summed by warp c % 4: lanes take bands lane, lane+32, ...
+    // in order, then a fixed shuffle tree
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int c = w; c < 7; c += (int)(blockDim.x >> 5)) {
+        double2 tot = make_double2(0.0, 0.0);
+        for (int r = lane; r < nb; r += 32) tot = cadd(tot, rows[(long)r * 8 + c]);
+        for (int off = 16; off > 0; off >>= 1) {
+            tot.x += __shfl_down_sync(0xffffffffu, tot.x, off);
+            tot.y += __shfl_down_sync(0xffffffffu, tot.y, off);
         }
-        warp_sum<7>(t);
-        if (lane == 0) {
-#pragma unroll
-            for (int i = 0; i < 7; ++i) out[i] = t[i];
-            *counter = 0u;
-        }
+        if (lane == 0) out[c] = tot;
     }
+    if (threadIdx.x == 0) *counter = 0u;
     for (int r = threadIdx.x; r < nb; r += blockDim.x) out[7 + r] = rows[(long)r * 8 + 2];  // acht_n1_loc
 }
 
@@ -591,13 +580,13 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
     }
     phase_mark(c, 3);
     if (r.nv > 0) {
-        flag_weights_kernel<<<ceil_div(r.nv * r.ng * 32, 256), 256, 0, st>>>(r.nv, r.ng, r.ldm, p.nch, F, r.aqsm,
-                                                                             r.vcoul, igp, acol, FW);
+        flag_weights_kernel<<<ceil_div(r.nv * r.ng * 6, 128), 128, 0, st>>>(r.nv, r.ng, r.ldm, p.nch, F, r.aqsm,
+                                                                            r.vcoul, igp, acol, FW);
         ++c.launches;
     }
     cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
-    rows_totals_kernel<<<ceil_div(r.nb, 8), 256, 0, st>>>(r.nb, r.nv, r.ng, p.KS * p.NT, P, p.KSs * p.NTs, S, FW,
-                                                          rows, counter, r.out);
+    rows_totals_kernel<<<ceil_div(r.nb * 7, 128), 128, 0, st>>>(r.nb, r.nv, r.ng, p.KS * p.NT, P, p.KSs * p.NTs, S,
+                                                                FW, rows, counter, r.out);
     c.launches += 1;
     phase_mark(c, 4);
     cudaError_t e = cudaGetLastError();
