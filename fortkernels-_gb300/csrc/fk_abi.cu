@@ -115,22 +115,28 @@ struct In {
     const void* d;
 };
 
+// A device array is used where it lies when it starts on a 16-byte boundary
+// (the kernels move it with 16-byte and bulk copies); host arrays and
+// misaligned device arrays are copied into the workspace.
+bool in_place(const In* i) { return !i->user || (i->dev && ((uintptr_t)i->user & 15) == 0); }
+
 size_t staged_bytes(const std::vector<In*>& v) {
     size_t s = 0;
     for (auto* i : v)
-        if (!i->dev) s += (i->bytes + 255) & ~size_t(255);
+        if (!in_place(i)) s += (i->bytes + 255) & ~size_t(255);
     return s;
 }
 
 fk_status stage(Ctx& c, const std::vector<In*>& v) {
     for (auto* i : v) {
-        if (i->dev || !i->user) {
+        if (in_place(i)) {
             i->d = i->user;
             continue;
         }
         void* d = c.ws.take(i->bytes);
         if (!d) return fail(c, FK_ENOMEM, "workspace: staging");
-        cudaError_t e = cudaMemcpyAsync(d, i->user, i->bytes, cudaMemcpyHostToDevice, c.stream);
+        cudaError_t e = cudaMemcpyAsync(d, i->user, i->bytes, i->dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                        c.stream);
         if (e != cudaSuccess) return cuda_fail(c, e, "staging copy");
         i->d = d;
     }

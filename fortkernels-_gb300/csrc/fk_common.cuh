@@ -51,6 +51,22 @@ FK_DEV float f64_to_f32_bits(double d) {
 }
 FK_DEV float2 c64_to_f32(double2 v) { return make_float2(f64_to_f32_bits(v.x), f64_to_f32_bits(v.y)); }
 
+// x[0] + x[stride] + ... + x[(n-1)*stride], added left to right; the loads
+// are issued in groups of eight ahead of the adds, so a long sum waits for
+// memory once per group instead of once per term.
+FK_DEV double2 ordered_sum(const double2* x, long stride, int n) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int i0 = 0; i0 < n; i0 += 8) {
+        double2 v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = i0 + j < n ? x[(long)(i0 + j) * stride] : make_double2(0.0, 0.0);
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (i0 + j < n) s = cadd(s, v[j]);
+    }
+    return s;
+}
+
 // --------------------------------------------- compensated FP32 accumulation
 // float-float (hi, lo) accumulator updated with Knuth's TwoSum: exact sum of
 // the running value and the incoming FP32 block sum, error kept in lo.

@@ -38,12 +38,9 @@ __global__ void ff_rows_kernel(int nb, int nf, int batches, int slots_per_batch,
                                const double2* P, double2* RW, double2* RS) {
     const int n1 = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
     if (n1 >= nb || b >= batches) return;
-    double2 s0 = make_double2(0.0, 0.0), s1 = s0;
-    for (int s = 0; s < slots_per_batch; ++s) {
-        const double2* q = P + (((long)b * slots_per_batch + s) * nb + n1) * 2;
-        s0 = cadd(s0, q[0]);
-        s1 = cadd(s1, q[1]);
-    }
+    const double2* q = P + ((long)b * slots_per_batch * nb + n1) * 2;
+    const double2 s0 = ordered_sum(q, 2L * nb, slots_per_batch);
+    const double2 s1 = RS ? ordered_sum(q + 1, 2L * nb, slots_per_batch) : make_double2(0.0, 0.0);
     const int f = planes[b];
     RW[(long)n1 * nf + f] = s0;
     if (RS) RS[(long)n1 * nf + f] = s1;

@@ -35,8 +35,6 @@ namespace {
 constexpr int PREP_THREADS = 256;
 constexpr int PREP_EPT = 2;  // elements per thread, FP64 prep
 constexpr int PREP_TILE = PREP_THREADS * PREP_EPT;
-constexpr int PREPM_EPT = 8;  // elements per thread, mixed prep
-constexpr int PREPM_TILE = PREP_THREADS * PREPM_EPT;
 constexpr int NVC = 2;  // flag bands contracted per prep pass
 constexpr double TO1 = 1e-6;
 constexpr float GUARD = 1e-5f;  // relative guard band of the FP32 branch tests
@@ -59,6 +57,7 @@ struct PrepArgs {
     int kstages; // mixed: k-stages per n-tile in the image
     double2* F;  // [nch][nv][ng][3][2]  (sch, ssx) flag-band sums over the chunk
     int nch;
+    int tile;    // mixed: plane waves per chunk (a multiple of PREP_THREADS)
     int n1base;  // first flag band handled by this pass
 };
 
@@ -215,58 +214,88 @@ __global__ void __launch_bounds__(PREP_THREADS) prep64_kernel(PrepArgs p) {
 // Exact FP64 re-evaluation of one (igp, ig, iw) element whose FP32 branch
 // quantities fell inside a guard band.  Kept out of line so that the compiler
 // does not if-convert it into the common path (it is rare; inlined and
-// predicated it would run on GB300's narrow FP64 pipe for every element).
-__device__ __noinline__ void exact_element(double wxt, double2 wt64, double2 ep64, double2 eq64, int need_ssx,
-                                           bool* A, bool* B, float2* dv, float2* sch, float2* ssx) {
-    Branch64 b = branch64(wxt, wt64);
-    *A = b.A;
-    *B = b.B;
-    *dv = c64_to_f32(cmul(b.delw, ep64));
-    *sch = b.A ? c64_to_f32(cmul(b.delw, eq64)) : make_float2(0.f, 0.f);
+// predicated it would run on GB300's narrow FP64 pipe for every element), and
+// returned by value so that the caller's variables stay in registers.
+struct Exact {
+    float2 dv, sch, ssx;
+    int A, B;
+};
+__device__ __noinline__ Exact exact_element(double wxt, double2 wt64, double2 ep64, double2 eq64, int need_ssx) {
+    const Branch64 b = branch64(wxt, wt64);
+    Exact r;
+    r.A = b.A;
+    r.B = b.B;
+    r.dv = c64_to_f32(cmul(b.delw, ep64));
+    r.sch = b.A ? c64_to_f32(cmul(b.delw, eq64)) : make_float2(0.f, 0.f);
+    r.ssx = make_float2(0.f, 0.f);
     if (need_ssx) {
         const double2 wt2d = cmul(wt64, wt64);
-        *ssx = c64_to_f32(ssx64(b, wxt, wt2d, cmul(wt2d, ep64)));
-    } else {
-        *ssx = make_float2(0.f, 0.f);
+        r.ssx = c64_to_f32(ssx64(b, wxt, wt2d, cmul(wt2d, ep64)));
     }
+    return r;
 }
+
+// Block (ch, my_igp) covers plane waves [ch*tile, (ch+1)*tile) of column
+// my_igp; the chunk count is chosen so that all blocks are resident at once
+// (no tail wave).  Each thread walks its elements with the next element's
+// inputs already loading while the current one is evaluated.
 // Writes D straight into the pre-split BF16 image consumed by the tensor-core
-// contraction (column j = my_igp*3 + iw lives in n-tile j / BN).
+// contraction (column j = my_igp*3 + iw lives in n-tile j / GPP_COLS).
 template <int Q, int BN>
-__global__ void __launch_bounds__(PREP_THREADS) prep_mixed_kernel(PrepArgs p) {
+__global__ void __launch_bounds__(PREP_THREADS, 2) prep_mixed_kernel(PrepArgs p) {
     __shared__ double2 sm[8 * NVC * 6];
-    const int my_igp = blockIdx.y, ch = blockIdx.x, tid = threadIdx.x;
-    const int igp = p.igp[my_igp];
+    const int tid = threadIdx.x, ch = blockIdx.x, my_igp = blockIdx.y;
     const int nflag = min(NVC, p.nv - p.n1base);
+    const int igp = p.igp[my_igp];
+    const bool flags = nflag > 0 && igp >= 0;
+    const float limitone = 250000.0f, limittwo = 0.25f, to1 = 1e-6f;
+    uint8_t* D = reinterpret_cast<uint8_t*>(p.D);
+    float iw2[3];
+    double wx64[3];
+#pragma unroll
+    for (int iw = 0; iw < 3; ++iw) {
+        wx64[iw] = p.wx[iw];
+        const float wxf = f64_to_f32_bits(wx64[iw]);
+        iw2[iw] = 1.0f / (wxf * wxf);
+    }
+    const double2* wrow = p.wt + (long)my_igp * p.nc;
+    const double2* erow = p.eps + (long)my_igp * p.nc;
+    const int ig_end = min(p.nc, (ch + 1) * p.tile);
     float2 acc[NVC * 6];
 #pragma unroll
     for (int i = 0; i < NVC * 6; ++i) acc[i] = make_float2(0.f, 0.f);
-    const float limitone = 250000.0f, limittwo = 0.25f, to1 = 1e-6f;
-    const double2* wrow = p.wt + (long)my_igp * p.nc;
-    const double2* erow = p.eps + (long)my_igp * p.nc;
-    uint8_t* D = reinterpret_cast<uint8_t*>(p.D);
-    float wxf[3], iw2[3];
+    // inputs of the next element
+    double2 wt_n = make_double2(0.0, 0.0), ep_n = wt_n, an_n[NVC];
+    auto load = [&](int ig) {
+        wt_n = wrow[ig];
+        ep_n = erow[ig];
 #pragma unroll
-    for (int iw = 0; iw < 3; ++iw) {
-        wxf[iw] = f64_to_f32_bits(p.wx[iw]);
-        iw2[iw] = 1.0f / (wxf[iw] * wxf[iw]);
-    }
-    for (int e = 0; e < PREPM_EPT; ++e) {
-        const int ig = ch * PREPM_TILE + e * PREP_THREADS + tid;
-        if (ig >= p.nc) continue;
-        const double2 wt64 = wrow[ig], ep64 = erow[ig];
+        for (int j = 0; j < NVC; ++j)
+            an_n[j] = (flags && j < nflag) ? p.aqsn[(long)(p.n1base + j) * p.nc + ig] : make_double2(0.0, 0.0);
+    };
+    int ig = ch * p.tile + tid;
+    if (ig < ig_end) load(ig);
+    for (; ig < ig_end; ig += PREP_THREADS) {
+        const double2 wt64 = wt_n, ep64 = ep_n;
+        float2 an[NVC];
+#pragma unroll
+        for (int j = 0; j < NVC; ++j) an[j] = c64_to_f32(an_n[j]);
+        if (ig + PREP_THREADS < ig_end) load(ig + PREP_THREADS);
         const float2 wt = c64_to_f32(wt64), ep = c64_to_f32(ep64);
         float2 wt2 = make_float2(0.f, 0.f), Om = wt2, eq = ep;
+        double2 eq64 = ep64;
         if (nflag > 0) {
             wt2 = cmulf(wt, wt);
             Om = cmulf(wt2, ep);
-            if (Q) eq = c64_to_f32(p.eps[(long)my_igp * p.ng + ig]);
+            if (Q) {
+                eq64 = p.eps[(long)my_igp * p.ng + ig];
+                eq = c64_to_f32(eq64);
+            }
         }
 #pragma unroll
         for (int iw = 0; iw < 3; ++iw) {
-            const double wxt = p.wx[iw];
             // wdiff from an FP64 subtraction: keeps full relative accuracy next to the pole
-            const float wdr = f64_to_f32_bits(__dsub_rn(wxt, wt64.x)), wdi = -wt.y;
+            const float wdr = f64_to_f32_bits(__dsub_rn(wx64[iw], wt64.x)), wdi = -wt.y;
             const float wdiffr = wdr * wdr + wdi * wdi;
             const float rden = __frcp_rn(wdiffr);
             float2 delw = cmulf(wt, make_float2(wdr, -wdi));
@@ -280,8 +309,12 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_mixed_kernel(PrepArgs p) {
                              fabsf(delwr - limitone) <= limitone * GUARD || fabsf(delwr - to1) <= to1 * GUARD;
             if (__any_sync(__activemask(), amb) && amb) {
                 // exact FP64 sequence for this element (rare)
-                exact_element(wxt, wt64, ep64, Q ? p.eps[(long)my_igp * p.ng + ig] : ep64, nflag > 0, &A, &B, &dv,
-                              &sch, &ssx);
+                const Exact x = exact_element(wx64[iw], wt64, ep64, eq64, nflag > 0);
+                A = x.A != 0;
+                B = x.B != 0;
+                dv = x.dv;
+                sch = x.sch;
+                ssx = x.ssx;
             } else {
                 A = (wdiffr > limittwo) && (delwr < limitone);
                 B = delwr > to1;
@@ -299,18 +332,13 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_mixed_kernel(PrepArgs p) {
                 }
             }
             if (D && igp >= 0 && (Q || A)) {
-                // n-tile my_igp / GPP_COLS holds complete (igp, iw) triples
                 const int nt = my_igp / GPP_COLS, row = (my_igp % GPP_COLS) * 3 + iw;
                 tcx::bimg_store<BN>(D + (long)nt * p.kstages * tcx::Cfg<BN>::B_BYTES, p.kstages, row, ig, dv.x, dv.y);
             }
-            if (nflag > 0 && igp >= 0) {
 #pragma unroll
-                for (int j = 0; j < NVC; ++j)
-                    if (j < nflag) {
-                        float2 an = c64_to_f32(p.aqsn[(long)(p.n1base + j) * p.nc + ig]);
-                        cfmaf(acc[(j * 3 + iw) * 2 + 0], an, sch);
-                        cfmaf(acc[(j * 3 + iw) * 2 + 1], an, ssx);
-                    }
+            for (int j = 0; j < NVC; ++j) {
+                cfmaf(acc[(j * 3 + iw) * 2 + 0], an[j], sch);
+                cfmaf(acc[(j * 3 + iw) * 2 + 1], an[j], ssx);
             }
         }
     }
@@ -318,7 +346,7 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_mixed_kernel(PrepArgs p) {
     double2 accd[NVC * 6];
     block_sum_ff<NVC * 6>(acc, sm, accd);
     if (tid < nflag * 6) {
-        int j = tid / 6, r = tid % 6;
+        const int j = tid / 6, r = tid % 6;
 #pragma unroll
         for (int i = 0; i < NVC * 6; ++i)
             if (i == tid) p.F[(((long)ch * p.nv + p.n1base + j) * p.ng + my_igp) * 6 + r] = accd[i];
@@ -338,83 +366,72 @@ FK_DEV void warp_sum(double2 (&v)[NV]) {
         }
 }
 
-// Flag bands: one thread per (n1, my_igp, iw, kind) sums its chunk partials in
-// order and applies the reference's weight (sch: 0.5*vcoul*conj(aqsm),
-// BGW-Kernels/gppKer.cpp:346,421; ssx: occ*vcoul*conj(aqsm), :419).
-// FW[n1][my_igp][6].
-__global__ void flag_weights_kernel(int nv, int ng, long ldm, int nch, const double2* F, const double2* aqsm,
-                                    const double* vcoul, const int* igp, const int* acol, double2* FW) {
-    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long)nv * ng * 6) return;
-    const int r = (int)(t % 6);
-    const int my_igp = (int)((t / 6) % ng), n1 = (int)(t / (6L * ng));
-    double2 s = make_double2(0.0, 0.0);
-    for (int ch = 0; ch < nch; ++ch) s = cadd(s, F[(((long)ch * nv + n1) * ng + my_igp) * 6 + r]);
-    const int g = igp[my_igp];
-    double2 o = make_double2(0.0, 0.0);
-    if (g >= 0) {
-        const double2 cm = cconj(aqsm[(long)n1 * ldm + acol[my_igp]]);
-        const double v = vcoul[g], occ = 1.0;
-        o = cscale(cmul(cm, s), (r & 1) ? occ * v : 0.5 * v);
+// Fixed shuffle tree: lane 0 receives the sum of the 32 lanes' values.
+FK_DEV double2 warp_tree(double2 v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        v.x = __dadd_rn(v.x, __shfl_down_sync(0xffffffffu, v.x, off));
+        v.y = __dadd_rn(v.y, __shfl_down_sync(0xffffffffu, v.y, off));
     }
-    FW[((long)n1 * ng + my_igp) * 6 + r] = o;
+    return v;
 }
 
-// Per-band sums: one thread per (band, complex component c of 7) adds its
-// partials in a fixed order.  rows[n1][8] = {sch iw0..2, ssx iw0..2, stat, 0}.
-// The last block to finish adds the bands in order and writes
-// out = [achtemp 3 | asxtemp 3 | achstemp | acht_n1_loc nb].
-__global__ void rows_totals_kernel(int nb, int nv, int ng, int nslots, const double2* P, int nslots_s,
-                                   const double2* S, const double2* FW, double2* rows, unsigned* counter,
-                                   double2* out) {
-    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < (long)nb * 7) {
-        const int n1 = (int)(t / 7), c = (int)(t % 7);
-        double2 v = make_double2(0.0, 0.0);
-        if (c == 6) {
-            if (S)
-                for (int s = 0; s < nslots_s; ++s) v = cadd(v, S[(long)s * nb + n1]);
-        } else if (n1 >= nv) {
-            if (c < 3) {
-                const int M = nb - nv, m = n1 - nv;
-                for (int s = 0; s < nslots; ++s) v = cadd(v, P[((long)s * M + m) * 3 + c]);
-            }
-        } else {
-            const int iw = c % 3, kind = c / 3;  // kind 0: sch, 1: ssx
-            for (int h = 0; h < ng; ++h) v = cadd(v, FW[((long)n1 * ng + h) * 6 + iw * 2 + kind]);
+// Per-band sums, one warp per (band n1, component c of 7); the lanes split the
+// partials, so every load of a sum is in flight at once, and a fixed shuffle
+// tree adds them (deterministic).  rows[n1][8] = {sch iw0..2, ssx iw0..2, stat, 0}.
+//   n1 >= nvband, c < 3: the contraction's k-slice partials P[slot][m][3];
+//   n1 <  nvband, c < 6: over columns my_igp, the chunk partials of the prep
+//     F[ch][n1][my_igp][6] times the reference's weight (sch: 0.5*vcoul*conj(aqsm),
+//     BGW-Kernels/gppKer.cpp:346,421; ssx: occ*vcoul*conj(aqsm), :419);
+//   c == 6: the static-remainder partials S[slot][n1].
+__global__ void rows_kernel(int nb, int nv, int ng, int nslots, const double2* P, int nslots_s, const double2* S,
+                            int nch, const double2* F, long ldm, const double2* aqsm, const double* vcoul,
+                            const int* igp, const int* acol, double2* rows) {
+    const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= (long)nb * 7) return;  // w is uniform over the warp
+    const int n1 = (int)(w / 7), c = (int)(w % 7);
+    double2 v = make_double2(0.0, 0.0);
+    if (c == 6) {
+        if (S && lane < nslots_s) v = ordered_sum(S + (long)lane * nb + n1, 32L * nb, (nslots_s - lane + 31) / 32);
+    } else if (n1 >= nv) {
+        const long M = nb - nv, m = n1 - nv;
+        if (c < 3 && lane < nslots) v = ordered_sum(P + ((long)lane * M + m) * 3 + c, 32 * M * 3, (nslots - lane + 31) / 32);
+    } else {
+        const int kind = c / 3, r = (c % 3) * 2 + kind;  // kind 0: sch, 1: ssx
+        const double occ = 1.0;
+        for (int h = lane; h < ng; h += 32) {
+            const int g = igp[h];
+            if (g < 0) continue;
+            const double2 sum = ordered_sum(F + ((long)n1 * ng + h) * 6 + r, (long)nv * ng * 6, nch);
+            const double2 cm = cconj(aqsm[(long)n1 * ldm + acol[h]]);
+            v = cadd(v, cscale(cmul(cm, sum), kind ? occ * vcoul[g] : 0.5 * vcoul[g]));
         }
-        rows[(long)n1 * 8 + c] = v;
     }
-    __shared__ bool last;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    // component c is summed by warp c % 4: lanes take bands lane, lane+32, ...
-    // in order, then a fixed shuffle tree
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int c = w; c < 7; c += (int)(blockDim.x >> 5)) {
-        double2 tot = make_double2(0.0, 0.0);
-        for (int r = lane; r < nb; r += 32) tot = cadd(tot, rows[(long)r * 8 + c]);
-        for (int off = 16; off > 0; off >>= 1) {
-            tot.x += __shfl_down_sync(0xffffffffu, tot.x, off);
-            tot.y += __shfl_down_sync(0xffffffffu, tot.y, off);
-        }
-        if (lane == 0) out[c] = tot;
+    v = warp_tree(v);
+    if (lane == 0) rows[(long)n1 * 8 + c] = v;
+}
+
+// Totals over bands, one warp per component (same split and tree), and the
+// per-band sch at iw = 2.  out = [achtemp 3 | asxtemp 3 | achstemp | acht_n1_loc nb].
+__global__ void totals_kernel(int nb, const double2* rows, double2* out) {
+    const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
+    if (c < 7) {
+        double2 v = lane < nb ? ordered_sum(rows + (long)lane * 8 + c, 32L * 8, (nb - lane + 31) / 32)
+                              : make_double2(0.0, 0.0);
+        v = warp_tree(v);
+        if (lane == 0) out[c] = v;
     }
-    if (threadIdx.x == 0) *counter = 0u;
     for (int r = threadIdx.x; r < nb; r += blockDim.x) out[7 + r] = rows[(long)r * 8 + 2];  // acht_n1_loc
 }
 
 struct Plan {
-    int nch, passes;
+    int nch, tile, passes;
     int BN, kstages, units;      // tensor-core contraction (mixed)
     int MT, NT, KS, kchunk;      // main contraction
     int MTs, NTs, KSs, kchunks;  // static remainder contraction
     bool mixed;
-    size_t bytesD, bytesF, bytesP, bytesS, bytesFW, bytesRows, bytesIgp, bytesW;
+    size_t bytesD, bytesF, bytesP, bytesS, bytesRows, bytesIgp, bytesW;
 };
 
 // k-slice count for the persistent tensor-core kernel: the fewest slices
@@ -445,7 +462,20 @@ void pick_split(int tiles, int K, int target, int& KS, int& kchunk) {
 Plan make_plan(const Ctx& c, const GppDev& r) {
     Plan p{};
     p.mixed = r.prec == FK_MIXED;
-    p.nch = ceil_div(r.nc, r.prec == FK_MIXED ? PREPM_TILE : PREP_TILE);
+    if (r.prec == FK_MIXED) {
+        // one wave: chunks x ngpown blocks fill the resident block slots
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, prep_mixed_kernel<0, 64>, PREP_THREADS, 0) !=
+                cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        const int nch = std::max(1, per_sm * c.sms / r.ng);
+        p.tile = ceil_div(ceil_div(r.nc, nch), PREP_THREADS) * PREP_THREADS;
+        p.nch = ceil_div(r.nc, p.tile);
+    } else {
+        p.tile = PREP_TILE;
+        p.nch = ceil_div(r.nc, PREP_TILE);
+    }
     p.passes = std::max(1, ceil_div(r.nv, NVC));
     const int M = r.nb - r.nv, N = 3 * r.ng;
     if (p.mixed) {
@@ -472,9 +502,8 @@ Plan make_plan(const Ctx& c, const GppDev& r) {
     p.bytesF = (size_t)p.nch * std::max(r.nv, 1) * r.ng * 6 * sizeof(double2);
     p.bytesP = M > 0 ? (size_t)p.KS * p.NT * M * 3 * sizeof(double2) : 0;
     p.bytesS = (r.flags & FK_GPP_ACHSTEMP) ? (size_t)p.KSs * p.NTs * r.nb * sizeof(double2) : 0;
-    p.bytesFW = (size_t)std::max(r.nv, 1) * r.ng * 6 * sizeof(double2);
     p.bytesRows = (size_t)r.nb * 8 * sizeof(double2);
-    p.bytesIgp = 2 * (size_t)r.ng * sizeof(int) + 256;  // igp, acol, the totals counter
+    p.bytesIgp = 2 * (size_t)r.ng * sizeof(int);  // igp, acol
     return p;
 }
 
@@ -487,7 +516,7 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 
 size_t gpp_workspace(const Ctx& c, const GppDev& r) {
     Plan p = make_plan(c, r);
-    return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesFW + p.bytesRows + p.bytesIgp + p.bytesW + 10 * 256;
+    return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesRows + p.bytesIgp + p.bytesW + 10 * 256;
 }
 
 fk_status gpp_run(Ctx& c, const GppDev& r) {
@@ -495,15 +524,13 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
     cudaStream_t st = c.stream;
     int* igp = (int*)c.ws.take(p.bytesIgp);
     int* acol = igp + r.ng;
-    unsigned* counter = (unsigned*)((char*)igp + (p.bytesIgp - 256));
     void* D = p.bytesD ? c.ws.take(p.bytesD) : nullptr;
     double2* F = (double2*)c.ws.take(p.bytesF);
     double2* P = p.bytesP ? (double2*)c.ws.take(p.bytesP) : nullptr;
     double2* S = p.bytesS ? (double2*)c.ws.take(p.bytesS) : nullptr;
-    double2* FW = (double2*)c.ws.take(p.bytesFW);
     double2* rows = (double2*)c.ws.take(p.bytesRows);
     float2* W = p.bytesW ? (float2*)c.ws.take(p.bytesW) : nullptr;
-    if (!igp || !F || !FW || !rows || (p.bytesD && !D) || (p.bytesP && !P) || (p.bytesS && !S) || (p.bytesW && !W))
+    if (!igp || !F || !rows || (p.bytesD && !D) || (p.bytesP && !P) || (p.bytesS && !S) || (p.bytesW && !W))
         return fail(c, FK_ENOMEM, "workspace too small for GPP request");
     if (p.mixed && D) {
         cudaError_t e = cudaMemsetAsync(D, 0, p.bytesD, st);  // padding rows and k >= ncouls stay zero
@@ -518,7 +545,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
     ++c.launches;
     for (int pass = 0; pass < p.passes; ++pass) {
         PrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, pass == 0 ? D : nullptr, p.kstages,
-                   F, p.nch, pass * NVC};
+                   F, p.nch, p.tile, pass * NVC};
         dim3 grid(p.nch, r.ng);
         if (p.mixed) {
             if (Q) prep_mixed_kernel<1, 64><<<grid, PREP_THREADS, 0, st>>>(a);
@@ -547,6 +574,8 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
             t.kstages_total = p.kstages;
             t.MT = p.MT; t.NT = p.NT; t.units = p.units;
             t.err = c.errword;
+            if (tcx::encode_rows_map(&t.amap, r.aqsn, r.nc, r.nc, r.nb) != cudaSuccess)
+                return fail(c, FK_ECUDA, "gpp: cannot describe aqsntemp as a tensor map (needs a 16-byte aligned array)");
             cudaMemsetAsync(c.errword, 0, sizeof(int), st);
             const int grid1 = std::min(p.units, c.sms);
             auto k = tcx::tc_contract_kernel<EPI_GPP, 64, false>;
@@ -579,15 +608,10 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
         ++c.launches;
     }
     phase_mark(c, 3);
-    if (r.nv > 0) {
-        flag_weights_kernel<<<ceil_div(r.nv * r.ng * 6, 128), 128, 0, st>>>(r.nv, r.ng, r.ldm, p.nch, F, r.aqsm,
-                                                                            r.vcoul, igp, acol, FW);
-        ++c.launches;
-    }
-    cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
-    rows_totals_kernel<<<ceil_div(r.nb * 7, 128), 128, 0, st>>>(r.nb, r.nv, r.ng, p.KS * p.NT, P, p.KSs * p.NTs, S,
-                                                                FW, rows, counter, r.out);
-    c.launches += 1;
+    rows_kernel<<<ceil_div(r.nb * 7, 8), 256, 0, st>>>(r.nb, r.nv, r.ng, p.KS * p.NT, P, p.KSs * p.NTs, S, p.nch, F,
+                                                       r.ldm, r.aqsm, r.vcoul, igp, acol, rows);
+    totals_kernel<<<1, 256, 0, st>>>(r.nb, rows, r.out);
+    c.launches += 2;
     phase_mark(c, 4);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "gpp kernels");

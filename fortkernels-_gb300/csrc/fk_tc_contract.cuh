@@ -24,6 +24,7 @@
 // i, i + gridDim.x, ...  Every wait is bounded; on timeout the CTA records
 // an error code and unwinds without further waits of unbounded length.
 #pragma once
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include "fk_gemm.cuh"
@@ -43,9 +44,10 @@ constexpr long long WAIT_LIMIT = 4000000000LL;  // ~2 s at 2 GHz
 template <int BN, bool WSMEM = false>
 struct Cfg {
     static_assert(BN == 64, "four accumulators x two buffers fill the 512 TMEM columns at BN = 64");
-    // WSMEM (FF): the per-unit weight tile conj(aqsm)[BN][BM] lives in shared
-    // memory, which leaves room for two operand stages.
-    static constexpr int STAGES = WSMEM ? 2 : 3;
+    // Two operand stages.  WSMEM (FF): the per-unit weight tile conj(aqsm)[BN][BM]
+    // lives in shared memory.  Otherwise (GPP) a 64 KB staging buffer receives
+    // the next stage's FP64 A rows by bulk copy while the current one converts.
+    static constexpr int STAGES = 2;
     static constexpr int CHUNK_STAGES = 2;  // k-values per TMEM accumulation = 64
     static constexpr uint32_t A_BYTES = NSUB * BM * 64;
     static constexpr uint32_t B_BYTES = NSUB * BN * 64;
@@ -53,10 +55,12 @@ struct Cfg {
     static constexpr uint32_t ACC_COLS = 4 * BN;       // main re, main im, corr re, corr im
     static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;  // double buffered
     static constexpr uint32_t W_BYTES = WSMEM ? (uint32_t)(BN * BM * sizeof(float2) + 4 * BN * sizeof(float)) : 0u;
-    static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + W_BYTES + 1024 + 256;
+    static constexpr uint32_t F64_BYTES = WSMEM ? 0u : (uint32_t)(BM * BK * sizeof(double2));
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + W_BYTES + F64_BYTES + 1024 + 256;
 };
 
 struct TcArgs {
+    CUtensorMap amap;     // GPP: A (FP64 complex rows) as a 2-D FP64 tensor, box 64 x BM, zero fill
     ContractArgs c;       // shapes, partial buffer (same meaning as fk_gemm.cuh)
     const uint8_t* Bimg;  // pre-split B tiles: [plane][nt][kstage][NSUB][BN rows][64 B]
     const uint8_t* Aimg;  // pre-split A tiles [mt][kstage][NSUB][BM rows][64 B] (AIMG kernels only)
@@ -107,21 +111,24 @@ __device__ __forceinline__ void bimg_store(uint8_t* img_nt, int kstage_total_unu
 }
 
 template <int EPI, int BN, bool AIMG>
-__global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(TcArgs t) {
+__global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(const __grid_constant__ TcArgs t) {
     using C = Cfg<BN, EPI == EPI_FF>;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-aligned operand area
     uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     float2* sW = (float2*)(base + C::STAGES * C::STAGE_BYTES);  // FF: [BN][BM] conj(aqsm)
     float* sV = (float*)(sW + BN * BM);                           // FF: vcoul[BN], one copy per epilogue warp
-    uint64_t* bars = (uint64_t*)(base + C::STAGES * C::STAGE_BYTES + C::W_BYTES);
+    double2* sF = (double2*)(base + C::STAGES * C::STAGE_BYTES + C::W_BYTES);  // GPP: FP64 rows [BM][BK]
+    uint64_t* bars = (uint64_t*)(base + C::STAGES * C::STAGE_BYTES + C::W_BYTES + C::F64_BYTES);
     uint64_t* fullA = bars;
     uint64_t* fullB = bars + C::STAGES;
     uint64_t* empty = bars + 2 * C::STAGES;
     uint64_t* accFull = bars + 3 * C::STAGES;
     uint64_t* accEmpty = accFull + 2;
     uint64_t* done = accEmpty + 2;
-    uint32_t* tslot = (uint32_t*)(done + 1);
+    uint64_t* fFull = done + 1;    // GPP: FP64 staging filled (tx bytes)
+    uint64_t* fEmpty = done + 2;   // GPP: FP64 staging read by all converter warps
+    uint32_t* tslot = (uint32_t*)(done + 3);
     __shared__ int s_abort_flag;
     volatile int& s_abort = s_abort_flag;
 
@@ -140,6 +147,8 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(TcArgs t) {
             tc::mbar_init(&accEmpty[b], 4);
         }
         tc::mbar_init(done, 1);
+        tc::mbar_init(fFull, 1);
+        tc::mbar_init(fEmpty, NCONV);
         tc::fence_barrier_init();
         s_abort = 0;
     }
@@ -232,34 +241,52 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(TcArgs t) {
             if (!tc::mbar_wait(done, 0, WAIT_LIMIT)) fail(4);
         }
     } else if (warp == 1) {
-        // -------------------------------------------------- B bulk copies
-        if (lane == 0) {
-            int g = 0;
-            bool ok = true;
-            for (int u = blockIdx.x; u < t.units && ok; u += gridDim.x) {
-                int mt, nt, ks, batch, k0, k1;
-                unit_coords(u, mt, nt, ks, batch);
-                krange(ks, k0, k1);
-                const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
-                const int plane = a.batch_plane ? a.batch_plane[batch] : batch;
-                for (int st = 0; st < nst; ++st, ++g) {
-                    const int s = g % C::STAGES;
-                    if (!tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, WAIT_LIMIT) || s_abort) {
-                        fail(8);
+        // ------------------------------------------------ bulk copies
+        // lane 0: pre-split B (and, for AIMG, A) tiles into the operand stage;
+        // all lanes (GPP): the next stage's FP64 A rows into the staging buffer.
+        int g = 0;
+        bool ok = true;
+        for (int u = blockIdx.x; u < t.units && ok; u += gridDim.x) {
+            int mt, nt, ks, batch, k0, k1;
+            unit_coords(u, mt, nt, ks, batch);
+            krange(ks, k0, k1);
+            const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
+            const int plane = a.batch_plane ? a.batch_plane[batch] : batch;
+            for (int st = 0; st < nst; ++st, ++g) {
+                const int s = g % C::STAGES;
+                const long kst = (long)(k0 / BK) + st;
+                if (!AIMG) {
+                    // FP64 rows: staging buffer free once every converter warp has read it
+                    if (!tc::mbar_wait(fEmpty, (g & 1) ^ 1, WAIT_LIMIT) || s_abort) {
+                        fail(64);
                         ok = false;
                         break;
                     }
-                    const long kst = (long)(k0 / BK) + st;
-                    const uint8_t* src =
-                        t.Bimg + (((long)plane * NTu + nt) * t.kstages_total + kst) * (long)C::B_BYTES;
-                    tc::mbar_arrive_expect_tx(&fullB[s], C::B_BYTES);
-                    tc::bulk_g2s(base + s * C::STAGE_BYTES + C::A_BYTES, src, C::B_BYTES, &fullB[s]);
-                    if (AIMG) {
-                        const uint8_t* asrc = t.Aimg + ((long)mt * t.kstages_total + kst) * (long)C::A_BYTES;
-                        tc::mbar_arrive_expect_tx(&fullA[s], C::A_BYTES);
-                        tc::bulk_g2s(base + s * C::STAGE_BYTES, asrc, C::A_BYTES, &fullA[s]);
+                    // one box: rows m0 + mt*BM .. +BM, k = kb .. kb+BK (as 2*BK doubles);
+                    // rows and columns past the array arrive as zeros and still count
+                    if (lane == 0) {
+                        tc::mbar_arrive_expect_tx(fFull, C::F64_BYTES);
+                        tc::tma_load_2d(sF, &t.amap, 2 * (k0 + st * BK), a.m0 + mt * BM, fFull);
                     }
                 }
+                if (lane == 0) {
+                    if (!tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, WAIT_LIMIT) || s_abort) {
+                        fail(8);
+                        ok = false;
+                    } else {
+                        const uint8_t* src =
+                            t.Bimg + (((long)plane * NTu + nt) * t.kstages_total + kst) * (long)C::B_BYTES;
+                        tc::mbar_arrive_expect_tx(&fullB[s], C::B_BYTES);
+                        tc::bulk_g2s(base + s * C::STAGE_BYTES + C::A_BYTES, src, C::B_BYTES, &fullB[s]);
+                        if (AIMG) {
+                            const uint8_t* asrc = t.Aimg + ((long)mt * t.kstages_total + kst) * (long)C::A_BYTES;
+                            tc::mbar_arrive_expect_tx(&fullA[s], C::A_BYTES);
+                            tc::bulk_g2s(base + s * C::STAGE_BYTES, asrc, C::A_BYTES, &fullA[s]);
+                        }
+                    }
+                }
+                ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+                if (!ok) break;
             }
         }
     } else if (warp >= 4 && warp < 8) {
@@ -366,84 +393,59 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(TcArgs t) {
         }
     } else {
         // ----------------------------------------------------- converters
-        // warp cw converts rows cw*16 .. cw*16+15 of each stage; lane = k, so
-        // every load instruction reads 512 contiguous bytes of one row.  The
-        // rows are handled in two halves and the loads of the next half are in
-        // flight while the current half is converted (software pipelining
-        // across stages), so HBM latency is not exposed once per stage.
+        // warp cw converts rows cw*16 .. cw*16+15 of each stage, lane = k:
+        // read the FP64 rows from the staging buffer (one conflict-free 512-byte
+        // row per instruction), release the buffer for the next stage's bulk
+        // copies, then split into BF16 pieces and store into the operand stage.
         if (!AIMG) {
             const int cw = warp < 4 ? warp - 2 : warp - 6;  // 0..7
             constexpr int RPW = BM / NCONV;                  // rows per converter warp
-            constexpr int HALF = RPW / 2;
-            // flattened (unit, stage) sequence of this CTA
-            struct Pos {
-                int u, st, nst, k0, k1, mt;
-            };
-            auto first = [&](Pos& p, int u) -> bool {
-                for (; u < t.units; u += gridDim.x) {
-                    int nt, ks, batch;
-                    unit_coords(u, p.mt, nt, ks, batch);
-                    krange(ks, p.k0, p.k1);
-                    p.nst = p.k1 > p.k0 ? (p.k1 - p.k0 + BK - 1) / BK : 0;
-                    if (p.nst > 0) {
-                        p.u = u;
-                        p.st = 0;
-                        return true;
-                    }
-                }
-                return false;
-            };
-            auto advance = [&](Pos& p) -> bool {
-                if (++p.st < p.nst) return true;
-                return first(p, p.u + gridDim.x);
-            };
-            auto load_half = [&](const Pos& p, int h, double2 (&v)[HALF]) {
-                const int k = p.k0 + p.st * BK + lane;
-#pragma unroll
-                for (int i = 0; i < HALF; ++i) {
-                    const int m = p.mt * BM + cw * RPW + h * HALF + i;
-                    v[i] = (m < a.M && k < p.k1) ? __ldg(a.A + (long)(a.m0 + m) * a.lda + k) : make_double2(0.0, 0.0);
-                }
-            };
-            auto store_half = [&](uint8_t* sa, int h, const double2 (&v)[HALF]) {
-#pragma unroll
-                for (int i = 0; i < HALF; ++i) {
-                    const uint32_t off = tc::sw64_offset(cw * RPW + h * HALF + i, lane);
-                    uint16_t hh, mm, ll;
-                    split3(f64_to_f32_bits(v[i].x), hh, mm, ll);
-                    *(uint16_t*)(sa + 0 * BM * 64 + off) = hh;
-                    *(uint16_t*)(sa + 1 * BM * 64 + off) = mm;
-                    *(uint16_t*)(sa + 2 * BM * 64 + off) = ll;
-                    split3(f64_to_f32_bits(v[i].y), hh, mm, ll);
-                    *(uint16_t*)(sa + 3 * BM * 64 + off) = hh;
-                    *(uint16_t*)(sa + 4 * BM * 64 + off) = mm;
-                    *(uint16_t*)(sa + 5 * BM * 64 + off) = ll;
-                }
-            };
-            Pos cur;
-            bool have = first(cur, blockIdx.x);
-            double2 va[HALF], vb[HALF];
-            if (have) load_half(cur, 0, va);
             int g = 0;
-            while (have) {
-                const int s = g % C::STAGES;
-                load_half(cur, 1, vb);
-                if (!tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, WAIT_LIMIT) || s_abort) {
-                    fail(32);
-                    break;
+            bool ok = true;
+            for (int u = blockIdx.x; u < t.units && ok; u += gridDim.x) {
+                int mt, nt, ks, batch, k0, k1;
+                unit_coords(u, mt, nt, ks, batch);
+                krange(ks, k0, k1);
+                const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
+                for (int st = 0; st < nst; ++st, ++g) {
+                    const int s = g % C::STAGES;
+                    const int k = k0 + st * BK + lane;
+                    if (!tc::mbar_wait(fFull, g & 1, WAIT_LIMIT) || s_abort) {
+                        fail(32);
+                        ok = false;
+                        break;
+                    }
+                    double2 v[RPW];
+#pragma unroll
+                    for (int i = 0; i < RPW; ++i) {
+                        const int r = cw * RPW + i;
+                        v[i] = (mt * BM + r < a.M && k < k1) ? sF[r * BK + lane] : make_double2(0.0, 0.0);
+                    }
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(fEmpty);
+                    if (!tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, WAIT_LIMIT) || s_abort) {
+                        fail(32);
+                        ok = false;
+                        break;
+                    }
+                    uint8_t* sa = base + s * C::STAGE_BYTES;
+#pragma unroll
+                    for (int i = 0; i < RPW; ++i) {
+                        const uint32_t off = tc::sw64_offset(cw * RPW + i, lane);
+                        uint16_t hh, mm, ll;
+                        split3(f64_to_f32_bits(v[i].x), hh, mm, ll);
+                        *(uint16_t*)(sa + 0 * BM * 64 + off) = hh;
+                        *(uint16_t*)(sa + 1 * BM * 64 + off) = mm;
+                        *(uint16_t*)(sa + 2 * BM * 64 + off) = ll;
+                        split3(f64_to_f32_bits(v[i].y), hh, mm, ll);
+                        *(uint16_t*)(sa + 3 * BM * 64 + off) = hh;
+                        *(uint16_t*)(sa + 4 * BM * 64 + off) = mm;
+                        *(uint16_t*)(sa + 5 * BM * 64 + off) = ll;
+                    }
+                    tc::fence_proxy_async_smem();
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(&fullA[s]);
                 }
-                uint8_t* sa = base + s * C::STAGE_BYTES;
-                store_half(sa, 0, va);
-                Pos nxt = cur;
-                const bool more = advance(nxt);
-                if (more) load_half(nxt, 0, va);
-                store_half(sa, 1, vb);
-                tc::fence_proxy_async_smem();
-                __syncwarp();
-                if (lane == 0) tc::mbar_arrive(&fullA[s]);
-                cur = nxt;
-                have = more;
-                ++g;
             }
         }
     }
@@ -496,6 +498,35 @@ static __global__ void aimg_convert_kernel(const double2* src, int rows, int K, 
     const double2 v = src[(long)m * K + k];
     uint8_t* tile = img + ((long)(m / BM) * kstages) * (long)(BM * NSUB * 64);
     img_store<BM>(tile, m % BM, k, f64_to_f32_bits(v.x), f64_to_f32_bits(v.y));
+}
+
+// Host: A (rows of complex FP64, row stride lda complex elements) as a 2-D FP64
+// tensor map for tma_load_2d: inner extent 2*K doubles, `rows` rows, box
+// 2*BK doubles x BM rows, elements outside the extents read as zero.  The
+// encoder comes from the driver through the runtime, so the library links
+// only the CUDA runtime.
+inline cudaError_t encode_rows_map(CUtensorMap* map, const double2* A, long lda, int K, int rows) {
+    using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static const Encode fn = []() -> Encode {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return (Encode)f;
+    }();
+    if (!fn) return cudaErrorNotSupported;
+    const cuuint64_t dims[2] = {(cuuint64_t)2 * K, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)lda * sizeof(double2)};
+    const cuuint32_t box[2] = {2 * BK, BM};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, (void*)A, dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
 }  // namespace tcx

@@ -138,6 +138,40 @@ def test_gpp_device_pointers_equal_host_pointers(ctx, fk):
         np.testing.assert_array_equal(dev[k].cpu().numpy(), host[k])
 
 
+def test_gpp_misaligned_device_arrays(ctx, fk):
+    """Device arrays that start 8 bytes past a 16-byte boundary are copied into
+    the workspace (the kernels move rows with 16-byte and bulk copies) and give
+    the same bits as host arrays."""
+    import ctypes
+    import torch
+    nb, nv, nc, ng = 70, 2, 1500, 11
+    p = fk.inputs.gpp_synthetic(nb, nv, nc, ng, seed=13, dist="branch", wx="stress")
+    keep = []
+
+    def dev(a, dtype):
+        raw = np.ascontiguousarray(a, dtype).view(np.uint8).ravel()
+        t = torch.zeros(raw.size + 8, dtype=torch.uint8, device="cuda")
+        t[8:] = torch.from_numpy(raw).cuda()
+        keep.append(t)
+        assert (t.data_ptr() + 8) % 16 == 8
+        return ctypes.c_void_p(t.data_ptr() + 8)
+
+    args = [dev(p["aqsmtemp"], np.complex128), dev(p["aqsntemp"], np.complex128),
+            dev(p["I_eps_array"], np.complex128), dev(p["wtilde_array"], np.complex128),
+            dev(p["vcoul"], np.float64), dev(p["inv_igp_index"], np.int32), dev(p["indinv"], np.int32),
+            dev(p["wx_array"], np.float64)]
+    for prec, code in (("fp64", fk.FK_FP64), ("mixed", fk.FK_MIXED)):
+        want = ctx.gpp(p, prec)
+        got = {"achtemp": np.zeros(3, np.complex128), "asxtemp": np.zeros(3, np.complex128),
+               "acht_n1_loc": np.zeros(nb, np.complex128)}
+        st = ctx.lib.fk_gpp(ctx.h, nb, nv, nc, ng, *args, code, 0,
+                            *[ctypes.c_void_p(got[k].ctypes.data) for k in ("achtemp", "asxtemp", "acht_n1_loc")],
+                            None)
+        assert st == 0, ctx.lib.fk_last_error(ctx.h)
+        for k in got:
+            np.testing.assert_array_equal(got[k], want[k])
+
+
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_gpp_bitwise_deterministic(ctx, fk, prec):
     p = fk.inputs.gpp_synthetic(200, 2, 3000, 24, seed=11, dist="uniform")
