@@ -22,7 +22,7 @@ FK_FF_SPLIT_ACHD = 0x4
 # Every symbol include/fk_abi.h declares.
 SYMBOLS = ("fk_create", "fk_destroy", "fk_set_stream", "fk_synchronize", "fk_reserve", "fk_strerror",
            "fk_last_error", "fk_version", "fk_gpp", "fk_ff", "fk_set_profiling", "fk_last_timings",
-           "fk_last_launches")
+           "fk_last_launches", "fk_gpp_static")
 
 
 class FKError(RuntimeError):
@@ -58,6 +58,7 @@ def load(path: str = LIB_PATH):
     L.fk_version.restype = ctypes.c_char_p
     L.fk_gpp.argtypes = [P, I, I, I, I] + [P] * 8 + [I, U] + [P] * 4
     L.fk_ff.argtypes = [P] + [I] * 6 + [P] * 11 + [D] * 4 + [I, U] + [P] * 6
+    L.fk_gpp_static.argtypes = [P, I, I, I, I] + [P] * 8 + [U] + [P] * 4
     L.fk_set_profiling.argtypes = [P, I]
     L.fk_last_timings.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
     L.fk_last_launches.argtypes = [P]

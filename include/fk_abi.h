@@ -113,6 +113,50 @@ fk_status fk_gpp(fk_ctx_t ctx, int number_bands, int nvband, int ncouls, int ngp
                  const double* wx_array, fk_precision precision, unsigned flags,
                  fk_c128* achtemp, fk_c128* asxtemp, fk_c128* acht_n1_loc, fk_c128* achstemp);
 
+/* Device scratch compiled into the library for fk_gpp_static, per GPU. */
+#define FK_GPP_STATIC_SCRATCH_BYTES (64u << 20)
+
+/*
+ * fk_gpp_static: the FP64 GPP sum of fk_gpp (same arguments and results as
+ * fk_gpp with precision FK_FP64) for callers that must not allocate device
+ * memory: a process whose GPU memory is already owned by another allocator
+ * (a framework's caching pool that has reserved the device), or a loop that
+ * cannot take the device-wide synchronisation of cudaMalloc/cudaFree.  No
+ * counterpart in the reference.
+ *
+ * Memory: every intermediate lives in one fixed array of
+ * FK_GPP_STATIC_SCRATCH_BYTES (64 MiB) of device memory per GPU, module data
+ * of the library; the call makes no cudaMalloc, cudaFree or other allocating
+ * call.  A request needs 48*ngpown*ncouls bytes plus its partial sums and
+ * per-band rows (about 1 MB at number_bands = 512; the benchmark size
+ * 512 2 32768 20 needs about 33 MB in all).  A request that does not fit
+ * returns FK_ENOMEM before any work is queued.  Nothing in the scratch needs
+ * to start at zero: every value a call reads was written earlier in the same
+ * call.
+ *
+ * Set-up: the first call on each device looks up the array's address
+ * (cudaGetSymbolAddress), which may load that part of the library onto the
+ * GPU; make the first call on a device before any stream capture.
+ *
+ * Concurrency: all calls on one GPU share the one array.  Calls whose work
+ * overlaps in time (from different threads, or on different streams without
+ * an event between them) overwrite each other's intermediates and return
+ * wrong results: serialise them.
+ *
+ * Arguments: stream is a cudaStream_t of the calling thread's current device
+ * (NULL: the legacy default stream).  Every input array must be device memory
+ * starting on a 16-byte boundary (else FK_EINVAL: staging a host array would
+ * need memory).  Outputs may be device memory (the call only enqueues work)
+ * or host memory (the call waits for the stream).  Errors are status codes
+ * only (there is no context to hold a message).
+ */
+fk_status fk_gpp_static(void* stream, int number_bands, int nvband, int ncouls, int ngpown,
+                        const fk_c128* aqsmtemp, const fk_c128* aqsntemp,
+                        const fk_c128* I_eps_array, const fk_c128* wtilde_array,
+                        const double* vcoul, const int* inv_igp_index, const int* indinv,
+                        const double* wx_array, unsigned flags,
+                        fk_c128* achtemp, fk_c128* asxtemp, fk_c128* acht_n1_loc, fk_c128* achstemp);
+
 /* -------------------------------------------------------------------- FF */
 
 /* Flags for fk_ff */
