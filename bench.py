@@ -104,6 +104,81 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(sm)}
 
 
+class NvmlSampler:
+    """SM clock, power and clock-event reasons read through NVML
+    (libnvidia-ml, by ctypes) every ~0.5 ms while the timed region runs."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, cuda_index=0):
+        import ctypes
+        self.ct = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        ok = False
+        try:
+            import torch
+            pr = torch.cuda.get_device_properties(cuda_index)
+            bus = "%08x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+            ok = self.lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(self.h)) == 0
+        except Exception:
+            ok = False
+        if not ok and self.lib.nvmlDeviceGetHandleByIndex_v2(cuda_index, ctypes.byref(self.h)) != 0:
+            raise OSError("no NVML handle")
+        self.rows, self.stop = [], threading.Event()
+        v = ctypes.c_uint()
+        self.max_mhz = float(v.value) if self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(v)) == 0 else None
+
+    def _sample(self):
+        ct, L = self.ct, self.lib
+        clk, pw, rs = ct.c_uint(), ct.c_uint(), ct.c_ulonglong()
+        while not self.stop.is_set():
+            if L.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(clk)) == 0:
+                L.nvmlDeviceGetPowerUsage(self.h, ct.byref(pw))
+                r = rs.value if L.nvmlDeviceGetCurrentClocksEventReasons(self.h, ct.byref(rs)) == 0 else 0
+                self.rows.append((float(clk.value), pw.value / 1000.0, r))
+            time.sleep(0.0005)
+
+    def __enter__(self):
+        self.t = threading.Thread(target=self._sample, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=2)
+
+    def summary(self):
+        sm = [r[0] for r in self.rows]
+        bits = 0
+        for r in self.rows:
+            bits |= r[2]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(n for b, n in self.REASONS.items() if bits & b),
+                "power_w_median": statistics.median(r[1] for r in self.rows) if self.rows else None,
+                "samples": len(sm), "source": "nvml"}
+
+
+def clock_sampler(index):
+    try:
+        return NvmlSampler(index)
+    except (OSError, AttributeError):
+        return ClockSampler(index)
+
+
+def measured_traffic(w):
+    """DRAM bytes per launch of the dominant kernel from a committed ncu
+    capture summary (profiles/traffic.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            t = json.load(f)
+        return t.get(w["name"], {}).get("dram_bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -234,9 +309,14 @@ def run_ours(a, w):
     prec = a.precision
     other = "fp64" if prec == "mixed" else "mixed"
     barrier()
-    with ClockSampler(local) as clk:
+    for _ in range(a.warmup):
+        call(prec)
+    barrier()
+    with clock_sampler(local) as clk:
         barrier()
-        per = timed(torch, stream, lambda: call(prec), a.steps, a.warmup, per_step=False)
+        torch.cuda.nvtx.range_push("timed")
+        per = timed(torch, stream, lambda: call(prec), a.steps, 0, per_step=False)
+        torch.cuda.nvtx.range_pop()
         barrier()
     ms = per[0]
     if world > 1:
@@ -305,7 +385,7 @@ def run_ours(a, w):
             "latency_ms": {"p50": statistics.median(lat), "p99": float(np.percentile(lat, 99))},
             "phase_ms": {"staging": phase[0], "prep": phase[1], "contraction": phase[2], "reduction": phase[3]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                         "frac": (achieved / hbm) if achieved else None, "traffic": measured_traffic(w),
                          "kernel": "contraction", "algorithmic_bytes": byts, "algorithmic_flops": flops,
                          "achieved_tflops": flops / (kms * 1e-3) / 1e12 if kms > 0 else None,
                          "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
@@ -359,7 +439,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
-    w = WORKLOADS[a.workload]
+    w = dict(WORKLOADS[a.workload], name=a.workload)
     if a.impl == "reference":
         run_reference(a, w)
     else:

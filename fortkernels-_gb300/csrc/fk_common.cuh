@@ -56,13 +56,25 @@ FK_DEV float2 c64_to_f32(double2 v) { return make_float2(f64_to_f32_bits(v.x), f
 // memory once per group instead of once per term.
 FK_DEV double2 ordered_sum(const double2* x, long stride, int n) {
     double2 s = make_double2(0.0, 0.0);
-    for (int i0 = 0; i0 < n; i0 += 8) {
+    int i0 = 0;
+    for (; i0 + 8 <= n; i0 += 8) {
+        double2 v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = x[(long)(i0 + j) * stride];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s = cadd(s, v[j]);
+    }
+    // tail: loads still issued together, adds only for the terms that exist
+    // (predicated-off FP64 adds would still occupy the narrow FP64 pipe)
+    if (i0 < n) {
         double2 v[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) v[j] = i0 + j < n ? x[(long)(i0 + j) * stride] : make_double2(0.0, 0.0);
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-            if (i0 + j < n) s = cadd(s, v[j]);
+        for (int j = 0; j < 8; ++j) {
+            if (i0 + j >= n) break;
+            s = cadd(s, v[j]);
+        }
     }
     return s;
 }

@@ -122,8 +122,9 @@ FK_DEV void block_sum(double2 (&v)[NV], double2* sm /* [8][NV] */) {
 }
 
 // Fixed-order block sum of FP32 values carried as float-float pairs (TwoSum
-// at every level), finished in FP64 across warps: FP32 instructions only in
-// the shuffle tree (the FP64 pipe of GB300 is narrow).
+// at every level, across the warps too); thread v < NV of the block widens
+// its pair to FP64 once.  FP32 instructions everywhere but that last step:
+// the FP64 pipe of GB300 takes ~16 cycles per warp instruction.
 template <int NV>
 FK_DEV void block_sum_ff(float2 (&v)[NV], double2* sm /* [8][NV] */, double2 (&out)[NV]) {
     float2 lo[NV];
@@ -143,16 +144,23 @@ FK_DEV void block_sum_ff(float2 (&v)[NV], double2* sm /* [8][NV] */, double2 (&o
         }
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float4* sm4 = reinterpret_cast<float4*>(sm);  // [warp][NV] (hi.x, hi.y, lo.x, lo.y)
     if (lane == 0)
 #pragma unroll
-        for (int i = 0; i < NV; ++i)
-            sm[warp * NV + i] = make_double2((double)v[i].x + (double)lo[i].x, (double)v[i].y + (double)lo[i].y);
+        for (int i = 0; i < NV; ++i) sm4[warp * NV + i] = make_float4(v[i].x, v[i].y, lo[i].x, lo[i].y);
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < NV; ++i) out[i] = make_double2(0.0, 0.0);
     if (threadIdx.x < NV) {
-        double2 s = make_double2(0.0, 0.0);
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s = cadd(s, sm[w * NV + threadIdx.x]);
+        ff32 a{0.f, 0.f}, b{0.f, 0.f};
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            const float4 q = sm4[w * NV + threadIdx.x];
+            a.lo += q.z;
+            b.lo += q.w;
+            ff_add(a, q.x);
+            ff_add(b, q.y);
+        }
+        const double2 s = make_double2((double)a.hi + (double)a.lo, (double)b.hi + (double)b.lo);
 #pragma unroll
         for (int i = 0; i < NV; ++i)
             if (i == (int)threadIdx.x) out[i] = s;
@@ -408,7 +416,9 @@ __global__ void rows_kernel(int nb, int nv, int ng, int nslots, const double2* P
             v = cadd(v, cscale(cmul(cm, sum), kind ? occ * vcoul[g] : 0.5 * vcoul[g]));
         }
     }
-    v = warp_tree(v);
+    // components with no terms (ssx of bands >= nvband, stat without S) skip the tree
+    const bool empty = (c == 6 && !S) || (n1 >= nv && c >= 3 && c < 6);
+    if (!empty) v = warp_tree(v);
     if (lane == 0) rows[(long)n1 * 8 + c] = v;
 }
 
