@@ -544,6 +544,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
         return fail(c, FK_ENOMEM, "workspace too small for GPP request");
     if (p.mixed && D) {
         cudaError_t e = cudaMemsetAsync(D, 0, p.bytesD, st);  // padding rows and k >= ncouls stay zero
+        if (e == cudaSuccess) e = cudaMemsetAsync(c.errword, 0, sizeof(int), st);  // bounded-wait status
         if (e != cudaSuccess) return cuda_fail(c, e, "gpp: image clear");
     }
     const bool Q = (r.flags & FK_GPP_ROOT_QUIRKS) != 0;
@@ -553,6 +554,12 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
     phase_mark(c, 1);
     igp_map_kernel<<<ceil_div(r.ng, 128), 128, 0, st>>>(r.ng, r.nc, r.inv, r.indinv, r.aqsm_compact ? 1 : 0, igp, acol);
     ++c.launches;
+    if (p.mixed && M > 0) {
+        // epilogue weights of the contraction (independent of the prep)
+        tcx::weight_table_kernel<<<dim3(ceil_div(M, 128), r.ng), 128, 0, st>>>(M, r.nv, r.ng, r.aqsm, r.ldm, r.vcoul,
+                                                                            igp, acol, 0.5, W, nullptr, nullptr);
+        ++c.launches;
+    }
     for (int pass = 0; pass < p.passes; ++pass) {
         PrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, pass == 0 ? D : nullptr, p.kstages,
                    F, p.nch, p.tile, pass * NVC};
@@ -575,8 +582,6 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
         a.aqsm = r.aqsm; a.ldm = r.ldm; a.vcoul = r.vcoul; a.igp = igp; a.acol = acol; a.wscale = 0.5; a.G = 3; a.P = P;
         dim3 grid(p.MT, p.NT * p.KS);
         if (p.mixed) {
-            tcx::weight_table_kernel<<<dim3(ceil_div(M, 128), r.ng), 128, 0, st>>>(M, r.nv, r.ng, r.aqsm, r.ldm, r.vcoul,
-                                                                                igp, acol, 0.5, W, nullptr, nullptr);
             tcx::TcArgs t{};
             t.c = a;
             t.Bimg = (const uint8_t*)D;
@@ -586,12 +591,10 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
             t.err = c.errword;
             if (tcx::encode_rows_map(&t.amap, r.aqsn, r.nc, r.nc, r.nb) != cudaSuccess)
                 return fail(c, FK_ECUDA, "gpp: cannot describe aqsntemp as a tensor map (needs a 16-byte aligned array)");
-            cudaMemsetAsync(c.errword, 0, sizeof(int), st);
             const int grid1 = std::min(p.units, c.sms);
             auto k = tcx::tc_contract_kernel<EPI_GPP, 64, false>;
             set_smem(k, tcx::Cfg<64>::SMEM);
             k<<<grid1, tcx::THREADS, tcx::Cfg<64>::SMEM, st>>>(t);
-            c.launches += 1;
         } else {
             auto k = d64::contract_kernel<EPI_GPP>;
             set_smem(k, d64::SMEM);
