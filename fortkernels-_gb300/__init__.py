@@ -24,7 +24,7 @@ from . import _native
 from ._native import (FK_FF_PHYSICS, FK_FF_SCHDT_GEMM, FK_FF_SPLIT_ACHD, FK_FP64, FK_GPP_ACHSTEMP,
                       FK_GPP_ROOT_QUIRKS, FK_MIXED, FKError)
 
-__all__ = ["Context", "gppKer", "ffKernel", "FKError", "FK_FP64", "FK_MIXED", "FK_GPP_ROOT_QUIRKS",
+__all__ = ["Context", "Server", "gppKer", "ffKernel", "FKError", "FK_FP64", "FK_MIXED", "FK_GPP_ROOT_QUIRKS",
            "FK_GPP_ACHSTEMP", "FK_FF_SCHDT_GEMM", "FK_FF_PHYSICS", "FK_FF_SPLIT_ACHD", "precision_code"]
 
 
@@ -153,6 +153,94 @@ class Context:
                             *optr)
         self._check(st, self.h)
         return out
+
+
+class Server:
+    """GPP request server (fk_server_* of include/fk_abi.h): requests of any
+    size are submitted as they arrive and run in fused steps on one GPU.
+    Input arrays (numpy or torch) are kept referenced until the request is
+    waited for."""
+
+    def __init__(self, device: int = 0, hbm_bytes: int = 8 << 30, max_active: int = 16, step_stages: int = 0):
+        self.lib = _native.load()
+        cfg = _native.ServerConfig(hbm_bytes, max_active, step_stages)
+        h = ctypes.c_void_p()
+        st = self.lib.fk_server_create(device, ctypes.byref(cfg), ctypes.byref(h))
+        if st != _native.FK_OK:
+            raise FKError(st, f"fk_server_create: {self.lib.fk_strerror(st).decode()}")
+        self.h = h
+        self._pending = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fk_server_destroy(self.h)
+            self.h = None
+            self._pending.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, what):
+        if st != _native.FK_OK:
+            raise FKError(st, f"{what}: {self.lib.fk_strerror(st).decode()}")
+
+    def resident_put(self, key: int, array):
+        ptr, keep = _arg(array, "c128", 1, "resident array")
+        n = keep.numel() * keep.element_size() if _is_torch(keep) else keep.nbytes
+        self._check(self.lib.fk_server_resident_put(self.h, key, ptr, n), "fk_server_resident_put")
+
+    def resident_evict(self, key: int):
+        self._check(self.lib.fk_server_resident_evict(self.h, key), "fk_server_resident_evict")
+
+    def submit(self, p: dict, flags: int = 0, eps_key=None, wtilde_key=None, out=None) -> int:
+        """Queue a GPP request (keys of fortkernels_gb300.inputs); returns its ticket.
+        eps_key / wtilde_key name resident arrays instead of p's I_eps_array /
+        wtilde_array."""
+        nb, nv, nc, ng = int(p["number_bands"]), int(p["nvband"]), int(p["ncouls"]), int(p["ngpown"])
+        keep = []
+
+        def a(key, kind, n):
+            ptr, k = _arg(p[key], kind, n, key)
+            keep.append(k)
+            return ptr
+
+        q = _native.GppRequest()
+        q.number_bands, q.nvband, q.ncouls, q.ngpown = nb, nv, nc, ng
+        q.aqsmtemp, q.aqsntemp = a("aqsmtemp", "c128", nb * nc), a("aqsntemp", "c128", nb * nc)
+        q.I_eps_array = None if eps_key is not None else a("I_eps_array", "c128", ng * nc)
+        q.wtilde_array = None if wtilde_key is not None else a("wtilde_array", "c128", ng * nc)
+        q.eps_key = eps_key or 0
+        q.wtilde_key = wtilde_key or 0
+        q.vcoul, q.inv_igp_index = a("vcoul", "f64", nc), a("inv_igp_index", "i32", ng)
+        q.indinv, q.wx_array = a("indinv", "i32", nc), a("wx_array", "f64", 3)
+        q.flags = flags
+        if out is None:
+            out = {"achtemp": np.zeros(3, np.complex128), "asxtemp": np.zeros(3, np.complex128),
+                   "acht_n1_loc": np.zeros(nb, np.complex128)}
+        q.achtemp, q.asxtemp = _data_ptr(out["achtemp"]), _data_ptr(out["asxtemp"])
+        q.acht_n1_loc = _data_ptr(out["acht_n1_loc"]) if out.get("acht_n1_loc") is not None else None
+        t = ctypes.c_ulonglong()
+        self._check(self.lib.fk_server_submit(self.h, ctypes.byref(q), ctypes.byref(t)), "fk_server_submit")
+        self._pending[t.value] = (keep, out)
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = -1.0):
+        """(outputs, latency in seconds) of a submitted request."""
+        lat = ctypes.c_double()
+        st = self.lib.fk_server_wait(self.h, ticket, timeout, ctypes.byref(lat))
+        keep, out = self._pending.get(ticket, (None, None))
+        if st != _native.FK_EBUSY:
+            self._pending.pop(ticket, None)
+        self._check(st, "fk_server_wait")
+        return out, lat.value
+
+    def stats(self) -> dict:
+        i = _native.ServerInfo()
+        self._check(self.lib.fk_server_stats(self.h, ctypes.byref(i)), "fk_server_stats")
+        return {f: getattr(i, f) for f, _ in _native.ServerInfo._fields_}
 
 
 def _data_ptr(x) -> int:

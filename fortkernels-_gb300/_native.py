@@ -22,7 +22,33 @@ FK_FF_SPLIT_ACHD = 0x4
 # Every symbol include/fk_abi.h declares.
 SYMBOLS = ("fk_create", "fk_destroy", "fk_set_stream", "fk_synchronize", "fk_reserve", "fk_strerror",
            "fk_last_error", "fk_version", "fk_gpp", "fk_ff", "fk_set_profiling", "fk_last_timings",
-           "fk_last_launches", "fk_gpp_static")
+           "fk_last_launches", "fk_gpp_static", "fk_server_create", "fk_server_destroy",
+           "fk_server_resident_put", "fk_server_resident_evict", "fk_server_submit", "fk_server_wait",
+           "fk_server_stats")
+
+
+class ServerConfig(ctypes.Structure):
+    """fk_server_config of include/fk_abi.h."""
+    _fields_ = [("hbm_bytes", ctypes.c_size_t), ("max_active", ctypes.c_int), ("step_stages", ctypes.c_int)]
+
+
+class GppRequest(ctypes.Structure):
+    """fk_gpp_request of include/fk_abi.h."""
+    _fields_ = [("number_bands", ctypes.c_int), ("nvband", ctypes.c_int), ("ncouls", ctypes.c_int),
+                ("ngpown", ctypes.c_int), ("aqsmtemp", ctypes.c_void_p), ("aqsntemp", ctypes.c_void_p),
+                ("I_eps_array", ctypes.c_void_p), ("wtilde_array", ctypes.c_void_p),
+                ("eps_key", ctypes.c_ulonglong), ("wtilde_key", ctypes.c_ulonglong), ("vcoul", ctypes.c_void_p),
+                ("inv_igp_index", ctypes.c_void_p), ("indinv", ctypes.c_void_p), ("wx_array", ctypes.c_void_p),
+                ("flags", ctypes.c_uint), ("achtemp", ctypes.c_void_p), ("asxtemp", ctypes.c_void_p),
+                ("acht_n1_loc", ctypes.c_void_p)]
+
+
+class ServerInfo(ctypes.Structure):
+    """fk_server_info of include/fk_abi.h."""
+    _fields_ = [("submitted", ctypes.c_ulonglong), ("completed", ctypes.c_ulonglong), ("steps", ctypes.c_ulonglong),
+                ("p50_s", ctypes.c_double), ("p99_s", ctypes.c_double), ("mean_s", ctypes.c_double),
+                ("terms_per_s", ctypes.c_double), ("mean_active", ctypes.c_double), ("peak_active", ctypes.c_int),
+                ("hbm_peak_bytes", ctypes.c_size_t)]
 
 
 class FKError(RuntimeError):
@@ -59,6 +85,14 @@ def load(path: str = LIB_PATH):
     L.fk_gpp.argtypes = [P, I, I, I, I] + [P] * 8 + [I, U] + [P] * 4
     L.fk_ff.argtypes = [P] + [I] * 6 + [P] * 11 + [D] * 4 + [I, U] + [P] * 6
     L.fk_gpp_static.argtypes = [P, I, I, I, I] + [P] * 8 + [U] + [P] * 4
+    UL = ctypes.c_ulonglong
+    L.fk_server_create.argtypes = [I, ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]
+    L.fk_server_destroy.argtypes = [P]
+    L.fk_server_resident_put.argtypes = [P, UL, P, ctypes.c_size_t]
+    L.fk_server_resident_evict.argtypes = [P, UL]
+    L.fk_server_submit.argtypes = [P, ctypes.POINTER(GppRequest), ctypes.POINTER(UL)]
+    L.fk_server_wait.argtypes = [P, UL, D, ctypes.POINTER(D)]
+    L.fk_server_stats.argtypes = [P, ctypes.POINTER(ServerInfo)]
     L.fk_set_profiling.argtypes = [P, I]
     L.fk_last_timings.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
     L.fk_last_launches.argtypes = [P]

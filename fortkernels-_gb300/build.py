@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libfk_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
                   "-I" + os.path.join(ROOT, "include")]
-SOURCES = ["fk_abi.cu", "fk_gpp.cu", "fk_ff.cu", "fk_static.cu"]
+SOURCES = ["fk_abi.cu", "fk_gpp.cu", "fk_ff.cu", "fk_static.cu", "fk_serve.cu"]
 CLIS = {"gppKer": "cli_gppKer.cpp", "ffKernel": "cli_ffKernel.cpp"}
 
 

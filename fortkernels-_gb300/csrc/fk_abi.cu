@@ -12,7 +12,7 @@
 
 #include "fk_internal.h"
 
-struct fk_ctx : public fk::Ctx {};
+
 
 namespace fk {
 

@@ -24,6 +24,8 @@
 // decisions remain those of the FP64 sequence; the bulk products run in FP32
 // with compensated accumulation.
 #include <algorithm>
+#include <cstring>
+#include <new>
 
 #include "fk_gemm.cuh"
 #include "fk_internal.h"
@@ -250,9 +252,8 @@ __device__ __noinline__ Exact exact_element(double wxt, double2 wt64, double2 ep
 // Writes D straight into the pre-split BF16 image consumed by the tensor-core
 // contraction (column j = my_igp*3 + iw lives in n-tile j / GPP_COLS).
 template <int Q, int BN>
-__global__ void __launch_bounds__(PREP_THREADS, 2) prep_mixed_kernel(PrepArgs p) {
-    __shared__ double2 sm[8 * NVC * 6];
-    const int tid = threadIdx.x, ch = blockIdx.x, my_igp = blockIdx.y;
+FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) {
+    const int tid = threadIdx.x;
     const int nflag = min(NVC, p.nv - p.n1base);
     const int igp = p.igp[my_igp];
     const bool flags = nflag > 0 && igp >= 0;
@@ -361,6 +362,12 @@ __global__ void __launch_bounds__(PREP_THREADS, 2) prep_mixed_kernel(PrepArgs p)
     }
 }
 
+template <int Q, int BN>
+__global__ void __launch_bounds__(PREP_THREADS, 2) prep_mixed_kernel(PrepArgs p) {
+    __shared__ double2 sm[8 * NVC * 6];
+    prep_mixed_item<Q, BN>(p, blockIdx.x, blockIdx.y, sm);
+}
+
 // ------------------------------------------------------------------ finalize
 // Warp-level fixed-order sum of NV double2 values (shuffle tree).
 template <int NV>
@@ -392,13 +399,27 @@ FK_DEV double2 warp_tree(double2 v) {
 //     F[ch][n1][my_igp][6] times the reference's weight (sch: 0.5*vcoul*conj(aqsm),
 //     BGW-Kernels/gppKer.cpp:346,421; ssx: occ*vcoul*conj(aqsm), :419);
 //   c == 6: the static-remainder partials S[slot][n1].
-__global__ void rows_kernel(int nb, int nv, int ng, int nslots, const double2* P, int nslots_s, const double2* S,
-                            int nch, const double2* F, long ldm, const double2* aqsm, const double* vcoul,
-                            const int* igp, const int* acol, double2* rows) {
-    const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (w >= (long)nb * 7) return;  // w is uniform over the warp
-    const int n1 = (int)(w / 7), c = (int)(w % 7);
+struct RowsArgs {
+    int nb, nv, ng, nslots;
+    const double2* P;
+    int nslots_s;
+    const double2* S;
+    int nch;
+    const double2* F;
+    long ldm;
+    const double2* aqsm;
+    const double* vcoul;
+    const int *igp, *acol;
+    double2* rows;
+};
+
+FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
+    const int nb = ra.nb, nv = ra.nv, ng = ra.ng, nslots = ra.nslots, nslots_s = ra.nslots_s, nch = ra.nch;
+    const double2 *P = ra.P, *S = ra.S, *F = ra.F, *aqsm = ra.aqsm;
+    const long ldm = ra.ldm;
+    const double* vcoul = ra.vcoul;
+    const int *igp = ra.igp, *acol = ra.acol;
+    double2* rows = ra.rows;
     double2 v = make_double2(0.0, 0.0);
     if (c == 6) {
         if (S && lane < nslots_s) v = ordered_sum(S + (long)lane * nb + n1, 32L * nb, (nslots_s - lane + 31) / 32);
@@ -422,9 +443,15 @@ __global__ void rows_kernel(int nb, int nv, int ng, int nslots, const double2* P
     if (lane == 0) rows[(long)n1 * 8 + c] = v;
 }
 
+__global__ void rows_kernel(RowsArgs ra) {
+    const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= (long)ra.nb * 7) return;  // w is uniform over the warp
+    rows_warp(ra, (int)(w / 7), (int)(w % 7), threadIdx.x & 31);
+}
+
 // Totals over bands, one warp per component (same split and tree), and the
 // per-band sch at iw = 2.  out = [achtemp 3 | asxtemp 3 | achstemp | acht_n1_loc nb].
-__global__ void totals_kernel(int nb, const double2* rows, double2* out) {
+FK_DEV void totals_block(int nb, const double2* rows, double2* out) {
     const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
     if (c < 7) {
         double2 v = lane < nb ? ordered_sum(rows + (long)lane * 8 + c, 32L * 8, (nb - lane + 31) / 32)
@@ -434,6 +461,8 @@ __global__ void totals_kernel(int nb, const double2* rows, double2* out) {
     }
     for (int r = threadIdx.x; r < nb; r += blockDim.x) out[7 + r] = rows[(long)r * 8 + 2];  // acht_n1_loc
 }
+
+__global__ void totals_kernel(int nb, const double2* rows, double2* out) { totals_block(nb, rows, out); }
 
 struct Plan {
     int nch, tile, passes;
@@ -469,7 +498,7 @@ void pick_split(int tiles, int K, int target, int& KS, int& kchunk) {
     KS = (K + kchunk - 1) / kchunk;
 }
 
-Plan make_plan(const Ctx& c, const GppDev& r) {
+Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0) {
     Plan p{};
     p.mixed = r.prec == FK_MIXED;
     if (r.prec == FK_MIXED) {
@@ -494,6 +523,11 @@ Plan make_plan(const Ctx& c, const GppDev& r) {
         p.MT = ceil_div(std::max(M, 1), tcx::BM);
         p.NT = ceil_div(r.ng, GPP_COLS);
         pick_split_tc(p.MT * p.NT, r.nc, c.sms, p.KS, p.kchunk);
+        if (ks_override > 0) {
+            const int ks = std::min(ks_override, std::max(1, ceil_div(r.nc, tcx::BK)));
+            p.kchunk = ceil_div(ceil_div(r.nc, ks), tcx::BK) * tcx::BK;
+            p.KS = ceil_div(r.nc, p.kchunk);
+        }
         p.units = p.MT * p.NT * p.KS;
     } else {
         p.MT = ceil_div(std::max(M, 1), d64::BM);
@@ -621,13 +655,314 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
         ++c.launches;
     }
     phase_mark(c, 3);
-    rows_kernel<<<ceil_div(r.nb * 7, 8), 256, 0, st>>>(r.nb, r.nv, r.ng, p.KS * p.NT, P, p.KSs * p.NTs, S, p.nch, F,
-                                                       r.ldm, r.aqsm, r.vcoul, igp, acol, rows);
+    const RowsArgs ra{r.nb, r.nv, r.ng, p.KS * p.NT, P, p.KSs * p.NTs, S, p.nch, F, r.ldm, r.aqsm, r.vcoul, igp, acol, rows};
+    rows_kernel<<<ceil_div(r.nb * 7, 8), 256, 0, st>>>(ra);
     totals_kernel<<<1, 256, 0, st>>>(r.nb, rows, r.out);
     c.launches += 2;
     phase_mark(c, 4);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "gpp kernels");
+    return FK_OK;
+}
+
+
+// ========================================================== served steps
+// A served request (GppJob) keeps its plan, workspace and descriptors on the
+// host; a step runs the first-step work (index map, weights, prep), a range
+// of contraction units and the last-step reduction of up to STEP_MAX
+// requests with five table-driven kernels, replayed from one captured graph.
+// A request's k-slices, partial slots and reduction order depend only on its
+// own shape and plan, never on which other requests share a step.
+namespace {
+
+constexpr int STEP_MAX = tcx::TC_MAXREQ;
+
+struct StepReq {
+    int nb, nv, nc, ng, M, compact, Q, passes;
+    const int *inv, *indinv;
+    int *igp, *acol;
+    const double2* aqsm;
+    long ldm;
+    const double* vcoul;
+    float2* W;
+    PrepArgs prep;
+    RowsArgs rows;
+    double2* out;
+};
+
+struct StepTable {
+    tcx::TcTable tc;
+    StepReq req[STEP_MAX];
+    int nfirst, nlast;
+    int first[STEP_MAX], last[STEP_MAX];
+    long setup_start[STEP_MAX + 1];  // threads: ng (index map) + M*ng (weights) per first-step request
+    int prep_start[STEP_MAX + 1];    // blocks: passes*nch*ng per first-step request
+    long rows_start[STEP_MAX + 1];   // warps: nb*7 per last-step request
+};
+
+template <class T>
+FK_DEV int find_range(const T* start, int n, T x) {  // largest i < n with start[i] <= x
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void step_setup_kernel(const StepTable* T) {
+    const long total = T->setup_start[T->nfirst];
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int f = find_range(T->setup_start, T->nfirst, t);
+        const StepReq& q = T->req[T->first[f]];
+        long i = t - T->setup_start[f];
+        if (i < q.ng) {
+            const int g = gpp_igp_of((int)i, q.nc, q.inv, q.indinv);
+            q.igp[i] = g;
+            q.acol[i] = g < 0 ? -1 : (q.compact ? (int)i : g);
+        } else {
+            i -= q.ng;
+            const int h = (int)(i / q.M), m = (int)(i % q.M);
+            const int g = gpp_igp_of(h, q.nc, q.inv, q.indinv);
+            float2 w = make_float2(0.f, 0.f);
+            if (g >= 0) w = tcx::weight_w1(q.aqsm[(long)(q.nv + m) * q.ldm + (q.compact ? h : g)], 0.5 * q.vcoul[g]);
+            q.W[(long)h * q.M + m] = w;
+        }
+    }
+}
+
+template <int BN>
+__global__ void __launch_bounds__(PREP_THREADS, 2) prep_table_kernel(const StepTable* T) {
+    __shared__ double2 sm[8 * NVC * 6];
+    const int total = T->prep_start[T->nfirst];
+    for (int it = blockIdx.x; it < total; it += gridDim.x) {
+        const int f = find_range(T->prep_start, T->nfirst, it);
+        const StepReq& q = T->req[T->first[f]];
+        int i = it - T->prep_start[f];
+        const int per_pass = q.prep.nch * q.ng;
+        const int pass = i / per_pass;
+        i -= pass * per_pass;
+        PrepArgs a = q.prep;
+        a.n1base = pass * NVC;
+        if (pass) a.D = nullptr;
+        if (q.Q) prep_mixed_item<1, BN>(a, i % a.nch, i / a.nch, sm);
+        else prep_mixed_item<0, BN>(a, i % a.nch, i / a.nch, sm);
+        __syncthreads();  // sm is reused by the next item
+    }
+}
+
+__global__ void rows_table_kernel(const StepTable* T) {
+    const long total = T->rows_start[T->nlast];
+    const long nw = (long)gridDim.x * blockDim.x / 32;
+    for (long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total; w += nw) {
+        const int l = find_range(T->rows_start, T->nlast, w);
+        const StepReq& q = T->req[T->last[l]];
+        const long i = w - T->rows_start[l];
+        rows_warp(q.rows, (int)(i / 7), (int)(i % 7), threadIdx.x & 31);
+    }
+}
+
+__global__ void totals_table_kernel(const StepTable* T) {
+    for (int l = blockIdx.x; l < T->nlast; l += gridDim.x) {
+        const StepReq& q = T->req[T->last[l]];
+        totals_block(q.nb, q.rows.rows, q.out);
+    }
+}
+
+}  // namespace
+
+struct GppJob {
+    GppDev r;
+    Plan p;
+    tcx::TcArgs tc;
+    StepReq req;
+    size_t bytes;
+};
+
+struct GppStep {
+    StepTable* dev = nullptr;
+    StepTable* host = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t done = nullptr;
+    bool launched = false;
+};
+
+size_t gpp_job_bytes(const Ctx& c, const GppDev& r, int ks) {
+    const Plan p = make_plan(c, r, ks);
+    return p.bytesD + p.bytesF + p.bytesP + p.bytesRows + p.bytesIgp + p.bytesW + (7 + (size_t)r.nb) * sizeof(double2) +
+           8 * 256;
+}
+
+int gpp_job_units(const GppJob* j) { return (j->r.nb - j->r.nv) > 0 ? j->p.units : 0; }
+int gpp_job_stages_per_unit(const GppJob* j) { return ceil_div(j->p.kchunk, tcx::BK); }
+double2* gpp_job_out(const GppJob* j) { return j->r.out; }
+int gpp_job_ks(const GppJob* j) { return j->p.KS; }
+void gpp_job_destroy(GppJob* j) { delete j; }
+
+GppJob* gpp_job_create(Ctx& c, const GppDev& r0, int ks, void* ws, size_t bytes, fk_status* st) {
+    *st = FK_OK;
+    if (r0.prec != FK_MIXED || (r0.flags & FK_GPP_ACHSTEMP)) {
+        *st = FK_ENOTSUP;
+        return nullptr;
+    }
+    GppJob* j = new (std::nothrow) GppJob();
+    if (!j) {
+        *st = FK_ENOMEM;
+        return nullptr;
+    }
+    j->r = r0;
+    j->p = make_plan(c, r0, ks);
+    j->bytes = bytes;
+    const Plan& p = j->p;
+    Workspace w;
+    w.base = ws;
+    w.cap = bytes;
+    int* igp = (int*)w.take(p.bytesIgp);
+    int* acol = igp ? igp + r0.ng : nullptr;
+    void* D = p.bytesD ? w.take(p.bytesD) : nullptr;
+    double2* F = (double2*)w.take(p.bytesF);
+    double2* P = p.bytesP ? (double2*)w.take(p.bytesP) : nullptr;
+    double2* rows = (double2*)w.take(p.bytesRows);
+    float2* W = p.bytesW ? (float2*)w.take(p.bytesW) : nullptr;
+    double2* out = (double2*)w.take((7 + (size_t)r0.nb) * sizeof(double2));
+    if (!igp || !F || !rows || !out || (p.bytesD && !D) || (p.bytesP && !P) || (p.bytesW && !W)) {
+        delete j;
+        *st = FK_ENOMEM;
+        return nullptr;
+    }
+    j->r.out = out;
+    const GppDev& r = j->r;
+    const int M = r.nb - r.nv;
+    StepReq& q = j->req;
+    q.nb = r.nb; q.nv = r.nv; q.nc = r.nc; q.ng = r.ng; q.M = M; q.compact = r.aqsm_compact ? 1 : 0;
+    q.Q = (r.flags & FK_GPP_ROOT_QUIRKS) ? 1 : 0;
+    q.passes = p.passes;
+    q.inv = r.inv; q.indinv = r.indinv; q.igp = igp; q.acol = acol;
+    q.aqsm = r.aqsm; q.ldm = r.ldm; q.vcoul = r.vcoul; q.W = W;
+    q.prep = PrepArgs{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, D, p.kstages, F, p.nch, p.tile, 0};
+    q.rows = RowsArgs{r.nb, r.nv, r.ng, p.KS * p.NT, P, 0, nullptr, p.nch, F, r.ldm, r.aqsm, r.vcoul, igp, acol, rows};
+    q.out = out;
+    if (M > 0) {
+        ContractArgs a{};
+        a.A = r.aqsn; a.lda = r.nc; a.m0 = r.nv; a.M = M;
+        a.B = D; a.ldb = r.nc; a.bstride = 0; a.N = 3 * r.ng; a.K = r.nc;
+        a.KS = p.KS; a.kchunk = p.kchunk; a.batches = 1; a.batch_plane = nullptr;
+        a.aqsm = r.aqsm; a.ldm = r.ldm; a.vcoul = r.vcoul; a.igp = igp; a.acol = acol; a.wscale = 0.5; a.G = 3; a.P = P;
+        tcx::TcArgs& t = j->tc;
+        t.c = a;
+        t.Bimg = (const uint8_t*)D;
+        t.W1 = W; t.W2 = nullptr; t.ldw = M; t.gpp_cols = GPP_COLS; t.Aimg = nullptr; t.vcol = nullptr;
+        t.kstages_total = p.kstages;
+        t.MT = p.MT; t.NT = p.NT; t.units = p.units;
+        t.err = c.errword;
+        if (tcx::encode_rows_map(&t.amap, r.aqsn, r.nc, r.nc, r.nb) != cudaSuccess) {
+            delete j;
+            *st = FK_ECUDA;
+            return nullptr;
+        }
+        // padding rows of the image and k >= ncouls must read as zero
+        if (cudaMemsetAsync(D, 0, p.bytesD, c.stream) != cudaSuccess) {
+            delete j;
+            *st = FK_ECUDA;
+            return nullptr;
+        }
+    }
+    return j;
+}
+
+GppStep* gpp_step_create(Ctx& c, fk_status* st) {
+    *st = FK_ECUDA;
+    GppStep* s = new (std::nothrow) GppStep();
+    if (!s) {
+        *st = FK_ENOMEM;
+        return nullptr;
+    }
+    auto bad = [&](fk_status code) -> GppStep* {
+        gpp_step_destroy(s);
+        cudaGetLastError();
+        *st = code;
+        return nullptr;
+    };
+    if (cudaMalloc(&s->dev, sizeof(StepTable)) != cudaSuccess) return bad(FK_ENOMEM);
+    if (cudaMallocHost(&s->host, sizeof(StepTable)) != cudaSuccess) return bad(FK_ENOMEM);
+    std::memset((void*)s->host, 0, sizeof(StepTable));
+    if (cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming) != cudaSuccess) return bad(FK_ECUDA);
+    auto tck = tcx::tc_contract_table_kernel<EPI_GPP, 64, false>;
+    if (set_smem(tck, tcx::Cfg<64>::SMEM) != cudaSuccess) return bad(FK_ECUDA);
+    int prep_per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&prep_per_sm, prep_table_kernel<64>, PREP_THREADS, 0) !=
+            cudaSuccess ||
+        prep_per_sm < 1)
+        prep_per_sm = 1;
+    // capture: table upload, error-word clear, the five kernels
+    cudaStream_t str = c.stream;
+    if (cudaStreamBeginCapture(str, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return bad(FK_ECUDA);
+    cudaMemcpyAsync(s->dev, s->host, sizeof(StepTable), cudaMemcpyHostToDevice, str);
+    cudaMemsetAsync(c.errword, 0, sizeof(int), str);
+    step_setup_kernel<<<c.sms * 4, 256, 0, str>>>(s->dev);
+    prep_table_kernel<64><<<c.sms * prep_per_sm, PREP_THREADS, 0, str>>>(s->dev);
+    tck<<<c.sms, tcx::THREADS, tcx::Cfg<64>::SMEM, str>>>(&s->dev->tc, c.errword);
+    rows_table_kernel<<<c.sms * 4, 256, 0, str>>>(s->dev);
+    totals_table_kernel<<<STEP_MAX, 256, 0, str>>>(s->dev);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(str, &g);
+    if (e != cudaSuccess || !g) return bad(FK_ECUDA);
+    e = cudaGraphInstantiate(&s->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return bad(FK_ECUDA);
+    *st = FK_OK;
+    return s;
+}
+
+void gpp_step_destroy(GppStep* s) {
+    if (!s) return;
+    if (s->launched) cudaEventSynchronize(s->done);
+    if (s->exec) cudaGraphExecDestroy(s->exec);
+    if (s->done) cudaEventDestroy(s->done);
+    if (s->dev) cudaFree(s->dev);
+    if (s->host) cudaFreeHost(s->host);
+    delete s;
+}
+
+int gpp_step_capacity() { return STEP_MAX; }
+
+fk_status gpp_step_launch(Ctx& c, GppStep* s, const GppStepItem* items, int n) {
+    if (n < 0 || n > STEP_MAX) return fail(c, FK_EINVAL, "step: too many requests");
+    // the previous step's table upload must be complete before the host table changes
+    if (s->launched && cudaEventSynchronize(s->done) != cudaSuccess) return cuda_fail(c, cudaGetLastError(), "step");
+    StepTable& T = *s->host;
+    T.tc.nreq = n;
+    T.nfirst = T.nlast = 0;
+    int units = 0;
+    T.setup_start[0] = 0;
+    T.prep_start[0] = 0;
+    T.rows_start[0] = 0;
+    for (int i = 0; i < n; ++i) {
+        const GppJob* j = items[i].job;
+        T.req[i] = j->req;
+        T.tc.req[i] = j->tc;
+        T.tc.ustart[i] = units;
+        T.tc.ulocal0[i] = items[i].u0;
+        units += items[i].u1 - items[i].u0;
+        if (items[i].first) {
+            const int f = T.nfirst++;
+            T.first[f] = i;
+            T.setup_start[f + 1] = T.setup_start[f] + j->r.ng + (long)j->req.M * j->r.ng;
+            T.prep_start[f + 1] = T.prep_start[f] + j->p.passes * j->p.nch * j->r.ng;
+        }
+        if (items[i].last) {
+            const int l = T.nlast++;
+            T.last[l] = i;
+            T.rows_start[l + 1] = T.rows_start[l] + (long)j->r.nb * 7;
+        }
+    }
+    T.tc.ustart[n] = units;
+    T.tc.units = units;
+    cudaError_t e = cudaGraphLaunch(s->exec, c.stream);
+    if (e == cudaSuccess) e = cudaEventRecord(s->done, c.stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "step launch");
+    s->launched = true;
     return FK_OK;
 }
 

@@ -69,6 +69,32 @@ struct GppDev {
 size_t gpp_workspace(const Ctx& c, const GppDev& r);
 fk_status gpp_run(Ctx& c, const GppDev& r);
 
+// Served GPP requests (mixed precision): a request's plan, workspace and
+// descriptors, and the captured step that runs several of them at once.
+struct GppJob;
+struct GppStep;
+struct GppStepItem {
+    GppJob* job;
+    int u0, u1;   // contraction units [u0, u1) of the request run in this step
+    bool first;   // index map, weights and prep run in this step (the request's first)
+    bool last;    // the reduction runs in this step (all units done)
+};
+// Device bytes of a request's workspace (plan with ks k-slices per tile, 0: default).
+size_t gpp_job_bytes(const Ctx& c, const GppDev& r, int ks);
+// r's pointers are device memory; the workspace is [ws, ws+bytes).  Clears the
+// request's image on c.stream.
+GppJob* gpp_job_create(Ctx& c, const GppDev& r, int ks, void* ws, size_t bytes, fk_status* st);
+void gpp_job_destroy(GppJob* j);
+int gpp_job_units(const GppJob* j);
+int gpp_job_stages_per_unit(const GppJob* j);
+int gpp_job_ks(const GppJob* j);
+double2* gpp_job_out(const GppJob* j);  // device [3 achtemp | 3 asxtemp | 1 | nb acht_n1_loc]
+GppStep* gpp_step_create(Ctx& c, fk_status* st);
+void gpp_step_destroy(GppStep* s);
+int gpp_step_capacity();
+// Runs one step on c.stream (waits for the previous step's table upload first).
+fk_status gpp_step_launch(Ctx& c, GppStep* s, const GppStepItem* items, int n);
+
 struct FfDev {
     int nb, nv, nc, ng, nf, ne;
     const double2 *aqsm, *aqsn, *epsR, *epsA, *brd;
@@ -88,3 +114,6 @@ void phase_mark(Ctx& c, int i);
 void phase_close(Ctx& c, int nphases);
 
 }  // namespace fk
+
+// The public context handle is the internal context.
+struct fk_ctx : public fk::Ctx {};

@@ -110,8 +110,42 @@ __device__ __forceinline__ void bimg_store(uint8_t* img_nt, int kstage_total_unu
     img_store<BN>(img_nt, n_in_tile, k, re, im);
 }
 
-template <int EPI, int BN, bool AIMG>
-__global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(const __grid_constant__ TcArgs t) {
+// Where a kernel's units come from.  OneReq: every unit belongs to the one
+// request in the launch parameters.  TableReqs: units of several requests,
+// laid end to end; request r owns global units [ustart[r], ustart[r+1]) and
+// they are its local units ulocal0[r], ulocal0[r]+1, ... (a step of a served
+// request may cover only part of its k-slices).  Each warp role walks units
+// in increasing order, so a cursor finds the request without a search.
+constexpr int TC_MAXREQ = 64;
+struct TcTable {
+    TcArgs req[TC_MAXREQ];
+    int nreq, units;
+    int ustart[TC_MAXREQ + 1];
+    int ulocal0[TC_MAXREQ];
+};
+struct OneReq {
+    const TcArgs& t;
+    __device__ int units() const { return t.units; }
+    __device__ const TcArgs& at(int u, int& lu) {
+        lu = u;
+        return t;
+    }
+    static constexpr bool kTable = false;
+};
+struct TableReqs {
+    const TcTable* tab;
+    int r;
+    __device__ int units() const { return tab->units; }
+    __device__ const TcArgs& at(int u, int& lu) {
+        while (r + 1 < tab->nreq && u >= tab->ustart[r + 1]) ++r;
+        lu = tab->ulocal0[r] + (u - tab->ustart[r]);
+        return tab->req[r];
+    }
+    static constexpr bool kTable = true;
+};
+
+template <int EPI, int BN, bool AIMG, class Src>
+__device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
     using C = Cfg<BN, EPI == EPI_FF>;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-aligned operand area
@@ -132,9 +166,7 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(const __grid_co
     __shared__ int s_abort_flag;
     volatile int& s_abort = s_abort_flag;
 
-    const ContractArgs& a = t.c;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int NTu = t.NT;
 
     if (tid == 0) {
         for (int s = 0; s < C::STAGES; ++s) {
@@ -161,33 +193,38 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(const __grid_co
     tc::tc_fence_after();
     const uint32_t tmem = *tslot;
 
-    auto unit_coords = [&](int u, int& mt, int& nt, int& ks, int& batch) {
+    // local unit -> (m-tile, n-tile, k-slice, batch) and the slice's k range
+    auto unit_coords = [&](const TcArgs& t, int u, int& mt, int& nt, int& ks, int& batch) {
         mt = u % t.MT;
         int r = u / t.MT;
-        nt = r % NTu;
-        r /= NTu;
-        ks = r % a.KS;
-        batch = r / a.KS;
+        nt = r % t.NT;
+        r /= t.NT;
+        ks = r % t.c.KS;
+        batch = r / t.c.KS;
     };
-    auto krange = [&](int ks, int& k0, int& k1) {
-        k0 = ks * a.kchunk;
-        k1 = min(a.K, k0 + a.kchunk);
+    auto krange = [&](const TcArgs& t, int ks, int& k0, int& k1) {
+        k0 = ks * t.c.kchunk;
+        k1 = min(t.c.K, k0 + t.c.kchunk);
     };
     auto fail = [&](int code) {
-        atomicOr(t.err, code);
+        atomicOr(err, code);
         s_abort = 1;
     };
 
+    Src src = src0;  // per-role cursor
     if (warp == 0) {
         // ------------------------------------------------------------ MMA
         if (lane == 0) {
             int g = 0, chunk = 0;
             bool ok = true;
             const uint32_t idp = tc::idesc_bf16(BM, BN, false), idn = tc::idesc_bf16(BM, BN, true);
-            for (int u = blockIdx.x; u < t.units && ok; u += gridDim.x) {
+            for (int u = blockIdx.x; u < src.units() && ok; u += gridDim.x) {
+                int lu;
+                const TcArgs& t = src.at(u, lu);
+                const ContractArgs& a = t.c;
                 int mt, nt, ks, batch, k0, k1;
-                unit_coords(u, mt, nt, ks, batch);
-                krange(ks, k0, k1);
+                unit_coords(t, lu, mt, nt, ks, batch);
+                krange(t, ks, k0, k1);
                 const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
                 for (int st0 = 0; st0 < nst && ok; st0 += C::CHUNK_STAGES, ++chunk) {
                     const int b = chunk & 1;
@@ -246,12 +283,20 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(const __grid_co
         // all lanes (GPP): the next stage's FP64 A rows into the staging buffer.
         int g = 0;
         bool ok = true;
-        for (int u = blockIdx.x; u < t.units && ok; u += gridDim.x) {
+        for (int u = blockIdx.x; u < src.units() && ok; u += gridDim.x) {
+            int lu;
+            const TcArgs& t = src.at(u, lu);
+            const ContractArgs& a = t.c;
             int mt, nt, ks, batch, k0, k1;
-            unit_coords(u, mt, nt, ks, batch);
-            krange(ks, k0, k1);
+            unit_coords(t, lu, mt, nt, ks, batch);
+            krange(t, ks, k0, k1);
             const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
             const int plane = a.batch_plane ? a.batch_plane[batch] : batch;
+            if (Src::kTable && !AIMG && lane == 0) {
+                // the table was written by copies before the launch: make its
+                // tensor map visible to the tensor-memory-access unit
+                asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&t.amap) : "memory");
+            }
             for (int st = 0; st < nst; ++st, ++g) {
                 const int s = g % C::STAGES;
                 const long kst = (long)(k0 / BK) + st;
@@ -275,7 +320,7 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(const __grid_co
                         ok = false;
                     } else {
                         const uint8_t* src =
-                            t.Bimg + (((long)plane * NTu + nt) * t.kstages_total + kst) * (long)C::B_BYTES;
+                            t.Bimg + (((long)plane * t.NT + nt) * t.kstages_total + kst) * (long)C::B_BYTES;
                         tc::mbar_arrive_expect_tx(&fullB[s], C::B_BYTES);
                         tc::bulk_g2s(base + s * C::STAGE_BYTES + C::A_BYTES, src, C::B_BYTES, &fullB[s]);
                         if (AIMG) {
@@ -300,10 +345,13 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(const __grid_co
         int chunk = 0;
         bool ok = true;
         constexpr int GC = BN / 3;  // 21 igp per GPP tile
-        for (int u = blockIdx.x; u < t.units && ok; u += gridDim.x) {
+        for (int u = blockIdx.x; u < src.units() && ok; u += gridDim.x) {
+            int lu;
+            const TcArgs& t = src.at(u, lu);
+            const ContractArgs& a = t.c;
             int mt, nt, ks, batch, k0, k1;
-            unit_coords(u, mt, nt, ks, batch);
-            krange(ks, k0, k1);
+            unit_coords(t, lu, mt, nt, ks, batch);
+            krange(t, ks, k0, k1);
             const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
             const int m = mt * BM + row;
             const int mc = min(m, a.M - 1);
@@ -387,7 +435,7 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(const __grid_co
             }
             if (!ok) break;
             if (m < a.M) {
-                const int slot = (batch * a.KS + ks) * NTu + nt;
+                const int slot = (batch * a.KS + ks) * t.NT + nt;
                 for (int gg = 0; gg < a.G; ++gg) a.P[((long)slot * a.M + m) * a.G + gg] = acc[gg];
             }
         }
@@ -402,10 +450,13 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(const __grid_co
             constexpr int RPW = BM / NCONV;                  // rows per converter warp
             int g = 0;
             bool ok = true;
-            for (int u = blockIdx.x; u < t.units && ok; u += gridDim.x) {
+            for (int u = blockIdx.x; u < src.units() && ok; u += gridDim.x) {
+                int lu;
+                const TcArgs& t = src.at(u, lu);
+                const ContractArgs& a = t.c;
                 int mt, nt, ks, batch, k0, k1;
-                unit_coords(u, mt, nt, ks, batch);
-                krange(ks, k0, k1);
+                unit_coords(t, lu, mt, nt, ks, batch);
+                krange(t, ks, k0, k1);
                 const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
                 for (int st = 0; st < nst; ++st, ++g) {
                     const int s = g % C::STAGES;
@@ -458,8 +509,22 @@ __global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(const __grid_co
     }
 }
 
+template <int EPI, int BN, bool AIMG>
+__global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(const __grid_constant__ TcArgs t) {
+    tc_contract_body<EPI, BN, AIMG>(OneReq{t}, t.err);
+}
+
+// Units of several requests from a device table (the served step).
+template <int EPI, int BN, bool AIMG>
+__global__ void __launch_bounds__(THREADS, 1) tc_contract_table_kernel(const TcTable* tab, int* err) {
+    tc_contract_body<EPI, BN, AIMG>(TableReqs{tab, 0}, err);
+}
+
 // Epilogue weight tables in FP32, column-major (row m contiguous):
 // W1[h][m] = wscale*vcoul[igp]*conj(aqsm[m0+m][igp]), W2[h][m] = conj(aqsm[m0+m][igp]).
+__device__ __forceinline__ float2 weight_w1(const double2 am, double s) {
+    return make_float2(f64_to_f32_bits(am.x * s), f64_to_f32_bits(-am.y * s));
+}
 static __global__ void weight_table_kernel(int M, int m0, int ncols, const double2* aqsm, long ldm, const double* vcoul,
                                     const int* igp, const int* acol, double wscale, float2* W1, float2* W2,
                                     float* vcol) {
@@ -469,8 +534,7 @@ static __global__ void weight_table_kernel(int M, int m0, int ncols, const doubl
     float2 w1 = make_float2(0.f, 0.f), w2 = w1;
     if (g >= 0) {
         const double2 am = aqsm[(long)(m0 + m) * ldm + acol[h]];
-        const double s = wscale * vcoul[g];
-        w1 = make_float2(f64_to_f32_bits(am.x * s), f64_to_f32_bits(-am.y * s));
+        w1 = weight_w1(am, wscale * vcoul[g]);
         w2 = make_float2(f64_to_f32_bits(am.x), f64_to_f32_bits(-am.y));
     }
     W1[(long)h * M + m] = w1;

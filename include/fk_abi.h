@@ -190,6 +190,74 @@ fk_status fk_ff(fk_ctx_t ctx, int number_bands, int nvband, int ncouls, int ngpo
                 fk_c128* achsDtemp, fk_c128* asxDtemp, fk_c128* achDtemp,
                 fk_c128* achDtemp_cor, fk_c128* ach2Dtemp, fk_c128* schDt_matrix);
 
+/* ---------------------------------------------------------------- serving */
+
+/*
+ * A GPP request server: a worker thread on one GPU takes requests of any
+ * (number_bands, ncouls, ngpown) as they are submitted, admits them while its
+ * device memory budget and active slots allow, and runs them in steps.  Each
+ * step is one replay of a captured CUDA graph whose kernels (index map and
+ * weights, prep, one persistent tcgen05 contraction over every request's
+ * units, reductions) read a table of the step's requests; a large request
+ * advances part of its k-range per step, a small one finishes in one step.
+ * A request's arithmetic (its k-slices and summation order) depends only on
+ * its own shape, so its result is the same alone and in any mix.  Mixed
+ * precision (FK_MIXED semantics of fk_gpp).  No counterpart in the reference
+ * (which runs one evaluation per process).
+ */
+typedef struct fk_server* fk_server_t;
+
+typedef struct {
+    size_t hbm_bytes; /* device memory for resident arrays and requests (one block) */
+    int max_active;   /* requests on the GPU at once, 1..64 */
+    int step_stages;  /* contraction work per step, in 32-wide k-stages per SM (0: 96) */
+} fk_server_config;
+
+typedef struct {
+    int number_bands, nvband, ncouls, ngpown;
+    const fk_c128* aqsmtemp;     /* [number_bands][ncouls], host or device */
+    const fk_c128* aqsntemp;     /* [number_bands][ncouls], host or device */
+    const fk_c128* I_eps_array;  /* [ngpown][ncouls], host or device; NULL: eps_key */
+    const fk_c128* wtilde_array; /* [ngpown][ncouls], host or device; NULL: wtilde_key */
+    unsigned long long eps_key, wtilde_key; /* fk_server_resident_put keys */
+    const double* vcoul;         /* [ncouls] */
+    const int* inv_igp_index;    /* [ngpown] */
+    const int* indinv;           /* [ncouls] */
+    const double* wx_array;      /* [3] */
+    unsigned flags;              /* 0 or FK_GPP_ROOT_QUIRKS */
+    fk_c128* achtemp;            /* [3] outputs, host or device, written at completion */
+    fk_c128* asxtemp;            /* [3] */
+    fk_c128* acht_n1_loc;        /* [number_bands] or NULL */
+} fk_gpp_request;
+
+typedef struct {
+    unsigned long long submitted, completed, steps;
+    double p50_s, p99_s, mean_s; /* submit-to-completion latency of completed requests */
+    double terms_per_s;          /* completed terms / (last completion - first submission) */
+    double mean_active;          /* requests per step */
+    int peak_active;
+    size_t hbm_peak_bytes;       /* most of the budget in use at once */
+} fk_server_info;
+
+fk_status fk_server_create(int device, const fk_server_config* cfg, fk_server_t* out);
+/* Finishes every submitted request, then stops the worker and frees the GPU memory. */
+fk_status fk_server_destroy(fk_server_t srv);
+/* Copies an array (host or device) to the server's memory under `key`, for
+ * requests that name it instead of passing I_eps_array / wtilde_array.
+ * FK_EINVAL if the key is in use, FK_EBUSY if it was evicted but running
+ * requests still read it. */
+fk_status fk_server_resident_put(fk_server_t srv, unsigned long long key, const void* data, size_t bytes);
+/* Frees a resident array once no admitted or waiting request uses it. */
+fk_status fk_server_resident_evict(fk_server_t srv, unsigned long long key);
+/* Queues a request (the input arrays must stay valid until it completes).
+ * FK_ENOMEM: the request can never fit in the server's memory budget. */
+fk_status fk_server_submit(fk_server_t srv, const fk_gpp_request* req, unsigned long long* ticket);
+/* Waits for a request (timeout_s < 0: no limit; FK_EBUSY on timeout) and
+ * returns its status; latency_s (may be NULL) gets submit-to-completion time.
+ * The ticket is consumed when the request has completed. */
+fk_status fk_server_wait(fk_server_t srv, unsigned long long ticket, double timeout_s, double* latency_s);
+fk_status fk_server_stats(fk_server_t srv, fk_server_info* out);
+
 /* ------------------------------------------------------------ measurement */
 
 /* Kernel-level timing of the most recent fk_gpp/fk_ff call, measured with
