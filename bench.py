@@ -39,6 +39,9 @@ WORKLOADS = {
     "gpp1638": dict(kind="gpp", nb=512, nv=2, nc=32768, ng=1638),
     # BASELINE config 2: FF full-frequency contraction
     "ff": dict(kind="ff", nb=512, nv=2, nc=4096, ng=512, nf=15, ne=10),
+    # BASELINE config 3: a served, uneven GPP request stream
+    "serve": dict(kind="serve", requests=256, nb_choices=(128, 256, 512, 1024), nc_lo=2048, nc_hi=32768,
+                  nc_levels=8, nv=2, load=0.8),
 }
 
 
@@ -217,6 +220,35 @@ def run_reference(a, w):
     import __graft_entry__
     fk = __graft_entry__.load_package()
     cores = os.cpu_count() or 1
+    if w["kind"] == "serve":
+        # the stream's requests in order, those under 2e9 terms (about a
+        # second each on the host), until ~20 s of CPU work per step
+        levels, reqs, _ = serve_stream(w)
+        small = [(nb, nc) for nb, nc in reqs if 3.0 * nb * nc * (nc // 64) <= 2e9]
+        times, done_terms, i = [], [], 0
+        for _ in range(a.warmup + a.steps):
+            t0 = time.perf_counter()
+            tt = 0.0
+            while time.perf_counter() - t0 < 20.0 / (a.warmup + a.steps):
+                nb, nc = small[i % len(small)]
+                i += 1
+                oracle.gpp(fk.inputs.gpp_synthetic(nb, w["nv"], nc, nc // 64, seed=i), nthreads=cores)
+                tt += 3.0 * nb * nc * (nc // 64)
+            times.append(time.perf_counter() - t0)
+            done_terms.append(tt)
+        times, done_terms = times[a.warmup:], done_terms[a.warmup:]
+        val = sum(done_terms) / sum(times)
+        sample = (f"the stream's requests of <= 2e9 terms ({len(small)} of {len(reqs)}), in order, "
+                  f"one after another, OpenMP {cores} threads; input generation included")
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": val, "unit": "terms/s", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "served GPP stream (CPU: sequential)", "ncouls_levels": levels},
+            "cpu_baseline": {"value": val, "unit": "terms/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": val, "unit": "terms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }), flush=True)
+        return
     p = make_inputs(fk, w)
     call = (lambda: oracle.gpp(p, nthreads=cores)) if w["kind"] == "gpp" else \
         (lambda: oracle.ff(p, flags=oracle.ORC_FF_SCHDT_GEMM, nthreads=cores))
@@ -443,6 +475,132 @@ def cpu_baseline(fk, w, p):
             "sample": f"first {nbs} of {w['nb']} bands ({tq:.3g} terms)"}
 
 
+def serve_stream(w, seed=2024):
+    """ncouls levels (log-spaced over [nc_lo, nc_hi], multiples of 64), and per
+    request (number_bands, ncouls) plus a unit-rate exponential gap."""
+    rng = np.random.default_rng(seed)
+    L = w["nc_levels"]
+    levels = sorted({int(round(w["nc_lo"] * (w["nc_hi"] / w["nc_lo"]) ** (i / (L - 1)) / 64)) * 64 for i in range(L)})
+    reqs = [(int(rng.choice(w["nb_choices"])), int(rng.choice(levels))) for _ in range(w["requests"])]
+    return levels, reqs, rng.exponential(1.0, w["requests"])
+
+
+def run_serve(a, w):
+    """BASELINE config 3: the request server (fk_server_*) on a stream of GPP
+    requests of uneven size.  First a burst (all requests at once: saturation
+    throughput), then Poisson arrivals at `load` x that rate (latency)."""
+    import torch
+    import __graft_entry__
+    fk = __graft_entry__.load_package()
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    levels, reqs, gaps = serve_stream(w, seed=2024 + rank)
+    srv = fk.Server(local, hbm_bytes=24 << 30, max_active=32)
+    pools = {}
+    for i, nc in enumerate(levels):
+        ng = nc // 64
+        gen = torch.Generator(device=f"cuda:{local}").manual_seed(1000 * (rank + 1) + i)
+
+        def cu(shape):
+            x = torch.rand(shape + (2,), generator=gen, device=f"cuda:{local}", dtype=torch.float64) - 0.5
+            return torch.view_as_complex(x).contiguous()
+        aqsm, aqsn, eps = cu((1024, nc)), cu((1024, nc)), cu((ng, nc))
+        wre = torch.rand((ng, nc), generator=gen, device=f"cuda:{local}", dtype=torch.float64) * 1.5 + 0.5
+        wim = (torch.rand((ng, nc), generator=gen, device=f"cuda:{local}", dtype=torch.float64) - 0.5) * 0.1
+        wt = torch.complex(wre, wim).contiguous()
+        srv.resident_put(2 * i + 1, eps)
+        srv.resident_put(2 * i + 2, wt)
+        del eps, wt
+        r = np.random.default_rng(i)
+        pools[nc] = dict(key=i, aqsm=aqsm, aqsn=aqsn, vcoul=r.uniform(0.1, 1.0, nc),
+                         inv=np.array([j * nc // ng for j in range(ng)], np.int32), indinv=np.arange(nc, dtype=np.int32))
+    wx = np.array([9.0, 10.0, 11.0])
+
+    def submit(nb, nc):
+        q = pools[nc]
+        p = {"number_bands": nb, "nvband": w["nv"], "ncouls": nc, "ngpown": nc // 64, "aqsmtemp": q["aqsm"][:nb],
+             "aqsntemp": q["aqsn"][:nb], "vcoul": q["vcoul"], "inv_igp_index": q["inv"], "indinv": q["indinv"],
+             "wx_array": wx}
+        return srv.submit(p, eps_key=2 * q["key"] + 1, wtilde_key=2 * q["key"] + 2)
+
+    def terms_of(nb, nc):
+        return 3.0 * nb * nc * (nc // 64)
+
+    # warm-up: every ncouls level once
+    for _ in range(max(1, a.warmup // 3)):
+        for t in [submit(128, nc) for nc in levels]:
+            srv.wait(t)
+    total = sum(terms_of(nb, nc) for nb, nc in reqs)
+    # burst: saturation throughput
+    with clock_sampler(local) as clk:
+        t0 = time.perf_counter()
+        tickets = [submit(nb, nc) for nb, nc in reqs]
+        for t in tickets:
+            srv.wait(t)
+        burst_s = time.perf_counter() - t0
+    sat = total / burst_s
+    steps0 = srv.stats()["steps"]
+    # Poisson arrivals at `load` x saturation
+    rate = w["load"] * sat / (total / len(reqs))
+    arrivals = np.cumsum(gaps / rate)
+    lat = []
+    t0 = time.perf_counter()
+    tickets = []
+    for (nb, nc), at in zip(reqs, arrivals):
+        dt = at - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        tickets.append(submit(nb, nc))
+    for t in tickets:
+        lat.append(srv.wait(t)[1])
+    pois_s = time.perf_counter() - t0
+    info = srv.stats()
+    srv.close()
+    cpu = None
+    if rank == 0 and not a.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        cores = os.cpu_count() or 1
+        q = fk.inputs.gpp_synthetic(128, 2, 2048, 32, seed=5)
+        t1 = time.perf_counter()
+        n = 0
+        while time.perf_counter() - t1 < 5.0:
+            oracle.gpp(q, nthreads=cores)
+            n += 1
+        dt = time.perf_counter() - t1
+        cpu = {"value": n * terms_of(128, 2048) / dt, "unit": "terms/s", "cores": cores, "kind": "port",
+               "sample": f"{n} calls of the smallest request shape (128 x 2048 x 32), ~5 s"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": world * sat, "unit": "terms/s", "n_gpus": world, "steps": len(reqs),
+            "warmup": a.warmup, "ms_per_step": 1e3 * burst_s / len(reqs), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 in / fp32 bulk + fp64 branch/reductions",
+            "data": "synthetic (seeded; wavefunction pools and epsilon/wtilde resident on the device)",
+            "config": {"workload": ("served GPP stream: %d requests, number_bands in %s, ncouls in %d log-spaced "
+                                    "levels over [%d, %d], ngpown = ncouls/64, nvband = %d; burst for throughput, "
+                                    "then Poisson arrivals at %.0f%% of it for latency"
+                                    % (len(reqs), list(w["nb_choices"]), len(levels), w["nc_lo"], w["nc_hi"],
+                                       w["nv"], 100 * w["load"])),
+                       "precision": "mixed", "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (pools of several GB)", "ncouls_levels": levels},
+            "precision": "mixed",
+            "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)), "p99": 1e3 * float(np.percentile(lat, 99)),
+                           "mean": 1e3 * float(np.mean(lat)), "arrival_rate_per_s": rate},
+            "served": {"burst_s": burst_s, "poisson_s": pois_s, "poisson_terms_per_s": total / pois_s,
+                       "steps_burst": steps0, "steps_total": info["steps"],
+                       "mean_requests_per_step": info["mean_active"], "peak_active": info["peak_active"],
+                       "hbm_peak_bytes": info["hbm_peak_bytes"]},
+            "roofline": None,
+            "e2e": {"value": world * sat, "unit": "terms/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                    "note": "requests through fk_server_submit/fk_server_wait; outputs returned to host"},
+            "gpu_launches": 5 * info["steps"],
+            "clocks": clk.summary(),
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -457,6 +615,8 @@ def main():
     w = dict(WORKLOADS[a.workload], name=a.workload)
     if a.impl == "reference":
         run_reference(a, w)
+    elif w["kind"] == "serve":
+        run_serve(a, w)
     else:
         run_ours(a, w)
 
