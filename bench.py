@@ -526,7 +526,9 @@ def run_serve(a, w):
     def terms_of(nb, nc):
         return 3.0 * nb * nc * (nc // 64)
 
-    # warm-up: every ncouls level once
+    # autotuned plans for every request shape of the stream, then a warm-up
+    shapes = sorted(set(reqs))
+    tuned = {f"{nb}x{nc}": srv.tune(nb, w["nv"], nc, nc // 64) for nb, nc in shapes}
     for _ in range(max(1, a.warmup // 3)):
         for t in [submit(128, nc) for nc in levels]:
             srv.wait(t)
@@ -589,7 +591,7 @@ def run_serve(a, w):
             "served": {"burst_s": burst_s, "poisson_s": pois_s, "poisson_terms_per_s": total / pois_s,
                        "steps_burst": steps0, "steps_total": info["steps"],
                        "mean_requests_per_step": info["mean_active"], "peak_active": info["peak_active"],
-                       "hbm_peak_bytes": info["hbm_peak_bytes"]},
+                       "hbm_peak_bytes": info["hbm_peak_bytes"], "autotuned_kslices": tuned},
             "roofline": None,
             "e2e": {"value": world * sat, "unit": "terms/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
                     "note": "requests through fk_server_submit/fk_server_wait; outputs returned to host"},

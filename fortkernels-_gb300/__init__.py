@@ -237,6 +237,13 @@ class Server:
         self._check(st, "fk_server_wait")
         return out, lat.value
 
+    def tune(self, number_bands: int, nvband: int, ncouls: int, ngpown: int, flags: int = 0) -> int:
+        """Autotune the plan of a request shape (server idle); returns the chosen k-slice count."""
+        ks = ctypes.c_int()
+        self._check(self.lib.fk_server_tune(self.h, number_bands, nvband, ncouls, ngpown, flags, ctypes.byref(ks)),
+                    "fk_server_tune")
+        return ks.value
+
     def stats(self) -> dict:
         i = _native.ServerInfo()
         self._check(self.lib.fk_server_stats(self.h, ctypes.byref(i)), "fk_server_stats")

@@ -24,7 +24,7 @@ SYMBOLS = ("fk_create", "fk_destroy", "fk_set_stream", "fk_synchronize", "fk_res
            "fk_last_error", "fk_version", "fk_gpp", "fk_ff", "fk_set_profiling", "fk_last_timings",
            "fk_last_launches", "fk_gpp_static", "fk_server_create", "fk_server_destroy",
            "fk_server_resident_put", "fk_server_resident_evict", "fk_server_submit", "fk_server_wait",
-           "fk_server_stats")
+           "fk_server_stats", "fk_server_tune")
 
 
 class ServerConfig(ctypes.Structure):
@@ -93,6 +93,7 @@ def load(path: str = LIB_PATH):
     L.fk_server_submit.argtypes = [P, ctypes.POINTER(GppRequest), ctypes.POINTER(UL)]
     L.fk_server_wait.argtypes = [P, UL, D, ctypes.POINTER(D)]
     L.fk_server_stats.argtypes = [P, ctypes.POINTER(ServerInfo)]
+    L.fk_server_tune.argtypes = [P, I, I, I, I, U, ctypes.POINTER(I)]
     L.fk_set_profiling.argtypes = [P, I]
     L.fk_last_timings.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
     L.fk_last_launches.argtypes = [P]

@@ -966,4 +966,45 @@ fk_status gpp_step_launch(Ctx& c, GppStep* s, const GppStepItem* items, int n) {
     return FK_OK;
 }
 
+fk_status gpp_time_plan(Ctx& c, GppStep* s, const GppDev& r, int ks, long step_budget, void* ws, size_t bytes,
+                        float* ms, int* units) {
+    fk_status st = FK_OK;
+    GppJob* j = gpp_job_create(c, r, ks, ws, bytes, &st);
+    if (!j) return st;
+    *units = gpp_job_units(j);
+    const int spu = std::max(1, gpp_job_stages_per_unit(j));
+    // the request alone through served steps of step_budget k-stages
+    auto run = [&]() -> fk_status {
+        int next = 0;
+        bool first = true;
+        do {
+            const int k = (int)std::min<long>(*units - next, std::max(1L, step_budget / spu));
+            GppStepItem it{j, next, next + k, first, next + k >= *units};
+            const fk_status e = gpp_step_launch(c, s, &it, 1);
+            if (e != FK_OK) return e;
+            next += k;
+            first = false;
+        } while (next < *units);
+        return FK_OK;
+    };
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    st = run();  // warm
+    if (st == FK_OK) {
+        cudaEventRecord(e0, c.stream);
+        st = run();
+        cudaEventRecord(e1, c.stream);
+    }
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (st == FK_OK && e != cudaSuccess) st = cuda_fail(c, e, "tune");
+    if (st == FK_OK) cudaEventElapsedTime(ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    gpp_job_destroy(j);
+    return st;
+}
+
+int gpp_default_ks(const Ctx& c, const GppDev& r) { return make_plan(c, r).KS; }
+
 }  // namespace fk

@@ -94,6 +94,12 @@ void gpp_step_destroy(GppStep* s);
 int gpp_step_capacity();
 // Runs one step on c.stream (waits for the previous step's table upload first).
 fk_status gpp_step_launch(Ctx& c, GppStep* s, const GppStepItem* items, int n);
+// The k-slice count the default plan picks, and the device time (ms) of a
+// request run alone through served steps of step_budget k-stages with ks
+// k-slices per tile (r: device inputs; [ws, ws+bytes) its workspace).
+int gpp_default_ks(const Ctx& c, const GppDev& r);
+fk_status gpp_time_plan(Ctx& c, GppStep* s, const GppDev& r, int ks, long step_budget, void* ws, size_t bytes,
+                        float* ms, int* units);
 
 struct FfDev {
     int nb, nv, nc, ng, nf, ne;

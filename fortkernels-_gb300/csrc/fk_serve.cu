@@ -171,6 +171,12 @@ struct fk_server {
     // pinned staging of finished outputs
     double2* pinned = nullptr;
     size_t pinned_n = 0;
+    // autotuned k-slice counts by request shape (nb, nvband, ncouls, ngpown, flags)
+    std::map<std::vector<long>, int> tuned;
+    int ks_for(const fk_gpp_request& q) const {
+        auto it = tuned.find({q.number_bands, q.nvband, q.ncouls, q.ngpown, (long)q.flags});
+        return it == tuned.end() ? 0 : it->second;
+    }
 
     void run();
     bool admit(fk::Request* r);
@@ -216,7 +222,8 @@ bool fk_server::admit(fk::Request* r) {
     using namespace fk;
     const fk_gpp_request& q = r->q;
     GppDev d = request_dev(q);
-    const size_t ws = gpp_job_bytes(*ctx, d, 0);
+    const int ks = ks_for(q);
+    const size_t ws = gpp_job_bytes(*ctx, d, ks);
     const size_t need = staged_bytes(*this, q) + ws + 4096;
     void* mem = arena.alloc(need);
     if (!mem) return false;
@@ -246,7 +253,7 @@ bool fk_server::admit(fk::Request* r) {
     d.wx = (const double*)stage(q.wx_array, 3 * sizeof(double));
     fk_status st2 = FK_OK;
     void* wsp = ok ? w.take(ws) : nullptr;
-    if (ok && wsp) r->job = gpp_job_create(*ctx, d, 0, wsp, ws, &st2);
+    if (ok && wsp) r->job = gpp_job_create(*ctx, d, ks, wsp, ws, &st2);
     if (!ok || !wsp || !r->job) {
         r->status = !ok ? FK_ECUDA : (st2 != FK_OK ? st2 : FK_ENOMEM);
         cudaGetLastError();
@@ -538,7 +545,7 @@ fk_status fk_server_submit(fk_server_t s, const fk_gpp_request* q, unsigned long
     // a request that could never fit is refused now
     fk::DevScope scope(s->ctx->device);
     fk::GppDev d = fk::request_dev(*q);
-    const size_t need = fk::staged_bytes(*s, *q) + fk::gpp_job_bytes(*s->ctx, d, 0) + 4096;
+    const size_t need = fk::staged_bytes(*s, *q) + fk::gpp_job_bytes(*s->ctx, d, s->ks_for(*q)) + 4096;
     if (fk::round256(need) > s->arena.capacity()) {
         delete r;
         return FK_ENOMEM;
@@ -570,6 +577,69 @@ fk_status fk_server_wait(fk_server_t s, unsigned long long ticket, double timeou
     s->reqs.erase(it);
     delete r;
     return st;
+}
+
+fk_status fk_server_tune(fk_server_t s, int nb, int nv, int nc, int ng, unsigned flags, int* chosen_ks) {
+    if (!s || nb <= 0 || nc <= 0 || ng <= 0 || nv < 0 || nv > nb || ng > 65535) return FK_EINVAL;
+    if (flags & ~(unsigned)FK_GPP_ROOT_QUIRKS) return FK_EINVAL;
+    if ((flags & FK_GPP_ROOT_QUIRKS) && ng > nc) return FK_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->waiting.empty() || !s->active.empty()) return FK_EBUSY;  // tune while idle
+    fk::DevScope scope(s->ctx->device);
+    fk::Ctx& c = *s->ctx;
+    // synthetic inputs of the shape: zeros, with an index map that stays in range
+    const size_t kE = sizeof(double2);
+    const size_t in_bytes = fk::round256((size_t)nb * nc * kE) * 2 + fk::round256((size_t)ng * nc * kE) * 2 +
+                            fk::round256((size_t)nc * 8) + fk::round256((size_t)ng * 4) + fk::round256((size_t)nc * 4) +
+                            256;
+    fk::GppDev d{};
+    d.nb = nb; d.nv = nv; d.nc = nc; d.ng = ng; d.prec = FK_MIXED; d.flags = flags; d.ldm = nc;
+    // candidates: the default plan, and k-slices of 16..256 k-stages
+    const int ks0 = fk::gpp_default_ks(c, d);
+    const int kst = (nc + 31) / 32;
+    std::vector<int> cand{ks0};
+    for (int L = 16; L <= 256; L *= 2) {
+        const int k = std::max(1, (kst + L - 1) / L);
+        if (std::find(cand.begin(), cand.end(), k) == cand.end()) cand.push_back(k);
+    }
+    size_t ws_max = 0;
+    for (int k : cand) ws_max = std::max(ws_max, fk::gpp_job_bytes(c, d, k));
+    void* mem = s->arena.alloc(in_bytes + ws_max + 4096);
+    if (!mem) return FK_ENOMEM;
+    fk::Workspace w;
+    w.base = mem;
+    w.cap = in_bytes + ws_max + 4096;
+    d.aqsm = (const double2*)w.take((size_t)nb * nc * kE);
+    d.aqsn = (const double2*)w.take((size_t)nb * nc * kE);
+    d.eps = (const double2*)w.take((size_t)ng * nc * kE);
+    d.wt = (const double2*)w.take((size_t)ng * nc * kE);
+    d.vcoul = (const double*)w.take((size_t)nc * 8);
+    d.inv = (const int*)w.take((size_t)ng * 4);
+    d.indinv = (const int*)w.take((size_t)nc * 4);
+    d.wx = (const double*)w.take(256);
+    cudaMemsetAsync(mem, 0, in_bytes, c.stream);
+    const double wx[3] = {9.0, 10.0, 11.0};
+    cudaMemcpyAsync((void*)d.wx, wx, sizeof(wx), cudaMemcpyHostToDevice, c.stream);
+    void* ws = w.take(ws_max);
+    // the fastest plan for the request served alone in this server's steps
+    std::vector<float> ms(cand.size(), 0.f);
+    std::vector<int> units(cand.size(), 0);
+    fk_status st = FK_OK;
+    for (size_t i = 0; i < cand.size() && st == FK_OK; ++i)
+        st = fk::gpp_time_plan(c, s->step, d, cand[i], s->step_stages * c.sms, ws, ws_max, &ms[i], &units[i]);
+    cudaStreamSynchronize(c.stream);
+    s->arena.release(mem);
+    if (st != FK_OK) return st;
+    int pick = ks0;
+    float best = 1e30f;
+    for (size_t i = 0; i < cand.size(); ++i)
+        if (ms[i] < best) {
+            best = ms[i];
+            pick = cand[i];
+        }
+    s->tuned[{nb, nv, nc, ng, (long)flags}] = pick;
+    if (chosen_ks) *chosen_ks = pick;
+    return FK_OK;
 }
 
 fk_status fk_server_stats(fk_server_t s, fk_server_info* out) {

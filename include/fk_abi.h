@@ -257,6 +257,13 @@ fk_status fk_server_submit(fk_server_t srv, const fk_gpp_request* req, unsigned 
  * The ticket is consumed when the request has completed. */
 fk_status fk_server_wait(fk_server_t srv, unsigned long long ticket, double timeout_s, double* latency_s);
 fk_status fk_server_stats(fk_server_t srv, fk_server_info* out);
+/* Autotunes the plan of one request shape (while the server is idle, else
+ * FK_EBUSY): runs the shape with synthetic inputs through the server's steps
+ * under each candidate k-split (the default plan's, and k-slices of 16, 32,
+ * ..., 256 k-stages) and keeps the fastest for later requests of that shape.
+ * chosen_ks (may be NULL) gets its k-slice count. */
+fk_status fk_server_tune(fk_server_t srv, int number_bands, int nvband, int ncouls, int ngpown, unsigned flags,
+                         int* chosen_ks);
 
 /* ------------------------------------------------------------ measurement */
 

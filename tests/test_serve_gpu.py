@@ -118,3 +118,23 @@ def test_admission_is_gated_by_memory(fk, reqs, ref64):
     for o in outs:
         for k in KEYS:
             assert rel(o[k], ref64[2][k]) <= TOL, k
+
+
+def test_autotuned_plan(fk, reqs, ref64):
+    """The tuner picks a k-split for a shape; requests of that shape then use
+    it and stay within tolerance, alone and in a mix."""
+    p = reqs[2]
+    srv = fk.Server(hbm_bytes=4 << 30, max_active=8, step_stages=8)
+    try:
+        with pytest.raises(fk.FKError):
+            srv.tune(p["number_bands"], p["nvband"], p["ncouls"], 0)
+        ks = srv.tune(p["number_bands"], p["nvband"], p["ncouls"], p["ngpown"])
+        assert ks >= 1
+        alone = srv.wait(srv.submit(p))[0]
+        tickets = [srv.submit(q) for q in reqs]
+        mixed = [srv.wait(t)[0] for t in tickets]
+    finally:
+        srv.close()
+    for k in KEYS:
+        assert rel(alone[k], ref64[2][k]) <= TOL, k
+        np.testing.assert_array_equal(mixed[2][k], alone[k])
