@@ -48,11 +48,11 @@ struct Cfg {
     // lives in shared memory.  Otherwise (GPP) a 64 KB staging buffer receives
     // the next stage's FP64 A rows by bulk copy while the current one converts.
     static constexpr int STAGES = 2;
-    static constexpr int CHUNK_STAGES = 2;  // k-values per TMEM accumulation = 64
+    static constexpr int CHUNK_STAGES = 1;  // k-values per TMEM accumulation = 32
     static constexpr uint32_t A_BYTES = NSUB * BM * 64;
     static constexpr uint32_t B_BYTES = NSUB * BN * 64;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
-    static constexpr uint32_t ACC_COLS = 4 * BN;       // main re, main im, corr re, corr im
+    static constexpr uint32_t ACC_COLS = 4 * BN;       // X = A_re x [B_re|B_im], Y = A_im x [B_re|B_im]
     static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;  // double buffered
     static constexpr uint32_t W_BYTES = WSMEM ? (uint32_t)(BN * BM * sizeof(float2) + 4 * BN * sizeof(float)) : 0u;
     static constexpr uint32_t F64_BYTES = WSMEM ? 0u : (uint32_t)(BM * BK * sizeof(double2));
@@ -88,26 +88,31 @@ __device__ __forceinline__ void split3(float f, uint16_t& h, uint16_t& m, uint16
 
 // Image element writer shared by the prep/conversion kernels: complex value
 // (re, im) of row `row` (within its ROWS-row tile) at k-value k of a tile
-// column whose k-stages are ROWS*NSUB*64 bytes apart.
-template <int ROWS>
+// column whose k-stages are ROWS*NSUB*64 bytes apart.  A tiles keep the
+// sub-tile order re h, m, l, im h, m, l (each one is an MMA A operand);
+// B tiles (PAIRED) put re and im of a piece next to each other -- re h, im h,
+// re m, im m, re l, im l -- so that [B_re | B_im] of a piece is one 2*ROWS-row
+// operand.
+template <int ROWS, bool PAIRED = false>
 __device__ __forceinline__ void img_store(uint8_t* img_tile, int row, int k, float re, float im) {
     uint8_t* st = img_tile + (long)(k / BK) * (ROWS * NSUB * 64);
     const uint32_t off = tc::sw64_offset(row, k % BK);
+    constexpr int RE0 = 0, RS = PAIRED ? 2 : 1, IM0 = PAIRED ? 1 : 3;
     uint16_t h, m, l;
     split3(re, h, m, l);
-    *(uint16_t*)(st + 0 * ROWS * 64 + off) = h;
-    *(uint16_t*)(st + 1 * ROWS * 64 + off) = m;
-    *(uint16_t*)(st + 2 * ROWS * 64 + off) = l;
+    *(uint16_t*)(st + (RE0 + 0 * RS) * ROWS * 64 + off) = h;
+    *(uint16_t*)(st + (RE0 + 1 * RS) * ROWS * 64 + off) = m;
+    *(uint16_t*)(st + (RE0 + 2 * RS) * ROWS * 64 + off) = l;
     split3(im, h, m, l);
-    *(uint16_t*)(st + 3 * ROWS * 64 + off) = h;
-    *(uint16_t*)(st + 4 * ROWS * 64 + off) = m;
-    *(uint16_t*)(st + 5 * ROWS * 64 + off) = l;
+    *(uint16_t*)(st + (IM0 + 0 * RS) * ROWS * 64 + off) = h;
+    *(uint16_t*)(st + (IM0 + 1 * RS) * ROWS * 64 + off) = m;
+    *(uint16_t*)(st + (IM0 + 2 * RS) * ROWS * 64 + off) = l;
 }
 template <int BN>
 __device__ __forceinline__ void bimg_store(uint8_t* img_nt, int kstage_total_unused, int n_in_tile, int k,
                                            float re, float im) {
     (void)kstage_total_unused;
-    img_store<BN>(img_nt, n_in_tile, k, re, im);
+    img_store<BN, true>(img_nt, n_in_tile, k, re, im);
 }
 
 // Where a kernel's units come from.  OneReq: every unit belongs to the one
@@ -217,7 +222,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
         if (lane == 0) {
             int g = 0, chunk = 0;
             bool ok = true;
-            const uint32_t idp = tc::idesc_bf16(BM, BN, false), idn = tc::idesc_bf16(BM, BN, true);
+            const uint32_t idp = tc::idesc_bf16(BM, 2 * BN, false);
             for (int u = blockIdx.x; u < src.units() && ok; u += gridDim.x) {
                 int lu;
                 const TcArgs& t = src.at(u, lu);
@@ -230,8 +235,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                     const int b = chunk & 1;
                     if (!tc::mbar_wait(&accEmpty[b], ((chunk >> 1) & 1) ^ 1, WAIT_LIMIT)) { fail(1); ok = false; break; }
                     tc::tc_fence_after();
-                    const uint32_t dR = tmem + (uint32_t)(b * C::ACC_COLS), dI = dR + BN;
-                    const uint32_t cR = dR + 2 * BN, cI = dR + 3 * BN;
+                    const uint32_t dX = tmem + (uint32_t)(b * C::ACC_COLS), dY = dX + 2 * BN;
                     const int st1 = min(nst, st0 + C::CHUNK_STAGES);
                     for (int st = st0; st < st1; ++st, ++g) {
                         const int s = g % C::STAGES;
@@ -246,26 +250,20 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                         const uint32_t sb = sa + C::A_BYTES;
 #pragma unroll
                         for (int kk = 0; kk < 2; ++kk) {
-                            // sub-tile descriptors at k offset kk*16 (32 bytes)
+                            // A sub-tile (re h,m,l, im h,m,l) and paired B piece [re|im], k offset kk*16
                             auto ad = [&](int sub) { return tc::sdesc_sw64(sa + sub * BM * 64) + 2 * kk; };
-                            auto bd = [&](int sub) { return tc::sdesc_sw64(sb + sub * BN * 64) + 2 * kk; };
+                            auto bd = [&](int piece) { return tc::sdesc_sw64(sb + piece * 2 * BN * 64) + 2 * kk; };
                             const uint32_t acc0 = (st > st0 || kk > 0) ? 1u : 0u;
-                            // correction pieces (ia, ib): mm, lh, hl, mh, hm
-                            const int PA[5] = {1, 2, 0, 1, 0};
-                            const int PB[5] = {1, 0, 2, 0, 1};
+                            // piece products (a, b): the five small ones (mm, lh, hl, mh, hm), then hh;
+                            // X += A_re,a x [B_re|B_im]_b, Y += A_im,a x [B_re|B_im]_b
+                            const int PA[6] = {1, 2, 0, 1, 0, 0};
+                            const int PB[6] = {1, 0, 2, 0, 1, 0};
 #pragma unroll
-                            for (int q = 0; q < 5; ++q) {
+                            for (int q = 0; q < 6; ++q) {
                                 const uint32_t first = (q == 0) ? acc0 : 1u;
-                                tc::mma_bf16(cR, ad(PA[q]), bd(PB[q]), idp, first);       // Ar*Br
-                                tc::mma_bf16(cR, ad(3 + PA[q]), bd(3 + PB[q]), idn, 1u);  // -Ai*Bi
-                                tc::mma_bf16(cI, ad(PA[q]), bd(3 + PB[q]), idp, first);   // Ar*Bi
-                                tc::mma_bf16(cI, ad(3 + PA[q]), bd(PB[q]), idp, 1u);      // Ai*Br
+                                tc::mma_bf16(dX, ad(PA[q]), bd(PB[q]), idp, first);
+                                tc::mma_bf16(dY, ad(3 + PA[q]), bd(PB[q]), idp, first);
                             }
-                            // main hh products
-                            tc::mma_bf16(dR, ad(0), bd(0), idp, acc0);
-                            tc::mma_bf16(dR, ad(3), bd(3), idn, 1u);
-                            tc::mma_bf16(dI, ad(0), bd(3), idp, acc0);
-                            tc::mma_bf16(dI, ad(3), bd(0), idp, 1u);
                         }
                         tc::mma_commit(&empty[s]);
                     }
@@ -390,16 +388,17 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                 float2 gsum[GMAX] = {make_float2(0, 0), make_float2(0, 0), make_float2(0, 0)};
 #pragma unroll
                 for (int c0 = 0; c0 < BN; c0 += 16) {
-                    float vr[16], vi[16], wr[16], wi[16];
-                    tc::tmem_ld16(tl + c0, vr);
-                    tc::tmem_ld16(tl + BN + c0, vi);
-                    tc::tmem_ld16(tl + 2 * BN + c0, wr);
-                    tc::tmem_ld16(tl + 3 * BN + c0, wi);
+                    // X = [A_re B_re | A_re B_im], Y = [A_im B_re | A_im B_im]
+                    float xr[16], xi[16], yr[16], yi[16];
+                    tc::tmem_ld16(tl + c0, xr);
+                    tc::tmem_ld16(tl + BN + c0, xi);
+                    tc::tmem_ld16(tl + 2 * BN + c0, yr);
+                    tc::tmem_ld16(tl + 3 * BN + c0, yi);
                     tc::tmem_ld_wait();
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         const int c = c0 + j;
-                        const float2 sv = make_float2(vr[j] + wr[j], vi[j] + wi[j]);
+                        const float2 sv = make_float2(xr[j] - yi[j], xi[j] + yr[j]);
                         if (EPI == EPI_GPP) {
                             // tile column c = 3*(igp offset) + iw; column 63 is padding
                             if (c < 3 * GC) cfmaf(gsum[c % 3], wreg[c / 3], sv);
