@@ -338,7 +338,9 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
                                                                                 igp, igp, 1.0, W, W + (size_t)r.nb * r.ng,
                                                                                 (float*)(W + 2 * (size_t)r.nb * r.ng));
         // aqsntemp is reused by every (plane, n-tile): split it to BF16 pieces once
-        cudaMemsetAsync(Aimg, 0, p.bytesAimg, st);
+        const int MTa = ceil_div(r.nb, tcx::BM);
+        if (tcx::img_needs_pad(tcx::BM, r.nb, 0, r.nc))
+            tcx::img_pad_kernel<tcx::BM><<<dim3(p.kstages, MTa, 1), 256, 0, st>>>(Aimg, MTa, p.kstages, r.nb, 0, r.nc);
         tcx::aimg_convert_kernel<<<dim3(ceil_div(r.nc, 256), r.nb), 256, 0, st>>>(r.aqsn, r.nb, r.nc, p.kstages, Aimg);
         c.launches += 2;
         cudaMemsetAsync(c.errword, 0, sizeof(int), st);
@@ -351,7 +353,10 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
         a.aqsm = r.aqsm; a.ldm = r.nc; a.vcoul = r.vcoul; a.igp = igp; a.acol = igp; a.wscale = 1.0; a.G = 2; a.P = P;
         if (p.mixed) {
             // pre-split B planes (bf16 x 3), then the tensor-core contraction
-            cudaMemsetAsync(img, 0, img_bytes, st);
+            const int NTb = ceil_div(r.ng, 64);
+            if (tcx::img_needs_pad(64, r.ng, 0, r.nc))
+                tcx::img_pad_kernel<64><<<dim3(p.kstages, NTb, nb_), 256, 0, st>>>(img, NTb, p.kstages, r.ng, 0, r.nc);
+            (void)img_bytes;
             dim3 gconv(ceil_div(r.nc, 256), r.ng, nb_);
             tcx::bimg_convert_kernel<64><<<gconv, 256, 0, st>>>(eps, a.bstride, r.ng, r.nc, pls, p.kstages, img);
             tcx::TcArgs t{};

@@ -340,9 +340,12 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
                     ssx = make_float2(0.f, 0.f);
                 }
             }
-            if (D && igp >= 0 && (Q || A)) {
+            if (D) {
+                // every element of the image is written (zero where the term is masked)
+                const bool keep = igp >= 0 && (Q || A);
                 const int nt = my_igp / GPP_COLS, row = (my_igp % GPP_COLS) * 3 + iw;
-                tcx::bimg_store<BN>(D + (long)nt * p.kstages * tcx::Cfg<BN>::B_BYTES, p.kstages, row, ig, dv.x, dv.y);
+                tcx::bimg_store<BN>(D + (long)nt * p.kstages * tcx::Cfg<BN>::B_BYTES, p.kstages, row, ig,
+                                    keep ? dv.x : 0.f, keep ? dv.y : 0.f);
             }
 #pragma unroll
             for (int j = 0; j < NVC; ++j) {
@@ -577,9 +580,12 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
     if (!igp || !F || !rows || (p.bytesD && !D) || (p.bytesP && !P) || (p.bytesS && !S) || (p.bytesW && !W))
         return fail(c, FK_ENOMEM, "workspace too small for GPP request");
     if (p.mixed && D) {
-        cudaError_t e = cudaMemsetAsync(D, 0, p.bytesD, st);  // padding rows and k >= ncouls stay zero
-        if (e == cudaSuccess) e = cudaMemsetAsync(c.errword, 0, sizeof(int), st);  // bounded-wait status
-        if (e != cudaSuccess) return cuda_fail(c, e, "gpp: image clear");
+        // the prep writes every (column, k) element; padding rows and k >= ncouls are zeroed here
+        if (tcx::img_needs_pad(64, r.ng, GPP_COLS, r.nc))
+            tcx::img_pad_kernel<64><<<dim3(p.kstages, p.NT, 1), 256, 0, st>>>((uint8_t*)D, p.NT, p.kstages, r.ng,
+                                                                            GPP_COLS, r.nc);
+        cudaError_t e = cudaMemsetAsync(c.errword, 0, sizeof(int), st);  // bounded-wait status
+        if (e != cudaSuccess) return cuda_fail(c, e, "gpp: error word");
     }
     const bool Q = (r.flags & FK_GPP_ROOT_QUIRKS) != 0;
     const int M = r.nb - r.nv;
@@ -861,8 +867,11 @@ GppJob* gpp_job_create(Ctx& c, const GppDev& r0, int ks, void* ws, size_t bytes,
             *st = FK_ECUDA;
             return nullptr;
         }
-        // padding rows of the image and k >= ncouls must read as zero
-        if (cudaMemsetAsync(D, 0, p.bytesD, c.stream) != cudaSuccess) {
+        // padding rows of the image and k >= ncouls must read as zero (the prep writes the rest)
+        if (tcx::img_needs_pad(64, r.ng, GPP_COLS, r.nc))
+            tcx::img_pad_kernel<64><<<dim3(p.kstages, p.NT, 1), 256, 0, c.stream>>>((uint8_t*)D, p.NT, p.kstages,
+                                                                                   r.ng, GPP_COLS, r.nc);
+        if (cudaGetLastError() != cudaSuccess) {
             delete j;
             *st = FK_ECUDA;
             return nullptr;

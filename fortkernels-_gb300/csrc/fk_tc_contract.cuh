@@ -226,7 +226,6 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
             for (int u = blockIdx.x; u < src.units() && ok; u += gridDim.x) {
                 int lu;
                 const TcArgs& t = src.at(u, lu);
-                const ContractArgs& a = t.c;
                 int mt, nt, ks, batch, k0, k1;
                 unit_coords(t, lu, mt, nt, ks, batch);
                 krange(t, ks, k0, k1);
@@ -552,6 +551,32 @@ __global__ void bimg_convert_kernel(const double2* src, long plane_stride, int r
     const int NT = (rows + BN - 1) / BN;
     uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * (long)Cfg<BN>::B_BYTES;
     bimg_store<BN>(img_nt, kstages, n % BN, k, f64_to_f32_bits(v.x), f64_to_f32_bits(v.y));
+}
+
+// Zeros the image positions that no converter writes: rows past a tile's
+// valid rows and k-values past K.  Valid rows of tile nt: 3*min(gpp_cols,
+// cols - gpp_cols*nt) when gpp_cols > 0 (GPP: gpp_cols igp triples per tile),
+// else min(ROWS, cols - ROWS*nt).  Grid (kstages, NT, planes).
+template <int ROWS>
+__global__ void img_pad_kernel(uint8_t* img, int NT, int kstages, int cols, int gpp_cols, int K) {
+    const int kst = blockIdx.x, nt = blockIdx.y, pl = blockIdx.z;
+    const int vr = gpp_cols > 0 ? 3 * min(gpp_cols, cols - gpp_cols * nt) : min(ROWS, cols - ROWS * nt);
+    const int kv = min(BK, K - kst * BK);  // valid k-values of this stage
+    if (vr >= ROWS && kv >= BK) return;
+    uint8_t* st = img + (((long)pl * NT + nt) * kstages + kst) * (long)(ROWS * NSUB * 64);
+    for (int i = threadIdx.x; i < ROWS * BK; i += blockDim.x) {
+        const int row = i / BK, k = i % BK;
+        if (row < vr && k < kv) continue;
+        const uint32_t off = tc::sw64_offset(row, k);
+#pragma unroll
+        for (int q = 0; q < NSUB; ++q) *(uint16_t*)(st + q * ROWS * 64 + off) = 0;
+    }
+}
+// True when some image position needs img_pad_kernel.
+inline bool img_needs_pad(int rows_per_tile, int cols, int gpp_cols, int K) {
+    if (K % BK) return true;
+    if (gpp_cols > 0) return 3 * gpp_cols < rows_per_tile || cols % gpp_cols;
+    return cols % rows_per_tile != 0;
 }
 
 // FP64 rows [rows][K] -> pre-split A image [mt][kstage][NSUB][BM][64 B].
