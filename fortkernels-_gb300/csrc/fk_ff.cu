@@ -277,7 +277,7 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
         p.kchunk = ((r.nc + p.KS - 1) / p.KS + 15) / 16 * 16;
         p.KS = (r.nc + p.kchunk - 1) / p.kchunk;
     }
-    const size_t slots = (size_t)p.KS * p.NT;
+    const size_t slots = (size_t)p.KS * p.NT * (p.mixed ? tcx::FF_EPI_WARPS : 1);  // partial slots per plane
     p.bytes = (slots * (p.planesR.size() + p.planesA.size()) * r.nb * 2 + 3 * (size_t)r.nb * r.nf +
                (size_t)r.ne * r.nb) * sizeof(double2) +
               r.nb * sizeof(FactRow) + (p.planesR.size() + p.planesA.size()) * sizeof(int) + r.ng * sizeof(int) +
@@ -304,7 +304,7 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
     const FfPlan p = make_plan(c, r, ekq.data(), grid.data());
     cudaStream_t st = c.stream;
     const int nR = (int)p.planesR.size(), nA = (int)p.planesA.size();
-    const size_t slots = (size_t)p.KS * p.NT;
+    const size_t slots = (size_t)p.KS * p.NT * (p.mixed ? tcx::FF_EPI_WARPS : 1);  // partial slots per plane
     int* igp = (int*)c.ws.take(r.ng * sizeof(int));
     int* planes = (int*)c.ws.take((nR + nA) * sizeof(int));
     FactRow* fact = (FactRow*)c.ws.take(r.nb * sizeof(FactRow));

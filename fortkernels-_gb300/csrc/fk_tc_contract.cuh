@@ -38,6 +38,10 @@ constexpr int BK = 32;            // complex k-values per stage (64 B of bf16 pe
 constexpr int NSPLIT = 3;         // bf16 pieces per real value
 constexpr int NSUB = 2 * NSPLIT;  // sub-tiles per operand: re h/m/l, im h/m/l
 constexpr int THREADS = 448;
+// FF (A operand pre-split, no converter work): the 12 warps 2..13 all drain
+// TMEM, three per lane quarter, each over its own 16-column groups and its
+// own partial-sum slot; GPP: warps 4..7, one per quarter, all columns.
+constexpr int FF_EPI_WARPS = 3;
 constexpr int NCONV = 8;          // converter warps
 constexpr long long WAIT_LIMIT = 4000000000LL;  // ~2 s at 2 GHz
 
@@ -181,7 +185,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&accFull[b], 1);
-            tc::mbar_init(&accEmpty[b], 4);
+            tc::mbar_init(&accEmpty[b], AIMG ? 4 * FF_EPI_WARPS : 4);
         }
         tc::mbar_init(done, 1);
         tc::mbar_init(fFull, 1);
@@ -331,13 +335,17 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                 if (!ok) break;
             }
         }
-    } else if (warp >= 4 && warp < 8) {
+    } else if ((warp >= 4 && warp < 8) || AIMG) {
         // ------------------------------------------------------- epilogue
         // Weights are fetched once per unit: GPP into registers (a 64-wide
         // tile holds complete (igp, iw) triples of GPP_COLS igp), FF into a
         // column-major shared-memory tile.  Columns are fully unrolled so every
         // register index is a compile-time constant.
-        const int q4 = warp - 4;  // TMEM lane quarter
+        constexpr int EW = AIMG ? FF_EPI_WARPS : 1;  // warps per lane quarter
+        const int q4 = warp & 3;                     // TMEM lane quarter
+        const int ej = warp < 4 ? 2 : (warp < 8 ? 0 : (warp < 12 ? 1 : 2));  // this warp's share
+        // 16-column groups of this warp: all for GPP; FF: {0, 3}, {1}, {2}
+        auto mine = [&](int grp) { return EW == 1 || (ej == 0 ? (grp == 0 || grp == 3) : grp == ej); };
         const int row = q4 * 32 + lane;
         int chunk = 0;
         bool ok = true;
@@ -365,16 +373,20 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                 __syncwarp();
 #pragma unroll 4
                 for (int c = 0; c < BN; ++c) {
+                    if (!mine(c >> 4)) continue;
                     const int n = nt * BN + c;
                     sW[c * BM + row] = (n < a.N && m < a.M) ? t.W2[(long)n * t.ldw + m] : make_float2(0.f, 0.f);
                 }
                 for (int c = lane; c < BN; c += 32) {
+                    if (!mine(c >> 4)) continue;
                     const int n = nt * BN + c;
                     sV[q4 * BN + c] = n < a.N ? t.vcol[n] : 0.f;
                 }
                 __syncwarp();
             }
-            double2 acc[GMAX] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+            // per-unit sums as FP32 float-float pairs (TwoSum): no FP64 instruction per drain
+            // (GB300's FP64 pipe takes ~16 cycles per warp instruction); widened once per unit
+            ff32 accx[GMAX] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, accy[GMAX] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
             for (int st0 = 0; st0 < nst; st0 += C::CHUNK_STAGES, ++chunk) {
                 const int b = chunk & 1;
                 if (!tc::mbar_wait(&accFull[b], (chunk >> 1) & 1, WAIT_LIMIT) || s_abort) {
@@ -387,6 +399,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                 float2 gsum[GMAX] = {make_float2(0, 0), make_float2(0, 0), make_float2(0, 0)};
 #pragma unroll
                 for (int c0 = 0; c0 < BN; c0 += 16) {
+                    if (!mine(c0 >> 4)) continue;
                     // X = [A_re B_re | A_re B_im], Y = [A_im B_re | A_im B_im]
                     float xr[16], xi[16], yr[16], yi[16];
                     tc::tmem_ld16(tl + c0, xr);
@@ -411,11 +424,11 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                             gsum[1].y += t2.y;
                         }
                     }
-                    if (EPI == EPI_FF && (c0 & 31) == 16) {
-                        // keep FP32 column sums short: fold every 32 columns into FP64
+                    if (EPI == EPI_FF) {
+                        // keep FP32 column sums short: fold every 16-column group into FP64
                         for (int gg = 0; gg < 2; ++gg) {
-                            acc[gg].x += (double)gsum[gg].x;
-                            acc[gg].y += (double)gsum[gg].y;
+                            ff_add(accx[gg], gsum[gg].x);
+                            ff_add(accy[gg], gsum[gg].y);
                             gsum[gg] = make_float2(0.f, 0.f);
                         }
                     }
@@ -426,15 +439,17 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                 if (EPI == EPI_GPP) {
 #pragma unroll
                     for (int gg = 0; gg < 3; ++gg) {
-                        acc[gg].x += (double)gsum[gg].x;
-                        acc[gg].y += (double)gsum[gg].y;
+                        ff_add(accx[gg], gsum[gg].x);
+                        ff_add(accy[gg], gsum[gg].y);
                     }
                 }
             }
             if (!ok) break;
             if (m < a.M) {
-                const int slot = (batch * a.KS + ks) * t.NT + nt;
-                for (int gg = 0; gg < a.G; ++gg) a.P[((long)slot * a.M + m) * a.G + gg] = acc[gg];
+                const int slot = ((batch * a.KS + ks) * t.NT + nt) * EW + ej * (EW > 1);
+                for (int gg = 0; gg < a.G; ++gg)
+                    a.P[((long)slot * a.M + m) * a.G + gg] =
+                        make_double2((double)accx[gg].hi + (double)accx[gg].lo, (double)accy[gg].hi + (double)accy[gg].lo);
             }
         }
     } else {
