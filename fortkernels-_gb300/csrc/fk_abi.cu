@@ -261,6 +261,12 @@ fk_status fk_destroy(fk_ctx_t c) {
         for (auto& e : c->ev)
             if (e) cudaEventDestroy(e);
         if (c->own_stream) cudaStreamDestroy(c->own_stream);
+        if (c->copy_stream) {
+            cudaStreamSynchronize(c->copy_stream);
+            cudaStreamDestroy(c->copy_stream);
+        }
+        for (auto& e : c->pipe_ev)
+            if (e) cudaEventDestroy(e);
     }
     delete c;
     return FK_OK;
@@ -300,6 +306,161 @@ fk_status fk_last_timings(fk_ctx_t c, float ms[4]) {
 
 int fk_last_launches(fk_ctx_t c) { return c ? c->launches : -1; }
 
+namespace fk {
+namespace {
+
+// fk_gpp for large host arrays (mixed precision).  Everything crosses the host
+// link on one copy stream, in the order the GPU needs it: the small inputs
+// (packed into one pinned block), eps and wtilde, the igp columns of aqsmtemp
+// (gathered on the host while eps and wtilde are in flight), then aqsntemp in
+// row blocks.  The compute stream runs the prep once the first block (with the
+// flag bands) has landed and each block's contraction as soon as that block
+// has; the outputs come back through pinned memory in one copy.
+fk_status gpp_host_pipelined(Ctx& x, GppDev r, const fk_c128* aqsmtemp, const fk_c128* aqsntemp,
+                             const fk_c128* I_eps_array, const fk_c128* wtilde_array, const double* vcoul,
+                             const int* inv_igp_index, const int* indinv, const double* wx_array, fk_c128* achtemp,
+                             fk_c128* asxtemp, fk_c128* acht_n1_loc, fk_c128* achstemp) {
+    const int nb = r.nb, nc = r.nc, ng = r.ng;
+    const size_t e16 = sizeof(double2), band = (size_t)nb * nc * e16, col = (size_t)ng * nc * e16;
+    auto r256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    // small inputs: device arrays on a 16-byte boundary are used in place, host ones packed
+    struct Small {
+        const void* user;
+        size_t bytes;
+        bool dev;
+        size_t off;
+    } sm[4] = {{vcoul, (size_t)nc * 8, false, 0}, {inv_igp_index, (size_t)ng * 4, false, 0},
+               {indinv, (size_t)nc * 4, false, 0}, {wx_array, 24, false, 0}};
+    size_t packed = 0;
+    for (auto& q : sm) {
+        q.dev = is_device_ptr(q.user) && ((uintptr_t)q.user & 15) == 0;
+        if (!q.dev) {
+            q.off = packed;
+            packed += r256(q.bytes);
+        }
+    }
+    const bool aqm_dev = is_device_ptr(aqsmtemp) && ((uintptr_t)aqsmtemp & 15) == 0;
+    const bool compact = !aqm_dev && (long)ng * 128 <= (long)nc;
+    const size_t aqm_off = packed;
+    const size_t aqm_bytes = compact ? (size_t)nb * ng * e16 : 0;
+    const size_t outn = 7 + (size_t)nb, out_off = r256(packed + aqm_bytes);
+    const size_t pinned_bytes = out_off + outn * e16;
+    if (compact) {
+        r.aqsm_compact = true;
+        r.ldm = ng;
+    }
+    const size_t need = 2 * r256(col) + r256(band) + r256(packed + aqm_bytes) +
+                        (!aqm_dev && !compact ? r256(band) : 0) + gpp_workspace(x, r, true) + outn * e16 + 4096;
+    fk_status st = ensure_workspace(x, need);
+    if (st != FK_OK) return st;
+    x.ws.reset();
+    double2* out = (double2*)x.ws.take(outn * e16);
+    GppPipe pipe{};
+    pipe.aqsn = (const double2*)aqsntemp;
+    pipe.eps = (const double2*)I_eps_array;
+    pipe.wt = (const double2*)wtilde_array;
+    pipe.eps_d = (double2*)x.ws.take(col);
+    pipe.wt_d = (double2*)x.ws.take(col);
+    pipe.aqsn_d = (double2*)x.ws.take(band);
+    uint8_t* small_d = (packed + aqm_bytes) ? (uint8_t*)x.ws.take(packed + aqm_bytes) : nullptr;
+    double2* aqsm_full = (!aqm_dev && !compact) ? (double2*)x.ws.take(band) : nullptr;
+    if (!out || !pipe.eps_d || !pipe.wt_d || !pipe.aqsn_d || ((packed + aqm_bytes) && !small_d) ||
+        (!aqm_dev && !compact && !aqsm_full))
+        return fail(x, FK_ENOMEM, "workspace: pipeline");
+    r.aqsn = pipe.aqsn_d;
+    r.eps = pipe.eps_d;
+    r.wt = pipe.wt_d;
+    phase_mark(x, 0);
+    uint8_t* pb = (uint8_t*)pinned_buffer(x, pinned_bytes);  // waits until the last call's outputs were read
+    if (!pb) return fail(x, FK_ENOMEM, "gpp: pinned staging");
+    if ((st = gpp_pipe_begin(x)) != FK_OK) return st;
+    cudaStream_t cs = x.copy_stream;
+    // 1. small inputs
+    for (auto& q : sm)
+        if (!q.dev) std::memcpy(pb + q.off, q.user, q.bytes);
+    if (packed && cudaMemcpyAsync(small_d, pb, packed, cudaMemcpyHostToDevice, cs) != cudaSuccess)
+        return cuda_fail(x, cudaGetLastError(), "gpp: small inputs");
+    // 2. eps and wtilde
+    if (cudaMemcpyAsync(pipe.eps_d, I_eps_array, col, cudaMemcpyHostToDevice, cs) != cudaSuccess ||
+        cudaMemcpyAsync(pipe.wt_d, wtilde_array, col, cudaMemcpyHostToDevice, cs) != cudaSuccess)
+        return cuda_fail(x, cudaGetLastError(), "gpp: eps / wtilde");
+    // 3. aqsmtemp: its igp columns gathered on the host meanwhile (or the whole array)
+    if (compact) {
+        std::vector<int> invh, indh;
+        const int* ip = inv_igp_index;
+        const int* dp = indinv;
+        if (sm[1].dev) {
+            invh.resize(ng);
+            if (cudaMemcpy(invh.data(), inv_igp_index, ng * sizeof(int), cudaMemcpyDefault) != cudaSuccess)
+                return cuda_fail(x, cudaGetLastError(), "gpp: reading inv_igp_index");
+            ip = invh.data();
+        }
+        if (sm[2].dev) {
+            indh.resize(nc);
+            if (cudaMemcpy(indh.data(), indinv, nc * sizeof(int), cudaMemcpyDefault) != cudaSuccess)
+                return cuda_fail(x, cudaGetLastError(), "gpp: reading indinv");
+            dp = indh.data();
+        }
+        std::vector<int> gcol(ng);
+        for (int h = 0; h < ng; ++h) {  // BGW-Kernels/gppKer.cpp:322-325
+            const int ind_ = ip[h];
+            int g = -1;
+            if (ind_ == nc) g = nc - 1;
+            else if (ind_ >= 0 && ind_ < nc) g = dp[ind_];
+            gcol[h] = g >= nc ? -1 : g;
+        }
+        fk_c128* buf = (fk_c128*)(pb + aqm_off);
+        for (int n1 = 0; n1 < nb; ++n1) {
+            const fk_c128* row = aqsmtemp + (size_t)n1 * nc;
+            for (int h = 0; h < ng; ++h) buf[(size_t)n1 * ng + h] = gcol[h] >= 0 ? row[gcol[h]] : fk_c128{0.0, 0.0};
+        }
+        if (cudaMemcpyAsync(small_d + aqm_off, pb + aqm_off, aqm_bytes, cudaMemcpyHostToDevice, cs) != cudaSuccess)
+            return cuda_fail(x, cudaGetLastError(), "gpp: aqsmtemp columns");
+        r.aqsm = (const double2*)(small_d + aqm_off);
+    } else if (aqm_dev) {
+        r.aqsm = (const double2*)aqsmtemp;
+    } else {
+        if (cudaMemcpyAsync(aqsm_full, aqsmtemp, band, cudaMemcpyHostToDevice, cs) != cudaSuccess)
+            return cuda_fail(x, cudaGetLastError(), "gpp: staging aqsmtemp");
+        r.aqsm = aqsm_full;
+    }
+    if (cudaEventRecord(x.pipe_ev[PIPE_READY], cs) != cudaSuccess)
+        return cuda_fail(x, cudaGetLastError(), "gpp: pipeline");
+    // 4. aqsntemp in row blocks
+    if ((st = gpp_pipe_copy(x, r, &pipe, 0, gpp_pipe_chunks(x, r))) != FK_OK) return st;
+    r.vcoul = sm[0].dev ? vcoul : (const double*)(small_d + sm[0].off);
+    r.inv = sm[1].dev ? inv_igp_index : (const int*)(small_d + sm[1].off);
+    r.indinv = sm[2].dev ? indinv : (const int*)(small_d + sm[2].off);
+    r.wx = sm[3].dev ? wx_array : (const double*)(small_d + sm[3].off);
+    r.out = out;
+    if ((st = gpp_run(x, r, &pipe)) != FK_OK) return st;
+    // outputs through pinned memory
+    double2* po = (double2*)(pb + out_off);
+    cudaError_t e = cudaMemcpyAsync(po, out, outn * e16, cudaMemcpyDeviceToHost, x.stream);
+    if (e == cudaSuccess) e = cudaEventRecord(x.pinned_ev, x.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(x.stream);
+    if (e != cudaSuccess) return cuda_fail(x, e, "gpp: synchronize");
+    phase_close(x, 4);
+    if ((st = check_errword(x)) != FK_OK) return st;
+    struct O {
+        fk_c128* dst;
+        size_t off, n;
+    } outs[4] = {{achtemp, 0, 3}, {asxtemp, 3, 3}, {achstemp, 6, 1}, {acht_n1_loc, 7, (size_t)nb}};
+    for (const O& o : outs) {
+        if (!o.dst) continue;
+        if (is_device_ptr(o.dst)) {
+            if (cudaMemcpy(o.dst, po + o.off, o.n * e16, cudaMemcpyHostToDevice) != cudaSuccess)
+                return cuda_fail(x, cudaGetLastError(), "gpp: output copy");
+        } else {
+            std::memcpy(o.dst, po + o.off, o.n * e16);
+        }
+    }
+    return FK_OK;
+}
+
+}  // namespace
+}  // namespace fk
+
 fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsmtemp, const fk_c128* aqsntemp,
                  const fk_c128* I_eps_array, const fk_c128* wtilde_array, const double* vcoul,
                  const int* inv_igp_index, const int* indinv, const double* wx_array, fk_precision precision,
@@ -330,6 +491,11 @@ fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsm
     r.nb = nb; r.nv = nv; r.nc = nc; r.ng = ng; r.prec = precision; r.flags = flags;
     r.ldm = nc;
     r.aqsm_compact = false;
+    // Large host arrays of a mixed-precision call: stream eps, wtilde and aqsntemp in
+    // k-chunks and compute each chunk as it lands (the host link is the bottleneck).
+    if (precision == FK_MIXED && !aqn.dev && !eps.dev && !wt.dev && nb > nv && band >= ((size_t)64 << 20))
+        return fk::gpp_host_pipelined(x, r, aqsmtemp, aqsntemp, I_eps_array, wtilde_array, vcoul, inv_igp_index,
+                                      indinv, wx_array, achtemp, asxtemp, acht_n1_loc, achstemp);
     // Host aqsmtemp: the sum reads only its ngpown columns igp(my_igp)
     // (BGW-Kernels/gppKer.cpp:322-325), so when those are few, gather them on
     // the host and stage nb x ngpown values instead of nb x ncouls.

@@ -61,6 +61,7 @@ struct PrepArgs {
     int nch;
     int tile;    // mixed: plane waves per chunk (a multiple of PREP_THREADS)
     int n1base;  // first flag band handled by this pass
+    int ch0;     // first chunk of this launch (blockIdx.x counts from it)
 };
 
 // ---------------------------------------------------------------- FP64 exact
@@ -368,7 +369,7 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
 template <int Q, int BN>
 __global__ void __launch_bounds__(PREP_THREADS, 2) prep_mixed_kernel(PrepArgs p) {
     __shared__ double2 sm[8 * NVC * 6];
-    prep_mixed_item<Q, BN>(p, blockIdx.x, blockIdx.y, sm);
+    prep_mixed_item<Q, BN>(p, p.ch0 + blockIdx.x, blockIdx.y, sm);
 }
 
 // ------------------------------------------------------------------ finalize
@@ -469,6 +470,7 @@ __global__ void totals_kernel(int nb, const double2* rows, double2* out) { total
 
 struct Plan {
     int nch, tile, passes;
+    int pipe_sub, pipe_chunks;   // pipelined host path: prep chunks (= k-slices) per k-chunk, k-chunks
     int BN, kstages, units;      // tensor-core contraction (mixed)
     int MT, NT, KS, kchunk;      // main contraction
     int MTs, NTs, KSs, kchunks;  // static remainder contraction
@@ -501,9 +503,12 @@ void pick_split(int tiles, int K, int target, int& KS, int& kchunk) {
     KS = (K + kchunk - 1) / kchunk;
 }
 
-Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0) {
+constexpr int PIPE_CHUNKS = 8;  // row blocks of the pipelined host path at most (events 0..7 of Ctx::pipe_ev)
+
+Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0, bool pipelined = false) {
     Plan p{};
     p.mixed = r.prec == FK_MIXED;
+    p.pipe_sub = p.pipe_chunks = 0;
     if (r.prec == FK_MIXED) {
         // one wave: chunks x ngpown blocks fill the resident block slots
         int per_sm = 0;
@@ -530,6 +535,15 @@ Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0) {
             const int ks = std::min(ks_override, std::max(1, ceil_div(r.nc, tcx::BK)));
             p.kchunk = ceil_div(ceil_div(r.nc, ks), tcx::BK) * tcx::BK;
             p.KS = ceil_div(r.nc, p.kchunk);
+        }
+        if (pipelined) {
+            // one launch per row block of pipe_sub m-tiles: enough k-slices for that block to fill the GPU
+            p.pipe_sub = ceil_div(p.MT, PIPE_CHUNKS);
+            p.pipe_chunks = ceil_div(p.MT, p.pipe_sub);
+            const int ks = std::max(1, std::min(c.sms / std::max(1, p.pipe_sub * p.NT), r.nc / 256));
+            p.kchunk = ceil_div(ceil_div(r.nc, ks), tcx::BK) * tcx::BK;
+            p.KS = ceil_div(r.nc, p.kchunk);
+            p.units = p.MT * p.NT * p.KS;
         }
         p.units = p.MT * p.NT * p.KS;
     } else {
@@ -561,13 +575,43 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 
 }  // namespace
 
-size_t gpp_workspace(const Ctx& c, const GppDev& r) {
-    Plan p = make_plan(c, r);
+size_t gpp_workspace(const Ctx& c, const GppDev& r, bool pipelined) {
+    Plan p = make_plan(c, r, 0, pipelined);
     return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesRows + p.bytesIgp + p.bytesW + 10 * 256;
 }
 
-fk_status gpp_run(Ctx& c, const GppDev& r) {
-    const Plan p = make_plan(c, r);
+int gpp_pipe_chunks(const Ctx& c, const GppDev& r) { return make_plan(c, r, 0, true).pipe_chunks; }
+
+fk_status gpp_pipe_begin(Ctx& c) {
+    if (!c.copy_stream && cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return cuda_fail(c, cudaGetLastError(), "gpp: copy stream");
+    for (auto& e : c.pipe_ev)
+        if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return cuda_fail(c, cudaGetLastError(), "gpp: pipeline events");
+    // the destinations are free once the work queued before this call is done
+    cudaError_t e = cudaEventRecord(c.pipe_ev[PIPE_FREE], c.stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c.copy_stream, c.pipe_ev[PIPE_FREE], 0);
+    return e == cudaSuccess ? FK_OK : cuda_fail(c, e, "gpp: pipeline start");
+}
+
+fk_status gpp_pipe_copy(Ctx& c, const GppDev& r, const GppPipe* pipe, int q0, int q1) {
+    const Plan p = make_plan(c, r, 0, true);
+    const size_t rowb = (size_t)r.nc * sizeof(double2);
+    for (int q = q0; q < std::min(q1, p.pipe_chunks); ++q) {
+        // rows of m-tiles q*pipe_sub .. ; block 0 also carries the flag bands 0 .. nvband-1
+        const long r0 = q == 0 ? 0 : r.nv + (long)q * p.pipe_sub * tcx::BM;
+        const long r1 = std::min((long)r.nb, r.nv + (long)(q + 1) * p.pipe_sub * tcx::BM);
+        cudaError_t e = cudaMemcpyAsync(pipe->aqsn_d + r0 * r.nc, pipe->aqsn + r0 * r.nc, (size_t)(r1 - r0) * rowb,
+                                        cudaMemcpyHostToDevice, c.copy_stream);
+        if (e == cudaSuccess) e = cudaEventRecord(c.pipe_ev[q], c.copy_stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "gpp: block copy");
+    }
+    return FK_OK;
+}
+
+fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
+    const Plan p = make_plan(c, r, 0, pipe != nullptr);
+    if (pipe && !p.pipe_chunks) return fail(c, FK_EINVAL, "gpp: pipelined staging needs the mixed path");
     cudaStream_t st = c.stream;
     int* igp = (int*)c.ws.take(p.bytesIgp);
     int* acol = igp + r.ng;
@@ -592,6 +636,8 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
     c.launches = 0;
 
     phase_mark(c, 1);
+    if (pipe && cudaStreamWaitEvent(st, c.pipe_ev[PIPE_READY], 0) != cudaSuccess)
+        return cuda_fail(c, cudaGetLastError(), "gpp: waiting for the small inputs");
     igp_map_kernel<<<ceil_div(r.ng, 128), 128, 0, st>>>(r.ng, r.nc, r.inv, r.indinv, r.aqsm_compact ? 1 : 0, igp, acol);
     ++c.launches;
     if (p.mixed && M > 0) {
@@ -600,9 +646,50 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
                                                                             igp, acol, 0.5, W, nullptr, nullptr);
         ++c.launches;
     }
-    for (int pass = 0; pass < p.passes; ++pass) {
+    // pipelined host path: the prep waits for row block 0 (the flag bands), each
+    // block's contraction for its own copy
+    if (pipe) {
+        if (cudaStreamWaitEvent(st, c.pipe_ev[0], 0) != cudaSuccess)
+            return cuda_fail(c, cudaGetLastError(), "gpp: waiting for a block");
+        for (int pass = 0; pass < p.passes; ++pass) {
+            PrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, pass == 0 ? D : nullptr, p.kstages,
+                       F, p.nch, p.tile, pass * NVC, 0};
+            if (Q) prep_mixed_kernel<1, 64><<<dim3(p.nch, r.ng), PREP_THREADS, 0, st>>>(a);
+            else prep_mixed_kernel<0, 64><<<dim3(p.nch, r.ng), PREP_THREADS, 0, st>>>(a);
+            ++c.launches;
+        }
+        if (p.mixed && M > 0) {
+            ContractArgs a{};
+            a.A = r.aqsn; a.lda = r.nc; a.m0 = r.nv; a.M = M;
+            a.B = D; a.ldb = r.nc; a.bstride = 0; a.N = 3 * r.ng; a.K = r.nc;
+            a.KS = p.KS; a.kchunk = p.kchunk; a.batches = 1; a.batch_plane = nullptr;
+            a.aqsm = r.aqsm; a.ldm = r.ldm; a.vcoul = r.vcoul; a.igp = igp; a.acol = acol; a.wscale = 0.5; a.G = 3;
+            a.P = P;
+            tcx::TcArgs t{};
+            t.c = a;
+            t.Bimg = (const uint8_t*)D;
+            t.W1 = W; t.W2 = nullptr; t.ldw = M; t.gpp_cols = GPP_COLS; t.Aimg = nullptr; t.vcol = nullptr;
+            t.kstages_total = p.kstages;
+            t.NT = p.NT;
+            t.err = c.errword;
+            if (tcx::encode_rows_map(&t.amap, r.aqsn, r.nc, r.nc, r.nb) != cudaSuccess)
+                return fail(c, FK_ECUDA, "gpp: cannot describe aqsntemp as a tensor map");
+            set_smem(tcx::tc_contract_kernel<EPI_GPP, 64, false>, tcx::Cfg<64>::SMEM);
+            for (int q = 0; q < p.pipe_chunks; ++q) {
+                if (q > 0 && cudaStreamWaitEvent(st, c.pipe_ev[q], 0) != cudaSuccess)
+                    return cuda_fail(c, cudaGetLastError(), "gpp: waiting for a block");
+                t.mt0 = q * p.pipe_sub;
+                t.MT = std::min(p.MT, t.mt0 + p.pipe_sub) - t.mt0;
+                t.units = t.MT * p.NT * p.KS;
+                tcx::tc_contract_kernel<EPI_GPP, 64, false>
+                    <<<std::min(t.units, c.sms), tcx::THREADS, tcx::Cfg<64>::SMEM, st>>>(t);
+                ++c.launches;
+            }
+        }
+    }
+    for (int pass = 0; pass < p.passes && !pipe; ++pass) {
         PrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, pass == 0 ? D : nullptr, p.kstages,
-                   F, p.nch, p.tile, pass * NVC};
+                   F, p.nch, p.tile, pass * NVC, 0};
         dim3 grid(p.nch, r.ng);
         if (p.mixed) {
             if (Q) prep_mixed_kernel<1, 64><<<grid, PREP_THREADS, 0, st>>>(a);
@@ -614,7 +701,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r) {
         ++c.launches;
     }
     phase_mark(c, 2);
-    if (M > 0) {
+    if (M > 0 && !pipe) {
         ContractArgs a{};
         a.A = r.aqsn; a.lda = r.nc; a.m0 = r.nv; a.M = M;
         a.B = D; a.ldb = r.nc; a.bstride = 0; a.N = 3 * r.ng; a.K = r.nc;
@@ -846,7 +933,7 @@ GppJob* gpp_job_create(Ctx& c, const GppDev& r0, int ks, void* ws, size_t bytes,
     q.passes = p.passes;
     q.inv = r.inv; q.indinv = r.indinv; q.igp = igp; q.acol = acol;
     q.aqsm = r.aqsm; q.ldm = r.ldm; q.vcoul = r.vcoul; q.W = W;
-    q.prep = PrepArgs{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, D, p.kstages, F, p.nch, p.tile, 0};
+    q.prep = PrepArgs{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, D, p.kstages, F, p.nch, p.tile, 0, 0};
     q.rows = RowsArgs{r.nb, r.nv, r.ng, p.KS * p.NT, P, 0, nullptr, p.nch, F, r.ldm, r.aqsm, r.vcoul, igp, acol, rows};
     q.out = out;
     if (M > 0) {

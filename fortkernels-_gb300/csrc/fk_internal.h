@@ -46,6 +46,10 @@ struct Ctx {
     };
     std::unordered_map<uint64_t, GraphEntry> graphs;
     bool use_graphs = true;
+    // host-input pipelining: a copy stream and events (one per k-chunk, plus
+    // "buffers free" and "small inputs ready"), created on first use
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t pipe_ev[10] = {};
 };
 
 // Set the context's last error and return the status.
@@ -65,9 +69,26 @@ struct GppDev {
     unsigned flags;
     double2* out;      // device [3 achtemp | 3 asxtemp | 1 achstemp | nb acht_n1_loc]
 };
+// Host arrays of a mixed-precision request streamed to the device in row
+// blocks while the blocks already copied are being computed (the host link is
+// far slower than HBM, so the copy is the call's critical path).
+struct GppPipe {
+    const double2 *aqsn, *eps, *wt;  // host sources, row-major as in GppDev
+    double2 *aqsn_d, *eps_d, *wt_d;  // device destinations (r.aqsn, r.eps, r.wt point at them)
+};
 // Bytes of workspace gpp_run needs for this request (excluding staged inputs).
-size_t gpp_workspace(const Ctx& c, const GppDev& r);
-fk_status gpp_run(Ctx& c, const GppDev& r);
+size_t gpp_workspace(const Ctx& c, const GppDev& r, bool pipelined = false);
+// Pipelined calls: aqsntemp moves in row blocks (chunk 0: the flag bands and the
+// first block of m-tiles; then one block per chunk); gpp_pipe_chunks gives their
+// number; gpp_pipe_begin makes c.copy_stream wait for the work already queued on
+// c.stream (the destinations' last users); gpp_pipe_copy queues the row blocks
+// [q0, q1) on c.copy_stream, each followed by its event.  The caller copies
+// eps, wtilde and the small inputs first and records pipe_ev[PIPE_READY].
+constexpr int PIPE_FREE = 8, PIPE_READY = 9;
+int gpp_pipe_chunks(const Ctx& c, const GppDev& r);
+fk_status gpp_pipe_begin(Ctx& c);
+fk_status gpp_pipe_copy(Ctx& c, const GppDev& r, const GppPipe* pipe, int q0, int q1);
+fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe = nullptr);
 
 // Served GPP requests (mixed precision): a request's plan, workspace and
 // descriptors, and the captured step that runs several of them at once.

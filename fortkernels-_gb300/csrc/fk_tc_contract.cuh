@@ -75,6 +75,7 @@ struct TcArgs {
     int gpp_cols;         // GPP: igp columns per n-tile (21: complete (igp, iw) triples)
     int kstages_total;    // k-stages per (plane, nt) in Bimg = ceil(K/32)
     int MT, NT, units;
+    int mt0;              // first m-tile of the launch (its units cover m-tiles mt0 .. mt0+MT-1)
     int* err;             // device error word (nonzero: a wait timed out)
 };
 
@@ -204,7 +205,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
 
     // local unit -> (m-tile, n-tile, k-slice, batch) and the slice's k range
     auto unit_coords = [&](const TcArgs& t, int u, int& mt, int& nt, int& ks, int& batch) {
-        mt = u % t.MT;
+        mt = t.mt0 + u % t.MT;
         int r = u / t.MT;
         nt = r % t.NT;
         r /= t.NT;
