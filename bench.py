@@ -39,6 +39,8 @@ WORKLOADS = {
     "gpp1638": dict(kind="gpp", nb=512, nv=2, nc=32768, ng=1638),
     # BASELINE config 2: FF full-frequency contraction
     "ff": dict(kind="ff", nb=512, nv=2, nc=4096, ng=512, nf=15, ne=10),
+    # BASELINE config 4: large FF contraction (I_epsR/I_epsA ~17 GB each, drawn on the GPU)
+    "ff4": dict(kind="ff", nb=2048, nv=2, nc=8192, ng=4096, nf=32, ne=10, device_inputs=True),
     # BASELINE config 3: a served, uneven GPP request stream
     "serve": dict(kind="serve", requests=256, nb_choices=(128, 256, 512, 1024), nc_lo=2048, nc_hi=32768,
                   nc_levels=8, nv=2, load=0.8),
@@ -84,7 +86,16 @@ def make_inputs(fk, w, seed=2024):
     if w["kind"] == "gpp":
         return fk.inputs.gpp_synthetic(w["nb"], w["nv"], w["nc"], w["ng"], seed=seed, dist="uniform",
                                        index="baseline", wx="baseline")
+    if w.get("device_inputs"):
+        return fk.inputs.ff_synthetic_device(w["nb"], w["nv"], w["nc"], w["ng"], w["nf"], w["ne"], seed=seed)
     return fk.inputs.ff_synthetic(w["nb"], w["nv"], w["nc"], w["ng"], w["nf"], w["ne"], seed=seed)
+
+
+def to_np(v):
+    """numpy view of an input array (torch tensors are copied to the host)."""
+    if type(v).__module__.startswith("torch"):
+        return v.detach().cpu().numpy()
+    return v
 
 
 class ClockSampler:
@@ -249,7 +260,13 @@ def run_reference(a, w):
             "e2e": {"value": val, "unit": "terms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }), flush=True)
         return
-    p = make_inputs(fk, w)
+    if w.get("device_inputs"):
+        # config 4 is far too large for the host cores: a bounded sample of it
+        # (8 bands, 2 frequency planes, full ncouls x ngpown) per step
+        w = dict(w, nb=8, nf=2)
+        p = fk.inputs.ff_synthetic(w["nb"], w["nv"], w["nc"], w["ng"], w["nf"], w["ne"], seed=2024)
+    else:
+        p = make_inputs(fk, w)
     call = (lambda: oracle.gpp(p, nthreads=cores)) if w["kind"] == "gpp" else \
         (lambda: oracle.ff(p, flags=oracle.ORC_FF_SCHDT_GEMM, nthreads=cores))
     for _ in range(a.warmup):
@@ -261,7 +278,8 @@ def run_reference(a, w):
         times.append(time.perf_counter() - t0)
     tot = sum(times)
     val = terms(w) * a.steps / tot
-    sample = f"full workload per step ({terms(w):.3g} terms), OpenMP {cores} threads"
+    sample = (f"{'a sample of the workload: %d bands, %d frequencies' % (w['nb'], w['nf']) if w.get('device_inputs') else 'full workload'}"
+              f" per step ({terms(w):.3g} terms), OpenMP {cores} threads")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": val, "unit": "terms/s", "n_gpus": a.gpus,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * tot / a.steps, "higher_is_better": True,
@@ -393,10 +411,17 @@ def run_ours(a, w):
     # end to end through the C ABI with pinned host buffers
     hp = dict(p)
     h2d = 0
-    for k in keys_c:
-        t = torch.from_numpy(np.ascontiguousarray(p[k])).pin_memory()
+    # arrays drawn on the GPU (config 4) go through host memory like the others
+    keys_h = keys_c + [k for k, v in p.items() if type(v).__module__.startswith("torch")]
+    for k in keys_h:
+        t = (p[k].cpu() if k not in keys_c else torch.from_numpy(np.ascontiguousarray(p[k]))).pin_memory()
         hp[k] = t
-        h2d += t.numel() * t.element_size()
+        n = t.numel() * t.element_size()
+        if w["kind"] == "gpp" and k == "aqsmtemp" and w["ng"] * 128 <= w["nc"]:
+            # the library reads only the ngpown igp columns of aqsmtemp (BGW-Kernels/gppKer.cpp:322-325),
+            # gathers them on the host and sends number_bands x ngpown values
+            n = w["nb"] * w["ng"] * t.element_size()
+        h2d += n
     d2h = sum(v.numel() * v.element_size() for v in outs.values() if v is not None)
     for _ in range(max(1, a.warmup)):
         host_call(prec, hp)
@@ -462,17 +487,22 @@ def cpu_baseline(fk, w, p):
         return {"value": terms(w) / dt, "unit": "terms/s", "cores": cores, "kind": "port",
                 "sample": f"one full call ({terms(w):.3g} terms)"}
     q = dict(p)
-    nbs = 64
+    big = w["ng"] * w["nc"] * w["nf"] > 1e9
+    nbs, nfs = (8, 4) if big else (64, w["nf"])
     for k in ("aqsmtemp", "aqsntemp"):
-        q[k] = p[k][:nbs]
+        q[k] = np.ascontiguousarray(to_np(p[k][:nbs]))
+    for k in ("I_epsR_array", "I_epsA_array"):
+        q[k] = np.ascontiguousarray(to_np(p[k][:nfs]))
+    for k in ("dFreqGrid", "dFreqBrd", "pref"):
+        q[k] = np.ascontiguousarray(p[k][:nfs])
     q["ekq"] = p["ekq"][:nbs]
-    q["number_bands"] = nbs
+    q["number_bands"], q["nFreq"] = nbs, nfs
     t0 = time.perf_counter()
     oracle.ff(q, flags=oracle.ORC_FF_SCHDT_GEMM, nthreads=cores)
     dt = time.perf_counter() - t0
-    tq = nbs * w["ng"] * w["nc"] * w["nf"]
+    tq = nbs * w["ng"] * w["nc"] * nfs
     return {"value": tq / dt, "unit": "terms/s", "cores": cores, "kind": "port",
-            "sample": f"first {nbs} of {w['nb']} bands ({tq:.3g} terms)"}
+            "sample": f"first {nbs} of {w['nb']} bands, {nfs} of {w['nf']} frequencies ({tq:.3g} terms)"}
 
 
 def serve_stream(w, seed=2024):

@@ -159,3 +159,34 @@ def ff_synthetic(number_bands: int, nvband: int, ncouls: int, ngpown: int, nFreq
         "pref_zb": 0.5 / 3.14, "freqevalmin": 0.0, "freqevalstep": 0.5, "occ": 1.0,
         "inv_igp_index": inv, "indinv": indinv,
     }
+
+
+def ff_synthetic_device(number_bands: int, nvband: int, ncouls: int, ngpown: int, nFreq: int, nfreqeval: int,
+                        seed: int = 0, device: str = "cuda") -> dict:
+    """ff_synthetic's distributions with the four large arrays (aqsmtemp,
+    aqsntemp, I_epsR_array, I_epsA_array) drawn on the GPU as torch tensors
+    (BASELINE config 4 holds ~17 GB per epsilon array); the small arrays are
+    numpy, as in ff_synthetic."""
+    import torch
+    gen = torch.Generator(device=device).manual_seed(seed)
+
+    def cu(shape):
+        x = torch.rand(tuple(shape) + (2,), generator=gen, device=device, dtype=torch.float64)
+        x -= 0.5
+        return torch.view_as_complex(x)
+
+    p = ff_synthetic(1, nvband, 1, 1, nFreq, nfreqeval, seed=seed)  # small arrays of the right kind
+    rng = np.random.default_rng(seed + 1)
+    epsR, epsA = cu((nFreq, ngpown, ncouls)), cu((nFreq, ngpown, ncouls))
+    idx = torch.arange(ngpown, device=device)
+    epsR[:, idx, idx] += 1.0
+    epsA[:, idx, idx] += 1.0
+    p.update({
+        "number_bands": number_bands, "ncouls": ncouls, "ngpown": ngpown,
+        "aqsmtemp": cu((number_bands, ncouls)), "aqsntemp": cu((number_bands, ncouls)),
+        "I_epsR_array": epsR, "I_epsA_array": epsA,
+        "vcoul": rng.uniform(0.1, 1.0, ncouls), "ekq": rng.uniform(-1.0, 1.0, number_bands),
+        "inv_igp_index": np.arange(ngpown, dtype=np.int32), "indinv": np.arange(ncouls, dtype=np.int32),
+    })
+    return p
+

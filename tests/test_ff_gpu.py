@@ -88,3 +88,20 @@ def test_ff_rejects_bad_arguments(ctx, fk):
     with pytest.raises(fk.FKError) as e:
         ctx.ff(q)  # ngpown > ncouls, rejected as in FFKer_cori/ffKernel.cpp:320
     assert e.value.status == 1
+
+
+def test_ff_config4_full_size(ctx, fk):
+    """BASELINE config 4 (number_bands=2048, ncouls=8192, ngpown=4096, nFreq=32;
+    I_epsR/I_epsA ~17 GB each, drawn on the GPU): the tensor-core path against
+    the FP64 DMMA path, every output within 1e-6 relative."""
+    import torch
+    free, _ = torch.cuda.mem_get_info()
+    if free < 80 << 30:
+        pytest.skip("needs ~80 GB of free device memory")
+    p = fk.inputs.ff_synthetic_device(2048, 2, 8192, 4096, 32, 10, seed=4)
+    f = fk.FK_FF_SCHDT_GEMM | fk.FK_FF_SPLIT_ACHD
+    res, ref = ctx.ff(p, "mixed", f), ctx.ff(p, "fp64", f)
+    del p
+    torch.cuda.empty_cache()
+    errs = {k: rel(res[k], ref[k]) for k in KEYS if np.max(np.abs(ref[k])) > 0}
+    assert errs and all(e <= TOLMX for e in errs.values()), errs
