@@ -41,6 +41,9 @@ WORKLOADS = {
     "ff": dict(kind="ff", nb=512, nv=2, nc=4096, ng=512, nf=15, ne=10),
     # BASELINE config 4: large FF contraction (I_epsR/I_epsA ~17 GB each, drawn on the GPU)
     "ff4": dict(kind="ff", nb=2048, nv=2, nc=8192, ng=4096, nf=32, ne=10, device_inputs=True),
+    # the FF shape whose (band, frequency, evaluation frequency) epilogue dominates
+    # (ffkernel.deslippe.best.f90's compute-bound example 8 2 1000 60 20000 30000)
+    "ffsigma": dict(kind="ff", nb=8, nv=2, nc=1000, ng=60, nf=20000, ne=30000, device_inputs=True),
     # BASELINE config 3: a served, uneven GPP request stream
     "serve": dict(kind="serve", requests=256, nb_choices=(128, 256, 512, 1024), nc_lo=2048, nc_hi=32768,
                   nc_levels=8, nv=2, load=0.8),

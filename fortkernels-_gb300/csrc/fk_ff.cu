@@ -76,19 +76,79 @@ FK_DEV double2 gc_div(double2 a, double2 b) {
     return make_double2(__ddiv_rn(num.x, den.x), __ddiv_rn(num.y, den.x));
 }
 
-// achDtemp_Kernel's schDi sum over ifreq for one (iw, n1), ffKernel.cpp:199-206.
-__global__ void ff_schdi_kernel(EpiArgs a) {
-    const int n1 = blockIdx.x * blockDim.x + threadIdx.x, iw = blockIdx.y;
-    if (n1 >= a.nb) return;
+// achDtemp_Kernel's schDi sum (FFKer_cori/ffKernel.cpp:199-206): for each
+// (iw, n1), sum over ifreq of -((0, pref[f]) x schDt[n1][f]) / (wx - coh[f]),
+// coh[f] = (grid[f] - brd[f].re, 0 - brd[f].im), wx = freqevalmin - ekq[n1] +
+// (iw-1)*freqevalstep.  The (n1, f) numerator and the f terms do not depend on
+// iw: they are formed once here (same FP64 operations as inside the loop), and
+// for the mixed path also as FP32 tables, with coh.re split into a float-float
+// pair so that the nearly cancelling difference wx - coh.re keeps its accuracy.
+struct SchdiTab {
+    double2 *num, *coh;  // [nb][nf], [nf]
+    float4* f32;         // [nb][nf]: (num.re, num.im, -coh.im, 0) as FP32
+    float2* cohr;        // [nf]: coh.re as (hi, lo)
+};
+
+__global__ void ff_schdi_tables_kernel(EpiArgs a, SchdiTab t) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x, n1 = blockIdx.y;
+    if (f >= a.nf) return;
+    const double2 coh = make_double2(__dsub_rn(a.grid[f], a.brd[f].x), 0.0 - a.brd[f].y);
+    const double2 num = cmul(make_double2(0.0, a.pref[f]), schdt_of(a, n1, f));
+    t.num[(long)n1 * a.nf + f] = num;
+    if (n1 == 0) t.coh[f] = coh;
+    if (t.f32) {
+        t.f32[(long)n1 * a.nf + f] =
+            make_float4(f64_to_f32_bits(num.x), f64_to_f32_bits(num.y), f64_to_f32_bits(0.0 - coh.y), 0.f);
+        if (n1 == 0) {
+            const float hi = f64_to_f32_bits(coh.x);
+            t.cohr[f] = make_float2(hi, f64_to_f32_bits(coh.x - (double)hi));
+        }
+    }
+}
+
+// FP64: the reference's operations per term (GPUComplex_divide), block = one band,
+// threads = consecutive iw, so every f-table load is uniform across the warp.
+__global__ void ff_schdi_kernel(EpiArgs a, SchdiTab t) {
+    const int iw = blockIdx.x * blockDim.x + threadIdx.x, n1 = blockIdx.y;
+    if (iw >= a.ne) return;
     double2 s = make_double2(0.0, 0.0);
     const double wx = a.fmin - a.ekq[n1] + (iw - 1) * a.fstep;
+    const double2* num = t.num + (long)n1 * a.nf;
     for (int f = 0; f < a.nf; ++f) {
-        const double2 coh = make_double2(__dsub_rn(a.grid[f], a.brd[f].x), 0.0 - a.brd[f].y);
-        const double2 num = cmul(make_double2(0.0, a.pref[f]), schdt_of(a, n1, f));
-        const double2 q = gc_div(num, make_double2(__dsub_rn(wx, coh.x), 0 - coh.y));
+        const double2 coh = t.coh[f];
+        const double2 q = gc_div(num[f], make_double2(__dsub_rn(wx, coh.x), 0 - coh.y));
         s = cadd(s, make_double2(0.0 - q.x, 0.0 - q.y));
     }
     a.SD[(long)iw * a.nb + n1] = s;
+}
+
+// Mixed: the same sum in FP32.  wx - coh.re = (wx_hi - coh_hi) + (wx_lo - coh_lo):
+// the first difference is exact when the two are close (Sterbenz), so the
+// denominator keeps full relative accuracy where it is small; terms are added
+// in FP32 over 32 frequencies, then into a float-float (TwoSum) accumulator.
+__global__ void ff_schdi32_kernel(EpiArgs a, SchdiTab t) {
+    const int iw = blockIdx.x * blockDim.x + threadIdx.x, n1 = blockIdx.y;
+    if (iw >= a.ne) return;
+    const double wx = a.fmin - a.ekq[n1] + (iw - 1) * a.fstep;
+    const float wh = f64_to_f32_bits(wx), wl = f64_to_f32_bits(wx - (double)wh);
+    const float4* tab = t.f32 + (long)n1 * a.nf;
+    ff32 ar{0.f, 0.f}, ai{0.f, 0.f};
+    for (int f0 = 0; f0 < a.nf; f0 += 32) {
+        float sr = 0.f, si = 0.f;
+        const int f1 = min(a.nf, f0 + 32);
+        for (int f = f0; f < f1; ++f) {
+            const float4 c = tab[f];
+            const float2 ch = t.cohr[f];
+            const float dr = (wh - ch.x) + (wl - ch.y), di = c.z;
+            const float r = __frcp_rn(fmaf(dr, dr, di * di));
+            // -(c / d) = -(c * conj(d)) / |d|^2
+            sr -= fmaf(c.x, dr, c.y * di) * r;
+            si -= fmaf(c.y, dr, -(c.x * di)) * r;
+        }
+        ff_add(ar, sr);
+        ff_add(ai, si);
+    }
+    a.SD[(long)iw * a.nb + n1] = make_double2((double)ar.hi + (double)ar.lo, (double)ai.hi + (double)ai.lo);
 }
 
 FK_DEV void bsum(double2& v, double2* sm) {
@@ -279,7 +339,8 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
     }
     const size_t slots = (size_t)p.KS * p.NT * (p.mixed ? tcx::FF_EPI_WARPS : 1);  // partial slots per plane
     p.bytes = (slots * (p.planesR.size() + p.planesA.size()) * r.nb * 2 + 3 * (size_t)r.nb * r.nf +
-               (size_t)r.ne * r.nb) * sizeof(double2) +
+               (size_t)r.ne * r.nb + (size_t)r.nb * r.nf + r.nf) * sizeof(double2) +
+              (p.mixed ? (size_t)r.nb * r.nf * sizeof(float4) + r.nf * sizeof(float2) : 0) + 4 * 256 +
               r.nb * sizeof(FactRow) + (p.planesR.size() + p.planesA.size()) * sizeof(int) + r.ng * sizeof(int) +
               p.bytesImgR + p.bytesImgA + p.bytesW + p.bytesAimg + 20 * 256;
     return p;
@@ -312,6 +373,13 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
     double2* PA = nA ? (double2*)c.ws.take(slots * nA * r.nb * 2 * sizeof(double2)) : nullptr;
     double2* tabs = (double2*)c.ws.take(3 * (size_t)r.nb * r.nf * sizeof(double2));
     double2* SD = (double2*)c.ws.take((size_t)r.ne * r.nb * sizeof(double2));
+    SchdiTab stab{};
+    stab.num = (double2*)c.ws.take((size_t)r.nb * r.nf * sizeof(double2));
+    stab.coh = (double2*)c.ws.take((size_t)r.nf * sizeof(double2));
+    if (p.mixed) {
+        stab.f32 = (float4*)c.ws.take((size_t)r.nb * r.nf * sizeof(float4));
+        stab.cohr = (float2*)c.ws.take((size_t)r.nf * sizeof(float2));
+    }
     uint8_t* imgR = p.bytesImgR ? (uint8_t*)c.ws.take(p.bytesImgR) : nullptr;
     uint8_t* imgA = p.bytesImgA ? (uint8_t*)c.ws.take(p.bytesImgA) : nullptr;
     float2* W = p.bytesW ? (float2*)c.ws.take(p.bytesW) : nullptr;
@@ -403,7 +471,10 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
     ea.fminI = phys ? r.fmin : (double)(int)r.fmin;
     ea.fstepI = phys ? r.fstep : (double)(int)r.fstep;
     ea.SD = SD; ea.out = r.out;
-    ff_schdi_kernel<<<dim3(ceil_div(r.nb, 128), r.ne), 128, 0, st>>>(ea);
+    ff_schdi_tables_kernel<<<dim3(ceil_div(r.nf, 128), r.nb), 128, 0, st>>>(ea, stab);
+    if (p.mixed) ff_schdi32_kernel<<<dim3(ceil_div(r.ne, 128), r.nb), 128, 0, st>>>(ea, stab);
+    else ff_schdi_kernel<<<dim3(ceil_div(r.ne, 128), r.nb), 128, 0, st>>>(ea, stab);
+    c.launches += 1;
     ff_epilogue_kernel<<<r.ne + 1, 256, 0, st>>>(ea);
     c.launches += 2;
     phase_mark(c, 4);

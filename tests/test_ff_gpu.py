@@ -105,3 +105,21 @@ def test_ff_config4_full_size(ctx, fk):
     torch.cuda.empty_cache()
     errs = {k: rel(res[k], ref[k]) for k in KEYS if np.max(np.abs(ref[k])) > 0}
     assert errs and all(e <= TOLMX for e in errs.values()), errs
+
+
+def test_ff_sigma_epilogue_at_scale(ctx, fk):
+    """The Fortran example's compute-bound FF shape (number_bands=8, ncouls=1000,
+    ngpown=60, nFreq=20000, nfreqeval=30000, with the band x G x G' schDt): the
+    (band, frequency, evaluation frequency) epilogue dominates; the mixed path's
+    FP32 epilogue within 1e-6 of the FP64 path on every output."""
+    import torch
+    free, _ = torch.cuda.mem_get_info()
+    if free < 60 << 30:
+        pytest.skip("needs ~60 GB of free device memory")
+    p = fk.inputs.ff_synthetic_device(8, 2, 1000, 60, 20000, 30000, seed=5)
+    f = fk.FK_FF_SCHDT_GEMM | fk.FK_FF_SPLIT_ACHD
+    res, ref = ctx.ff(p, "mixed", f), ctx.ff(p, "fp64", f)
+    del p
+    torch.cuda.empty_cache()
+    errs = {k: rel(res[k], ref[k]) for k in KEYS if np.max(np.abs(ref[k])) > 0}
+    assert "achDtemp" in errs and all(e <= TOLMX for e in errs.values()), errs
