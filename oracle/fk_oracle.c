@@ -105,6 +105,109 @@ static inline void gpp_solver(double wxt, cx wtilde, cx wtilde2, cx Omega2,
     *scha = cx_mul(matngmatmgp, sch);
 }
 
+/* std::complex division and magnitude as the textbook forms: a*conj(b)/|b|^2
+ * and hypot(re, im) (the reference's libstdc++ results agree to ~1 ulp). */
+static inline cx cx_div(cx a, cx b) {
+    const double n = b.re * b.re + b.im * b.im;
+    return cx_make((a.re * b.re + a.im * b.im) / n, (a.im * b.re - a.re * b.im) / n);
+}
+static inline double cx_abs(cx a) { return hypot(a.re, a.im); }
+
+/* gppsum == 1, one (n1, my_igp): gppKerSeq.cpp's flagOCC_solver (:90-139) for
+ * occupied bands, else its driver's block loop (:430-447) over
+ * noflagOCC_solver (:206-242).  igmax = igp.  sch_array/ssx_array as the
+ * driver accumulates them (before the vcoul weight). */
+static void gpp_half_sum(int occ_band, int n1, int igp, int nc, const double* aqsm, const double* aqsn,
+                         const double* erow, const double* wrow, const double* wx, cx sch_array[3],
+                         cx ssx_array[3]) {
+    const double to1 = 1e-6, gamma = 0.5;
+    const double limitone = 1.0 / (to1 * 4.0), limittwo = 0.5 * 0.5;
+    const int igmax = igp;
+    const cx aqm = cx_ld(aqsm, (long)n1 * nc + igp);
+    const cx mygpvar1 = cx_conj(aqm), mygpvar2 = aqm;
+    const double* mrow = aqsm + 2L * n1 * nc;
+    const double* nrow = aqsn + 2L * n1 * nc;
+    if (occ_band) {
+        for (int iw = 0; iw < 3; ++iw) {
+            const double wxt = wx[iw];
+            cx ssxt = {0, 0}, scht = {0, 0}, matngpmatmg = {0, 0};
+            for (int ig = 0; ig < igmax; ++ig) {
+                const cx wt = cx_ld(wrow, ig), eps = cx_ld(erow, ig);
+                const cx wt2 = cx_mul(wt, wt);
+                const cx Omega2 = cx_mul(wt2, eps);
+                if (cx_abs(Omega2) < to1) break;
+                const cx matngmatmgp = cx_mul(cx_ld(nrow, ig), mygpvar1);
+                if (ig != igp) matngpmatmg = cx_mul(cx_conj(cx_ld(mrow, ig)), mygpvar2);
+                const cx halfinvwtilde = cx_div(cx_make(0.5, 0.0), wt);
+                const cx wmw = cx_make(wxt - wt.re, -wt.im);
+                const cx delw = cx_mul(wmw, halfinvwtilde);
+                const double ad = cx_abs(delw), delw2 = ad * ad;
+                cx sch, ssx;
+                if (cx_abs(wmw) < gamma || delw2 < to1) {
+                    sch = cx_make(0.0, 0.0);
+                    if (cx_abs(wt) > to1)
+                        ssx = cx_div(cx_make(-Omega2.re, -Omega2.im),
+                                     cx_mul(cx_scale(wt2, 4.0), cx_make(1.0 + delw.re, delw.im)));
+                    else
+                        ssx = cx_make(0.0, 0.0);
+                } else {
+                    sch = cx_div(cx_mul(wt, eps), wmw);
+                    ssx = cx_div(Omega2, cx_make(wxt * wxt - wt2.re, -wt2.im));
+                }
+                /* the sexcut test (:119-120) requires abs(wxt) < 0 and never fires */
+                cx ssxa, scha;
+                if (ig != igp - 1) {
+                    ssxa = cx_add(cx_mul(matngmatmgp, ssx), cx_mul(matngpmatmg, cx_conj(ssx)));
+                    scha = cx_add(cx_mul(matngmatmgp, sch), cx_mul(matngpmatmg, cx_conj(sch)));
+                } else {
+                    ssxa = cx_mul(matngmatmgp, ssx);
+                    scha = cx_mul(matngmatmgp, sch);
+                }
+                ssxt = cx_add(ssxt, ssxa);
+                scht = cx_add(scht, scha);
+            }
+            ssx_array[iw] = cx_add(ssx_array[iw], ssxt);
+            sch_array[iw] = cx_add(sch_array[iw], cx_scale(scht, 0.5));
+        }
+        return;
+    }
+    const int igblk = 512;
+    for (int igbeg = 0; igbeg < igmax; igbeg += igblk) {
+        const int igend = igbeg + igblk - 1 < igmax ? igbeg + igblk - 1 : igmax;
+        for (int iw = 0; iw < 3; ++iw) {
+            const double wxt = wx[iw];
+            cx scht = {0, 0};
+            const int top = igend < igmax - 1 ? igend : igmax - 1;
+            /* the interior range (:210): both terms of the pair */
+            for (int ig = igbeg; ig < top; ++ig) {
+                const cx wt = cx_ld(wrow, ig);
+                const cx matngmatmgp = cx_mul(cx_ld(nrow, ig), mygpvar1);
+                const cx wdiff = cx_make(wxt - wt.re, -wt.im);
+                const cx delw = cx_div(wt, wdiff);
+                const double delw2 = cx_norm2(delw), wdiffr = cx_norm2(wdiff);
+                const double mult = (fabs(wdiffr) < limittwo || delw2 > limitone) ? 1.0 : 0.0;
+                const cx sch = cx_scale(cx_mul(delw, cx_ld(erow, ig)), mult);
+                const cx scha = cx_add(cx_mul(matngmatmgp, sch),
+                                       cx_mul(cx_mul(cx_conj(cx_ld(mrow, ig)), mygpvar2), cx_conj(sch)));
+                scht = cx_add(scht, scha);
+            }
+            /* the diagonal ig = igmax (:225-240), reached only when igend == igmax-1 */
+            if (igend == igmax - 1) {
+                const int ig = igmax;
+                const cx wt = cx_ld(wrow, ig);
+                const cx matngmatmgp = cx_mul(cx_ld(nrow, ig), mygpvar1);
+                const cx wdiff = cx_make(wxt - wt.re, -wt.im);
+                const cx delw = cx_div(wt, wdiff);
+                const double delw2 = cx_norm2(delw), wdiffr = cx_norm2(wdiff);
+                const double mult = (fabs(wdiffr) < limittwo || delw2 > limitone) ? 1.0 : 0.0;
+                const cx sch = cx_scale(cx_mul(delw, cx_ld(erow, ig)), mult);
+                scht = cx_add(scht, cx_mul(matngmatmgp, sch));
+            }
+            sch_array[iw] = cx_add(sch_array[iw], cx_scale(scht, 0.5));
+        }
+    }
+}
+
 int orc_gpp(int nb, int nv, int nc, int ng,
             const double* aqsm, const double* aqsn,
             const double* I_eps, const double* wtilde, const double* vcoul,
@@ -140,7 +243,9 @@ int orc_gpp(int nb, int nv, int nc, int ng,
             const double* erow = I_eps + 2L * my_igp * nc;
             const double* nrow = aqsn + 2L * n1 * nc;
             const cx aqm = cx_ld(aqsm, (long)n1 * nc + igp);
-            if (flag_occ) {
+            if (flags & ORC_GPP_HALF_SUM) {
+                gpp_half_sum(flag_occ, n1, igp, nc, aqsm, aqsn, erow, wrow, wx, sch_array, ssx_array);
+            } else if (flag_occ) {
                 /* flagOCC_solver, BGW-Kernels/gppKer.cpp:130-159 */
                 for (int iw = 0; iw < 3; ++iw) {
                     cx ssxt = {0, 0}, scht = {0, 0};

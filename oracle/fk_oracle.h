@@ -32,6 +32,10 @@ extern "C" {
                                      I_eps[my_igp*ngpown+ig] (gppKer.cpp:139) */
 #define ORC_GPP_ACHSTEMP    0x2u  /* compute the static-CH remainder achstemp
                                      as in gppkernel.deslippe.09.30.2014.f90:195-229 */
+#define ORC_GPP_HALF_SUM    0x4u  /* gppsum == 1 of gppKerSeq.cpp: the sum over ig
+                                     runs below igp with the conjugate pair term
+                                     (flagOCC_solver :90-139, noflagOCC_solver
+                                     :206-242, driver blocking :430-447) */
 
 /*
  * GPP self-energy sum, BGW-Kernels/gppKer.cpp:303-439.

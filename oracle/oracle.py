@@ -22,6 +22,7 @@ REF_DIR = os.path.join(HERE, "_ref")
 
 ORC_GPP_ROOT_QUIRKS = 0x1
 ORC_GPP_ACHSTEMP = 0x2
+ORC_GPP_HALF_SUM = 0x4
 ORC_FF_SCHDT_GEMM = 0x1
 ORC_FF_PHYSICS = 0x2
 ORC_FF_SPLIT_ACHD = 0x4
@@ -163,8 +164,9 @@ def run_ref_driver(name: str, args, threads: int = 8) -> dict:
     return res
 
 
-def ref_gpp_pairs(p: dict, igp: np.ndarray) -> dict:
-    """Per-(n1, my_igp, iw) sch/ssx from the reference's own solver functions."""
+def ref_gpp_pairs(p: dict, igp: np.ndarray, gppsum: int = 0) -> dict:
+    """Per-(n1, my_igp, iw) sch/ssx from the reference's own solver functions
+    (gppsum=1: gppKerSeq.cpp's half-sum mode)."""
     nb, nv, nc, ng = p["number_bands"], p["nvband"], p["ncouls"], p["ngpown"]
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
@@ -173,7 +175,8 @@ def ref_gpp_pairs(p: dict, igp: np.ndarray) -> dict:
                 f.write(_c(p[k]).tobytes())
             f.write(np.ascontiguousarray(p["wx_array"], np.float64).tobytes())
             f.write(np.ascontiguousarray(igp, np.int32).tobytes())
-        subprocess.run([os.path.join(REF_DIR, "ref_harness_gpp")] + [str(x) for x in (nb, nv, nc, ng, fin, fout)],
+        subprocess.run([os.path.join(REF_DIR, "ref_harness_gpp")] + [str(x) for x in (nb, nv, nc, ng, fin, fout)] +
+                       ([str(gppsum)] if gppsum else []),
                        check=True,
                        env=dict(os.environ, OMP_NUM_THREADS="1"))
         raw = np.fromfile(fout, dtype=np.complex128)

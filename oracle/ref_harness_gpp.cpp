@@ -13,7 +13,11 @@
 // the sch_array / ssx_array values the reference main accumulates
 // (BGW-Kernels/gppKer.cpp:337-413) before the vcoul weight.
 //
-// usage: ref_harness_gpp nb nv nc ng in.bin out.bin
+// With a seventh argument 1 it runs gppKerSeq.cpp's gppsum == 1 mode instead:
+// its own flagOCC_solver (:90-139) for occupied bands and its driver's block
+// loop (:430-447) over noflagOCC_solver, igmax = igp.
+//
+// usage: ref_harness_gpp nb nv nc ng in.bin out.bin [gppsum]
 //   in.bin : aqsm[nb*nc] aqsn[nb*nc] I_eps[ng*nc] wtilde[ng*nc] (complex128)
 //            wx[3] (float64) igp[ng] (int32; the resolved column index)
 //   out.bin: sch[nb][ng][3] ssx[nv][ng][3] (complex128)
@@ -30,9 +34,15 @@ void flagOCC_solver(double wxt, cd* wtilde_array_tmp, int my_igp, int n1, cd* aq
 void noflagOCC_solver(int igbeg, int igend, int igblk, double wxt, cd** wtilde_array, int my_igp, int n1,
                       cd** aqsmtemp, cd** aqsntemp, cd** I_eps_array, int gppsum, cd& ssxt, cd& scht, int igmax,
                       int ncouls, int igp);
+void fk_ref_seq_flagOCC_solver(double wxt, cd** wtilde_array, int my_igp, int n1, cd** aqsmtemp, cd** aqsntemp,
+                               cd** I_eps_array, int gppsum, cd& ssxt, cd& scht, int igmax, int ncouls, int igp);
 
 int main(int argc, char** argv) {
-    if (argc != 7) { std::fprintf(stderr, "usage: %s nb nv nc ng in.bin out.bin\n", argv[0]); return 2; }
+    if (argc != 7 && argc != 8) {
+        std::fprintf(stderr, "usage: %s nb nv nc ng in.bin out.bin [gppsum]\n", argv[0]);
+        return 2;
+    }
+    const int gppsum = argc == 8 ? std::atoi(argv[7]) : 0;
     const int nb = std::atoi(argv[1]), nv = std::atoi(argv[2]), nc = std::atoi(argv[3]), ng = std::atoi(argv[4]);
     std::vector<cd> aqsm((size_t)nb * nc), aqsn((size_t)nb * nc), eps((size_t)ng * nc), wt((size_t)ng * nc);
     double wx[3];
@@ -72,7 +82,28 @@ int main(int argc, char** argv) {
             const int igp = igpv[my_igp];
             if (igp < 0) continue;
             cd sch_array[3], ssx_array[3];
-            if (n1 < nv) {
+            if (gppsum == 1) {
+                const int igmax = igp;
+                for (int iw = 0; iw < 3; ++iw) {
+                    if (n1 < nv) {
+                        cd scht(0, 0), ssxt(0, 0);
+                        fk_ref_seq_flagOCC_solver(wx[iw], pw.data(), my_igp, n1, pm.data(), pn.data(), pe.data(), 1,
+                                                  ssxt, scht, igmax, nc, igp);
+                        ssx_array[iw] += ssxt;
+                        sch_array[iw] += 0.5 * scht;
+                    }
+                }
+                if (n1 >= nv)
+                    for (int igbeg = 0; igbeg < igmax; igbeg += 512) {
+                        const int igend = igbeg + 511 < igmax ? igbeg + 511 : igmax;
+                        for (int iw = 0; iw < 3; ++iw) {
+                            cd scht(0, 0), ssxt(0, 0);
+                            noflagOCC_solver(igbeg, igend, 512, wx[iw], pw.data(), my_igp, n1, pm.data(), pn.data(),
+                                             pe.data(), 1, ssxt, scht, igmax, nc, igp);
+                            sch_array[iw] += 0.5 * scht;
+                        }
+                    }
+            } else if (n1 < nv) {
                 for (int iw = 0; iw < 3; ++iw) {
                     cd scht(0, 0), ssxt(0, 0);
                     flagOCC_solver(wx[iw], wt.data(), my_igp, n1, aqsm.data(), aqsn.data(), eps.data(), ssxt, scht,

@@ -35,6 +35,7 @@ inputs = __graft_entry__.load_package().inputs
 GPP_SIZES = [(64, 2, 512, 4), (32, 2, 1000, 8), (128, 4, 777, 7), (512, 2, 2048, 32), (40, 0, 600, 6),
              (24, 24, 256, 4)]
 FF_SIZES = [(16, 3, 300, 40, 6, 7), (64, 2, 512, 64, 15, 10), (512, 2, 4096, 512, 15, 10)]
+SEQ_SIZES = [(64, 2, 1024, 4, 1), (32, 3, 2048, 8, 1), (16, 2, 1536, 6, 1)]
 
 
 def cx(z):
@@ -76,6 +77,11 @@ def main(big: bool):
             out["gppKer_root"].append({"args": list(s), "achtemp": [cx(r[f"achtemp[{i}]"]) for i in range(3)],
                                        "achtemp_exact": exact_constant_gpp(*s),
                                        "achstemp_printed": cx(r["achstemp"])})
+    # gppKerSeq.cpp: the same driver with its gppsum argument (1: the half sum)
+    out["gppKer_seq"] = []
+    for s in SEQ_SIZES:
+        r = oracle.run_ref_driver("gppKer_seq", s, threads=1)
+        out["gppKer_seq"].append({"args": list(s), "achtemp": [cx(r[f"achtemp[{i}]"]) for i in range(3)]})
     r = oracle.run_ref_driver("gppKer_orig", (512, 2, 2048, 32))
     out["gppKer_orig"].append({"args": [512, 2, 2048, 32], "achtemp": [cx(r[f"achtemp[{i}]"]) for i in range(3)]})
     for s in FF_SIZES:
@@ -93,6 +99,14 @@ def main(big: bool):
         h = oracle.ref_gpp_pairs(p, igp)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), sch=h["sch"], ssx=h["ssx"],
                             **{k: np.asarray(v) for k, v in p.items()})
+    # gppsum == 1 (gppKerSeq.cpp): ncouls 1536 puts igp 512 and 1024 on the
+    # driver's 512-wide blocks (diagonal terms, skipped block ends)
+    p = inputs.gpp_synthetic(7, 3, 1536, 6, seed=21, dist="branch", index="reference", wx="stress")
+    inv, nc = p["inv_igp_index"], p["ncouls"]
+    igp = np.array([nc - 1 if i == nc else p["indinv"][i] for i in inv], np.int32)
+    h = oracle.ref_gpp_pairs(p, igp, gppsum=1)
+    np.savez_compressed(os.path.join(HERE, "gpp_pairs_halfsum.npz"), sch=h["sch"], ssx=h["ssx"],
+                        **{k: np.asarray(v) for k, v in p.items()})
     p = inputs.ff_synthetic(9, 3, 96, 12, 4, 5, seed=5)
     # schDt_matrix from the band x G x G' contraction, fed to the reference's
     # own achDtemp_Kernel (the reference C++ leaves it zero)

@@ -145,3 +145,28 @@ def test_gpp_oracle_thread_count_independent(fk, orc):
     b = orc.gpp(p, nthreads=3)
     np.testing.assert_array_equal(a["achtemp"], b["achtemp"])
     np.testing.assert_array_equal(a["asxtemp"], b["asxtemp"])
+
+
+@pytest.mark.parametrize("entry", drivers()["gppKer_seq"], ids=lambda e: "x".join(map(str, e["args"])))
+def test_gpp_half_sum_oracle_matches_seq_driver(fk, orc, entry):
+    """gppsum == 1 of gppKerSeq.cpp against what its driver printed."""
+    nb, nv, nc, npg, gppsum = entry["args"]
+    assert gppsum == 1
+    o = orc.gpp(fk.inputs.gpp_reference_init(nb, nv, nc, npg), flags=orc.ORC_GPP_HALF_SUM)
+    assert rel(o["achtemp"], cx(entry["achtemp"])) < 1e-13
+
+
+def test_gpp_half_sum_oracle_vs_reference_solvers(orc):
+    """Per-(n1, my_igp, iw) sch/ssx of gppKerSeq.cpp's own gppsum == 1
+    functions (flagOCC_solver, noflagOCC_solver and the driver's block loop) on
+    branch-stress inputs with igp on the 512-wide block edges.  The reference's
+    std::complex division, abs and pow round differently from the oracle's
+    textbook forms, hence 1e-13 rather than bit equality."""
+    z = np.load(os.path.join(GOLD, "gpp_pairs_halfsum.npz"))
+    p = {k: z[k] for k in z.files if k not in ("sch", "ssx")}
+    for k in ("number_bands", "nvband", "ncouls", "ngpown"):
+        p[k] = int(p[k])
+    o = orc.gpp(p, flags=orc.ORC_GPP_HALF_SUM, per_pair=True)
+    assert rel(o["sch"], z["sch"]) < 1e-13
+    assert rel(o["ssx"], z["ssx"]) < 1e-13
+    assert np.max(np.abs(z["sch"][p["nvband"]:])) > 0  # the noflag half sum is exercised
