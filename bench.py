@@ -37,6 +37,9 @@ WORKLOADS = {
     "gpp": dict(kind="gpp", nb=512, nv=2, nc=32768, ng=20),
     # the reference's canonical run `gppKer 512 2 32768 20` (ngpown = 32768/20)
     "gpp1638": dict(kind="gpp", nb=512, nv=2, nc=32768, ng=1638),
+    # gppKerSeq.cpp's half sum (gppsum = 1) at the config-1 size; its inverted noflag mask keeps only
+    # near-pole terms, which the uniform draw never produces, so wtilde comes from the branch-stress draw
+    "gpphalf": dict(kind="gpp", nb=512, nv=2, nc=32768, ng=20, half=True, dist="branch"),
     # BASELINE config 2: FF full-frequency contraction
     "ff": dict(kind="ff", nb=512, nv=2, nc=4096, ng=512, nf=15, ne=10),
     # BASELINE config 4: large FF contraction (I_epsR/I_epsA ~17 GB each, drawn on the GPU)
@@ -51,6 +54,9 @@ WORKLOADS = {
 
 
 def terms(w):
+    if w["kind"] == "gpp" and w.get("half"):
+        # the (n1, igp, ig, iw) the half sum visits: ig < igp for the baseline columns igp = i*ncouls/ngpown
+        return w["nb"] * 3 * sum(i * w["nc"] // w["ng"] for i in range(w["ng"]))
     if w["kind"] == "gpp":
         return w["nb"] * w["ng"] * w["nc"] * 3
     return w["nb"] * w["ng"] * w["nc"] * w["nf"]
@@ -87,7 +93,7 @@ def roofline(w, prec, byts, flops, kms, peaks):
 
 def make_inputs(fk, w, seed=2024):
     if w["kind"] == "gpp":
-        return fk.inputs.gpp_synthetic(w["nb"], w["nv"], w["nc"], w["ng"], seed=seed, dist="uniform",
+        return fk.inputs.gpp_synthetic(w["nb"], w["nv"], w["nc"], w["ng"], seed=seed, dist=w.get("dist", "uniform"),
                                        index="baseline", wx="baseline")
     if w.get("device_inputs"):
         return fk.inputs.ff_synthetic_device(w["nb"], w["nv"], w["nc"], w["ng"], w["nf"], w["ne"], seed=seed)
@@ -270,7 +276,8 @@ def run_reference(a, w):
         p = fk.inputs.ff_synthetic(w["nb"], w["nv"], w["nc"], w["ng"], w["nf"], w["ne"], seed=2024)
     else:
         p = make_inputs(fk, w)
-    call = (lambda: oracle.gpp(p, nthreads=cores)) if w["kind"] == "gpp" else \
+    gflags = oracle.ORC_GPP_HALF_SUM if w.get("half") else 0
+    call = (lambda: oracle.gpp(p, flags=gflags, nthreads=cores)) if w["kind"] == "gpp" else \
         (lambda: oracle.ff(p, flags=oracle.ORC_FF_SCHDT_GEMM, nthreads=cores))
     for _ in range(a.warmup):
         call()
@@ -298,12 +305,15 @@ METRIC = "GPP/FF self-energy terms/s + p99 latency, mixed vs FP64 at <=1e-6 rel 
 
 
 def workload_config(a, w):
-    c = {"workload": ("GPP self-energy sum, number_bands=%d nvband=%d ncouls=%d ngpown=%d" %
-                      (w["nb"], w["nv"], w["nc"], w["ng"])) if w["kind"] == "gpp" else
+    c = {"workload": ("GPP self-energy %s, number_bands=%d nvband=%d ncouls=%d ngpown=%d" %
+                      ("half sum (gppsum=1)" if w.get("half") else "sum", w["nb"], w["nv"], w["nc"], w["ng"]))
+         if w["kind"] == "gpp" else
          ("FF full-frequency contraction, number_bands=%d nvband=%d ncouls=%d ngpown=%d nFreq=%d nfreqeval=%d"
           % (w["nb"], w["nv"], w["nc"], w["ng"], w["nf"], w["ne"])),
          "precision": a.precision, "parallelism": f"replicas x{a.gpus}",
          "l2": "inputs larger than L2 (aqsntemp %.0f MB)" % (16 * w["nb"] * w["nc"] / 1e6)}
+    if w.get("dist"):
+        c["distribution"] = w["dist"]
     return c
 
 
@@ -352,9 +362,9 @@ def run_ours(a, w):
         outs = {k: torch.zeros(n, dtype=torch.complex128, device=f"cuda:{local}")
                 for k, n in (("achtemp", 3), ("asxtemp", 3), ("acht_n1_loc", w["nb"]))}
         outs["achstemp"] = None
-        call = lambda prec: ctx.gpp(d, prec, 0, out=outs)
-        host_call = lambda prec, hp: ctx.gpp(hp, prec, 0)
-        flags = 0
+        flags = fk.FK_GPP_HALF_SUM if w.get("half") else 0
+        call = lambda prec: ctx.gpp(d, prec, flags, out=outs)
+        host_call = lambda prec, hp: ctx.gpp(hp, prec, flags)
     else:
         flags = fk.FK_FF_SCHDT_GEMM | fk.FK_FF_SPLIT_ACHD
         outs = {"achsDtemp": torch.zeros(1, dtype=torch.complex128, device=f"cuda:{local}"),
@@ -420,7 +430,7 @@ def run_ours(a, w):
         t = (p[k].cpu() if k not in keys_c else torch.from_numpy(np.ascontiguousarray(p[k]))).pin_memory()
         hp[k] = t
         n = t.numel() * t.element_size()
-        if w["kind"] == "gpp" and k == "aqsmtemp" and w["ng"] * 128 <= w["nc"]:
+        if w["kind"] == "gpp" and k == "aqsmtemp" and w["ng"] * 128 <= w["nc"] and not w.get("half"):
             # the library reads only the ngpown igp columns of aqsmtemp (BGW-Kernels/gppKer.cpp:322-325),
             # gathers them on the host and sends number_bands x ngpown values
             n = w["nb"] * w["ng"] * t.element_size()
@@ -450,7 +460,7 @@ def run_ours(a, w):
         except OSError:
             pass
         byts, flops = algorithmic(w)
-        kms = phase[2]
+        kms = phase[2] / (2 if w.get("half") else 1)  # the half sum runs the contraction twice (A = aqsn, aqsm)
         T = terms(w)
         line = {
             "metric": METRIC, "value": world * T / (ms * 1e-3), "unit": "terms/s", "n_gpus": world,
@@ -485,7 +495,7 @@ def cpu_baseline(fk, w, p):
     cores = os.cpu_count() or 1
     if w["kind"] == "gpp":
         t0 = time.perf_counter()
-        oracle.gpp(p, nthreads=cores)
+        oracle.gpp(p, flags=oracle.ORC_GPP_HALF_SUM if w.get("half") else 0, nthreads=cores)
         dt = time.perf_counter() - t0
         return {"value": terms(w) / dt, "unit": "terms/s", "cores": cores, "kind": "port",
                 "sample": f"one full call ({terms(w):.3g} terms)"}

@@ -22,10 +22,10 @@ import numpy as np
 
 from . import _native
 from ._native import (FK_FF_PHYSICS, FK_FF_SCHDT_GEMM, FK_FF_SPLIT_ACHD, FK_FP64, FK_GPP_ACHSTEMP,
-                      FK_GPP_ROOT_QUIRKS, FK_MIXED, FKError)
+                      FK_GPP_HALF_SUM, FK_GPP_ROOT_QUIRKS, FK_MIXED, FKError)
 
 __all__ = ["Context", "Server", "gppKer", "ffKernel", "FKError", "FK_FP64", "FK_MIXED", "FK_GPP_ROOT_QUIRKS",
-           "FK_GPP_ACHSTEMP", "FK_FF_SCHDT_GEMM", "FK_FF_PHYSICS", "FK_FF_SPLIT_ACHD", "precision_code"]
+           "FK_GPP_ACHSTEMP", "FK_GPP_HALF_SUM", "FK_FF_SCHDT_GEMM", "FK_FF_PHYSICS", "FK_FF_SPLIT_ACHD", "precision_code"]
 
 
 def precision_code(p) -> int:

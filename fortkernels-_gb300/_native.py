@@ -15,6 +15,7 @@ FK_OK, FK_EINVAL, FK_ENOMEM, FK_ECUDA, FK_ETIMEOUT, FK_EBUSY, FK_ENOTSUP = range
 FK_FP64, FK_MIXED = 0, 1
 FK_GPP_ROOT_QUIRKS = 0x1
 FK_GPP_ACHSTEMP = 0x2
+FK_GPP_HALF_SUM = 0x4
 FK_FF_SCHDT_GEMM = 0x1
 FK_FF_PHYSICS = 0x2
 FK_FF_SPLIT_ACHD = 0x4

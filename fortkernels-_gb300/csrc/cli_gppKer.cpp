@@ -3,6 +3,11 @@
 // Same command line and output lines as BGW-Kernels/gppKer.cpp:161-449:
 //   gppKer <number_bands> <number_valence_bands> <number_plane_waves> <nodes_per_mpi_group>
 //          [--precision=fp64|mixed] [--quirks] [--achstemp] [--device=N]
+// and, with a fifth number, those of gppKerSeq.cpp:263-500:
+//   gppKer <number_bands> <number_valence_bands> <number_plane_waves> <nodes_per_mpi_group> <gppsum>
+// where gppsum = 1 is its half sum (FK_GPP_HALF_SUM).  gppsum = 0 of that
+// driver drops ig = 511 mod 512 from every block (its igend is one short,
+// gppKerSeq.cpp:459) and is refused rather than reproduced.
 // The arrays are built exactly as that main() builds them (constant 0.5+0.5i
 // fills, inv_igp_index[i] = (i+1)*ncouls/ngpown, indinv = identity, wx =
 // e_lk - e_n1kq + dw*(iw-1)); the sum itself runs on the GPU through fk_gpp.
@@ -20,7 +25,7 @@
 #include "fk_abi.h"
 
 int main(int argc, char** argv) {
-    int pos[4], npos = 0;
+    int pos[5], npos = 0;
     fk_precision prec = FK_FP64;
     unsigned flags = 0;
     int device = 0;
@@ -29,9 +34,16 @@ int main(int argc, char** argv) {
         else if (!std::strcmp(argv[i], "--quirks")) flags |= FK_GPP_ROOT_QUIRKS;
         else if (!std::strcmp(argv[i], "--achstemp")) flags |= FK_GPP_ACHSTEMP;
         else if (!std::strncmp(argv[i], "--device=", 9)) device = std::atoi(argv[i] + 9);
-        else if (npos < 4) pos[npos++] = std::atoi(argv[i]);
+        else if (npos < 5) pos[npos++] = std::atoi(argv[i]);
     }
-    if (npos != 4) {
+    const bool seq = npos == 5;
+    if (seq && pos[4] != 1) {
+        std::fprintf(stderr, "gppsum = %d: only gppsum = 1 (the half sum) is provided; the full sum is the "
+                             "four-argument form\n", pos[4]);
+        return 1;
+    }
+    if (seq) flags |= FK_GPP_HALF_SUM;
+    if (npos != 4 && !seq) {
         std::cout << "The correct form of input is : " << std::endl;
         std::cout << " ./a.out <number_bands> <number_valence_bands> <number_plane_waves> <nodes_per_mpi_group> "
                   << std::endl;
@@ -52,7 +64,9 @@ int main(int argc, char** argv) {
     }
     std::cout << "Device = CUDA device " << device << " (" << fk_version() << ")" << std::endl;
     std::cout << "number_bands = " << number_bands << "\t nvband = " << nvband << "\t ncouls = " << ncouls
-              << "\t nodes_per_group  = " << nodes_per_group << "\t ngpown = " << ngpown << "\t nend = " << nend
+              << "\t nodes_per_group  = " << nodes_per_group;
+    if (seq) std::cout << "\t gppsum = " << pos[4];
+    std::cout << "\t ngpown = " << ngpown << "\t nend = " << nend
               << "\t nstart = " << nstart << "\t gamma = " << gamma << "\t sexcut = " << sexcut
               << "\t limitone = " << limitone << "\t limittwo = " << limittwo << std::endl;
 

@@ -473,7 +473,12 @@ fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsm
         !wx_array || !achtemp || !asxtemp)
         return fk::fail(x, FK_EINVAL, "gpp: null required pointer");
     if (precision != FK_FP64 && precision != FK_MIXED) return fk::fail(x, FK_EINVAL, "gpp: bad precision");
-    if (flags & ~(FK_GPP_ROOT_QUIRKS | FK_GPP_ACHSTEMP)) return fk::fail(x, FK_EINVAL, "gpp: unknown flag");
+    if (flags & ~(FK_GPP_ROOT_QUIRKS | FK_GPP_ACHSTEMP | FK_GPP_HALF_SUM))
+        return fk::fail(x, FK_EINVAL, "gpp: unknown flag");
+    if ((flags & FK_GPP_HALF_SUM) && (flags & FK_GPP_ROOT_QUIRKS))
+        return fk::fail(x, FK_EINVAL, "gpp: FK_GPP_HALF_SUM and FK_GPP_ROOT_QUIRKS are different drivers");
+    if ((flags & FK_GPP_HALF_SUM) && (flags & FK_GPP_ACHSTEMP))
+        return fk::fail(x, FK_ENOTSUP, "gpp: achstemp of the half sum is not provided");
     if ((flags & FK_GPP_ROOT_QUIRKS) && ng > nc)
         return fk::fail(x, FK_EINVAL, "gpp: FK_GPP_ROOT_QUIRKS indexes I_eps[my_igp*ngpown+ig] and needs ngpown <= ncouls");
     if (ng > 65535) return fk::fail(x, FK_ENOTSUP, "gpp: ngpown > 65535");
@@ -493,13 +498,14 @@ fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsm
     r.aqsm_compact = false;
     // Large host arrays of a mixed-precision call: stream eps, wtilde and aqsntemp in
     // k-chunks and compute each chunk as it lands (the host link is the bottleneck).
-    if (precision == FK_MIXED && !aqn.dev && !eps.dev && !wt.dev && nb > nv && band >= ((size_t)64 << 20))
+    if (precision == FK_MIXED && !(flags & FK_GPP_HALF_SUM) && !aqn.dev && !eps.dev && !wt.dev && nb > nv &&
+        band >= ((size_t)64 << 20))
         return fk::gpp_host_pipelined(x, r, aqsmtemp, aqsntemp, I_eps_array, wtilde_array, vcoul, inv_igp_index,
                                       indinv, wx_array, achtemp, asxtemp, acht_n1_loc, achstemp);
     // Host aqsmtemp: the sum reads only its ngpown columns igp(my_igp)
     // (BGW-Kernels/gppKer.cpp:322-325), so when those are few, gather them on
     // the host and stage nb x ngpown values instead of nb x ncouls.
-    if (!aqm.dev && (long)ng * 128 <= (long)nc) {
+    if (!aqm.dev && !(flags & FK_GPP_HALF_SUM) && (long)ng * 128 <= (long)nc) {
         std::vector<int> invh(ng), indh(nc);
         const int* ip = inv_igp_index;
         const int* dp = indinv;

@@ -62,6 +62,9 @@ struct PrepArgs {
     int tile;    // mixed: plane waves per chunk (a multiple of PREP_THREADS)
     int n1base;  // first flag band handled by this pass
     int ch0;     // first chunk of this launch (blockIdx.x counts from it)
+    // half-sum mode (FK_GPP_HALF_SUM)
+    const double2* aqsm;  // full [nb][nc]
+    const int* brk;       // [ng]: first ig whose |Omega2| < 1e-6 (the flag bands stop there)
 };
 
 // ---------------------------------------------------------------- FP64 exact
@@ -218,6 +221,141 @@ __global__ void __launch_bounds__(PREP_THREADS) prep64_kernel(PrepArgs p) {
     if (tid < nflag * 6) {
         int j = tid / 6, r = tid % 6;
         p.F[(((long)ch * p.nv + p.n1base + j) * p.ng + my_igp) * 6 + r] = acc[tid];
+    }
+}
+
+// ------------------------------------------------------ half sum (gppsum == 1)
+// gppKerSeq.cpp with gppsum == 1: for column igp the sum over ig runs below
+// igp.  Every term of a band n1 >= nvband is
+//   conj(aqsm[n1][igp]) aqsn[n1][ig] sch + aqsm[n1][igp] conj(aqsm[n1][ig]) conj(sch)
+// with sch = mask' * (wtilde / (wx - wtilde)) * I_eps and the inverted mask
+// mask' = |wdiff|^2 < limittwo || |delw|^2 > limitone (noflagOCC_solver :206-242).
+// The driver's blocks (:430-447) take ig < igp-1 except ig = 511 mod 512, and
+// add the diagonal ig = igp (first term only) when igp is a multiple of 512.
+// The second term summed over ig is aqsm[n1][igp] conj(sum_ig aqsm[n1][ig] sch):
+// the same contraction with A = aqsmtemp, conjugated.  Occupied bands follow
+// flagOCC_solver (:90-139), which stops at the first ig with |Omega2| < to1.
+
+// complex division a * conj(b) / |b|^2, round-to-nearest FP64
+FK_DEV double2 cdiv_rn(double2 a, double2 b) {
+    const double n = __dadd_rn(__dmul_rn(b.x, b.x), __dmul_rn(b.y, b.y));
+    return make_double2(__ddiv_rn(__dadd_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), n),
+                        __ddiv_rn(__dsub_rn(__dmul_rn(a.y, b.x), __dmul_rn(a.x, b.y)), n));
+}
+
+// D'(my_igp, iw, ig) of the half sum (without the block membership test)
+FK_DEV double2 half_sch(double wxt, double2 wt, double2 eps) {
+    const double limitone = 1.0 / (1e-6 * 4.0), limittwo = 0.25;
+    const double2 wdiff = make_double2(__dsub_rn(wxt, wt.x), 0.0 - wt.y);
+    const double2 delw = cdiv_rn(wt, wdiff);
+    const double delw2 = cnorm2(delw), wdiffr = cnorm2(wdiff);
+    const bool on = fabs(wdiffr) < limittwo || delw2 > limitone;
+    return on ? cmul(delw, eps) : make_double2(0.0, 0.0);
+}
+
+// ig takes part in column igp's noflag sum (the driver's 512-wide blocks)
+FK_DEV bool half_member(int ig, int igp) { return ig < igp - 1 && (ig & 511) != 511; }
+
+// brk[my_igp] = the first ig < igp with |wtilde^2 * I_eps| < to1 (brk starts above every igp)
+__global__ void half_break_kernel(int ng, int nc, const int* igpm, const double2* eps, const double2* wt, int* brk) {
+    const int my_igp = blockIdx.y;
+    const int igp = igpm[my_igp];
+    for (int ig = blockIdx.x * blockDim.x + threadIdx.x; ig < nc; ig += gridDim.x * blockDim.x) {
+        if (igp < 0 || ig >= igp) break;
+        const double2 w = wt[(long)my_igp * nc + ig];
+        const double2 o = cmul(cmul(w, w), eps[(long)my_igp * nc + ig]);
+        if (hypot(o.x, o.y) < 1e-6) atomicMin(&brk[my_igp], ig);
+    }
+}
+
+// The diagonal value sch(igp) for columns on a block edge (igp % 512 == 0), else 0.
+__global__ void half_diag_kernel(int ng, int nc, const int* igpm, const double2* eps, const double2* wt,
+                                 const double* wx, double2* schd) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ng * 3) return;
+    const int my_igp = t / 3, iw = t % 3, igp = igpm[my_igp];
+    double2 v = make_double2(0.0, 0.0);
+    if (igp > 0 && (igp & 511) == 0)
+        v = half_sch(wx[iw], wt[(long)my_igp * nc + igp], eps[(long)my_igp * nc + igp]);
+    schd[t] = v;
+}
+
+// The flag-band terms of one (ig, iw): sch and ssx of flagOCC_solver (gppsum == 1)
+FK_DEV void half_flag_terms(double wxt, double2 wt, double2 eps, double2& sch, double2& ssx) {
+    const double to1 = 1e-6, gamma = 0.5;
+    const double2 wt2 = cmul(wt, wt), Omega2 = cmul(wt2, eps);
+    const double2 halfinv = cdiv_rn(make_double2(0.5, 0.0), wt);
+    const double2 wmw = make_double2(__dsub_rn(wxt, wt.x), 0.0 - wt.y);
+    const double2 delw = cmul(wmw, halfinv);
+    const double ad = hypot(delw.x, delw.y);
+    if (hypot(wmw.x, wmw.y) < gamma || __dmul_rn(ad, ad) < to1) {
+        sch = make_double2(0.0, 0.0);
+        ssx = hypot(wt.x, wt.y) > to1
+                  ? cdiv_rn(make_double2(0.0 - Omega2.x, 0.0 - Omega2.y),
+                            cmul(cscale(wt2, 4.0), make_double2(__dadd_rn(1.0, delw.x), delw.y)))
+                  : make_double2(0.0, 0.0);
+    } else {
+        sch = cdiv_rn(cmul(wt, eps), wmw);
+        ssx = cdiv_rn(Omega2, make_double2(__dsub_rn(__dmul_rn(wxt, wxt), wt2.x), 0.0 - wt2.y));
+    }
+}
+
+// Prep of the half sum, FP64 arithmetic for both precisions: D' as FP64 rows
+// (IMG = 0) or as the pre-split BF16 image of the tensor-core contraction
+// (IMG = 1); flag bands n1base .. n1base+NVC-1 accumulate, per (iw, sch/ssx),
+// S1 = sum_ig aqsn[n1][ig] x and S2 = sum_ig aqsm[n1][ig] x (S2 without
+// ig = igp-1) over ig < brk: F[ch][n1][my_igp][12], entry ((iw*2 + kind)*2 + part).
+template <int IMG>
+__global__ void __launch_bounds__(PREP_THREADS) prep_half_kernel(PrepArgs p) {
+    __shared__ double2 sm[8 * NVC * 12];
+    const int my_igp = blockIdx.y, ch = p.ch0 + blockIdx.x, tid = threadIdx.x;
+    const int igp = p.igp[my_igp];
+    const int nflag = min(NVC, p.nv - p.n1base);
+    const int stop = igp < 0 ? 0 : min(igp, p.brk[my_igp]);
+    double2 acc[NVC * 12];
+#pragma unroll
+    for (int i = 0; i < NVC * 12; ++i) acc[i] = make_double2(0.0, 0.0);
+    const double2* wrow = p.wt + (long)my_igp * p.nc;
+    const double2* erow = p.eps + (long)my_igp * p.nc;
+    for (int ig = ch * p.tile + tid; ig < min(p.nc, (ch + 1) * p.tile); ig += PREP_THREADS) {
+        const double2 wt = wrow[ig], ep = erow[ig];
+#pragma unroll
+        for (int iw = 0; iw < 3; ++iw) {
+            const double wxt = p.wx[iw];
+            if (p.D) {
+                const double2 dv = (igp >= 0 && half_member(ig, igp)) ? half_sch(wxt, wt, ep) : make_double2(0.0, 0.0);
+                if (IMG) {
+                    const int nt = my_igp / GPP_COLS, row = (my_igp % GPP_COLS) * 3 + iw;
+                    tcx::bimg_store<64>((uint8_t*)p.D + (long)nt * p.kstages * tcx::Cfg<64>::B_BYTES, p.kstages, row,
+                                        ig, f64_to_f32_bits(dv.x), f64_to_f32_bits(dv.y));
+                } else {
+                    ((double2*)p.D)[((long)my_igp * 3 + iw) * p.nc + ig] = dv;
+                }
+            }
+            if (nflag > 0 && ig < stop) {
+                double2 sch, ssx;
+                half_flag_terms(wxt, wt, ep, sch, ssx);
+#pragma unroll
+                for (int j = 0; j < NVC; ++j)
+                    if (j < nflag) {
+                        const long row = (long)(p.n1base + j) * p.nc + ig;
+                        const double2 an = p.aqsn[row], am = p.aqsm[row];
+                        double2* a = acc + j * 12 + iw * 4;
+                        cfma(a[0], an, sch);
+                        cfma(a[2], an, ssx);
+                        if (ig != igp - 1) {
+                            cfma(a[1], am, sch);
+                            cfma(a[3], am, ssx);
+                        }
+                    }
+            }
+        }
+    }
+    if (nflag <= 0) return;
+    block_sum<NVC * 12>(acc, sm);
+    if (tid < nflag * 12) {
+        const int j = tid / 12, r = tid % 12;
+        p.F[(((long)ch * p.nv + p.n1base + j) * p.ng + my_igp) * 12 + r] = acc[tid];
     }
 }
 
@@ -415,6 +553,11 @@ struct RowsArgs {
     const double* vcoul;
     const int *igp, *acol;
     double2* rows;
+    // half-sum mode: partials of the A = aqsmtemp contraction, diagonal values, aqsntemp
+    const double2* P2;
+    const double2* schd;  // [ng][3]
+    const double2* aqsn;  // [nb][nc]
+    int nc;
 };
 
 FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
@@ -430,6 +573,30 @@ FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
     } else if (n1 >= nv) {
         const long M = nb - nv, m = n1 - nv;
         if (c < 3 && lane < nslots) v = ordered_sum(P + ((long)lane * M + m) * 3 + c, 32 * M * 3, (nslots - lane + 31) / 32);
+        if (c < 3 && ra.P2) {
+            // half sum: + conj(A = aqsmtemp contraction) + diagonal terms on block edges
+            if (lane < nslots)
+                v = cadd(v, cconj(ordered_sum(ra.P2 + ((long)lane * M + m) * 3 + c, 32 * M * 3, (nslots - lane + 31) / 32)));
+            for (int h = lane; h < ng; h += 32) {
+                const int g = igp[h];
+                if (g <= 0 || (g & 511)) continue;
+                const double2 t = cmul(cmul(cconj(aqsm[(long)n1 * ldm + acol[h]]), ra.aqsn[(long)n1 * ra.nc + g]),
+                                       ra.schd[h * 3 + c]);
+                v = cadd(v, cscale(t, 0.5 * vcoul[g]));
+            }
+        }
+    } else if (ra.P2) {
+        // half sum, occupied band: weight * (cm S1 + conj(cm S2)) per column
+        const int kind = c / 3, r = ((c % 3) * 2 + kind) * 2;
+        const double occ = 1.0;
+        for (int h = lane; h < ng; h += 32) {
+            const int g = igp[h];
+            if (g < 0) continue;
+            const double2 s1 = ordered_sum(F + ((long)n1 * ng + h) * 12 + r, (long)nv * ng * 12, nch);
+            const double2 s2 = ordered_sum(F + ((long)n1 * ng + h) * 12 + r + 1, (long)nv * ng * 12, nch);
+            const double2 cm = cconj(aqsm[(long)n1 * ldm + acol[h]]);
+            v = cadd(v, cscale(cadd(cmul(cm, s1), cconj(cmul(cm, s2))), kind ? occ * vcoul[g] : 0.5 * vcoul[g]));
+        }
     } else {
         const int kind = c / 3, r = (c % 3) * 2 + kind;  // kind 0: sch, 1: ssx
         const double occ = 1.0;
@@ -523,6 +690,11 @@ Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0, bool pipeline
         p.tile = PREP_TILE;
         p.nch = ceil_div(r.nc, PREP_TILE);
     }
+    const bool half = (r.flags & FK_GPP_HALF_SUM) != 0;
+    if (half) {  // FP64 prep for both precisions (prep_half_kernel)
+        p.tile = PREP_TILE;
+        p.nch = ceil_div(r.nc, PREP_TILE);
+    }
     p.passes = std::max(1, ceil_div(r.nv, NVC));
     const int M = r.nb - r.nv, N = 3 * r.ng;
     if (p.mixed) {
@@ -560,7 +732,7 @@ Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0, bool pipeline
                : p.mixed ? (size_t)p.NT * p.kstages * tcx::Cfg<64>::B_BYTES
                          : (size_t)N * r.nc * sizeof(double2);
     p.bytesW = (p.mixed && M > 0) ? (size_t)M * r.ng * sizeof(float2) : 0;
-    p.bytesF = (size_t)p.nch * std::max(r.nv, 1) * r.ng * 6 * sizeof(double2);
+    p.bytesF = (size_t)p.nch * std::max(r.nv, 1) * r.ng * (half ? 12 : 6) * sizeof(double2);
     p.bytesP = M > 0 ? (size_t)p.KS * p.NT * M * 3 * sizeof(double2) : 0;
     p.bytesS = (r.flags & FK_GPP_ACHSTEMP) ? (size_t)p.KSs * p.NTs * r.nb * sizeof(double2) : 0;
     p.bytesRows = (size_t)r.nb * 8 * sizeof(double2);
@@ -577,7 +749,8 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 
 size_t gpp_workspace(const Ctx& c, const GppDev& r, bool pipelined) {
     Plan p = make_plan(c, r, 0, pipelined);
-    return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesRows + p.bytesIgp + p.bytesW + 10 * 256;
+    const size_t half = (r.flags & FK_GPP_HALF_SUM) ? p.bytesP + (size_t)r.ng * (4 + 3 * sizeof(double2)) + 512 : 0;
+    return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesRows + p.bytesIgp + p.bytesW + half + 10 * 256;
 }
 
 int gpp_pipe_chunks(const Ctx& c, const GppDev& r) { return make_plan(c, r, 0, true).pipe_chunks; }
@@ -609,7 +782,96 @@ fk_status gpp_pipe_copy(Ctx& c, const GppDev& r, const GppPipe* pipe, int q0, in
     return FK_OK;
 }
 
+// The half-sum mode (FK_GPP_HALF_SUM): prep in FP64, then the contraction of
+// the image with A = aqsntemp (partials P) and with A = aqsmtemp (partials P2).
+fk_status gpp_run_half(Ctx& c, const GppDev& r) {
+    const Plan p = make_plan(c, r);
+    cudaStream_t st = c.stream;
+    const int M = r.nb - r.nv;
+    int* igp = (int*)c.ws.take(p.bytesIgp);
+    int* acol = igp ? igp + r.ng : nullptr;
+    void* D = p.bytesD ? c.ws.take(p.bytesD) : nullptr;
+    double2* F = (double2*)c.ws.take(p.bytesF);
+    double2* P = p.bytesP ? (double2*)c.ws.take(p.bytesP) : nullptr;
+    double2* P2 = p.bytesP ? (double2*)c.ws.take(p.bytesP) : nullptr;
+    double2* rows = (double2*)c.ws.take(p.bytesRows);
+    float2* W = p.bytesW ? (float2*)c.ws.take(p.bytesW) : nullptr;
+    int* brk = (int*)c.ws.take((size_t)r.ng * sizeof(int));
+    double2* schd = (double2*)c.ws.take((size_t)r.ng * 3 * sizeof(double2));
+    if (!igp || !F || !rows || !brk || !schd || (p.bytesD && !D) || (p.bytesP && (!P || !P2)) || (p.bytesW && !W))
+        return fail(c, FK_ENOMEM, "workspace too small for GPP request");
+    if (r.aqsm_compact || r.ldm != r.nc) return fail(c, FK_EINVAL, "gpp: the half sum needs all of aqsmtemp");
+    c.launches = 0;
+    if (p.mixed && D) {
+        if (tcx::img_needs_pad(64, r.ng, GPP_COLS, r.nc))
+            tcx::img_pad_kernel<64><<<dim3(p.kstages, p.NT, 1), 256, 0, st>>>((uint8_t*)D, p.NT, p.kstages, r.ng,
+                                                                            GPP_COLS, r.nc);
+        if (cudaMemsetAsync(c.errword, 0, sizeof(int), st) != cudaSuccess)
+            return cuda_fail(c, cudaGetLastError(), "gpp: error word");
+    }
+    phase_mark(c, 1);
+    igp_map_kernel<<<ceil_div(r.ng, 128), 128, 0, st>>>(r.ng, r.nc, r.inv, r.indinv, 0, igp, acol);
+    if (p.mixed && M > 0)
+        tcx::weight_table_kernel<<<dim3(ceil_div(M, 128), r.ng), 128, 0, st>>>(M, r.nv, r.ng, r.aqsm, r.ldm, r.vcoul,
+                                                                            igp, acol, 0.5, W, nullptr, nullptr);
+    if (cudaMemsetAsync(brk, 0x7f, (size_t)r.ng * sizeof(int), st) != cudaSuccess)
+        return cuda_fail(c, cudaGetLastError(), "gpp: break table");
+    half_break_kernel<<<dim3(std::max(1, std::min(ceil_div(r.nc, 256), 64)), r.ng), 256, 0, st>>>(r.ng, r.nc, igp,
+                                                                                                 r.eps, r.wt, brk);
+    half_diag_kernel<<<ceil_div(r.ng * 3, 128), 128, 0, st>>>(r.ng, r.nc, igp, r.eps, r.wt, r.wx, schd);
+    c.launches += p.mixed && M > 0 ? 4 : 3;
+    for (int pass = 0; pass < p.passes; ++pass) {
+        PrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, (pass == 0 && M > 0) ? D : nullptr,
+                   p.kstages, F, p.nch, p.tile, pass * NVC, 0, r.aqsm, brk};
+        if (p.mixed) prep_half_kernel<1><<<dim3(p.nch, r.ng), PREP_THREADS, 0, st>>>(a);
+        else prep_half_kernel<0><<<dim3(p.nch, r.ng), PREP_THREADS, 0, st>>>(a);
+        ++c.launches;
+    }
+    phase_mark(c, 2);
+    for (int pass = 0; pass < 2 && M > 0; ++pass) {
+        const double2* A = pass == 0 ? r.aqsn : r.aqsm;
+        ContractArgs a{};
+        a.A = A; a.lda = r.nc; a.m0 = r.nv; a.M = M;
+        a.B = D; a.ldb = r.nc; a.bstride = 0; a.N = 3 * r.ng; a.K = r.nc;
+        a.KS = p.KS; a.kchunk = p.kchunk; a.batches = 1; a.batch_plane = nullptr;
+        a.aqsm = r.aqsm; a.ldm = r.ldm; a.vcoul = r.vcoul; a.igp = igp; a.acol = acol; a.wscale = 0.5; a.G = 3;
+        a.P = pass == 0 ? P : P2;
+        if (p.mixed) {
+            tcx::TcArgs t{};
+            t.c = a;
+            t.Bimg = (const uint8_t*)D;
+            t.W1 = W; t.W2 = nullptr; t.ldw = M; t.gpp_cols = GPP_COLS; t.Aimg = nullptr; t.vcol = nullptr;
+            t.kstages_total = p.kstages;
+            t.MT = p.MT; t.NT = p.NT; t.units = p.units;
+            t.err = c.errword;
+            if (tcx::encode_rows_map(&t.amap, A, r.nc, r.nc, r.nb) != cudaSuccess)
+                return fail(c, FK_ECUDA, "gpp: cannot describe an input as a tensor map (needs a 16-byte aligned array)");
+            auto k = tcx::tc_contract_kernel<EPI_GPP, 64, false>;
+            set_smem(k, tcx::Cfg<64>::SMEM);
+            k<<<std::min(p.units, c.sms), tcx::THREADS, tcx::Cfg<64>::SMEM, st>>>(t);
+        } else {
+            auto k = d64::contract_kernel<EPI_GPP>;
+            set_smem(k, d64::SMEM);
+            k<<<dim3(p.MT, p.NT * p.KS), d64::THREADS, d64::SMEM, st>>>(a);
+        }
+        ++c.launches;
+    }
+    phase_mark(c, 3);
+    RowsArgs ra{r.nb, r.nv, r.ng, P ? p.KS * p.NT : 0, P, 0, nullptr, p.nch, F, r.ldm, r.aqsm, r.vcoul, igp, acol, rows};
+    ra.P2 = P2 ? P2 : (const double2*)F;  // non-null selects the half sum even without contraction partials
+    ra.schd = schd;
+    ra.aqsn = r.aqsn;
+    ra.nc = r.nc;
+    rows_kernel<<<ceil_div(r.nb * 7, 8), 256, 0, st>>>(ra);
+    totals_kernel<<<1, 256, 0, st>>>(r.nb, rows, r.out);
+    c.launches += 2;
+    phase_mark(c, 4);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FK_OK : cuda_fail(c, e, "gpp kernels (half sum)");
+}
+
 fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
+    if (r.flags & FK_GPP_HALF_SUM) return pipe ? fail(c, FK_EINVAL, "gpp: no pipelined half sum") : gpp_run_half(c, r);
     const Plan p = make_plan(c, r, 0, pipe != nullptr);
     if (pipe && !p.pipe_chunks) return fail(c, FK_EINVAL, "gpp: pipelined staging needs the mixed path");
     cudaStream_t st = c.stream;

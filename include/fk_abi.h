@@ -93,6 +93,11 @@ const char* fk_version(void);
                                    (gppKer.cpp:139) */
 #define FK_GPP_ACHSTEMP    0x2u /* also compute the static-CH remainder achstemp
                                    (gppkernel.deslippe.09.30.2014.f90:195-229) */
+#define FK_GPP_HALF_SUM    0x4u /* gppsum == 1 of gppKerSeq.cpp: for column igp the
+                                   sum over ig runs below igp and each term carries its
+                                   conjugate pair (noflagOCC_solver :206-242 with the
+                                   driver's 512-wide blocks :430-447, flagOCC_solver
+                                   :90-139); not with FK_GPP_ROOT_QUIRKS or FK_GPP_ACHSTEMP */
 
 /*
  * GPP self-energy sum (BGW-Kernels/gppKer.cpp:303-439).

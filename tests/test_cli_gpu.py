@@ -38,6 +38,20 @@ def test_gppKer_cli_prints_reference_values(prec):
     assert np.max(np.abs(got - want)) / np.max(np.abs(want)) <= (1e-13 if prec == "fp64" else 1e-6)
 
 
+def test_gppKer_cli_half_sum_prints_seq_driver_values():
+    """Five arguments: gppKerSeq.cpp's command line; gppsum = 1 is the half sum."""
+    with open(GOLD) as f:
+        e = json.load(f)["gppKer_seq"][0]
+    out, v = run("gppKer", *e["args"])
+    assert "gppsum = 1" in out
+    got = np.array([v[f"achtemp[{i}]"] for i in range(3)])
+    want = np.array([complex(*z) for z in e["achtemp"]])
+    assert np.max(np.abs(got - want)) / np.max(np.abs(want)) <= 1e-13
+    r = subprocess.run([os.path.join(BIN, "gppKer")] + [str(a) for a in e["args"][:4]] + ["0"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 1 and "gppsum = 0" in r.stderr
+
+
 def test_gppKer_cli_usage_line():
     out = subprocess.run([os.path.join(BIN, "gppKer")], capture_output=True, text=True).stdout
     assert "The correct form of input is" in out
