@@ -52,6 +52,32 @@ def gpp_reference_init(number_bands: int, nvband: int, ncouls: int, nodes_per_gr
     }
 
 
+def gpp_real_reference_init(number_bands: int, nvband: int, ncouls: int, nodes_per_group: int) -> dict:
+    """Arrays of the real-valued driver main() (gppKer_real.cpp:212-295): every
+    array 0.5, vcoul = 1, the index map and frequencies of the complex driver."""
+    ngpown = ncouls // nodes_per_group
+    inv, indinv = gpp_reference_index(ncouls, ngpown)
+    return {
+        "number_bands": number_bands, "nvband": nvband, "ncouls": ncouls, "ngpown": ngpown,
+        "aqsmtemp": np.full((number_bands, ncouls), 0.5), "aqsntemp": np.full((number_bands, ncouls), 0.5),
+        "I_eps_array": np.full((ngpown, ncouls), 0.5), "wtilde_array": np.full((ngpown, ncouls), 0.5),
+        "vcoul": np.ones(ncouls, np.float64), "inv_igp_index": inv, "indinv": indinv, "wx_array": gpp_wx(),
+    }
+
+
+def gpp_real_synthetic(number_bands: int, nvband: int, ncouls: int, ngpown: int, seed: int = 0,
+                       dist: str = "uniform", index: str = "baseline", wx: str = "baseline") -> dict:
+    """Seeded inputs of the real-valued GPP: the real parts of gpp_synthetic's
+    arrays (same options).  With dist="branch" wtilde lies around each
+    frequency, so the noflag mask is false for many elements (the real driver
+    then re-adds the value left at that block offset) and every branch of the
+    real solver is taken."""
+    p = gpp_synthetic(number_bands, nvband, ncouls, ngpown, seed=seed, dist=dist, index=index, wx=wx)
+    for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array"):
+        p[k] = np.ascontiguousarray(p[k].real)
+    return p
+
+
 def _cu(rng, shape, lo=-0.5, hi=0.5):
     return rng.uniform(lo, hi, shape) + 1j * rng.uniform(lo, hi, shape)
 

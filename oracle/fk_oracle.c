@@ -339,6 +339,148 @@ int orc_gpp(int nb, int nv, int nc, int ng,
     return 0;
 }
 
+/* ------------------------------------------------------ real-valued GPP */
+
+/* ssxt_scht_solver of gppKer_real.cpp:17-63 (the sexcut test at :58-59 needs
+ * abs(wxt) < 0 and never fires); returns ssx and sch before the
+ * matngmatmgp factor. */
+static inline void gpp_real_solver(double wxt, double wtilde, double wtilde2, double Omega2, double ieps,
+                                   double* ssx, double* sch) {
+    const double to1 = 1e-6;
+    const double limitone = 1.0 / (to1 * 4.0), limittwo = 0.5 * 0.5;
+    const double wdiff = wxt - wtilde;
+    double cden = wdiff;
+    double rden = 1 / (cden * cden);
+    const double delw = wtilde * cden * rden;
+    const double delwr = delw * delw, wdiffr = wdiff * wdiff;
+    if ((wdiffr > limittwo) && (delwr < limitone)) {
+        *sch = delw * ieps;
+        cden = wxt * wxt; /* pow(wxt,2) */
+        rden = 1.00 / (cden * cden);
+        *ssx = Omega2 * cden * rden;
+    } else if (delwr > to1) {
+        *sch = 0.0;
+        cden = 4.00 * wtilde2 * (delw + 0.50);
+        rden = 1.00 / (cden * cden);
+        *ssx = -Omega2 * cden * rden * delw;
+    } else {
+        *sch = 0.0;
+        *ssx = 0.0;
+    }
+}
+
+int orc_gpp_real(int nb, int nv, int nc, int ng,
+                 const double* aqsm, const double* aqsn,
+                 const double* I_eps, const double* wtilde, const double* vcoul,
+                 const int* inv_igp_index, const int* indinv, int indinv_len,
+                 const double* wx, unsigned flags, int nthreads,
+                 double* achtemp, double* asxtemp, double* acht_n1_loc,
+                 double* sch_out, double* ssx_out) {
+    if (nb <= 0 || nc <= 0 || ng <= 0 || nv < 0 || nv > nb) return -1;
+    set_threads(nthreads);
+    const double limitone = 1.0 / (1e-6 * 4.0), limittwo = 0.5 * 0.5;
+    const int zero_masked = (flags & ORC_GPP_REAL_ZERO_MASKED) != 0;
+    int* igpmap = (int*)malloc(sizeof(int) * (size_t)ng);
+    double* sch = (double*)calloc((size_t)nb * ng * 3, sizeof(double));
+    double* ssx = (double*)calloc((size_t)(nv > 0 ? nv : 1) * ng * 3, sizeof(double));
+    if (!igpmap || !sch || !ssx) { free(igpmap); free(sch); free(ssx); return -2; }
+    for (int i = 0; i < ng; ++i) igpmap[i] = gpp_igp(i, nc, inv_igp_index, indinv, indinv_len);
+
+    for (int n1 = 0; n1 < nb; ++n1) {
+        const int flag_occ = n1 < nv;
+#pragma omp parallel for schedule(dynamic)
+        for (int my_igp = 0; my_igp < ng; ++my_igp) {
+            const int igp = igpmap[my_igp];
+            if (igp < 0) continue;
+            const double* erow = I_eps + (size_t)my_igp * nc;
+            const double* wrow = wtilde + (size_t)my_igp * nc;
+            const double* nrow = aqsn + (size_t)n1 * nc;
+            const double mygpvar1 = aqsm[(size_t)n1 * nc + igp];
+            double sch_array[3] = {0, 0, 0}, ssx_array[3] = {0, 0, 0};
+            if (flag_occ) {
+                /* flagOCC_solver, gppKer_real.cpp:124-153 */
+                for (int iw = 0; iw < 3; ++iw) {
+                    const double wxt = wx[iw];
+                    double ssxt = 0.0, scht = 0.0;
+                    for (int ig = 0; ig < nc; ++ig) {
+                        const double w = wrow[ig];
+                        const double w2 = w * w; /* std::pow(wtilde, 2) */
+                        const double Omega2 = w2 * erow[ig];
+                        const double matngmatmgp = nrow[ig] * mygpvar1;
+                        double x, h;
+                        gpp_real_solver(wxt, w, w2, Omega2, erow[ig], &x, &h);
+                        ssxt += matngmatmgp * x;
+                        scht += matngmatmgp * h;
+                    }
+                    ssx_array[iw] += ssxt;
+                    sch_array[iw] += 0.5 * scht;
+                }
+            } else {
+                /* the driver's block loop, gppKer_real.cpp:341-383: scha persists
+                 * over blocks and frequencies of this (n1, my_igp) */
+                const int igblk = 512;
+                double scha[512];
+                memset(scha, 0, sizeof scha);
+                for (int igbeg = 0, nblk = 0; igbeg < nc; igbeg += igblk, ++nblk) {
+                    const int igend = igblk < nc - igblk * nblk ? igblk : nc - igblk * nblk;
+                    for (int iw = 0; iw < 3; ++iw) {
+                        const double wxt = wx[iw];
+                        double scht = 0.0;
+                        for (int ig = 0; ig < igend; ++ig) {
+                            const int g = ig + nblk * igblk;
+                            const double wdiff = wxt - wrow[g];
+                            const double cden = wdiff;
+                            double rden = cden * cden;
+                            rden = 1 / rden;
+                            const double delw = wrow[g] * cden * rden;
+                            const double delwr = delw * delw, wdiffr = wdiff * wdiff;
+                            if ((wdiffr > limittwo) && (delwr < limitone))
+                                scha[ig] = mygpvar1 * nrow[g] * delw * erow[g];
+                            else if (zero_masked)
+                                scha[ig] = 0.0;
+                        }
+                        for (int ig = 0; ig < igend; ++ig) scht += scha[ig];
+                        sch_array[iw] += 0.5 * scht;
+                    }
+                }
+            }
+            double* so = sch + ((size_t)n1 * ng + my_igp) * 3;
+            for (int iw = 0; iw < 3; ++iw) so[iw] = sch_array[iw];
+            if (flag_occ) {
+                double* xo = ssx + ((size_t)n1 * ng + my_igp) * 3;
+                for (int iw = 0; iw < 3; ++iw) xo[iw] = ssx_array[iw];
+            }
+        }
+    }
+
+    /* accumulation into the outputs, gppKer_real.cpp:385-412 */
+    ksum acc[3] = {{0, 0}, {0, 0}, {0, 0}}, asx[3] = {{0, 0}, {0, 0}, {0, 0}};
+    const double occ = 1.0;
+    for (int n1 = 0; n1 < nb; ++n1) {
+        ksum n1loc = {0, 0};
+        for (int my_igp = 0; my_igp < ng; ++my_igp) {
+            const int igp = igpmap[my_igp];
+            if (igp < 0) continue;
+            const double* so = sch + ((size_t)n1 * ng + my_igp) * 3;
+            for (int iw = 0; iw < 3; ++iw) ks_add(&acc[iw], so[iw] * vcoul[igp]);
+            ks_add(&n1loc, so[2] * vcoul[igp]);
+            if (n1 < nv) {
+                const double* xo = ssx + ((size_t)n1 * ng + my_igp) * 3;
+                for (int iw = 0; iw < 3; ++iw) ks_add(&asx[iw], xo[iw] * occ * vcoul[igp]);
+            }
+        }
+        if (acht_n1_loc) acht_n1_loc[n1] = ks_val(&n1loc);
+    }
+    for (int iw = 0; iw < 3; ++iw) {
+        achtemp[iw] = ks_val(&acc[iw]);
+        asxtemp[iw] = ks_val(&asx[iw]);
+    }
+    if (sch_out) memcpy(sch_out, sch, sizeof(double) * (size_t)nb * ng * 3);
+    if (ssx_out && nv > 0) memcpy(ssx_out, ssx, sizeof(double) * (size_t)nv * ng * 3);
+    free(igpmap); free(sch); free(ssx);
+    return 0;
+}
+
 /* ------------------------------------------------------------------- FF */
 
 void orc_ff_compute_fact(double wx, int nFreq, const double* dFreqGrid,

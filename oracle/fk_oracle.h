@@ -55,6 +55,30 @@ int orc_gpp(int nb, int nv, int nc, int ng,
             double* achtemp, double* asxtemp, double* acht_n1_loc,
             double* achstemp, double* sch_out, double* ssx_out);
 
+/* Real-valued GPP flags */
+#define ORC_GPP_REAL_ZERO_MASKED 0x10u /* a masked noflag term contributes 0 (the
+                                          commented-out else of gppKer_real.cpp:372-373)
+                                          instead of the value left in scha[ig] */
+
+/*
+ * Real-valued GPP, gppKer_real.cpp:297-396: the loop nest of the GPP sum on
+ * double arrays (aqsmtemp/aqsntemp [nb][ncouls], I_eps/wtilde [ngpown][ncouls]).
+ * Occupied bands: flagOCC_solver (:124-153) over ssxt_scht_solver (:17-63).
+ * Other bands: the driver's 512-wide blocks (:341-383), where a masked term
+ * leaves scha[ig] as it was (the value of the last unmasked term at that
+ * block offset, for the same (n1, my_igp), or 0) and every block sum adds all
+ * of scha[0 .. igend).  Outputs (real): achtemp[3], asxtemp[3],
+ * acht_n1_loc[nb] (nullable), sch_out[nb][ng][3], ssx_out[nv][ng][3]
+ * (nullable; per-(n1, my_igp) sch_array / ssx_array before the vcoul weight).
+ */
+int orc_gpp_real(int nb, int nv, int nc, int ng,
+                 const double* aqsm, const double* aqsn,
+                 const double* I_eps, const double* wtilde, const double* vcoul,
+                 const int* inv_igp_index, const int* indinv, int indinv_len,
+                 const double* wx, unsigned flags, int nthreads,
+                 double* achtemp, double* asxtemp, double* acht_n1_loc,
+                 double* sch_out, double* ssx_out);
+
 /* FF flags */
 #define ORC_FF_SCHDT_GEMM  0x1u  /* schDt_matrix from the band x G x G' contraction
                                     (ffkernel.deslippe.best.f90.back1:402-418);

@@ -23,6 +23,7 @@ REF_DIR = os.path.join(HERE, "_ref")
 ORC_GPP_ROOT_QUIRKS = 0x1
 ORC_GPP_ACHSTEMP = 0x2
 ORC_GPP_HALF_SUM = 0x4
+ORC_GPP_REAL_ZERO_MASKED = 0x10
 ORC_FF_SCHDT_GEMM = 0x1
 ORC_FF_PHYSICS = 0x2
 ORC_FF_SPLIT_ACHD = 0x4
@@ -48,6 +49,9 @@ def lib():
         ip = ctypes.POINTER(ctypes.c_int)
         L.orc_gpp.restype = ctypes.c_int
         L.orc_gpp.argtypes = [ctypes.c_int] * 4 + [dp] * 5 + [ip, ip, ctypes.c_int, dp, ctypes.c_uint, ctypes.c_int] + [dp] * 6
+        L.orc_gpp_real.restype = ctypes.c_int
+        L.orc_gpp_real.argtypes = ([ctypes.c_int] * 4 + [dp] * 5 + [ip, ip, ctypes.c_int, dp, ctypes.c_uint,
+                                   ctypes.c_int] + [dp] * 5)
         L.orc_ff.restype = ctypes.c_int
         L.orc_ff.argtypes = ([ctypes.c_int] * 6 + [dp] * 5 + [ip, ip] + [dp] * 4 +
                              [ctypes.c_double] * 4 + [ctypes.c_uint, ctypes.c_int] + [dp] * 6)
@@ -98,6 +102,27 @@ def gpp(p: dict, flags: int = 0, nthreads: int = 0, per_pair: bool = False) -> d
     return out
 
 
+def gpp_real(p: dict, flags: int = 0, nthreads: int = 0, per_pair: bool = False) -> dict:
+    """Oracle real-valued GPP (gppKer_real.cpp) on a dict of real arrays."""
+    nb, nv, nc, ng = p["number_bands"], p["nvband"], p["ncouls"], p["ngpown"]
+    f = {k: np.ascontiguousarray(p[k], dtype=np.float64)
+         for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array", "vcoul", "wx_array")}
+    inv = np.ascontiguousarray(p["inv_igp_index"], dtype=np.int32)
+    indinv = np.ascontiguousarray(p["indinv"], dtype=np.int32)
+    ach, asx, n1loc = np.zeros(3), np.zeros(3), np.zeros(nb)
+    sch = np.zeros((nb, ng, 3)) if per_pair else None
+    ssx = np.zeros((max(nv, 1), ng, 3)) if per_pair else None
+    rc = lib().orc_gpp_real(nb, nv, nc, ng, _dp(f["aqsmtemp"]), _dp(f["aqsntemp"]), _dp(f["I_eps_array"]),
+                            _dp(f["wtilde_array"]), _dp(f["vcoul"]), _ip(inv), _ip(indinv), len(indinv),
+                            _dp(f["wx_array"]), flags, nthreads, _dp(ach), _dp(asx), _dp(n1loc), _dp(sch), _dp(ssx))
+    if rc != 0:
+        raise ValueError(f"orc_gpp_real rc={rc}")
+    out = {"achtemp": ach, "asxtemp": asx, "acht_n1_loc": n1loc}
+    if per_pair:
+        out["sch"], out["ssx"] = sch, ssx[:nv]
+    return out
+
+
 def ff(p: dict, flags: int = 0, nthreads: int = 0) -> dict:
     """Oracle FF on the input dict produced by fortkernels_gb300.inputs."""
     nb, nv, nc, ng = p["number_bands"], p["nvband"], p["ncouls"], p["ngpown"]
@@ -141,6 +166,7 @@ def have_ref() -> bool:
 
 
 _CPLX = re.compile(r"\(\s*([-+0-9.eEinfa]+)\s*,\s*([-+0-9.eEinfa]+)\s*\)")
+_REAL = re.compile(r"\s*([-+]?[0-9.]+(?:[eE][-+]?[0-9]+)?)\s*$")
 
 
 def run_ref_driver(name: str, args, threads: int = 8) -> dict:
@@ -154,10 +180,13 @@ def run_ref_driver(name: str, args, threads: int = 8) -> dict:
         if not m:
             continue
         c = _CPLX.search(m.group(4))
-        if not c:
-            continue
         key = m.group(1) + (f"[{m.group(3)}]" if m.group(2) else "")
-        res[key] = complex(float(c.group(1)), float(c.group(2)))
+        if c:
+            res[key] = complex(float(c.group(1)), float(c.group(2)))
+            continue
+        r = _REAL.match(m.group(4))  # the real-valued driver prints plain numbers
+        if r:
+            res[key] = float(r.group(1))
     t = re.search(r"Chrono Time Taken \*+= ([0-9.eE+-]+)", out)
     if t:
         res["seconds"] = float(t.group(1))
@@ -183,6 +212,22 @@ def ref_gpp_pairs(p: dict, igp: np.ndarray, gppsum: int = 0) -> dict:
     sch = raw[: nb * ng * 3].reshape(nb, ng, 3)
     ssx = raw[nb * ng * 3:].reshape(nv, ng, 3) if nv > 0 else np.zeros((0, ng, 3), np.complex128)
     return {"sch": sch, "ssx": ssx}
+
+
+def ref_gpp_real_pairs(p: dict, igp: np.ndarray) -> dict:
+    """Per-(n1 < nvband, my_igp, iw) sch/ssx of the real-valued driver's own
+    flagOCC_solver (gppKer_real.cpp)."""
+    nb, nv, nc, ng = p["number_bands"], p["nvband"], p["ncouls"], p["ngpown"]
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        with open(fin, "wb") as f:
+            for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array", "wx_array"):
+                f.write(np.ascontiguousarray(p[k], np.float64).tobytes())
+            f.write(np.ascontiguousarray(igp, np.int32).tobytes())
+        subprocess.run([os.path.join(REF_DIR, "ref_harness_gpp_real")] + [str(x) for x in (nb, nv, nc, ng, fin, fout)],
+                       check=True, env=dict(os.environ, OMP_NUM_THREADS="1"))
+        raw = np.fromfile(fout, dtype=np.float64)
+    return {"sch": raw[: nv * ng * 3].reshape(nv, ng, 3), "ssx": raw[nv * ng * 3:].reshape(nv, ng, 3)}
 
 
 def ref_ff(p: dict, schDt=None) -> dict:

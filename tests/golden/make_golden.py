@@ -3,11 +3,13 @@
 Needs the reference tree (its drivers and harnesses are compiled into
 oracle/_ref/ by `make -C oracle ref`).  It runs:
   * the unmodified reference drivers (BGW-Kernels/gppKer.cpp, repo-root
-    gppKer.cpp, gppKer_orig.cpp, FFKer_cori/ffKernel.cpp) with their own
-    constant inputs, recording what they print;
+    gppKer.cpp, gppKer_orig.cpp, gppKerSeq.cpp, gppKer_real.cpp,
+    FFKer_cori/ffKernel.cpp) with their own constant inputs, recording what
+    they print;
   * the harnesses that call the reference's own solver functions
-    (oracle/ref_harness_gpp.cpp, oracle/ref_harness_ff.cpp) on small seeded
-    random inputs, stored together with the inputs.
+    (oracle/ref_harness_gpp.cpp, oracle/ref_harness_gpp_real.cpp,
+    oracle/ref_harness_ff.cpp) on small seeded random inputs, stored together
+    with the inputs.
 The oracle and the CUDA library are then checked against these files on any
 machine, without the reference.
 
@@ -36,6 +38,7 @@ GPP_SIZES = [(64, 2, 512, 4), (32, 2, 1000, 8), (128, 4, 777, 7), (512, 2, 2048,
              (24, 24, 256, 4)]
 FF_SIZES = [(16, 3, 300, 40, 6, 7), (64, 2, 512, 64, 15, 10), (512, 2, 4096, 512, 15, 10)]
 SEQ_SIZES = [(64, 2, 1024, 4, 1), (32, 3, 2048, 8, 1), (16, 2, 1536, 6, 1)]
+REAL_SIZES = [(64, 2, 1024, 4), (512, 2, 2048, 32), (33, 5, 1000, 10), (40, 0, 777, 7)]
 
 
 def cx(z):
@@ -64,6 +67,30 @@ def exact_constant_gpp(nb, nv, nc, npg):
     return out
 
 
+def exact_constant_gpp_real(nb, nv, nc, npg):
+    """Closed form of the real-valued driver's achtemp (every array 0.5,
+    vcoul = 1, wx = {3,4,5}): every term takes the first branch, so
+    achtemp[iw] = nb*ngpown*nc*delw(iw)/16 with delw = 0.5/(wx - 0.5)."""
+    from fractions import Fraction as F
+    ng = nc // npg
+    return [float(F(nb * ng * nc, 16) * F(1, 2) / (wx - F(1, 2))) for wx in (F(3), F(4), F(5))]
+
+
+def real_fixtures(out: dict) -> None:
+    """gppKer_real.cpp: its driver's prints and its own flagOCC_solver on seeded inputs."""
+    out["gppKer_real"] = []
+    for s in REAL_SIZES:
+        r = oracle.run_ref_driver("gppKer_real", s, threads=1)
+        out["gppKer_real"].append({"args": list(s), "achtemp": [r[f"achtemp[{i}]"] for i in range(3)],
+                                   "achtemp_exact": exact_constant_gpp_real(*s)})
+    p = inputs.gpp_real_synthetic(7, 3, 700, 5, seed=11, dist="branch", index="reference", wx="stress")
+    inv, nc = p["inv_igp_index"], p["ncouls"]
+    igp = np.array([nc - 1 if i == nc else p["indinv"][i] for i in inv], np.int32)
+    h = oracle.ref_gpp_real_pairs(p, igp)
+    np.savez_compressed(os.path.join(HERE, "gpp_real_pairs.npz"), sch=h["sch"], ssx=h["ssx"],
+                        **{k: np.asarray(v) for k, v in p.items()})
+
+
 def main(big: bool):
     oracle.build()
     out = {"gppKer_bgw": [], "gppKer_root": [], "gppKer_orig": [], "ffKernel": []}
@@ -82,6 +109,7 @@ def main(big: bool):
     for s in SEQ_SIZES:
         r = oracle.run_ref_driver("gppKer_seq", s, threads=1)
         out["gppKer_seq"].append({"args": list(s), "achtemp": [cx(r[f"achtemp[{i}]"]) for i in range(3)]})
+    real_fixtures(out)
     r = oracle.run_ref_driver("gppKer_orig", (512, 2, 2048, 32))
     out["gppKer_orig"].append({"args": [512, 2, 2048, 32], "achtemp": [cx(r[f"achtemp[{i}]"]) for i in range(3)]})
     for s in FF_SIZES:

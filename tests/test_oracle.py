@@ -170,3 +170,74 @@ def test_gpp_half_sum_oracle_vs_reference_solvers(orc):
     assert rel(o["sch"], z["sch"]) < 1e-13
     assert rel(o["ssx"], z["ssx"]) < 1e-13
     assert np.max(np.abs(z["sch"][p["nvband"]:])) > 0  # the noflag half sum is exercised
+
+
+# ---------------------------------------------------------------- real-valued GPP (gppKer_real.cpp)
+
+@pytest.mark.parametrize("entry", drivers()["gppKer_real"], ids=lambda e: "x".join(map(str, e["args"])))
+def test_gpp_real_oracle_matches_real_driver(fk, orc, entry):
+    p = fk.inputs.gpp_real_reference_init(*entry["args"])
+    o = orc.gpp_real(p)
+    assert rel(o["achtemp"], entry["achtemp_exact"]) < 1e-14
+    # the printed values carry the driver's own summation error (~1e-12)
+    assert rel(o["achtemp"], entry["achtemp"]) < 1e-11
+
+
+def test_gpp_real_oracle_bitexact_vs_reference_flag_solver(orc):
+    """Occupied bands: the reference's own real flagOCC_solver on branch-stress inputs."""
+    z = np.load(os.path.join(GOLD, "gpp_real_pairs.npz"))
+    p = {k: z[k] for k in z.files if k not in ("sch", "ssx")}
+    for k in ("number_bands", "nvband", "ncouls", "ngpown"):
+        p[k] = int(p[k])
+    o = orc.gpp_real(p, per_pair=True)
+    nv = p["nvband"]
+    np.testing.assert_array_equal(o["sch"][:nv], z["sch"])
+    np.testing.assert_array_equal(o["ssx"], z["ssx"])
+    assert np.max(np.abs(z["ssx"])) > 0
+
+
+def carry_noflag(p, n1, my_igp, igp, zero_masked=False):
+    """An independent restatement of gppKer_real.cpp:341-383 for one (n1,
+    my_igp): sch_array[3] before the vcoul weight.  scha[] persists across the
+    blocks and frequencies; a masked term leaves its entry unchanged."""
+    nc = p["ncouls"]
+    wt, eps = p["wtilde_array"][my_igp], p["I_eps_array"][my_igp]
+    an, am = p["aqsntemp"][n1], p["aqsmtemp"][n1][igp]
+    scha = [0.0] * 512
+    sch = [0.0, 0.0, 0.0]
+    for b in range((nc + 511) // 512):
+        igend = min(512, nc - 512 * b)
+        for iw in range(3):
+            wxt = p["wx_array"][iw]
+            for ig in range(igend):
+                g = ig + 512 * b
+                wdiff = wxt - wt[g]
+                rden = 1 / (wdiff * wdiff)
+                delw = wt[g] * wdiff * rden
+                if wdiff * wdiff > 0.25 and delw * delw < 1.0 / (1e-6 * 4.0):
+                    scha[ig] = am * an[g] * delw * eps[g]
+                elif zero_masked:
+                    scha[ig] = 0.0
+            sch[iw] += 0.5 * sum(scha[:igend])
+    return np.array(sch)
+
+
+@pytest.mark.parametrize("zero_masked", [False, True])
+def test_gpp_real_oracle_noflag_carry(fk, orc, zero_masked):
+    p = fk.inputs.gpp_real_synthetic(4, 1, 1100, 3, seed=5, dist="branch", index="reference", wx="stress")
+    o = orc.gpp_real(p, flags=orc.ORC_GPP_REAL_ZERO_MASKED if zero_masked else 0, per_pair=True)
+    inv, nc = p["inv_igp_index"], p["ncouls"]
+    for my_igp in range(3):
+        igp = nc - 1 if inv[my_igp] == nc else int(p["indinv"][inv[my_igp]])
+        for n1 in range(1, 4):
+            want = carry_noflag(p, n1, my_igp, igp, zero_masked)
+            assert rel(o["sch"][n1, my_igp], want) < 1e-13
+
+
+def test_gpp_real_carry_changes_the_result(fk, orc):
+    """On inputs where the noflag mask is often false, keeping the stale value
+    (the reference) and zeroing it give different sums."""
+    p = fk.inputs.gpp_real_synthetic(16, 2, 1500, 6, seed=6, dist="branch", wx="stress")
+    a = orc.gpp_real(p)["achtemp"]
+    b = orc.gpp_real(p, flags=orc.ORC_GPP_REAL_ZERO_MASKED)["achtemp"]
+    assert rel(a, b) > 1e-3
