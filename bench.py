@@ -40,6 +40,9 @@ WORKLOADS = {
     # gppKerSeq.cpp's half sum (gppsum = 1) at the config-1 size; its inverted noflag mask keeps only
     # near-pole terms, which the uniform draw never produces, so wtilde comes from the branch-stress draw
     "gpphalf": dict(kind="gpp", nb=512, nv=2, nc=32768, ng=20, half=True, dist="branch"),
+    # gppKer_real.cpp's real-valued sum at the config-1 size; branch-stress wtilde so that the driver's
+    # carried noflag values (masked terms) occur
+    "gppreal": dict(kind="gpp", nb=512, nv=2, nc=32768, ng=20, real=True, dist="branch"),
     # BASELINE config 2: FF full-frequency contraction
     "ff": dict(kind="ff", nb=512, nv=2, nc=4096, ng=512, nf=15, ne=10),
     # BASELINE config 4: large FF contraction (I_epsR/I_epsA ~17 GB each, drawn on the GPU)
@@ -64,6 +67,10 @@ def terms(w):
 
 def algorithmic(w):
     """(bytes, flops) of the dominant contraction kernel per launch."""
+    if w["kind"] == "gpp" and w.get("real"):
+        # FP64 reals of aqsntemp once, the operand at 4 B per real; a real MAC is 2 flops
+        M, N, K = w["nb"] - w["nv"], 3 * w["ng"], w["nc"]
+        return 8 * M * K + 4 * N * K, 2 * M * N * K
     if w["kind"] == "gpp":
         M, N, K = w["nb"] - w["nv"], 3 * w["ng"], w["nc"]
         return 16 * M * K + 8 * N * K, 8 * M * N * K
@@ -92,6 +99,9 @@ def roofline(w, prec, byts, flops, kms, peaks):
 
 
 def make_inputs(fk, w, seed=2024):
+    if w["kind"] == "gpp" and w.get("real"):
+        return fk.inputs.gpp_real_synthetic(w["nb"], w["nv"], w["nc"], w["ng"], seed=seed, dist=w.get("dist", "uniform"),
+                                            index="baseline", wx="baseline")
     if w["kind"] == "gpp":
         return fk.inputs.gpp_synthetic(w["nb"], w["nv"], w["nc"], w["ng"], seed=seed, dist=w.get("dist", "uniform"),
                                        index="baseline", wx="baseline")
@@ -277,7 +287,8 @@ def run_reference(a, w):
     else:
         p = make_inputs(fk, w)
     gflags = oracle.ORC_GPP_HALF_SUM if w.get("half") else 0
-    call = (lambda: oracle.gpp(p, flags=gflags, nthreads=cores)) if w["kind"] == "gpp" else \
+    call = (lambda: oracle.gpp_real(p, nthreads=cores)) if w.get("real") else \
+        (lambda: oracle.gpp(p, flags=gflags, nthreads=cores)) if w["kind"] == "gpp" else \
         (lambda: oracle.ff(p, flags=oracle.ORC_FF_SCHDT_GEMM, nthreads=cores))
     for _ in range(a.warmup):
         call()
@@ -306,12 +317,13 @@ METRIC = "GPP/FF self-energy terms/s + p99 latency, mixed vs FP64 at <=1e-6 rel 
 
 def workload_config(a, w):
     c = {"workload": ("GPP self-energy %s, number_bands=%d nvband=%d ncouls=%d ngpown=%d" %
-                      ("half sum (gppsum=1)" if w.get("half") else "sum", w["nb"], w["nv"], w["nc"], w["ng"]))
+                      ("half sum (gppsum=1)" if w.get("half") else "real-valued sum (gppKer_real)" if w.get("real")
+                       else "sum", w["nb"], w["nv"], w["nc"], w["ng"]))
          if w["kind"] == "gpp" else
          ("FF full-frequency contraction, number_bands=%d nvband=%d ncouls=%d ngpown=%d nFreq=%d nfreqeval=%d"
           % (w["nb"], w["nv"], w["nc"], w["ng"], w["nf"], w["ne"])),
          "precision": a.precision, "parallelism": f"replicas x{a.gpus}",
-         "l2": "inputs larger than L2 (aqsntemp %.0f MB)" % (16 * w["nb"] * w["nc"] / 1e6)}
+         "l2": "inputs larger than L2 (aqsntemp %.0f MB)" % ((8 if w.get("real") else 16) * w["nb"] * w["nc"] / 1e6)}
     if w.get("dist"):
         c["distribution"] = w["dist"]
     return c
@@ -358,7 +370,13 @@ def run_ours(a, w):
     d = dict(p)
     for k in keys_c:
         d[k] = torch.from_numpy(np.ascontiguousarray(p[k])).to(f"cuda:{local}")
-    if w["kind"] == "gpp":
+    if w["kind"] == "gpp" and w.get("real"):
+        outs = {k: torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}")
+                for k, n in (("achtemp", 3), ("asxtemp", 3), ("acht_n1_loc", w["nb"]))}
+        flags = 0
+        call = lambda prec: ctx.gpp_real(d, prec, flags, out=outs)
+        host_call = lambda prec, hp: ctx.gpp_real(hp, prec, flags)
+    elif w["kind"] == "gpp":
         outs = {k: torch.zeros(n, dtype=torch.complex128, device=f"cuda:{local}")
                 for k, n in (("achtemp", 3), ("asxtemp", 3), ("acht_n1_loc", w["nb"]))}
         outs["achstemp"] = None
@@ -495,7 +513,10 @@ def cpu_baseline(fk, w, p):
     cores = os.cpu_count() or 1
     if w["kind"] == "gpp":
         t0 = time.perf_counter()
-        oracle.gpp(p, flags=oracle.ORC_GPP_HALF_SUM if w.get("half") else 0, nthreads=cores)
+        if w.get("real"):
+            oracle.gpp_real(p, nthreads=cores)
+        else:
+            oracle.gpp(p, flags=oracle.ORC_GPP_HALF_SUM if w.get("half") else 0, nthreads=cores)
         dt = time.perf_counter() - t0
         return {"value": terms(w) / dt, "unit": "terms/s", "cores": cores, "kind": "port",
                 "sample": f"one full call ({terms(w):.3g} terms)"}

@@ -22,10 +22,10 @@ import numpy as np
 
 from . import _native
 from ._native import (FK_FF_PHYSICS, FK_FF_SCHDT_GEMM, FK_FF_SPLIT_ACHD, FK_FP64, FK_GPP_ACHSTEMP,
-                      FK_GPP_HALF_SUM, FK_GPP_ROOT_QUIRKS, FK_MIXED, FKError)
+                      FK_GPP_HALF_SUM, FK_GPP_REAL_ZERO_MASKED, FK_GPP_ROOT_QUIRKS, FK_MIXED, FKError)
 
 __all__ = ["Context", "Server", "gppKer", "ffKernel", "FKError", "FK_FP64", "FK_MIXED", "FK_GPP_ROOT_QUIRKS",
-           "FK_GPP_ACHSTEMP", "FK_GPP_HALF_SUM", "FK_FF_SCHDT_GEMM", "FK_FF_PHYSICS", "FK_FF_SPLIT_ACHD", "precision_code"]
+           "FK_GPP_ACHSTEMP", "FK_GPP_HALF_SUM", "FK_GPP_REAL_ZERO_MASKED", "FK_FF_SCHDT_GEMM", "FK_FF_PHYSICS", "FK_FF_SPLIT_ACHD", "precision_code"]
 
 
 def precision_code(p) -> int:
@@ -124,6 +124,27 @@ class Context:
         optr = [ctypes.c_void_p(_data_ptr(out[k])) if out.get(k) is not None else None
                 for k in ("achtemp", "asxtemp", "acht_n1_loc", "achstemp")]
         st = self.lib.fk_gpp(self.h, nb, nv, nc, ng, *args, precision_code(precision), flags, *optr)
+        self._check(st, self.h)
+        return out
+
+    def gpp_real(self, p: dict, precision="fp64", flags: int = 0, out=None) -> dict:
+        """Real-valued GPP sum (gppKer_real.cpp) on a dict of float64 arrays."""
+        nb, nv, nc, ng = int(p["number_bands"]), int(p["nvband"]), int(p["ncouls"]), int(p["ngpown"])
+        keep = []
+
+        def a(key, kind, n):
+            ptr, k = _arg(p[key], kind, n, key)
+            keep.append(k)
+            return ptr
+
+        args = [a("aqsmtemp", "f64", nb * nc), a("aqsntemp", "f64", nb * nc), a("I_eps_array", "f64", ng * nc),
+                a("wtilde_array", "f64", ng * nc), a("vcoul", "f64", nc), a("inv_igp_index", "i32", ng),
+                a("indinv", "i32", nc), a("wx_array", "f64", 3)]
+        if out is None:
+            out = {"achtemp": np.zeros(3), "asxtemp": np.zeros(3), "acht_n1_loc": np.zeros(nb)}
+        optr = [ctypes.c_void_p(_data_ptr(out[k])) if out.get(k) is not None else None
+                for k in ("achtemp", "asxtemp", "acht_n1_loc")]
+        st = self.lib.fk_gpp_real(self.h, nb, nv, nc, ng, *args, precision_code(precision), flags, *optr)
         self._check(st, self.h)
         return out
 

@@ -16,6 +16,7 @@ FK_FP64, FK_MIXED = 0, 1
 FK_GPP_ROOT_QUIRKS = 0x1
 FK_GPP_ACHSTEMP = 0x2
 FK_GPP_HALF_SUM = 0x4
+FK_GPP_REAL_ZERO_MASKED = 0x10
 FK_FF_SCHDT_GEMM = 0x1
 FK_FF_PHYSICS = 0x2
 FK_FF_SPLIT_ACHD = 0x4
@@ -23,7 +24,7 @@ FK_FF_SPLIT_ACHD = 0x4
 # Every symbol include/fk_abi.h declares.
 SYMBOLS = ("fk_create", "fk_destroy", "fk_set_stream", "fk_synchronize", "fk_reserve", "fk_strerror",
            "fk_last_error", "fk_version", "fk_gpp", "fk_ff", "fk_set_profiling", "fk_last_timings",
-           "fk_last_launches", "fk_gpp_static", "fk_server_create", "fk_server_destroy",
+           "fk_last_launches", "fk_gpp_static", "fk_gpp_real", "fk_server_create", "fk_server_destroy",
            "fk_server_resident_put", "fk_server_resident_evict", "fk_server_submit", "fk_server_wait",
            "fk_server_stats", "fk_server_tune")
 
@@ -86,6 +87,8 @@ def load(path: str = LIB_PATH):
     L.fk_gpp.argtypes = [P, I, I, I, I] + [P] * 8 + [I, U] + [P] * 4
     L.fk_ff.argtypes = [P] + [I] * 6 + [P] * 11 + [D] * 4 + [I, U] + [P] * 6
     L.fk_gpp_static.argtypes = [P, I, I, I, I] + [P] * 8 + [U] + [P] * 4
+    L.fk_gpp_real.restype = I
+    L.fk_gpp_real.argtypes = [P, I, I, I, I] + [P] * 8 + [I, U] + [P] * 3
     UL = ctypes.c_ulonglong
     L.fk_server_create.argtypes = [I, ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]
     L.fk_server_destroy.argtypes = [P]

@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
                   "-I" + os.path.join(ROOT, "include")]
 SOURCES = ["fk_abi.cu", "fk_gpp.cu", "fk_ff.cu", "fk_static.cu", "fk_serve.cu"]
-CLIS = {"gppKer": "cli_gppKer.cpp", "ffKernel": "cli_ffKernel.cpp"}
+CLIS = {"gppKer": "cli_gppKer.cpp", "gppKer_real": "cli_gppKer_real.cpp", "ffKernel": "cli_ffKernel.cpp"}
 
 
 def nvcc() -> str:

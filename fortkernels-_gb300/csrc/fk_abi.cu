@@ -611,6 +611,84 @@ fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsm
     return s;
 }
 
+fk_status fk_gpp_real(fk_ctx_t c, int nb, int nv, int nc, int ng, const double* aqsmtemp, const double* aqsntemp,
+                      const double* I_eps_array, const double* wtilde_array, const double* vcoul,
+                      const int* inv_igp_index, const int* indinv, const double* wx_array, fk_precision precision,
+                      unsigned flags, double* achtemp, double* asxtemp, double* acht_n1_loc) {
+    if (!c) return FK_EINVAL;
+    Ctx& x = *c;
+    if (nb <= 0 || nc <= 0 || ng <= 0 || nv < 0 || nv > nb)
+        return fk::fail(x, FK_EINVAL, "gpp_real: need number_bands, ncouls, ngpown > 0 and 0 <= nvband <= number_bands");
+    if (!aqsmtemp || !aqsntemp || !I_eps_array || !wtilde_array || !vcoul || !inv_igp_index || !indinv ||
+        !wx_array || !achtemp || !asxtemp)
+        return fk::fail(x, FK_EINVAL, "gpp_real: null required pointer");
+    if (precision != FK_FP64 && precision != FK_MIXED) return fk::fail(x, FK_EINVAL, "gpp_real: bad precision");
+    if (flags & ~FK_GPP_REAL_ZERO_MASKED) return fk::fail(x, FK_EINVAL, "gpp_real: unknown flag");
+    if (ng > 65535) return fk::fail(x, FK_ENOTSUP, "gpp_real: ngpown > 65535");
+    fk::DeviceGuard g(x.device);
+    if (!g.ok) return fk::fail(x, FK_ECUDA, "gpp_real: cannot select device");
+
+    const size_t band = (size_t)nb * nc * sizeof(double), col = (size_t)ng * nc * sizeof(double);
+    fk::In aqm{aqsmtemp, band}, eps{I_eps_array, col}, wt{wtilde_array, col}, vc{vcoul, (size_t)nc * sizeof(double)},
+        inv{inv_igp_index, (size_t)ng * sizeof(int)}, ind{indinv, (size_t)nc * sizeof(int)},
+        wx{wx_array, 3 * sizeof(double)};
+    std::vector<fk::In*> ins{&aqm, &eps, &wt, &vc, &inv, &ind, &wx};
+    for (auto* i : ins) i->dev = fk::is_device_ptr(i->user);
+    // aqsntemp is read as rows of complex pairs: in place when its rows have an
+    // even length and start on 16-byte boundaries, else copied with a padded
+    // (even) row stride whose pad column is zero
+    const bool aqn_dev = fk::is_device_ptr(aqsntemp);
+    const bool aqn_in_place = aqn_dev && (nc % 2 == 0) && ((uintptr_t)aqsntemp & 15) == 0;
+    const long lda = nc + (nc & 1);
+    const size_t aqn_bytes = aqn_in_place ? 0 : ((size_t)nb * lda * sizeof(double) + 255) & ~(size_t)255;
+
+    fk::GppRealDev r{};
+    r.nb = nb; r.nv = nv; r.nc = nc; r.ng = ng; r.prec = precision; r.flags = flags;
+    r.lda = aqn_in_place ? nc : lda;
+    const size_t outn = 6 + (size_t)nb;
+    const size_t need = fk::staged_bytes(ins) + aqn_bytes + fk::gpp_real_workspace(x, r) + outn * sizeof(double) + 4096;
+    fk_status s = fk::ensure_workspace(x, need);
+    if (s != FK_OK) return s;
+    x.ws.reset();
+    double* out = (double*)x.ws.take(outn * sizeof(double));
+    fk::phase_mark(x, 0);
+    if ((s = fk::stage(x, ins)) != FK_OK) return s;
+    if (aqn_in_place) {
+        r.aqsn = aqsntemp;
+    } else {
+        double* d = (double*)x.ws.take(aqn_bytes);
+        if (!out || !d) return fk::fail(x, FK_ENOMEM, "workspace: staging");
+        cudaError_t e = cudaMemcpy2DAsync(d, lda * sizeof(double), aqsntemp, nc * sizeof(double), nc * sizeof(double),
+                                          nb, aqn_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, x.stream);
+        if (e == cudaSuccess && (nc & 1))
+            e = cudaMemset2DAsync(d + nc, lda * sizeof(double), 0, sizeof(double), nb, x.stream);
+        if (e != cudaSuccess) return fk::cuda_fail(x, e, "gpp_real: staging aqsntemp");
+        r.aqsn = d;
+    }
+    r.aqsm = (const double*)aqm.d; r.eps = (const double*)eps.d; r.wt = (const double*)wt.d;
+    r.vcoul = (const double*)vc.d; r.inv = (const int*)inv.d; r.indinv = (const int*)ind.d;
+    r.wx = (const double*)wx.d; r.out = out;
+    if ((s = fk::gpp_real_run(x, r)) != FK_OK) return s;
+    bool host_out = false;
+    struct Out {
+        double* dst;
+        size_t off, n;
+    } outs[3] = {{achtemp, 0, 3}, {asxtemp, 3, 3}, {acht_n1_loc, 6, (size_t)nb}};
+    for (const Out& o : outs) {
+        if (!o.dst) continue;
+        host_out = host_out || !fk::is_device_ptr(o.dst);
+        cudaError_t e = cudaMemcpyAsync(o.dst, out + o.off, o.n * sizeof(double), cudaMemcpyDefault, x.stream);
+        if (e != cudaSuccess) return fk::cuda_fail(x, e, "gpp_real: output copy");
+    }
+    if (host_out || x.profiling) {
+        cudaError_t e = cudaStreamSynchronize(x.stream);
+        if (e != cudaSuccess) return fk::cuda_fail(x, e, "gpp_real: synchronize");
+        fk::phase_close(x, 4);
+        if ((s = fk::check_errword(x)) != FK_OK) return s;
+    }
+    return FK_OK;
+}
+
 fk_status fk_ff(fk_ctx_t c, int nb, int nv, int nc, int ng, int nf, int ne, const fk_c128* aqsmtemp,
                 const fk_c128* aqsntemp, const fk_c128* I_epsR_array, const fk_c128* I_epsA_array,
                 const double* vcoul, const int* inv_igp_index, const int* indinv, const double* ekq,

@@ -558,6 +558,7 @@ struct RowsArgs {
     const double2* schd;  // [ng][3]
     const double2* aqsn;  // [nb][nc]
     int nc;
+    bool re_only;         // real-valued sum: the contraction partials carry it in their real parts
 };
 
 FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
@@ -573,6 +574,7 @@ FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
     } else if (n1 >= nv) {
         const long M = nb - nv, m = n1 - nv;
         if (c < 3 && lane < nslots) v = ordered_sum(P + ((long)lane * M + m) * 3 + c, 32 * M * 3, (nslots - lane + 31) / 32);
+        if (ra.re_only) v.y = 0.0;
         if (c < 3 && ra.P2) {
             // half sum: + conj(A = aqsmtemp contraction) + diagonal terms on block edges
             if (lane < nslots)
@@ -743,6 +745,172 @@ Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0, bool pipeline
 template <class K>
 cudaError_t set_smem(K kernel, size_t bytes) {
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+// ----------------------------------------------------- real-valued sum (gppKer_real.cpp)
+// The real driver's noflag blocks (gppKer_real.cpp:341-383) keep one scha[512]
+// per (n1, my_igp) across blocks and frequencies and assign scha[ig] only
+// where the mask holds; every block sum adds all of scha[0 .. igend).  The
+// mask and delw*I_eps depend on (my_igp, iw, ig) alone, so for each block
+// offset j the value in scha[j] at any step comes from a source element
+// (g = 512*b' + j, iw') fixed by the inputs, and
+//   sch_array[iw] = 0.5 * aqsm[n1][igp] * sum_g aqsn[n1][g] * E[my_igp][iw][g]
+// where E[iw][g] adds D(g, iw') once for every block sum of frequency iw that
+// found (g, iw') in scha[j].  The prep evaluates the mask and D; the carry
+// kernel replays the driver's sequence per (my_igp, j) and writes E.
+//
+// A real dot product is the real part of a complex one over half the length:
+// with a[k] = A[2k] + i A[2k+1] (the row of doubles read as complex pairs, in
+// place) and b[k] = E[2k] - i E[2k+1], Re(a[k] b[k]) = A[2k] E[2k] + A[2k+1] E[2k+1].
+// So E is written in that pair form and the complex contraction engines run
+// unchanged over ncouls/2 (rounded up) pairs; the per-band reduction keeps
+// the real part.
+
+struct RealPrepArgs {
+    int nb, nv, nc, ng;
+    const double *aqsn, *eps, *wt, *wx;
+    long lda;          // row stride of aqsn
+    const int* igp;
+    double* Dv;        // [ng][3][nc] delw*I_eps of every element; nullptr = not written by this pass
+    uint8_t* mask;     // [ng][nc] bit iw: the noflag mask of (iw, ig)
+    double2* F;        // [nch][nv][ng][6] flag-band (sch, ssx) sums, as (value, 0)
+    int nch, n1base;
+};
+
+// Per element: the noflag mask and value (gppKer_real.cpp:351-366) and, for
+// the flag bands of this pass, ssxt_scht_solver's sch and ssx (:17-63) times
+// aqsn[n1][ig] (flagOCC_solver :124-153), FP64 round-to-nearest without
+// contraction so that every branch matches the reference's.
+__global__ void __launch_bounds__(PREP_THREADS) real_prep_kernel(RealPrepArgs p) {
+    __shared__ double2 sm[8 * NVC * 6];
+    const int my_igp = blockIdx.y, ch = blockIdx.x, tid = threadIdx.x;
+    const int igp = p.igp[my_igp];
+    const int nflag = igp < 0 ? 0 : min(NVC, p.nv - p.n1base);
+    const double to1 = 1e-6, limitone = 1.0 / (to1 * 4.0), limittwo = 0.25;
+    double2 acc[NVC * 6];
+#pragma unroll
+    for (int i = 0; i < NVC * 6; ++i) acc[i] = make_double2(0.0, 0.0);
+    for (int ig = ch * PREP_TILE + tid; ig < min(p.nc, (ch + 1) * PREP_TILE); ig += PREP_THREADS) {
+        const double w = p.wt[(long)my_igp * p.nc + ig], ep = p.eps[(long)my_igp * p.nc + ig];
+        const double w2 = __dmul_rn(w, w), Om = __dmul_rn(w2, ep);
+        int bits = 0;
+#pragma unroll
+        for (int iw = 0; iw < 3; ++iw) {
+            const double wxt = p.wx[iw];
+            const double wdiff = __dsub_rn(wxt, w);
+            const double rden = __ddiv_rn(1.0, __dmul_rn(wdiff, wdiff));
+            const double delw = __dmul_rn(__dmul_rn(w, wdiff), rden);
+            const double delwr = __dmul_rn(delw, delw), wdiffr = __dmul_rn(wdiff, wdiff);
+            const bool A = wdiffr > limittwo && delwr < limitone;
+            if (p.Dv) {
+                p.Dv[((long)my_igp * 3 + iw) * p.nc + ig] = __dmul_rn(delw, ep);
+                bits |= (int)A << iw;
+            }
+            if (nflag > 0) {
+                double sch = 0.0, ssx = 0.0;
+                if (A) {
+                    sch = __dmul_rn(delw, ep);
+                    const double cden = __dmul_rn(wxt, wxt);
+                    ssx = __dmul_rn(__dmul_rn(Om, cden), __ddiv_rn(1.0, __dmul_rn(cden, cden)));
+                } else if (delwr > to1) {
+                    const double cden = __dmul_rn(__dmul_rn(4.0, w2), __dadd_rn(delw, 0.5));
+                    ssx = __dmul_rn(__dmul_rn(__dmul_rn(0.0 - Om, cden), __ddiv_rn(1.0, __dmul_rn(cden, cden))), delw);
+                }
+#pragma unroll
+                for (int j = 0; j < NVC; ++j)
+                    if (j < nflag) {
+                        const double an = p.aqsn[(long)(p.n1base + j) * p.lda + ig];
+                        acc[(j * 3 + iw) * 2 + 0].x = __dadd_rn(acc[(j * 3 + iw) * 2 + 0].x, __dmul_rn(an, sch));
+                        acc[(j * 3 + iw) * 2 + 1].x = __dadd_rn(acc[(j * 3 + iw) * 2 + 1].x, __dmul_rn(an, ssx));
+                    }
+            }
+        }
+        if (p.Dv) p.mask[(long)my_igp * p.nc + ig] = (uint8_t)bits;
+    }
+    if (p.nv - p.n1base <= 0) return;
+    block_sum<NVC * 6>(acc, sm);
+    const int nf = min(NVC, p.nv - p.n1base);
+    if (tid < nf * 6) {
+        const int j = tid / 6, r = tid % 6;
+        p.F[(((long)ch * p.nv + p.n1base + j) * p.ng + my_igp) * 6 + r] = acc[tid];
+    }
+}
+
+struct RealCarryArgs {
+    int nc, ng;
+    long K2;             // complex pairs per row of the operand
+    const int* igp;
+    const double* Dv;
+    const uint8_t* mask;
+    int carry;           // 1: the driver's stale scha; 0: a masked term contributes 0
+    double* D64;         // FP64 operand rows [3*ng][2*K2] (pair form), or nullptr
+    uint8_t* img;        // mixed: the pre-split B image, or nullptr
+    int kstages;
+};
+
+// One thread per (my_igp, block offset j): the driver's sequence of blocks b
+// and frequencies iw at offset j, with the current source of scha[j] and the
+// sums owed to it; E of every g = 512*b + j is written exactly once.
+template <int IMG>
+__global__ void real_carry_kernel(RealCarryArgs a) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int my_igp = (int)(t >> 9), j = (int)(t & 511);
+    if (my_igp >= a.ng) return;
+    const bool col = a.igp[my_igp] >= 0;
+    auto put = [&](int iw, int g, double v) {
+        const double s = (g & 1) ? 0.0 - v : v;
+        if (IMG) {
+            const int nt = my_igp / GPP_COLS, row = (my_igp % GPP_COLS) * 3 + iw;
+            tcx::bimg_store_part<64>(a.img + (long)nt * a.kstages * tcx::Cfg<64>::B_BYTES, row, g >> 1, g & 1,
+                                     f64_to_f32_bits(s));
+        } else {
+            a.D64[((long)my_igp * 3 + iw) * 2 * a.K2 + g] = s;
+        }
+    };
+    int gs = -1;
+    double val = 0.0, acc[3] = {0.0, 0.0, 0.0};
+    for (int g = j; g < a.nc; g += 512) {
+        const int m = col ? a.mask[(long)my_igp * a.nc + g] : 0;
+        if (!a.carry) {
+#pragma unroll
+            for (int iw = 0; iw < 3; ++iw) put(iw, g, ((m >> iw) & 1) ? a.Dv[((long)my_igp * 3 + iw) * a.nc + g] : 0.0);
+            continue;
+        }
+#pragma unroll
+        for (int iw = 0; iw < 3; ++iw) {
+            if ((m >> iw) & 1) {
+                if (gs != g) {
+                    if (gs >= 0)
+                        for (int k = 0; k < 3; ++k) put(k, gs, acc[k]);
+                    acc[0] = acc[1] = acc[2] = 0.0;
+                    gs = g;
+                }
+                val = a.Dv[((long)my_igp * 3 + iw) * a.nc + g];
+            }
+            if (gs >= 0) acc[iw] = __dadd_rn(acc[iw], val);
+        }
+        if (gs != g)
+            for (int iw = 0; iw < 3; ++iw) put(iw, g, 0.0);
+    }
+    if (gs >= 0)
+        for (int iw = 0; iw < 3; ++iw) put(iw, gs, acc[iw]);
+    // odd ncouls: the imaginary half of the last pair has no element behind it
+    if ((a.nc & 1) && j == (a.nc - 1) % 512)
+        for (int iw = 0; iw < 3; ++iw) put(iw, a.nc, 0.0);
+}
+
+// aqsmtemp's igp columns as complex (value, 0), [nb][ng]: the epilogue weights' source.
+__global__ void real_columns_kernel(int nb, int nc, int ng, const double* aqsm, const int* igp, double2* ac) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long)nb * ng) return;
+    const int n1 = (int)(t / ng), h = (int)(t % ng), g = igp[h];
+    ac[t] = make_double2(g >= 0 ? aqsm[(long)n1 * nc + g] : 0.0, 0.0);
+}
+
+// [achtemp 3 | asxtemp 3 | achstemp | acht_n1_loc nb] complex -> [3 | 3 | nb] real
+__global__ void real_out_kernel(int nb, const double2* outc, double* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 6 + nb; i += gridDim.x * blockDim.x)
+        out[i] = outc[i < 6 ? i : i + 1].x;
 }
 
 }  // namespace
@@ -1364,5 +1532,129 @@ fk_status gpp_time_plan(Ctx& c, GppStep* s, const GppDev& r, int ks, long step_b
 }
 
 int gpp_default_ks(const Ctx& c, const GppDev& r) { return make_plan(c, r).KS; }
+
+
+// ------------------------------------------------------------ real-valued run
+namespace {
+struct RealPlan {
+    Plan c;         // the complex contraction over K2 pairs
+    GppDev cd;      // its shape
+    long K2;
+    int nch;
+    size_t bytesDv, bytesMask, bytesF, bytesAC, bytesOutc, bytesD64;
+};
+
+RealPlan make_real_plan(const Ctx& c, const GppRealDev& r) {
+    RealPlan q{};
+    q.K2 = (r.nc + 1) / 2;
+    q.cd = GppDev{};
+    q.cd.nb = r.nb; q.cd.nv = r.nv; q.cd.nc = (int)q.K2; q.cd.ng = r.ng; q.cd.prec = r.prec; q.cd.flags = 0;
+    q.c = make_plan(c, q.cd);
+    q.nch = ceil_div(r.nc, PREP_TILE);
+    q.bytesDv = (size_t)r.ng * 3 * r.nc * sizeof(double);
+    q.bytesMask = (size_t)r.ng * r.nc;
+    q.bytesF = (size_t)q.nch * std::max(r.nv, 1) * r.ng * 6 * sizeof(double2);
+    q.bytesAC = (size_t)r.nb * r.ng * sizeof(double2);
+    q.bytesOutc = (7 + (size_t)r.nb) * sizeof(double2);
+    return q;
+}
+}  // namespace
+
+size_t gpp_real_workspace(const Ctx& c, const GppRealDev& r) {
+    const RealPlan q = make_real_plan(c, r);
+    return q.c.bytesD + q.c.bytesW + q.c.bytesP + q.c.bytesRows + q.c.bytesIgp + q.bytesDv + q.bytesMask + q.bytesF +
+           q.bytesAC + q.bytesOutc + 12 * 256;
+}
+
+fk_status gpp_real_run(Ctx& c, const GppRealDev& r) {
+    const RealPlan q = make_real_plan(c, r);
+    const Plan& p = q.c;
+    cudaStream_t st = c.stream;
+    const int M = r.nb - r.nv;
+    if (r.lda < 2 * q.K2 || (r.lda & 1)) return fail(c, FK_EINVAL, "gpp_real: aqsntemp rows must have an even stride");
+    int* igp = (int*)c.ws.take(p.bytesIgp);
+    int* acol = igp ? igp + r.ng : nullptr;
+    void* D = p.bytesD ? c.ws.take(p.bytesD) : nullptr;
+    double2* P = p.bytesP ? (double2*)c.ws.take(p.bytesP) : nullptr;
+    double2* rows = (double2*)c.ws.take(p.bytesRows);
+    float2* W = p.bytesW ? (float2*)c.ws.take(p.bytesW) : nullptr;
+    double* Dv = (double*)c.ws.take(q.bytesDv);
+    uint8_t* mask = (uint8_t*)c.ws.take(q.bytesMask);
+    double2* F = (double2*)c.ws.take(q.bytesF);
+    double2* AC = (double2*)c.ws.take(q.bytesAC);
+    double2* outc = (double2*)c.ws.take(q.bytesOutc);
+    if (!igp || !rows || !Dv || !mask || !F || !AC || !outc || (p.bytesD && !D) || (p.bytesP && !P) ||
+        (p.bytesW && !W))
+        return fail(c, FK_ENOMEM, "workspace too small for the real-valued GPP request");
+    c.launches = 0;
+    if (p.mixed && D) {
+        if (tcx::img_needs_pad(64, r.ng, GPP_COLS, (int)q.K2))
+            tcx::img_pad_kernel<64><<<dim3(p.kstages, p.NT, 1), 256, 0, st>>>((uint8_t*)D, p.NT, p.kstages, r.ng,
+                                                                            GPP_COLS, (int)q.K2);
+        if (cudaMemsetAsync(c.errword, 0, sizeof(int), st) != cudaSuccess)
+            return cuda_fail(c, cudaGetLastError(), "gpp_real: error word");
+    }
+    phase_mark(c, 1);
+    igp_map_kernel<<<ceil_div(r.ng, 128), 128, 0, st>>>(r.ng, r.nc, r.inv, r.indinv, 1, igp, acol);
+    real_columns_kernel<<<ceil_div(r.nb * r.ng, 256), 256, 0, st>>>(r.nb, r.nc, r.ng, r.aqsm, igp, AC);
+    c.launches += 2;
+    if (p.mixed && M > 0) {
+        tcx::weight_table_kernel<<<dim3(ceil_div(M, 128), r.ng), 128, 0, st>>>(M, r.nv, r.ng, AC, r.ng, r.vcoul, igp,
+                                                                            acol, 0.5, W, nullptr, nullptr);
+        ++c.launches;
+    }
+    const int passes = std::max(1, ceil_div(r.nv, NVC));
+    for (int pass = 0; pass < passes; ++pass) {
+        RealPrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, r.lda, igp,
+                       (pass == 0 && M > 0) ? Dv : nullptr, mask, F, q.nch, pass * NVC};
+        real_prep_kernel<<<dim3(q.nch, r.ng), PREP_THREADS, 0, st>>>(a);
+        ++c.launches;
+    }
+    if (M > 0) {
+        RealCarryArgs ca{r.nc, r.ng, q.K2, igp, Dv, mask, (r.flags & FK_GPP_REAL_ZERO_MASKED) ? 0 : 1,
+                         p.mixed ? nullptr : (double*)D, p.mixed ? (uint8_t*)D : nullptr, p.kstages};
+        const int blocks = ceil_div(r.ng * 512, 256);
+        if (p.mixed) real_carry_kernel<1><<<blocks, 256, 0, st>>>(ca);
+        else real_carry_kernel<0><<<blocks, 256, 0, st>>>(ca);
+        ++c.launches;
+    }
+    phase_mark(c, 2);
+    if (M > 0) {
+        ContractArgs a{};
+        a.A = (const double2*)r.aqsn; a.lda = r.lda / 2; a.m0 = r.nv; a.M = M;
+        a.B = D; a.ldb = q.K2; a.bstride = 0; a.N = 3 * r.ng; a.K = (int)q.K2;
+        a.KS = p.KS; a.kchunk = p.kchunk; a.batches = 1; a.batch_plane = nullptr;
+        a.aqsm = AC; a.ldm = r.ng; a.vcoul = r.vcoul; a.igp = igp; a.acol = acol; a.wscale = 0.5; a.G = 3; a.P = P;
+        if (p.mixed) {
+            tcx::TcArgs t{};
+            t.c = a;
+            t.Bimg = (const uint8_t*)D;
+            t.W1 = W; t.W2 = nullptr; t.ldw = M; t.gpp_cols = GPP_COLS; t.Aimg = nullptr; t.vcol = nullptr;
+            t.kstages_total = p.kstages;
+            t.MT = p.MT; t.NT = p.NT; t.units = p.units;
+            t.err = c.errword;
+            if (tcx::encode_rows_map(&t.amap, a.A, a.lda, a.K, r.nb) != cudaSuccess)
+                return fail(c, FK_ECUDA, "gpp_real: cannot describe aqsntemp as a tensor map");
+            auto k = tcx::tc_contract_kernel<EPI_GPP, 64, false>;
+            set_smem(k, tcx::Cfg<64>::SMEM);
+            k<<<std::min(p.units, c.sms), tcx::THREADS, tcx::Cfg<64>::SMEM, st>>>(t);
+        } else {
+            auto k = d64::contract_kernel<EPI_GPP>;
+            set_smem(k, d64::SMEM);
+            k<<<dim3(p.MT, p.NT * p.KS), d64::THREADS, d64::SMEM, st>>>(a);
+        }
+        ++c.launches;
+    }
+    phase_mark(c, 3);
+    RowsArgs ra{r.nb, r.nv, r.ng, P ? p.KS * p.NT : 0, P, 0, nullptr, q.nch, F, r.ng, AC, r.vcoul, igp, acol, rows};
+    ra.re_only = true;
+    rows_kernel<<<ceil_div(r.nb * 7, 8), 256, 0, st>>>(ra);
+    totals_kernel<<<1, 256, 0, st>>>(r.nb, rows, outc);
+    real_out_kernel<<<std::max(1, std::min(ceil_div(6 + r.nb, 256), 64)), 256, 0, st>>>(r.nb, outc, r.out);
+    c.launches += 3;
+    phase_mark(c, 4);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FK_OK : cuda_fail(c, e, "gpp_real kernels");
+}
 
 }  // namespace fk

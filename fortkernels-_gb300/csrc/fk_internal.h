@@ -90,6 +90,21 @@ fk_status gpp_pipe_begin(Ctx& c);
 fk_status gpp_pipe_copy(Ctx& c, const GppDev& r, const GppPipe* pipe, int q0, int q1);
 fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe = nullptr);
 
+// The real-valued GPP sum (gppKer_real.cpp) on device arrays.
+struct GppRealDev {
+    int nb, nv, nc, ng;
+    const double *aqsm, *aqsn, *eps, *wt;  // [nb][nc] (aqsn: row stride lda), [ng][nc]
+    long lda;          // row stride of aqsn in doubles: even, >= nc; the pad column (if any) is 0
+    const double* vcoul;
+    const int *inv, *indinv;
+    const double* wx;  // device [3]
+    fk_precision prec;
+    unsigned flags;
+    double* out;       // device [3 achtemp | 3 asxtemp | nb acht_n1_loc]
+};
+size_t gpp_real_workspace(const Ctx& c, const GppRealDev& r);
+fk_status gpp_real_run(Ctx& c, const GppRealDev& r);
+
 // Served GPP requests (mixed precision): a request's plan, workspace and
 // descriptors, and the captured step that runs several of them at once.
 struct GppJob;

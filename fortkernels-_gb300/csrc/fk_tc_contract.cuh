@@ -120,6 +120,20 @@ __device__ __forceinline__ void bimg_store(uint8_t* img_nt, int kstage_total_unu
     img_store<BN, true>(img_nt, n_in_tile, k, re, im);
 }
 
+// One half of a paired B element: the three pieces of its real (part 0) or
+// imaginary (part 1) component, for writers that produce the two halves
+// separately.
+template <int BN>
+__device__ __forceinline__ void bimg_store_part(uint8_t* img_nt, int n_in_tile, int k, int part, float v) {
+    uint8_t* st = img_nt + (long)(k / BK) * (BN * NSUB * 64);
+    const uint32_t off = tc::sw64_offset(n_in_tile, k % BK);
+    uint16_t h, m, l;
+    split3(v, h, m, l);
+    *(uint16_t*)(st + (part + 0) * BN * 64 + off) = h;
+    *(uint16_t*)(st + (part + 2) * BN * 64 + off) = m;
+    *(uint16_t*)(st + (part + 4) * BN * 64 + off) = l;
+}
+
 // Where a kernel's units come from.  OneReq: every unit belongs to the one
 // request in the launch parameters.  TableReqs: units of several requests,
 // laid end to end; request r owns global units [ustart[r], ustart[r+1]) and

@@ -98,6 +98,10 @@ const char* fk_version(void);
                                    conjugate pair (noflagOCC_solver :206-242 with the
                                    driver's 512-wide blocks :430-447, flagOCC_solver
                                    :90-139); not with FK_GPP_ROOT_QUIRKS or FK_GPP_ACHSTEMP */
+#define FK_GPP_REAL_ZERO_MASKED 0x10u /* fk_gpp_real only: a masked noflag term
+                                   contributes 0 (the else left commented out at
+                                   gppKer_real.cpp:371-372) instead of the value the
+                                   driver's scha[ig] still holds */
 
 /*
  * GPP self-energy sum (BGW-Kernels/gppKer.cpp:303-439).
@@ -117,6 +121,24 @@ fk_status fk_gpp(fk_ctx_t ctx, int number_bands, int nvband, int ncouls, int ngp
                  const double* vcoul, const int* inv_igp_index, const int* indinv,
                  const double* wx_array, fk_precision precision, unsigned flags,
                  fk_c128* achtemp, fk_c128* asxtemp, fk_c128* acht_n1_loc, fk_c128* achstemp);
+
+/*
+ * Real-valued GPP sum (gppKer_real.cpp:297-412): the same loop nest on double
+ * arrays, aqsmtemp/aqsntemp [number_bands][ncouls], I_eps_array/wtilde_array
+ * [ngpown][ncouls], with the index map and frequencies of fk_gpp.  As in the
+ * reference, a masked noflag term leaves the value of the last unmasked term
+ * at its offset in the 512-wide block (gppKer_real.cpp:341-383) in the block
+ * sums; FK_GPP_REAL_ZERO_MASKED counts it as 0 instead.  Outputs: achtemp[3],
+ * asxtemp[3], acht_n1_loc[number_bands] (may be NULL).  aqsntemp is read in
+ * place when it is device memory on a 16-byte boundary with an even ncouls;
+ * otherwise it is staged.  Flags: 0 or FK_GPP_REAL_ZERO_MASKED.
+ */
+fk_status fk_gpp_real(fk_ctx_t ctx, int number_bands, int nvband, int ncouls, int ngpown,
+                      const double* aqsmtemp, const double* aqsntemp,
+                      const double* I_eps_array, const double* wtilde_array,
+                      const double* vcoul, const int* inv_igp_index, const int* indinv,
+                      const double* wx_array, fk_precision precision, unsigned flags,
+                      double* achtemp, double* asxtemp, double* acht_n1_loc);
 
 /* Device scratch compiled into the library for fk_gpp_static, per GPU. */
 #define FK_GPP_STATIC_SCRATCH_BYTES (64u << 20)

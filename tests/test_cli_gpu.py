@@ -52,6 +52,18 @@ def test_gppKer_cli_half_sum_prints_seq_driver_values():
     assert r.returncode == 1 and "gppsum = 0" in r.stderr
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_gppKer_real_cli_prints_reference_values(prec):
+    with open(GOLD) as f:
+        e = json.load(f)["gppKer_real"][1]
+    out = subprocess.run([os.path.join(BIN, "gppKer_real")] + [str(a) for a in e["args"]] + [f"--precision={prec}"],
+                         capture_output=True, text=True, check=True, timeout=300).stdout
+    assert "Chrono Time Taken" in out
+    got = np.array([float(re.search(rf"achtemp\[{i}\] = (\S+)", out).group(1)) for i in range(3)])
+    want = np.array(e["achtemp_exact"])
+    assert np.max(np.abs(got - want)) / np.max(np.abs(want)) <= (1e-13 if prec == "fp64" else 1e-6)
+
+
 def test_gppKer_cli_usage_line():
     out = subprocess.run([os.path.join(BIN, "gppKer")], capture_output=True, text=True).stdout
     assert "The correct form of input is" in out
