@@ -103,6 +103,12 @@ class Context:
     def last_launches(self) -> int:
         return int(self.lib.fk_last_launches(self.h))
 
+    def last_kernel_time(self):
+        """(milliseconds, launches) of the dominant kernel in the last profiled call."""
+        ms, n = ctypes.c_float(), ctypes.c_int()
+        self._check(self.lib.fk_last_kernel_time(self.h, ctypes.byref(ms), ctypes.byref(n)), self.h)
+        return float(ms.value), int(n.value)
+
     # ------------------------------------------------------------------ GPP
     def gpp(self, p: dict, precision="fp64", flags: int = 0, out=None) -> dict:
         """GPP sum on the input dict (keys as in fortkernels_gb300.inputs)."""

@@ -27,7 +27,17 @@ fk_status cuda_fail(Ctx& c, cudaError_t e, const char* where) {
 }
 
 void phase_mark(Ctx& c, int i) {
+    if (i == 0) c.nk = 0;
     if (c.profiling && i >= 0 && i < 5) cudaEventRecord(c.ev[i], c.stream);
+}
+
+void kernel_begin(Ctx& c) {
+    if (c.profiling && c.nk < Ctx::KEV && c.kev[2 * c.nk]) cudaEventRecord(c.kev[2 * c.nk], c.stream);
+}
+
+void kernel_end(Ctx& c) {
+    if (c.profiling && c.nk < Ctx::KEV && c.kev[2 * c.nk + 1]) cudaEventRecord(c.kev[2 * c.nk + 1], c.stream);
+    ++c.nk;
 }
 
 void phase_close(Ctx& c, int nphases) {
@@ -36,6 +46,15 @@ void phase_close(Ctx& c, int nphases) {
     for (int i = 0; i < nphases && i < 4; ++i) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, c.ev[i], c.ev[i + 1]) == cudaSuccess) c.timings[i] = ms;
+    }
+    c.kernel_ms = 0.f;
+    c.kernel_launches = 0;
+    for (int k = 0; k < c.nk && k < Ctx::KEV; ++k) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, c.kev[2 * k], c.kev[2 * k + 1]) == cudaSuccess) {
+            c.kernel_ms += ms;
+            ++c.kernel_launches;
+        }
     }
 }
 
@@ -244,6 +263,12 @@ fk_status fk_create(int device, fk_ctx_t* out) {
             delete c;
             return FK_ECUDA;
         }
+    for (auto& e : c->kev)
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            cudaGetLastError();
+            delete c;
+            return FK_ECUDA;
+        }
     *out = c;
     return FK_OK;
 }
@@ -259,6 +284,8 @@ fk_status fk_destroy(fk_ctx_t c) {
         if (c->pinned) cudaFreeHost(c->pinned);
         if (c->pinned_ev) cudaEventDestroy(c->pinned_ev);
         for (auto& e : c->ev)
+            if (e) cudaEventDestroy(e);
+        for (auto& e : c->kev)
             if (e) cudaEventDestroy(e);
         if (c->own_stream) cudaStreamDestroy(c->own_stream);
         if (c->copy_stream) {
@@ -305,6 +332,13 @@ fk_status fk_last_timings(fk_ctx_t c, float ms[4]) {
 }
 
 int fk_last_launches(fk_ctx_t c) { return c ? c->launches : -1; }
+
+fk_status fk_last_kernel_time(fk_ctx_t c, float* ms, int* launches) {
+    if (!c || !ms || !launches) return FK_EINVAL;
+    *ms = c->kernel_ms;
+    *launches = c->kernel_launches;
+    return FK_OK;
+}
 
 namespace fk {
 namespace {

@@ -440,13 +440,17 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
             auto k = tcx::tc_contract_kernel<EPI_FF, 64, true>;
             constexpr size_t smem = tcx::Cfg<64, true>::SMEM;
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            kernel_begin(c);
             k<<<grid1, tcx::THREADS, smem, st>>>(t);
+            kernel_end(c);
             c.launches += 2;
         } else {
             dim3 grid(p.MT, p.NT * p.KS * nb_);
             auto k = d64::contract_kernel<EPI_FF>;
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d64::SMEM);
+            kernel_begin(c);
             k<<<grid, d64::THREADS, d64::SMEM, st>>>(a);
+            kernel_end(c);
             ++c.launches;
         }
     };

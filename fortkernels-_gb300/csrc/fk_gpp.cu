@@ -1016,11 +1016,15 @@ fk_status gpp_run_half(Ctx& c, const GppDev& r) {
                 return fail(c, FK_ECUDA, "gpp: cannot describe an input as a tensor map (needs a 16-byte aligned array)");
             auto k = tcx::tc_contract_kernel<EPI_GPP, 64, false>;
             set_smem(k, tcx::Cfg<64>::SMEM);
+            kernel_begin(c);
             k<<<std::min(p.units, c.sms), tcx::THREADS, tcx::Cfg<64>::SMEM, st>>>(t);
+            kernel_end(c);
         } else {
             auto k = d64::contract_kernel<EPI_GPP>;
             set_smem(k, d64::SMEM);
+            kernel_begin(c);
             k<<<dim3(p.MT, p.NT * p.KS), d64::THREADS, d64::SMEM, st>>>(a);
+            kernel_end(c);
         }
         ++c.launches;
     }
@@ -1111,8 +1115,10 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
                 t.mt0 = q * p.pipe_sub;
                 t.MT = std::min(p.MT, t.mt0 + p.pipe_sub) - t.mt0;
                 t.units = t.MT * p.NT * p.KS;
+                kernel_begin(c);
                 tcx::tc_contract_kernel<EPI_GPP, 64, false>
                     <<<std::min(t.units, c.sms), tcx::THREADS, tcx::Cfg<64>::SMEM, st>>>(t);
+                kernel_end(c);
                 ++c.launches;
             }
         }
@@ -1151,11 +1157,15 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
             const int grid1 = std::min(p.units, c.sms);
             auto k = tcx::tc_contract_kernel<EPI_GPP, 64, false>;
             set_smem(k, tcx::Cfg<64>::SMEM);
+            kernel_begin(c);
             k<<<grid1, tcx::THREADS, tcx::Cfg<64>::SMEM, st>>>(t);
+            kernel_end(c);
         } else {
             auto k = d64::contract_kernel<EPI_GPP>;
             set_smem(k, d64::SMEM);
+            kernel_begin(c);
             k<<<grid, d64::THREADS, d64::SMEM, st>>>(a);
+            kernel_end(c);
         }
         ++c.launches;
     }
@@ -1637,11 +1647,15 @@ fk_status gpp_real_run(Ctx& c, const GppRealDev& r) {
                 return fail(c, FK_ECUDA, "gpp_real: cannot describe aqsntemp as a tensor map");
             auto k = tcx::tc_contract_kernel<EPI_GPP, 64, false>;
             set_smem(k, tcx::Cfg<64>::SMEM);
+            kernel_begin(c);
             k<<<std::min(p.units, c.sms), tcx::THREADS, tcx::Cfg<64>::SMEM, st>>>(t);
+            kernel_end(c);
         } else {
             auto k = d64::contract_kernel<EPI_GPP>;
             set_smem(k, d64::SMEM);
+            kernel_begin(c);
             k<<<dim3(p.MT, p.NT * p.KS), d64::THREADS, d64::SMEM, st>>>(a);
+            kernel_end(c);
         }
         ++c.launches;
     }

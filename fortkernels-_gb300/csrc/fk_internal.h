@@ -38,6 +38,12 @@ struct Ctx {
     cudaEvent_t ev[5] = {};
     float timings[4] = {0, 0, 0, 0};
     int launches = 0;
+    // profiling: events around each launch of the dominant (contraction) kernel
+    static constexpr int KEV = 8;
+    cudaEvent_t kev[2 * KEV] = {};
+    int nk = 0;                 // launches bracketed in the current call
+    float kernel_ms = 0.f;      // their summed device time in the last profiled call
+    int kernel_launches = 0;
     int* errword = nullptr;      // device error word of the tensor-core kernels (bounded waits)
     // Graphs of repeated fully device-resident calls: key -> (times seen, executable graph).
     struct GraphEntry {
@@ -154,6 +160,9 @@ fk_status ff_run(Ctx& c, const FfDev& r);
 // Phase timing helpers (no-ops unless profiling is on).
 void phase_mark(Ctx& c, int i);
 void phase_close(Ctx& c, int nphases);
+// Bracket one launch of the dominant kernel (profiling only).
+void kernel_begin(Ctx& c);
+void kernel_end(Ctx& c);
 
 }  // namespace fk
 

@@ -302,6 +302,10 @@ fk_status fk_set_profiling(fk_ctx_t ctx, int enable);
 fk_status fk_last_timings(fk_ctx_t ctx, float ms[4]);
 /* Number of kernels the most recent call launched. */
 int fk_last_launches(fk_ctx_t ctx);
+/* Device time of the dominant kernel alone in the most recent profiled call:
+ * the milliseconds summed over its launches (CUDA events recorded on the
+ * launch stream right before and after each launch) and their count. */
+fk_status fk_last_kernel_time(fk_ctx_t ctx, float* ms, int* launches);
 
 #ifdef __cplusplus
 }

@@ -240,3 +240,20 @@ def test_gpp_graph_replay_tracks_new_data(ctx, fk, prec):
     ctx.gpp(d, prec, out=out)
     ctx.synchronize()
     np.testing.assert_array_equal(out["achtemp"].cpu().numpy(), 2.0 * res[0])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_profiling_times_the_contraction_kernel(ctx, fk, prec):
+    """With profiling on, the library brackets each launch of the dominant
+    kernel with events: one launch for the plain sum, two for the half sum."""
+    p = fk.inputs.gpp_synthetic(96, 2, 2000, 10, seed=15)
+    ctx.set_profiling(True)
+    try:
+        ctx.gpp(p, prec)
+        ms, n = ctx.last_kernel_time()
+        assert n == 1 and 0 < ms < sum(ctx.last_timings())
+        ctx.gpp(p, prec, fk.FK_GPP_HALF_SUM)
+        ms2, n2 = ctx.last_kernel_time()
+        assert n2 == 2 and ms2 > 0
+    finally:
+        ctx.set_profiling(False)
