@@ -50,7 +50,10 @@ struct Cfg {
     static_assert(BN == 64, "four accumulators x two buffers fill the 512 TMEM columns at BN = 64");
     // Two operand stages.  WSMEM (FF): the per-unit weight tile conj(aqsm)[BN][BM]
     // lives in shared memory.  Otherwise (GPP) a 64 KB staging buffer receives
-    // the next stage's FP64 A rows by bulk copy while the current one converts.
+    // FP64 A rows by TMA in two halves of BK/2 k-values, so that one half is in
+    // flight while the converters read the other.  (Two full stagings do not fit
+    // beside two operand stages; one operand stage with two stagings measured
+    // slower: the converters then wait for each stage's MMAs.)
     static constexpr int STAGES = 2;
     static constexpr int CHUNK_STAGES = 1;  // k-values per TMEM accumulation = 32
     static constexpr uint32_t A_BYTES = NSUB * BM * 64;
@@ -64,7 +67,7 @@ struct Cfg {
 };
 
 struct TcArgs {
-    CUtensorMap amap;     // GPP: A (FP64 complex rows) as a 2-D FP64 tensor, box 64 x BM, zero fill
+    CUtensorMap amap;     // GPP: A (FP64 complex rows) as a 2-D FP64 tensor, box 32 x BM (half a stage), zero fill
     ContractArgs c;       // shapes, partial buffer (same meaning as fk_gemm.cuh)
     const uint8_t* Bimg;  // pre-split B tiles: [plane][nt][kstage][NSUB][BN rows][64 B]
     const uint8_t* Aimg;  // pre-split A tiles [mt][kstage][NSUB][BM rows][64 B] (AIMG kernels only)
@@ -184,9 +187,9 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
     uint64_t* accFull = bars + 3 * C::STAGES;
     uint64_t* accEmpty = accFull + 2;
     uint64_t* done = accEmpty + 2;
-    uint64_t* fFull = done + 1;    // GPP: FP64 staging filled (tx bytes)
-    uint64_t* fEmpty = done + 2;   // GPP: FP64 staging read by all converter warps
-    uint32_t* tslot = (uint32_t*)(done + 3);
+    uint64_t* fFull = done + 1;    // [2] GPP: FP64 staging half filled (tx bytes)
+    uint64_t* fEmpty = done + 3;   // [2] GPP: FP64 staging half read by all converter warps
+    uint32_t* tslot = (uint32_t*)(done + 5);
     __shared__ int s_abort_flag;
     volatile int& s_abort = s_abort_flag;
 
@@ -203,8 +206,10 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
             tc::mbar_init(&accEmpty[b], AIMG ? 4 * FF_EPI_WARPS : 4);
         }
         tc::mbar_init(done, 1);
-        tc::mbar_init(fFull, 1);
-        tc::mbar_init(fEmpty, NCONV);
+        for (int h = 0; h < 2; ++h) {
+            tc::mbar_init(&fFull[h], 1);
+            tc::mbar_init(&fEmpty[h], NCONV);
+        }
         tc::fence_barrier_init();
         s_abort = 0;
     }
@@ -317,18 +322,21 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                 const int s = g % C::STAGES;
                 const long kst = (long)(k0 / BK) + st;
                 if (!AIMG) {
-                    // FP64 rows: staging buffer free once every converter warp has read it
-                    if (!tc::mbar_wait(fEmpty, (g & 1) ^ 1, WAIT_LIMIT) || s_abort) {
-                        fail(64);
-                        ok = false;
-                        break;
+                    // FP64 rows in two halves of BK/2 k-values, each into its own half of the
+                    // staging buffer as soon as the converters have read that half of the last stage
+                    for (int h = 0; h < 2 && ok; ++h) {
+                        if (!tc::mbar_wait(&fEmpty[h], (g & 1) ^ 1, WAIT_LIMIT) || s_abort) {
+                            fail(64);
+                            ok = false;
+                            break;
+                        }
+                        if (lane == 0) {
+                            tc::mbar_arrive_expect_tx(&fFull[h], C::F64_BYTES / 2);
+                            tc::tma_load_2d(sF + h * (BM * BK / 2), &t.amap, 2 * (k0 + st * BK + h * (BK / 2)),
+                                            a.m0 + mt * BM, &fFull[h]);
+                        }
                     }
-                    // one box: rows m0 + mt*BM .. +BM, k = kb .. kb+BK (as 2*BK doubles);
-                    // rows and columns past the array arrive as zeros and still count
-                    if (lane == 0) {
-                        tc::mbar_arrive_expect_tx(fFull, C::F64_BYTES);
-                        tc::tma_load_2d(sF, &t.amap, 2 * (k0 + st * BK), a.m0 + mt * BM, fFull);
-                    }
+                    if (!ok) break;
                 }
                 if (lane == 0) {
                     if (!tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, WAIT_LIMIT) || s_abort) {
@@ -469,10 +477,12 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
         }
     } else {
         // ----------------------------------------------------- converters
-        // warp cw converts rows cw*16 .. cw*16+15 of each stage, lane = k:
-        // read the FP64 rows from the staging buffer (one conflict-free 512-byte
-        // row per instruction), release the buffer for the next stage's bulk
-        // copies, then split into BF16 pieces and store into the operand stage.
+        // warp cw converts rows cw*16 .. cw*16+15 of each stage.  The staging
+        // buffer holds the stage in two halves of BK/2 k-values, each filled by
+        // its own TMA box: read a half (lane = (row pair, k), one conflict-free
+        // 512-byte read per instruction), release it so that the next stage's
+        // half is copied while the other half is read, then split everything
+        // into BF16 pieces and store it into the operand stage.
         if (!AIMG) {
             const int cw = warp < 4 ? warp - 2 : warp - 6;  // 0..7
             constexpr int RPW = BM / NCONV;                  // rows per converter warp
@@ -488,20 +498,32 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                 const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
                 for (int st = 0; st < nst; ++st, ++g) {
                     const int s = g % C::STAGES;
-                    const int k = k0 + st * BK + lane;
-                    if (!tc::mbar_wait(fFull, g & 1, WAIT_LIMIT) || s_abort) {
+                    if (!tc::mbar_wait(&fFull[0], g & 1, WAIT_LIMIT) || s_abort) {
                         fail(32);
                         ok = false;
                         break;
                     }
+                    // lane -> (row pair offset lane>>4, k within the half lane&15)
                     double2 v[RPW];
+                    const int kk = lane & 15, rr = lane >> 4;
 #pragma unroll
-                    for (int i = 0; i < RPW; ++i) {
-                        const int r = cw * RPW + i;
-                        v[i] = (mt * BM + r < a.M && k < k1) ? sF[r * BK + lane] : make_double2(0.0, 0.0);
+                    for (int h = 0; h < 2; ++h) {
+                        if (h == 1 && (!tc::mbar_wait(&fFull[1], g & 1, WAIT_LIMIT) || s_abort)) {
+                            fail(32);
+                            ok = false;
+                            break;
+                        }
+                        const double2* sh = sF + h * (BM * BK / 2);
+                        const int kh = k0 + st * BK + h * (BK / 2) + kk;
+#pragma unroll
+                        for (int i = 0; i < RPW / 2; ++i) {
+                            const int r = cw * RPW + 2 * i + rr;
+                            v[h * (RPW / 2) + i] = (mt * BM + r < a.M && kh < k1) ? sh[r * (BK / 2) + kk] : make_double2(0.0, 0.0);
+                        }
+                        __syncwarp();
+                        if (lane == 0) tc::mbar_arrive(&fEmpty[h]);
                     }
-                    __syncwarp();
-                    if (lane == 0) tc::mbar_arrive(fEmpty);
+                    if (!ok) break;
                     if (!tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, WAIT_LIMIT) || s_abort) {
                         fail(32);
                         ok = false;
@@ -510,7 +532,9 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                     uint8_t* sa = base + s * C::STAGE_BYTES;
 #pragma unroll
                     for (int i = 0; i < RPW; ++i) {
-                        const uint32_t off = tc::sw64_offset(cw * RPW + i, lane);
+                        // v[i]: half i / (RPW/2), row pair i % (RPW/2)
+                        const uint32_t off =
+                            tc::sw64_offset(cw * RPW + 2 * (i % (RPW / 2)) + rr, (i / (RPW / 2)) * (BK / 2) + kk);
                         uint16_t hh, mm, ll;
                         split3(f64_to_f32_bits(v[i].x), hh, mm, ll);
                         *(uint16_t*)(sa + 0 * BM * 64 + off) = hh;
@@ -620,7 +644,7 @@ static __global__ void aimg_convert_kernel(const double2* src, int rows, int K, 
 
 // Host: A (rows of complex FP64, row stride lda complex elements) as a 2-D FP64
 // tensor map for tma_load_2d: inner extent 2*K doubles, `rows` rows, box
-// 2*BK doubles x BM rows, elements outside the extents read as zero.  The
+// BK doubles (half a stage) x BM rows, elements outside the extents read as zero.  The
 // encoder comes from the driver through the runtime, so the library links
 // only the CUDA runtime.
 inline cudaError_t encode_rows_map(CUtensorMap* map, const double2* A, long lda, int K, int rows) {
@@ -639,7 +663,7 @@ inline cudaError_t encode_rows_map(CUtensorMap* map, const double2* A, long lda,
     if (!fn) return cudaErrorNotSupported;
     const cuuint64_t dims[2] = {(cuuint64_t)2 * K, (cuuint64_t)rows};
     const cuuint64_t strides[1] = {(cuuint64_t)lda * sizeof(double2)};
-    const cuuint32_t box[2] = {2 * BK, BM};
+    const cuuint32_t box[2] = {BK, BM};  // half a stage: BK/2 complex values of BM rows
     const cuuint32_t estr[2] = {1, 1};
     const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, (void*)A, dims, strides, box, estr,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
