@@ -63,9 +63,44 @@ struct PrepArgs {
     int n1base;  // first flag band handled by this pass
     int ch0;     // first chunk of this launch (blockIdx.x counts from it)
     // half-sum mode (FK_GPP_HALF_SUM)
-    const double2* aqsm;  // full [nb][nc]
+    const double2* aqsm;  // full [nb][nc] (half sum); the weights' source (set-up, below)
     const int* brk;       // [ng]: first ig whose |Omega2| < 1e-6 (the flag bands stop there)
+    // Set-up folded into the first pass (setup != 0): the column map is computed
+    // from inv/indinv rather than read from igp, and the first chunk of each
+    // column writes igp/acol, the epilogue weights W (mixed) and, in the last
+    // column of a tensor-core tile, the image's padding rows; block (0, 0)
+    // clears the reduction's completion counter.
+    int setup;
+    const int *inv, *indinv;
+    int* igp_out;
+    int* acol_out;
+    int compact;          // aqsm holds column my_igp at position my_igp (stride ldm)
+    long ldm;
+    const double* vcoul;
+    float2* W;            // [ng][M] 0.5*vcoul*conj(aqsm[nv+m][igp]) in FP32, or nullptr
+    int M;
+    int* counter;
 };
+
+// The set-up work of block (ch, my_igp) other than the image padding.
+FK_DEV int prep_setup(const PrepArgs& p, int ch, int my_igp) {
+    if (!p.setup) return p.igp[my_igp];
+    const int igp = gpp_igp_of(my_igp, p.nc, p.inv, p.indinv);
+    if (ch == 0) {
+        const int acol = igp < 0 ? -1 : (p.compact ? my_igp : igp);
+        if (threadIdx.x == 0) {
+            p.igp_out[my_igp] = igp;
+            p.acol_out[my_igp] = acol;
+            if (my_igp == 0 && p.counter) *p.counter = 0;
+        }
+        if (p.W)
+            for (int m = threadIdx.x; m < p.M; m += blockDim.x)
+                p.W[(long)my_igp * p.M + m] =
+                    igp >= 0 ? tcx::weight_w1(p.aqsm[(long)(p.nv + m) * p.ldm + acol], 0.5 * p.vcoul[igp])
+                             : make_float2(0.f, 0.f);
+    }
+    return igp;
+}
 
 // ---------------------------------------------------------------- FP64 exact
 struct Branch64 {
@@ -177,7 +212,7 @@ template <int Q>  // Q = 1: root gppKer.cpp semantics
 __global__ void __launch_bounds__(PREP_THREADS) prep64_kernel(PrepArgs p) {
     __shared__ double2 sm[8 * NVC * 6];
     const int my_igp = blockIdx.y, ch = blockIdx.x, tid = threadIdx.x;
-    const int igp = p.igp[my_igp];
+    const int igp = prep_setup(p, ch, my_igp);
     const int nflag = min(NVC, p.nv - p.n1base);
     double2 acc[NVC * 6];
 #pragma unroll
@@ -394,7 +429,7 @@ template <int Q, int BN>
 FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) {
     const int tid = threadIdx.x;
     const int nflag = min(NVC, p.nv - p.n1base);
-    const int igp = p.igp[my_igp];
+    const int igp = prep_setup(p, ch, my_igp);
     const bool flags = nflag > 0 && igp >= 0;
     const float limitone = 250000.0f, limittwo = 0.25f, to1 = 1e-6f;
     uint8_t* D = reinterpret_cast<uint8_t*>(p.D);
@@ -493,6 +528,22 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
             }
         }
     }
+    if (p.setup && D) {
+        // zeros of the image that no column writes: the padding rows of this
+        // column's tile (written by the tile's last column) and, in the last
+        // chunk, k from ncouls to the end of the last k-stage
+        const int c = my_igp % GPP_COLS, nt = my_igp / GPP_COLS;
+        const bool lastcol = c == GPP_COLS - 1 || my_igp == p.ng - 1;
+        const int r0 = lastcol ? 3 * (c + 1) : 3 * c + 3;  // first padding row (none unless lastcol)
+        uint8_t* tile = D + (long)nt * p.kstages * tcx::Cfg<BN>::B_BYTES;
+        const int kend = p.kstages * tcx::BK;
+        if (lastcol)
+            for (int k = ch * p.tile + tid; k < min(p.nc, (ch + 1) * p.tile); k += PREP_THREADS)
+                for (int r = r0; r < BN; ++r) tcx::bimg_store<BN>(tile, p.kstages, r, k, 0.f, 0.f);
+        if ((ch + 1) * p.tile >= p.nc)
+            for (int k = p.nc + tid; k < kend; k += PREP_THREADS)
+                for (int r = 3 * c; r < (lastcol ? BN : 3 * c + 3); ++r) tcx::bimg_store<BN>(tile, p.kstages, r, k, 0.f, 0.f);
+    }
     if (nflag <= 0) return;
     double2 accd[NVC * 6];
     block_sum_ff<NVC * 6>(acc, sm, accd);
@@ -559,6 +610,9 @@ struct RowsArgs {
     const double2* aqsn;  // [nb][nc]
     int nc;
     bool re_only;         // real-valued sum: the contraction partials carry it in their real parts
+    // totals folded in: the last block to finish (counter, zero at entry) writes out
+    int* counter;
+    double2* out;
 };
 
 FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
@@ -616,10 +670,22 @@ FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
     if (lane == 0) rows[(long)n1 * 8 + c] = v;
 }
 
+FK_DEV void totals_block(int nb, const double2* rows, double2* out);
+
 __global__ void rows_kernel(RowsArgs ra) {
     const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (w >= (long)ra.nb * 7) return;  // w is uniform over the warp
-    rows_warp(ra, (int)(w / 7), (int)(w % 7), threadIdx.x & 31);
+    if (w < (long)ra.nb * 7) rows_warp(ra, (int)(w / 7), (int)(w % 7), threadIdx.x & 31);  // w is warp-uniform
+    if (!ra.counter) return;
+    // the last block to finish adds the bands (fixed order, as totals_kernel)
+    __shared__ int last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ra.counter, 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    totals_block(ra.nb, ra.rows, ra.out);
+    if (threadIdx.x == 0) *ra.counter = 0;
 }
 
 // Totals over bands, one warp per component (same split and tree), and the
@@ -918,7 +984,7 @@ __global__ void real_out_kernel(int nb, const double2* outc, double* out) {
 size_t gpp_workspace(const Ctx& c, const GppDev& r, bool pipelined) {
     Plan p = make_plan(c, r, 0, pipelined);
     const size_t half = (r.flags & FK_GPP_HALF_SUM) ? p.bytesP + (size_t)r.ng * (4 + 3 * sizeof(double2)) + 512 : 0;
-    return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesRows + p.bytesIgp + p.bytesW + half + 10 * 256;
+    return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesRows + p.bytesIgp + p.bytesW + half + 11 * 256;
 }
 
 int gpp_pipe_chunks(const Ctx& c, const GppDev& r) { return make_plan(c, r, 0, true).pipe_chunks; }
@@ -1055,39 +1121,45 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
     double2* S = p.bytesS ? (double2*)c.ws.take(p.bytesS) : nullptr;
     double2* rows = (double2*)c.ws.take(p.bytesRows);
     float2* W = p.bytesW ? (float2*)c.ws.take(p.bytesW) : nullptr;
-    if (!igp || !F || !rows || (p.bytesD && !D) || (p.bytesP && !P) || (p.bytesS && !S) || (p.bytesW && !W))
+    int* counter = (int*)c.ws.take(sizeof(int));
+    if (!igp || !F || !rows || !counter || (p.bytesD && !D) || (p.bytesP && !P) || (p.bytesS && !S) ||
+        (p.bytesW && !W))
         return fail(c, FK_ENOMEM, "workspace too small for GPP request");
     if (p.mixed && D) {
-        // the prep writes every (column, k) element; padding rows and k >= ncouls are zeroed here
-        if (tcx::img_needs_pad(64, r.ng, GPP_COLS, r.nc))
-            tcx::img_pad_kernel<64><<<dim3(p.kstages, p.NT, 1), 256, 0, st>>>((uint8_t*)D, p.NT, p.kstages, r.ng,
-                                                                            GPP_COLS, r.nc);
         cudaError_t e = cudaMemsetAsync(c.errword, 0, sizeof(int), st);  // bounded-wait status
         if (e != cudaSuccess) return cuda_fail(c, e, "gpp: error word");
     }
     const bool Q = (r.flags & FK_GPP_ROOT_QUIRKS) != 0;
     const int M = r.nb - r.nv;
     c.launches = 0;
+    // the first prep pass also maps the columns, writes the epilogue weights and
+    // the image's padding, and clears the reduction's counter
+    auto prep_args = [&](int pass) {
+        PrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, pass == 0 ? D : nullptr, p.kstages,
+                   F, p.nch, p.tile, pass * NVC, 0};
+        if (pass == 0) {
+            a.setup = 1;
+            a.inv = r.inv; a.indinv = r.indinv;
+            a.igp_out = igp; a.acol_out = acol;
+            a.compact = r.aqsm_compact ? 1 : 0;
+            a.aqsm = r.aqsm; a.ldm = r.ldm; a.vcoul = r.vcoul;
+            a.W = (p.mixed && M > 0) ? W : nullptr;
+            a.M = M;
+            a.counter = counter;
+        }
+        return a;
+    };
 
     phase_mark(c, 1);
     if (pipe && cudaStreamWaitEvent(st, c.pipe_ev[PIPE_READY], 0) != cudaSuccess)
         return cuda_fail(c, cudaGetLastError(), "gpp: waiting for the small inputs");
-    igp_map_kernel<<<ceil_div(r.ng, 128), 128, 0, st>>>(r.ng, r.nc, r.inv, r.indinv, r.aqsm_compact ? 1 : 0, igp, acol);
-    ++c.launches;
-    if (p.mixed && M > 0) {
-        // epilogue weights of the contraction (independent of the prep)
-        tcx::weight_table_kernel<<<dim3(ceil_div(M, 128), r.ng), 128, 0, st>>>(M, r.nv, r.ng, r.aqsm, r.ldm, r.vcoul,
-                                                                            igp, acol, 0.5, W, nullptr, nullptr);
-        ++c.launches;
-    }
     // pipelined host path: the prep waits for row block 0 (the flag bands), each
     // block's contraction for its own copy
     if (pipe) {
         if (cudaStreamWaitEvent(st, c.pipe_ev[0], 0) != cudaSuccess)
             return cuda_fail(c, cudaGetLastError(), "gpp: waiting for a block");
         for (int pass = 0; pass < p.passes; ++pass) {
-            PrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, pass == 0 ? D : nullptr, p.kstages,
-                       F, p.nch, p.tile, pass * NVC, 0};
+            const PrepArgs a = prep_args(pass);
             if (Q) prep_mixed_kernel<1, 64><<<dim3(p.nch, r.ng), PREP_THREADS, 0, st>>>(a);
             else prep_mixed_kernel<0, 64><<<dim3(p.nch, r.ng), PREP_THREADS, 0, st>>>(a);
             ++c.launches;
@@ -1124,8 +1196,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
         }
     }
     for (int pass = 0; pass < p.passes && !pipe; ++pass) {
-        PrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, pass == 0 ? D : nullptr, p.kstages,
-                   F, p.nch, p.tile, pass * NVC, 0};
+        const PrepArgs a = prep_args(pass);
         dim3 grid(p.nch, r.ng);
         if (p.mixed) {
             if (Q) prep_mixed_kernel<1, 64><<<grid, PREP_THREADS, 0, st>>>(a);
@@ -1188,10 +1259,11 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
         ++c.launches;
     }
     phase_mark(c, 3);
-    const RowsArgs ra{r.nb, r.nv, r.ng, p.KS * p.NT, P, p.KSs * p.NTs, S, p.nch, F, r.ldm, r.aqsm, r.vcoul, igp, acol, rows};
+    RowsArgs ra{r.nb, r.nv, r.ng, p.KS * p.NT, P, p.KSs * p.NTs, S, p.nch, F, r.ldm, r.aqsm, r.vcoul, igp, acol, rows};
+    ra.counter = counter;  // the last block also writes the totals
+    ra.out = r.out;
     rows_kernel<<<ceil_div(r.nb * 7, 8), 256, 0, st>>>(ra);
-    totals_kernel<<<1, 256, 0, st>>>(r.nb, rows, r.out);
-    c.launches += 2;
+    ++c.launches;
     phase_mark(c, 4);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "gpp kernels");
