@@ -50,6 +50,15 @@ FK_DEV float f64_to_f32_bits(double d) {
     return __uint_as_float(f | sign);
 }
 FK_DEV float2 c64_to_f32(double2 v) { return make_float2(f64_to_f32_bits(v.x), f64_to_f32_bits(v.y)); }
+// FP32 -> FP64 with integer instructions (exact); zeros and subnormals give a
+// signed zero, infinities and NaNs are not expected by the callers
+FK_DEV double f32_to_f64_bits(float f) {
+    const unsigned u = __float_as_uint(f), e = (u >> 23) & 0xFFu;
+    const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+    if (e == 0) return __longlong_as_double((long long)s);
+    return __longlong_as_double(
+        (long long)(s | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
 
 // x[0] + x[stride] + ... + x[(n-1)*stride], added left to right; the loads
 // are issued in groups of eight ahead of the adds, so a long sum waits for

@@ -291,22 +291,41 @@ FK_DEV double2 half_sch(double wxt, double2 wt, double2 eps) {
 // ig takes part in column igp's noflag sum (the driver's 512-wide blocks)
 FK_DEV bool half_member(int ig, int igp) { return ig < igp - 1 && (ig & 511) != 511; }
 
-// brk[my_igp] = the first ig < igp with |wtilde^2 * I_eps| < to1 (brk starts above every igp)
+// brk[my_igp] = the first ig < igp with |wtilde^2 * I_eps| < to1 (brk starts above
+// every igp).  The test runs in FP32 on |Omega2|^2 against to1^2; inside a relative
+// guard band of 1e-5 around it (the FP32 error is ~1e-7) the FP64 test decides, so
+// every decision is the FP64 one.
+__device__ __noinline__ bool half_break64(double2 w, double2 ep) {
+    const double2 o = cmul(cmul(w, w), ep);
+    return hypot(o.x, o.y) < 1e-6;
+}
 __global__ void half_break_kernel(int ng, int nc, const int* igpm, const double2* eps, const double2* wt, int* brk) {
     const int my_igp = blockIdx.y;
     const int igp = igpm[my_igp];
-    for (int ig = blockIdx.x * blockDim.x + threadIdx.x; ig < nc; ig += gridDim.x * blockDim.x) {
-        if (igp < 0 || ig >= igp) break;
-        const double2 w = wt[(long)my_igp * nc + ig];
-        const double2 o = cmul(cmul(w, w), eps[(long)my_igp * nc + ig]);
-        if (hypot(o.x, o.y) < 1e-6) atomicMin(&brk[my_igp], ig);
+    if (igp <= 0) return;  // block-uniform
+    // warps walk [0, igp) together; the first hit of each warp goes to one atomicMin
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x; base < igp; base += stride) {
+        const int ig = base + threadIdx.x;
+        int first = 0x7fffffff;
+        if (ig < igp) {
+            const double2 w64 = wt[(long)my_igp * nc + ig], e64 = eps[(long)my_igp * nc + ig];
+            const float2 w = c64_to_f32(w64), o = cmulf(cmulf(w, w), c64_to_f32(e64));
+            const float o2 = o.x * o.x + o.y * o.y;
+            bool hit = o2 < 1e-12f;
+            if (!(o2 < 1e30f) || fabsf(o2 - 1e-12f) <= 1e-12f * GUARD || !(o2 > 1e-36f)) hit = half_break64(w64, e64);
+            if (hit) first = ig;
+        }
+        first = __reduce_min_sync(0xffffffffu, first);
+        if ((threadIdx.x & 31) == 0 && first != 0x7fffffff) atomicMin(&brk[my_igp], first);
     }
 }
 
 // The diagonal value sch(igp) for columns on a block edge (igp % 512 == 0), else 0.
 __global__ void half_diag_kernel(int ng, int nc, const int* igpm, const double2* eps, const double2* wt,
-                                 const double* wx, double2* schd) {
+                                 const double* wx, double2* schd, int* counter) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) *counter = 0;  // the band reduction's completion count
     if (t >= ng * 3) return;
     const int my_igp = t / 3, iw = t % 3, igp = igpm[my_igp];
     double2 v = make_double2(0.0, 0.0);
@@ -391,6 +410,127 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_half_kernel(PrepArgs p) {
     if (tid < nflag * 12) {
         const int j = tid / 12, r = tid % 12;
         p.F[(((long)ch * p.nv + p.n1base + j) * p.ng + my_igp) * 12 + r] = acc[tid];
+    }
+}
+
+// Mixed-precision prep of the half sum: the same outputs as prep_half_kernel<1>
+// with the branch quantities in FP32 from an FP64 wx - wtilde; inside a relative
+// guard band of 1e-5 around a threshold (or outside FP32's comfortable range)
+// the FP64 sequence decides and supplies the values, so every branch is the
+// FP64 one.  Flag-band sums in FP32 float-float (block_sum_ff).
+__device__ __noinline__ double2 half_sch_rare(double wxt, double2 wt, double2 eps) { return half_sch(wxt, wt, eps); }
+__device__ __noinline__ void half_flag_rare(double wxt, double2 wt, double2 eps, float2& sch, float2& ssx) {
+    double2 a, b;
+    half_flag_terms(wxt, wt, eps, a, b);
+    sch = c64_to_f32(a);
+    ssx = c64_to_f32(b);
+}
+FK_DEV float2 cdivf(float2 a, float2 b) {
+    const float r = __frcp_rn(b.x * b.x + b.y * b.y);
+    return make_float2((a.x * b.x + a.y * b.y) * r, (a.y * b.x - a.x * b.y) * r);
+}
+
+__global__ void __launch_bounds__(PREP_THREADS, 2) prep_half_mixed_kernel(PrepArgs p) {
+    __shared__ double2 sm[8 * NVC * 12];
+    const int my_igp = blockIdx.y, ch = p.ch0 + blockIdx.x, tid = threadIdx.x;
+    const int igp = p.igp[my_igp];
+    const int nflag = min(NVC, p.nv - p.n1base);
+    const int stop = igp < 0 ? 0 : min(igp, p.brk[my_igp]);
+    const float limitone = 250000.0f, limittwo = 0.25f, to1 = 1e-6f, to1sq = 1e-12f;
+    float2 acc[NVC * 12];
+#pragma unroll
+    for (int i = 0; i < NVC * 12; ++i) acc[i] = make_float2(0.f, 0.f);
+    double wx64[3];
+    float wxsq[3];
+#pragma unroll
+    for (int iw = 0; iw < 3; ++iw) {
+        wx64[iw] = p.wx[iw];
+        const float wf = f64_to_f32_bits(wx64[iw]);
+        wxsq[iw] = wf * wf;
+    }
+    const double2* wrow = p.wt + (long)my_igp * p.nc;
+    const double2* erow = p.eps + (long)my_igp * p.nc;
+    for (int ig = ch * p.tile + tid; ig < min(p.nc, (ch + 1) * p.tile); ig += PREP_THREADS) {
+        const double2 wt64 = wrow[ig], ep64 = erow[ig];
+        const float2 wt = c64_to_f32(wt64), ep = c64_to_f32(ep64);
+        const bool member = igp >= 0 && half_member(ig, igp);
+        const bool flag = nflag > 0 && ig < stop;
+        float2 wt2 = make_float2(0.f, 0.f), Om = wt2, hinv = wt2;
+        float wtsq = 0.f;
+        float2 an[NVC], am[NVC];
+        if (flag) {
+            wt2 = cmulf(wt, wt);
+            Om = cmulf(wt2, ep);
+            wtsq = wt.x * wt.x + wt.y * wt.y;
+            const float r = __frcp_rn(wtsq);
+            hinv = make_float2(0.5f * wt.x * r, -0.5f * wt.y * r);  // 0.5 / wtilde
+#pragma unroll
+            for (int j = 0; j < NVC; ++j) {
+                const long row = (long)(p.n1base + j) * p.nc + ig;
+                an[j] = j < nflag ? c64_to_f32(p.aqsn[row]) : make_float2(0.f, 0.f);
+                am[j] = j < nflag ? c64_to_f32(p.aqsm[row]) : make_float2(0.f, 0.f);
+            }
+        }
+#pragma unroll
+        for (int iw = 0; iw < 3; ++iw) {
+            const float2 wdiff = make_float2(f64_to_f32_bits(__dsub_rn(wx64[iw], wt64.x)), -wt.y);
+            const float wdiffr = wdiff.x * wdiff.x + wdiff.y * wdiff.y;
+            if (p.D) {
+                float2 dv = make_float2(0.f, 0.f);
+                if (member) {
+                    const float2 delw = cdivf(wt, wdiff);
+                    const float delw2 = delw.x * delw.x + delw.y * delw.y;
+                    const bool amb = !(wdiffr > 1e-30f) || !(delw2 < 1e30f) ||
+                                     fabsf(wdiffr - limittwo) <= limittwo * GUARD ||
+                                     fabsf(delw2 - limitone) <= limitone * GUARD;
+                    if (__any_sync(__activemask(), amb) && amb) dv = c64_to_f32(half_sch_rare(wx64[iw], wt64, ep64));
+                    else if (wdiffr < limittwo || delw2 > limitone) dv = cmulf(delw, ep);
+                }
+                const int nt = my_igp / GPP_COLS, row = (my_igp % GPP_COLS) * 3 + iw;
+                tcx::bimg_store<64>((uint8_t*)p.D + (long)nt * p.kstages * tcx::Cfg<64>::B_BYTES, p.kstages, row, ig,
+                                    dv.x, dv.y);
+            }
+            if (flag) {
+                // flagOCC_solver (gppsum = 1): wmw = wdiff, delw = wmw * 0.5/wtilde
+                const float2 delw = cmulf(wdiff, hinv);
+                const float ad2 = delw.x * delw.x + delw.y * delw.y;
+                const bool amb = !(wtsq > 1e-30f) || !(wdiffr > 1e-30f) || !(ad2 < 1e30f) || !(wtsq < 1e30f) ||
+                                 fabsf(wdiffr - limittwo) <= limittwo * GUARD || fabsf(ad2 - to1) <= to1 * GUARD ||
+                                 fabsf(wtsq - to1sq) <= to1sq * GUARD;
+                float2 sch, ssx;
+                if (__any_sync(__activemask(), amb) && amb) {
+                    half_flag_rare(wx64[iw], wt64, ep64, sch, ssx);
+                } else if (wdiffr < limittwo || ad2 < to1) {
+                    sch = make_float2(0.f, 0.f);
+                    ssx = wtsq > to1sq ? cdivf(make_float2(-Om.x, -Om.y),
+                                               cmulf(make_float2(4.f * wt2.x, 4.f * wt2.y),
+                                                     make_float2(1.f + delw.x, delw.y)))
+                                       : make_float2(0.f, 0.f);
+                } else {
+                    sch = cdivf(cmulf(wt, ep), wdiff);
+                    ssx = cdivf(Om, make_float2(wxsq[iw] - wt2.x, -wt2.y));
+                }
+#pragma unroll
+                for (int j = 0; j < NVC; ++j) {
+                    float2* a = acc + j * 12 + iw * 4;
+                    cfmaf(a[0], an[j], sch);
+                    cfmaf(a[2], an[j], ssx);
+                    if (ig != igp - 1) {
+                        cfmaf(a[1], am[j], sch);
+                        cfmaf(a[3], am[j], ssx);
+                    }
+                }
+            }
+        }
+    }
+    if (nflag <= 0) return;
+    double2 accd[NVC * 12];
+    block_sum_ff<NVC * 12>(acc, sm, accd);
+    if (tid < nflag * 12) {
+        const int j = tid / 12, r = tid % 12;
+#pragma unroll
+        for (int i = 0; i < NVC * 12; ++i)
+            if (i == tid) p.F[(((long)ch * p.nv + p.n1base + j) * p.ng + my_igp) * 12 + r] = accd[i];
     }
 }
 
@@ -759,9 +899,13 @@ Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0, bool pipeline
         p.nch = ceil_div(r.nc, PREP_TILE);
     }
     const bool half = (r.flags & FK_GPP_HALF_SUM) != 0;
-    if (half) {  // FP64 prep for both precisions (prep_half_kernel)
-        p.tile = PREP_TILE;
-        p.nch = ceil_div(r.nc, PREP_TILE);
+    if (half) {
+        // FP64: tiles of the FP64 prep; mixed: chunks of one resident wave (two
+        // blocks per SM), so that the band reduction adds few chunk partials
+        p.tile = r.prec == FK_MIXED
+                     ? ceil_div(ceil_div(r.nc, std::max(1, 2 * c.sms / r.ng)), PREP_THREADS) * PREP_THREADS
+                     : PREP_TILE;
+        p.nch = ceil_div(r.nc, p.tile);
     }
     p.passes = std::max(1, ceil_div(r.nv, NVC));
     const int M = r.nb - r.nv, N = 3 * r.ng;
@@ -841,6 +985,7 @@ struct RealPrepArgs {
     uint8_t* mask;     // [ng][nc] bit iw: the noflag mask of (iw, ig)
     double2* F;        // [nch][nv][ng][6] flag-band (sch, ssx) sums, as (value, 0)
     int nch, n1base;
+    int tile;          // plane waves per chunk (a multiple of PREP_THREADS)
 };
 
 // Per element: the noflag mask and value (gppKer_real.cpp:351-366) and, for
@@ -856,7 +1001,7 @@ __global__ void __launch_bounds__(PREP_THREADS) real_prep_kernel(RealPrepArgs p)
     double2 acc[NVC * 6];
 #pragma unroll
     for (int i = 0; i < NVC * 6; ++i) acc[i] = make_double2(0.0, 0.0);
-    for (int ig = ch * PREP_TILE + tid; ig < min(p.nc, (ch + 1) * PREP_TILE); ig += PREP_THREADS) {
+    for (int ig = ch * p.tile + tid; ig < min(p.nc, (ch + 1) * p.tile); ig += PREP_THREADS) {
         const double w = p.wt[(long)my_igp * p.nc + ig], ep = p.eps[(long)my_igp * p.nc + ig];
         const double w2 = __dmul_rn(w, w), Om = __dmul_rn(w2, ep);
         int bits = 0;
@@ -902,6 +1047,122 @@ __global__ void __launch_bounds__(PREP_THREADS) real_prep_kernel(RealPrepArgs p)
     }
 }
 
+// Mixed precision: the branch quantities of real_prep_kernel in FP32 from an FP64
+// wx - wtilde, the FP64 sequence inside a relative guard band of 1e-5 around
+// every threshold (so every branch is the FP64 one), flag-band sums in FP32
+// float-float.  Dv and the mask mean what they mean in the FP64 kernel.
+struct RealTerm {
+    double dv, sch, ssx;
+    int A;
+};
+__device__ __noinline__ RealTerm real_term_rare(double wxt, double w, double ep) {
+    const double to1 = 1e-6, limitone = 1.0 / (to1 * 4.0), limittwo = 0.25;
+    const double w2 = __dmul_rn(w, w), Om = __dmul_rn(w2, ep);
+    const double wdiff = __dsub_rn(wxt, w);
+    const double rden = __ddiv_rn(1.0, __dmul_rn(wdiff, wdiff));
+    const double delw = __dmul_rn(__dmul_rn(w, wdiff), rden);
+    const double delwr = __dmul_rn(delw, delw), wdiffr = __dmul_rn(wdiff, wdiff);
+    RealTerm t;
+    t.A = wdiffr > limittwo && delwr < limitone;
+    t.dv = __dmul_rn(delw, ep);
+    t.sch = 0.0;
+    t.ssx = 0.0;
+    if (t.A) {
+        t.sch = t.dv;
+        const double cden = __dmul_rn(wxt, wxt);
+        t.ssx = __dmul_rn(__dmul_rn(Om, cden), __ddiv_rn(1.0, __dmul_rn(cden, cden)));
+    } else if (delwr > to1) {
+        const double cden = __dmul_rn(__dmul_rn(4.0, w2), __dadd_rn(delw, 0.5));
+        t.ssx = __dmul_rn(__dmul_rn(__dmul_rn(0.0 - Om, cden), __ddiv_rn(1.0, __dmul_rn(cden, cden))), delw);
+    }
+    return t;
+}
+
+__global__ void __launch_bounds__(PREP_THREADS) real_prep_mixed_kernel(RealPrepArgs p) {
+    __shared__ double2 sm[8 * NVC * 6];
+    const int my_igp = blockIdx.y, ch = blockIdx.x, tid = threadIdx.x;
+    const int igp = p.igp[my_igp];
+    const int nflag = igp < 0 ? 0 : min(NVC, p.nv - p.n1base);
+    const float to1 = 1e-6f, limitone = 250000.0f, limittwo = 0.25f;
+    float2 acc[NVC * 6];
+#pragma unroll
+    for (int i = 0; i < NVC * 6; ++i) acc[i] = make_float2(0.f, 0.f);
+    double wx64[3];
+    float wxsq[3];
+#pragma unroll
+    for (int iw = 0; iw < 3; ++iw) {
+        wx64[iw] = p.wx[iw];
+        const float wf = f64_to_f32_bits(wx64[iw]);
+        wxsq[iw] = wf * wf;
+    }
+    for (int ig = ch * p.tile + tid; ig < min(p.nc, (ch + 1) * p.tile); ig += PREP_THREADS) {
+        const double w64 = p.wt[(long)my_igp * p.nc + ig], ep64 = p.eps[(long)my_igp * p.nc + ig];
+        const float w = f64_to_f32_bits(w64), ep = f64_to_f32_bits(ep64);
+        const float w2 = w * w, Om = w2 * ep;
+        float an[NVC];
+#pragma unroll
+        for (int j = 0; j < NVC; ++j) an[j] = j < nflag ? f64_to_f32_bits(p.aqsn[(long)(p.n1base + j) * p.lda + ig]) : 0.f;
+        int bits = 0;
+#pragma unroll
+        for (int iw = 0; iw < 3; ++iw) {
+            const double wd64 = __dsub_rn(wx64[iw], w64);
+            const float wdiff = f64_to_f32_bits(wd64);
+            const float wdiffr = wdiff * wdiff;
+            const float delw = __fdiv_rn(w, wdiff);  // = w*wdiff/wdiff^2, correctly rounded
+            const float delwr = delw * delw;
+            const bool amb = !(wdiffr > 1e-30f) || !(delwr < 1e30f) || fabsf(wdiffr - limittwo) <= limittwo * GUARD ||
+                             fabsf(delwr - limitone) <= limitone * GUARD ||
+                             (nflag > 0 && fabsf(delwr - to1) <= to1 * GUARD);
+            bool A;
+            float dv, sch = 0.f, ssx = 0.f;
+            double dv64;
+            if (__any_sync(__activemask(), amb) && amb) {
+                const RealTerm t = real_term_rare(wx64[iw], w64, ep64);
+                A = t.A != 0;
+                dv64 = t.dv;
+                dv = f64_to_f32_bits(t.dv);
+                sch = f64_to_f32_bits(t.sch);
+                ssx = f64_to_f32_bits(t.ssx);
+            } else {
+                A = wdiffr > limittwo && delwr < limitone;
+                // the value to FP64 accuracy (it is summed, then rounded once for the
+                // tensor cores): one FP64 correction of the FP32 quotient w / wdiff
+                double q = f32_to_f64_bits(delw);
+                q = __fma_rn(__fma_rn(-q, wd64, w64), f32_to_f64_bits(__frcp_rn(wdiff)), q);
+                dv64 = __dmul_rn(q, ep64);
+                dv = f64_to_f32_bits(dv64);
+                if (A) {
+                    sch = dv;
+                    ssx = __fdiv_rn(Om, wxsq[iw]);
+                } else if (delwr > to1) {
+                    const float cden = 4.f * w2 * (delw + 0.5f);
+                    ssx = __fdiv_rn(-Om * delw, cden);
+                }
+            }
+            if (p.Dv) {
+                p.Dv[((long)my_igp * 3 + iw) * p.nc + ig] = dv64;
+                bits |= (int)A << iw;
+            }
+#pragma unroll
+            for (int j = 0; j < NVC; ++j) {
+                acc[(j * 3 + iw) * 2 + 0].x = fmaf(an[j], sch, acc[(j * 3 + iw) * 2 + 0].x);
+                acc[(j * 3 + iw) * 2 + 1].x = fmaf(an[j], ssx, acc[(j * 3 + iw) * 2 + 1].x);
+            }
+        }
+        if (p.Dv) p.mask[(long)my_igp * p.nc + ig] = (uint8_t)bits;
+    }
+    if (p.nv - p.n1base <= 0) return;
+    double2 accd[NVC * 6];
+    block_sum_ff<NVC * 6>(acc, sm, accd);
+    const int nf = min(NVC, p.nv - p.n1base);
+    if (tid < nf * 6) {
+        const int j = tid / 6, r = tid % 6;
+#pragma unroll
+        for (int i = 0; i < NVC * 6; ++i)
+            if (i == tid) p.F[(((long)ch * p.nv + p.n1base + j) * p.ng + my_igp) * 6 + r] = accd[i];
+    }
+}
+
 struct RealCarryArgs {
     int nc, ng;
     long K2;             // complex pairs per row of the operand
@@ -914,60 +1175,77 @@ struct RealCarryArgs {
     int kstages;
 };
 
-// One thread per (my_igp, block offset j): the driver's sequence of blocks b
-// and frequencies iw at offset j, with the current source of scha[j] and the
-// sums owed to it; E of every g = 512*b + j is written exactly once.
+// At block offset j the driver's block sums happen at times t = 3*b + iw
+// (block b, frequency iw) for the blocks that reach j; the source of scha[j]
+// changes at the times whose mask bit is set.  A source (g, iw') set at t0 and
+// replaced at t1 adds D(g, iw') to E[iw][g] once for every t in [t0, t1) with
+// t = iw (mod 3), so
+//   E[iw][g] = sum over set bits iw' of g's mask of D(g, iw') * #{t in [t0, t1): t = iw mod 3},
+// t1 being the next set bit of the same block, else the first set time of a
+// later block at the same offset.  E of an element thus depends on its own
+// mask and values and on that first later set time only: one thread per
+// element, looking ahead through the masks of the later blocks (usually one).
 template <int IMG>
 __global__ void real_carry_kernel(RealCarryArgs a) {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int my_igp = (int)(t >> 9), j = (int)(t & 511);
-    if (my_igp >= a.ng) return;
-    const bool col = a.igp[my_igp] >= 0;
-    auto put = [&](int iw, int g, double v) {
-        const double s = (g & 1) ? 0.0 - v : v;
+    if (t >= (long)a.ng * a.nc) return;
+    const int my_igp = (int)(t / a.nc), g = (int)(t % a.nc);
+    auto put = [&](int iw, int gg, double v) {
+        const double s = (gg & 1) ? 0.0 - v : v;
         if (IMG) {
             const int nt = my_igp / GPP_COLS, row = (my_igp % GPP_COLS) * 3 + iw;
-            tcx::bimg_store_part<64>(a.img + (long)nt * a.kstages * tcx::Cfg<64>::B_BYTES, row, g >> 1, g & 1,
+            tcx::bimg_store_part<64>(a.img + (long)nt * a.kstages * tcx::Cfg<64>::B_BYTES, row, gg >> 1, gg & 1,
                                      f64_to_f32_bits(s));
         } else {
-            a.D64[((long)my_igp * 3 + iw) * 2 * a.K2 + g] = s;
+            a.D64[((long)my_igp * 3 + iw) * 2 * a.K2 + gg] = s;
         }
     };
-    int gs = -1;
-    double val = 0.0, acc[3] = {0.0, 0.0, 0.0};
-    for (int g = j; g < a.nc; g += 512) {
-        const int m = col ? a.mask[(long)my_igp * a.nc + g] : 0;
+    const uint8_t* mrow = a.mask + (long)my_igp * a.nc;
+    const int m = a.igp[my_igp] >= 0 ? mrow[g] : 0;
+    double e[3] = {0.0, 0.0, 0.0};
+    if (m) {
+        double dv[3];
+#pragma unroll
+        for (int iw = 0; iw < 3; ++iw) dv[iw] = a.Dv[((long)my_igp * 3 + iw) * a.nc + g];
         if (!a.carry) {
 #pragma unroll
-            for (int iw = 0; iw < 3; ++iw) put(iw, g, ((m >> iw) & 1) ? a.Dv[((long)my_igp * 3 + iw) * a.nc + g] : 0.0);
-            continue;
-        }
-#pragma unroll
-        for (int iw = 0; iw < 3; ++iw) {
-            if ((m >> iw) & 1) {
-                if (gs != g) {
-                    if (gs >= 0)
-                        for (int k = 0; k < 3; ++k) put(k, gs, acc[k]);
-                    acc[0] = acc[1] = acc[2] = 0.0;
-                    gs = g;
+            for (int iw = 0; iw < 3; ++iw) e[iw] = ((m >> iw) & 1) ? dv[iw] : 0.0;
+        } else {
+            const int j = g & 511, b = g >> 9;
+            int tnext = 3 * ((a.nc - j + 511) / 512);  // no later set time: the end of offset j's blocks
+            for (int g2 = g + 512; g2 < a.nc; g2 += 512) {
+                const int m2 = mrow[g2];
+                if (m2) {
+                    tnext = 3 * (g2 >> 9) + __ffs(m2) - 1;
+                    break;
                 }
-                val = a.Dv[((long)my_igp * 3 + iw) * a.nc + g];
             }
-            if (gs >= 0) acc[iw] = __dadd_rn(acc[iw], val);
+            auto upto = [](int T, int iw) { return (T - iw + 2) / 3; };  // #{t < T : t = iw mod 3}
+#pragma unroll
+            for (int ws = 0; ws < 3; ++ws) {
+                if (!((m >> ws) & 1)) continue;
+                const int t0 = 3 * b + ws, later = m >> (ws + 1);
+                const int t1 = later ? t0 + __ffs(later) : tnext;
+#pragma unroll
+                for (int iw = 0; iw < 3; ++iw) {
+                    const int n = upto(t1, iw) - upto(t0, iw);
+                    if (n) e[iw] = __fma_rn((double)n, dv[ws], e[iw]);
+                }
+            }
         }
-        if (gs != g)
-            for (int iw = 0; iw < 3; ++iw) put(iw, g, 0.0);
     }
-    if (gs >= 0)
-        for (int iw = 0; iw < 3; ++iw) put(iw, gs, acc[iw]);
+#pragma unroll
+    for (int iw = 0; iw < 3; ++iw) put(iw, g, e[iw]);
     // odd ncouls: the imaginary half of the last pair has no element behind it
-    if ((a.nc & 1) && j == (a.nc - 1) % 512)
+    if ((a.nc & 1) && g == a.nc - 1)
         for (int iw = 0; iw < 3; ++iw) put(iw, a.nc, 0.0);
 }
 
 // aqsmtemp's igp columns as complex (value, 0), [nb][ng]: the epilogue weights' source.
-__global__ void real_columns_kernel(int nb, int nc, int ng, const double* aqsm, const int* igp, double2* ac) {
+__global__ void real_columns_kernel(int nb, int nc, int ng, const double* aqsm, const int* igp, double2* ac,
+                                    int* counter) {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) *counter = 0;  // the band reduction's completion count
     if (t >= (long)nb * ng) return;
     const int n1 = (int)(t / ng), h = (int)(t % ng), g = igp[h];
     ac[t] = make_double2(g >= 0 ? aqsm[(long)n1 * nc + g] : 0.0, 0.0);
@@ -983,7 +1261,7 @@ __global__ void real_out_kernel(int nb, const double2* outc, double* out) {
 
 size_t gpp_workspace(const Ctx& c, const GppDev& r, bool pipelined) {
     Plan p = make_plan(c, r, 0, pipelined);
-    const size_t half = (r.flags & FK_GPP_HALF_SUM) ? p.bytesP + (size_t)r.ng * (4 + 3 * sizeof(double2)) + 512 : 0;
+    const size_t half = (r.flags & FK_GPP_HALF_SUM) ? p.bytesP + (size_t)r.ng * (4 + 3 * sizeof(double2)) + 768 : 0;
     return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesRows + p.bytesIgp + p.bytesW + half + 11 * 256;
 }
 
@@ -1032,7 +1310,8 @@ fk_status gpp_run_half(Ctx& c, const GppDev& r) {
     float2* W = p.bytesW ? (float2*)c.ws.take(p.bytesW) : nullptr;
     int* brk = (int*)c.ws.take((size_t)r.ng * sizeof(int));
     double2* schd = (double2*)c.ws.take((size_t)r.ng * 3 * sizeof(double2));
-    if (!igp || !F || !rows || !brk || !schd || (p.bytesD && !D) || (p.bytesP && (!P || !P2)) || (p.bytesW && !W))
+    int* counter = (int*)c.ws.take(sizeof(int));
+    if (!igp || !F || !rows || !brk || !schd || !counter || (p.bytesD && !D) || (p.bytesP && (!P || !P2)) || (p.bytesW && !W))
         return fail(c, FK_ENOMEM, "workspace too small for GPP request");
     if (r.aqsm_compact || r.ldm != r.nc) return fail(c, FK_EINVAL, "gpp: the half sum needs all of aqsmtemp");
     c.launches = 0;
@@ -1052,12 +1331,12 @@ fk_status gpp_run_half(Ctx& c, const GppDev& r) {
         return cuda_fail(c, cudaGetLastError(), "gpp: break table");
     half_break_kernel<<<dim3(std::max(1, std::min(ceil_div(r.nc, 256), 64)), r.ng), 256, 0, st>>>(r.ng, r.nc, igp,
                                                                                                  r.eps, r.wt, brk);
-    half_diag_kernel<<<ceil_div(r.ng * 3, 128), 128, 0, st>>>(r.ng, r.nc, igp, r.eps, r.wt, r.wx, schd);
+    half_diag_kernel<<<ceil_div(r.ng * 3, 128), 128, 0, st>>>(r.ng, r.nc, igp, r.eps, r.wt, r.wx, schd, counter);
     c.launches += p.mixed && M > 0 ? 4 : 3;
     for (int pass = 0; pass < p.passes; ++pass) {
         PrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, (pass == 0 && M > 0) ? D : nullptr,
                    p.kstages, F, p.nch, p.tile, pass * NVC, 0, r.aqsm, brk};
-        if (p.mixed) prep_half_kernel<1><<<dim3(p.nch, r.ng), PREP_THREADS, 0, st>>>(a);
+        if (p.mixed) prep_half_mixed_kernel<<<dim3(p.nch, r.ng), PREP_THREADS, 0, st>>>(a);
         else prep_half_kernel<0><<<dim3(p.nch, r.ng), PREP_THREADS, 0, st>>>(a);
         ++c.launches;
     }
@@ -1100,9 +1379,10 @@ fk_status gpp_run_half(Ctx& c, const GppDev& r) {
     ra.schd = schd;
     ra.aqsn = r.aqsn;
     ra.nc = r.nc;
+    ra.counter = counter;  // the last block also writes the totals
+    ra.out = r.out;
     rows_kernel<<<ceil_div(r.nb * 7, 8), 256, 0, st>>>(ra);
-    totals_kernel<<<1, 256, 0, st>>>(r.nb, rows, r.out);
-    c.launches += 2;
+    ++c.launches;
     phase_mark(c, 4);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FK_OK : cuda_fail(c, e, "gpp kernels (half sum)");
@@ -1622,7 +1902,7 @@ struct RealPlan {
     Plan c;         // the complex contraction over K2 pairs
     GppDev cd;      // its shape
     long K2;
-    int nch;
+    int nch, tile;
     size_t bytesDv, bytesMask, bytesF, bytesAC, bytesOutc, bytesD64;
 };
 
@@ -1632,7 +1912,10 @@ RealPlan make_real_plan(const Ctx& c, const GppRealDev& r) {
     q.cd = GppDev{};
     q.cd.nb = r.nb; q.cd.nv = r.nv; q.cd.nc = (int)q.K2; q.cd.ng = r.ng; q.cd.prec = r.prec; q.cd.flags = 0;
     q.c = make_plan(c, q.cd);
-    q.nch = ceil_div(r.nc, PREP_TILE);
+    // FP64: tiles of the FP64 prep; mixed: chunks of one resident wave
+    q.tile = r.prec == FK_MIXED ? ceil_div(ceil_div(r.nc, std::max(1, 4 * c.sms / r.ng)), PREP_THREADS) * PREP_THREADS
+                                : PREP_TILE;
+    q.nch = ceil_div(r.nc, q.tile);
     q.bytesDv = (size_t)r.ng * 3 * r.nc * sizeof(double);
     q.bytesMask = (size_t)r.ng * r.nc;
     q.bytesF = (size_t)q.nch * std::max(r.nv, 1) * r.ng * 6 * sizeof(double2);
@@ -1645,7 +1928,7 @@ RealPlan make_real_plan(const Ctx& c, const GppRealDev& r) {
 size_t gpp_real_workspace(const Ctx& c, const GppRealDev& r) {
     const RealPlan q = make_real_plan(c, r);
     return q.c.bytesD + q.c.bytesW + q.c.bytesP + q.c.bytesRows + q.c.bytesIgp + q.bytesDv + q.bytesMask + q.bytesF +
-           q.bytesAC + q.bytesOutc + 12 * 256;
+           q.bytesAC + q.bytesOutc + 13 * 256;
 }
 
 fk_status gpp_real_run(Ctx& c, const GppRealDev& r) {
@@ -1665,7 +1948,8 @@ fk_status gpp_real_run(Ctx& c, const GppRealDev& r) {
     double2* F = (double2*)c.ws.take(q.bytesF);
     double2* AC = (double2*)c.ws.take(q.bytesAC);
     double2* outc = (double2*)c.ws.take(q.bytesOutc);
-    if (!igp || !rows || !Dv || !mask || !F || !AC || !outc || (p.bytesD && !D) || (p.bytesP && !P) ||
+    int* counter = (int*)c.ws.take(sizeof(int));
+    if (!igp || !rows || !Dv || !mask || !F || !AC || !outc || !counter || (p.bytesD && !D) || (p.bytesP && !P) ||
         (p.bytesW && !W))
         return fail(c, FK_ENOMEM, "workspace too small for the real-valued GPP request");
     c.launches = 0;
@@ -1678,7 +1962,7 @@ fk_status gpp_real_run(Ctx& c, const GppRealDev& r) {
     }
     phase_mark(c, 1);
     igp_map_kernel<<<ceil_div(r.ng, 128), 128, 0, st>>>(r.ng, r.nc, r.inv, r.indinv, 1, igp, acol);
-    real_columns_kernel<<<ceil_div(r.nb * r.ng, 256), 256, 0, st>>>(r.nb, r.nc, r.ng, r.aqsm, igp, AC);
+    real_columns_kernel<<<ceil_div(r.nb * r.ng, 256), 256, 0, st>>>(r.nb, r.nc, r.ng, r.aqsm, igp, AC, counter);
     c.launches += 2;
     if (p.mixed && M > 0) {
         tcx::weight_table_kernel<<<dim3(ceil_div(M, 128), r.ng), 128, 0, st>>>(M, r.nv, r.ng, AC, r.ng, r.vcoul, igp,
@@ -1688,14 +1972,16 @@ fk_status gpp_real_run(Ctx& c, const GppRealDev& r) {
     const int passes = std::max(1, ceil_div(r.nv, NVC));
     for (int pass = 0; pass < passes; ++pass) {
         RealPrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, r.lda, igp,
-                       (pass == 0 && M > 0) ? Dv : nullptr, mask, F, q.nch, pass * NVC};
-        real_prep_kernel<<<dim3(q.nch, r.ng), PREP_THREADS, 0, st>>>(a);
+                       (pass == 0 && M > 0) ? Dv : nullptr, mask, F, q.nch, pass * NVC, q.tile};
+        if (p.mixed) real_prep_mixed_kernel<<<dim3(q.nch, r.ng), PREP_THREADS, 0, st>>>(a);
+        else real_prep_kernel<<<dim3(q.nch, r.ng), PREP_THREADS, 0, st>>>(a);
         ++c.launches;
     }
     if (M > 0) {
         RealCarryArgs ca{r.nc, r.ng, q.K2, igp, Dv, mask, (r.flags & FK_GPP_REAL_ZERO_MASKED) ? 0 : 1,
                          p.mixed ? nullptr : (double*)D, p.mixed ? (uint8_t*)D : nullptr, p.kstages};
-        const int blocks = ceil_div(r.ng * 512, 256);
+        const long threads = (long)r.ng * r.nc;  // one per element
+        const int blocks = (int)((threads + 255) / 256);
         if (p.mixed) real_carry_kernel<1><<<blocks, 256, 0, st>>>(ca);
         else real_carry_kernel<0><<<blocks, 256, 0, st>>>(ca);
         ++c.launches;
@@ -1734,10 +2020,11 @@ fk_status gpp_real_run(Ctx& c, const GppRealDev& r) {
     phase_mark(c, 3);
     RowsArgs ra{r.nb, r.nv, r.ng, P ? p.KS * p.NT : 0, P, 0, nullptr, q.nch, F, r.ng, AC, r.vcoul, igp, acol, rows};
     ra.re_only = true;
+    ra.counter = counter;  // the last block also writes the totals
+    ra.out = outc;
     rows_kernel<<<ceil_div(r.nb * 7, 8), 256, 0, st>>>(ra);
-    totals_kernel<<<1, 256, 0, st>>>(r.nb, rows, outc);
     real_out_kernel<<<std::max(1, std::min(ceil_div(6 + r.nb, 256), 64)), 256, 0, st>>>(r.nb, outc, r.out);
-    c.launches += 3;
+    c.launches += 2;
     phase_mark(c, 4);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FK_OK : cuda_fail(c, e, "gpp_real kernels");
