@@ -84,14 +84,20 @@ def roofline(w, prec, byts, flops, kms, launches, peaks):
     device time over one call, summed over its launches (CUDA events the
     library records on its stream right around each launch); byts/flops are
     the algorithmic work of those launches, so achieved = work / time is the
-    launch-weighted average rate.  GPP: HBM-bound (algorithmic bytes).  FF:
-    tensor-bound (algorithmic FP64-equivalent flops against the bf16 peak; the
-    BF16x3 emulation executes 6 piece products per complex product)."""
+    launch-weighted average rate.  The bound is the higher floor: algorithmic
+    bytes at the copy peak (GPP at small ngpown), or algorithmic flops, which
+    the BF16x3 emulation executes as 6 piece products each, at the bf16 peak
+    (FF; GPP at large ngpown).  A tensor-bound frac is algorithmic flops over
+    the bf16 peak, so 1/6 is the emulation's ceiling."""
     t = kms * 1e-3 if kms and kms > 0 else None
     common = {"kernel": "contraction", "algorithmic_bytes": byts, "algorithmic_flops": flops,
               "traffic": measured_traffic(w) if prec == "mixed" else None,
               "launches_per_call": launches, "duration_ms": kms / launches if kms and launches else None}
-    if w["kind"] == "ff" and prec == "mixed":
+    # the bound is whichever floor is higher: the algorithmic bytes at the copy peak, or the
+    # executed BF16 piece products (6 per complex MAC's worth of flops) at the bf16 peak
+    hbm_floor = byts / (peaks.get("hbm_gbs", 6800.0) * 1e9)
+    tensor_floor = 6 * flops / (peaks.get("bf16_tflops", 1900.0) * 1e12)
+    if prec == "mixed" and tensor_floor > hbm_floor:
         peak = peaks.get("bf16_tflops", 1900.0)
         ach = flops / t / 1e12 if t else None
         return dict(common, bound="tensor", achieved=ach, peak=peak, unit="TFLOP/s", frac=ach / peak if ach else None,
