@@ -245,6 +245,24 @@ def measured_traffic(w):
         return None
 
 
+def max_over_ranks(x: float, device=None) -> float:
+    """The largest of every rank's x (x itself when not distributed).  The
+    ranks are independent replicas (no data-path collective): this and the
+    barriers around the timed region are the only cross-rank communication."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world: int, units_per_rank: float, seconds: float) -> float:
+    """Whole-job throughput: the units every rank processed over the slowest rank's time."""
+    return world * units_per_rank / seconds
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -432,11 +450,7 @@ def run_ours(a, w):
         per = timed(torch, stream, lambda: call(prec), a.steps, 0, per_step=False)
         torch.cuda.nvtx.range_pop()
         barrier()
-    ms = per[0]
-    if world > 1:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(per[0], f"cuda:{local}")
     launches = ctx.last_launches()
     # per-step latency distribution (events around each call)
     lat = timed(torch, stream, lambda: call(prec), a.steps, 1, per_step=True)
@@ -477,11 +491,7 @@ def run_ours(a, w):
     for _ in range(ke):
         host_call(prec, hp)
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / ke
-    if world > 1:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / ke, f"cuda:{local}")
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
         cpu = cpu_baseline(fk, w, p)
@@ -496,18 +506,18 @@ def run_ours(a, w):
         kms = kernel_ms
         T = terms(w)
         line = {
-            "metric": METRIC, "value": world * T / (ms * 1e-3), "unit": "terms/s", "n_gpus": world,
+            "metric": METRIC, "value": job_value(world, T, ms * 1e-3), "unit": "terms/s", "n_gpus": world,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64 in / fp32 bulk + fp64 branch/reductions" if prec == "mixed" else "f64",
             "data": "synthetic (seeded, benchmark value distributions)", "config": workload_config(a, w),
             "precision": prec,
-            "fp64_value" if prec == "mixed" else "mixed_value": world * T / (ms_other * 1e-3),
+            "fp64_value" if prec == "mixed" else "mixed_value": job_value(world, T, ms_other * 1e-3),
             "mixed_vs_fp64": (ms_other / ms) if prec == "mixed" else (ms / ms_other),
             "rel_err_mixed_vs_fp64": errs,
             "latency_ms": {"p50": statistics.median(lat), "p99": float(np.percentile(lat, 99))},
             "phase_ms": {"staging": phase[0], "prep": phase[1], "contraction": phase[2], "reduction": phase[3]},
             "roofline": roofline(w, prec, byts, flops, kms, kernel_launches, peaks),
-            "e2e": {"value": world * T / e2e_s, "unit": "terms/s", "h2d_bytes_per_step": h2d,
+            "e2e": {"value": job_value(world, T, e2e_s), "unit": "terms/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
             "gpu_launches": launches * a.steps,
             "clocks": clk.summary(),
