@@ -88,6 +88,23 @@ FK_DEV double2 ordered_sum(const double2* x, long stride, int n) {
     return s;
 }
 
+// The same left-to-right sum with every load of up to 16 terms issued before
+// the first add (one memory round trip for short sums).
+FK_DEV double2 ordered_sum16(const double2* x, long stride, int n) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int i0 = 0; i0 < n; i0 += 16) {
+        double2 v[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = i0 + j < n ? x[(long)(i0 + j) * stride] : make_double2(0.0, 0.0);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            if (i0 + j >= n) break;
+            s = cadd(s, v[j]);
+        }
+    }
+    return s;
+}
+
 // --------------------------------------------- compensated FP32 accumulation
 // float-float (hi, lo) accumulator updated with Knuth's TwoSum: exact sum of
 // the running value and the incoming FP32 block sum, error kept in lo.

@@ -80,6 +80,7 @@ struct PrepArgs {
     float2* W;            // [ng][M] 0.5*vcoul*conj(aqsm[nv+m][igp]) in FP32, or nullptr
     int M;
     int* counter;
+    double2* wf;          // [nv][ng][2] flag-band weights (sch: 0.5*vcoul*conj(aqsm), ssx: occ*vcoul*conj(aqsm)), or nullptr
 };
 
 // The set-up work of block (ch, my_igp) other than the image padding.
@@ -93,6 +94,18 @@ FK_DEV int prep_setup(const PrepArgs& p, int ch, int my_igp) {
             p.acol_out[my_igp] = acol;
             if (my_igp == 0 && p.counter) *p.counter = 0;
         }
+        if (p.wf)
+            for (int n1 = threadIdx.x; n1 < p.nv; n1 += blockDim.x) {
+                double2 a = make_double2(0.0, 0.0), b = a;
+                if (igp >= 0) {
+                    const double2 cm = cconj(p.aqsm[(long)n1 * p.ldm + acol]);
+                    const double occ = 1.0;
+                    a = cscale(cm, 0.5 * p.vcoul[igp]);
+                    b = cscale(cm, occ * p.vcoul[igp]);
+                }
+                p.wf[((long)n1 * p.ng + my_igp) * 2 + 0] = a;
+                p.wf[((long)n1 * p.ng + my_igp) * 2 + 1] = b;
+            }
         if (p.W)
             for (int m = threadIdx.x; m < p.M; m += blockDim.x)
                 p.W[(long)my_igp * p.M + m] =
@@ -753,6 +766,7 @@ struct RowsArgs {
     // totals folded in: the last block to finish (counter, zero at entry) writes out
     int* counter;
     double2* out;
+    const double2* wf;    // flag-band weights from the prep ([nv][ng][2]), or nullptr
 };
 
 FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
@@ -793,6 +807,14 @@ FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
             const double2 cm = cconj(aqsm[(long)n1 * ldm + acol[h]]);
             v = cadd(v, cscale(cadd(cmul(cm, s1), cconj(cmul(cm, s2))), kind ? occ * vcoul[g] : 0.5 * vcoul[g]));
         }
+    } else if (ra.wf) {
+        // weights from the prep; the chunk sums' loads all in flight at once
+        const int kind = c / 3, r = (c % 3) * 2 + kind;  // kind 0: sch, 1: ssx
+        for (int h = lane; h < ng; h += 32) {
+            const double2 w = ra.wf[((long)n1 * ng + h) * 2 + kind];
+            const double2 sum = ordered_sum16(F + ((long)n1 * ng + h) * 6 + r, (long)nv * ng * 6, nch);
+            v = cadd(v, cmul(w, sum));
+        }
     } else {
         const int kind = c / 3, r = (c % 3) * 2 + kind;  // kind 0: sch, 1: ssx
         const double occ = 1.0;
@@ -816,11 +838,15 @@ __global__ void rows_kernel(RowsArgs ra) {
     const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (w < (long)ra.nb * 7) rows_warp(ra, (int)(w / 7), (int)(w % 7), threadIdx.x & 31);  // w is warp-uniform
     if (!ra.counter) return;
-    // the last block to finish adds the bands (fixed order, as totals_kernel)
+    // the last block to finish adds the bands (fixed order, as totals_kernel):
+    // the barrier orders the block's row writes before thread 0's device-scope
+    // fence and count, as in a grid-wide barrier
     __shared__ int last;
-    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(ra.counter, 1) == (int)gridDim.x - 1;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(ra.counter, 1) == (int)gridDim.x - 1;
+    }
     __syncthreads();
     if (!last) return;
     __threadfence();
@@ -1262,7 +1288,8 @@ __global__ void real_out_kernel(int nb, const double2* outc, double* out) {
 size_t gpp_workspace(const Ctx& c, const GppDev& r, bool pipelined) {
     Plan p = make_plan(c, r, 0, pipelined);
     const size_t half = (r.flags & FK_GPP_HALF_SUM) ? p.bytesP + (size_t)r.ng * (4 + 3 * sizeof(double2)) + 768 : 0;
-    return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesRows + p.bytesIgp + p.bytesW + half + 11 * 256;
+    const size_t wf = (size_t)r.nv * r.ng * 2 * sizeof(double2);
+    return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesRows + p.bytesIgp + p.bytesW + half + wf + 12 * 256;
 }
 
 int gpp_pipe_chunks(const Ctx& c, const GppDev& r) { return make_plan(c, r, 0, true).pipe_chunks; }
@@ -1402,8 +1429,9 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
     double2* rows = (double2*)c.ws.take(p.bytesRows);
     float2* W = p.bytesW ? (float2*)c.ws.take(p.bytesW) : nullptr;
     int* counter = (int*)c.ws.take(sizeof(int));
+    double2* wf = r.nv > 0 ? (double2*)c.ws.take((size_t)r.nv * r.ng * 2 * sizeof(double2)) : nullptr;
     if (!igp || !F || !rows || !counter || (p.bytesD && !D) || (p.bytesP && !P) || (p.bytesS && !S) ||
-        (p.bytesW && !W))
+        (p.bytesW && !W) || (r.nv > 0 && !wf))
         return fail(c, FK_ENOMEM, "workspace too small for GPP request");
     if (p.mixed && D) {
         cudaError_t e = cudaMemsetAsync(c.errword, 0, sizeof(int), st);  // bounded-wait status
@@ -1426,6 +1454,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
             a.W = (p.mixed && M > 0) ? W : nullptr;
             a.M = M;
             a.counter = counter;
+            a.wf = wf;
         }
         return a;
     };
@@ -1542,6 +1571,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
     RowsArgs ra{r.nb, r.nv, r.ng, p.KS * p.NT, P, p.KSs * p.NTs, S, p.nch, F, r.ldm, r.aqsm, r.vcoul, igp, acol, rows};
     ra.counter = counter;  // the last block also writes the totals
     ra.out = r.out;
+    ra.wf = wf;
     rows_kernel<<<ceil_div(r.nb * 7, 8), 256, 0, st>>>(ra);
     ++c.launches;
     phase_mark(c, 4);
