@@ -441,7 +441,7 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
             constexpr size_t smem = tcx::Cfg<64, true>::SMEM;
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             kernel_begin(c);
-            k<<<grid1, tcx::THREADS, smem, st>>>(t);
+            k<<<grid1, tcx::THREADS_FF, smem, st>>>(t);
             kernel_end(c);
             c.launches += 2;
         } else {

@@ -37,31 +37,33 @@ constexpr int BM = 128;
 constexpr int BK = 32;            // complex k-values per stage (64 B of bf16 per row)
 constexpr int NSPLIT = 3;         // bf16 pieces per real value
 constexpr int NSUB = 2 * NSPLIT;  // sub-tiles per operand: re h/m/l, im h/m/l
-constexpr int THREADS = 448;
-// FF (A operand pre-split, no converter work): the 12 warps 2..13 all drain
-// TMEM, three per lane quarter, each over its own 16-column groups and its
-// own partial-sum slot; GPP: warps 4..7, one per quarter, all columns.
-constexpr int FF_EPI_WARPS = 3;
+constexpr int THREADS = 448;     // GPP: MMA, producer, 8 converter warps, 4 epilogue warps
+constexpr int THREADS_FF = 576;  // FF: MMA, producer, 16 epilogue warps
+// FF (A operand pre-split, no converter work): the 16 warps 2..17 all drain
+// TMEM, four per lane quarter, each over one 16-column group with its own
+// weights in registers and its own partial-sum slot; GPP: warps 4..7, one per
+// quarter, all columns.
+constexpr int FF_EPI_WARPS = 4;
 constexpr int NCONV = 8;          // converter warps
 constexpr long long WAIT_LIMIT = 4000000000LL;  // ~2 s at 2 GHz
 
 template <int BN, bool WSMEM = false>
 struct Cfg {
     static_assert(BN == 64, "four accumulators x two buffers fill the 512 TMEM columns at BN = 64");
-    // Two operand stages.  WSMEM (FF): the per-unit weight tile conj(aqsm)[BN][BM]
-    // lives in shared memory.  Otherwise (GPP) a 64 KB staging buffer receives
+    // Operand stages: FF three (its epilogue keeps the per-unit weights in
+    // registers, so shared memory holds operands only), GPP two.  GPP: a 64 KB staging buffer receives
     // FP64 A rows by TMA in two halves of BK/2 k-values, so that one half is in
     // flight while the converters read the other.  (Two full stagings do not fit
     // beside two operand stages; one operand stage with two stagings measured
     // slower: the converters then wait for each stage's MMAs.)
-    static constexpr int STAGES = 2;
+    static constexpr int STAGES = WSMEM ? 3 : 2;
     static constexpr int CHUNK_STAGES = 1;  // k-values per TMEM accumulation = 32
     static constexpr uint32_t A_BYTES = NSUB * BM * 64;
     static constexpr uint32_t B_BYTES = NSUB * BN * 64;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
     static constexpr uint32_t ACC_COLS = 4 * BN;       // X = A_re x [B_re|B_im], Y = A_im x [B_re|B_im]
     static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;  // double buffered
-    static constexpr uint32_t W_BYTES = WSMEM ? (uint32_t)(BN * BM * sizeof(float2) + 4 * BN * sizeof(float)) : 0u;
+    static constexpr uint32_t W_BYTES = 0u;
     static constexpr uint32_t F64_BYTES = WSMEM ? 0u : (uint32_t)(BM * BK * sizeof(double2));
     static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + W_BYTES + F64_BYTES + 1024 + 256;
 };
@@ -177,8 +179,6 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-aligned operand area
     uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    float2* sW = (float2*)(base + C::STAGES * C::STAGE_BYTES);  // FF: [BN][BM] conj(aqsm)
-    float* sV = (float*)(sW + BN * BM);                           // FF: vcoul[BN], one copy per epilogue warp
     double2* sF = (double2*)(base + C::STAGES * C::STAGE_BYTES + C::W_BYTES);  // GPP: FP64 rows [BM][BK]
     uint64_t* bars = (uint64_t*)(base + C::STAGES * C::STAGE_BYTES + C::W_BYTES + C::F64_BYTES);
     uint64_t* fullA = bars;
@@ -360,15 +360,14 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
         }
     } else if ((warp >= 4 && warp < 8) || AIMG) {
         // ------------------------------------------------------- epilogue
-        // Weights are fetched once per unit: GPP into registers (a 64-wide
-        // tile holds complete (igp, iw) triples of GPP_COLS igp), FF into a
-        // column-major shared-memory tile.  Columns are fully unrolled so every
-        // register index is a compile-time constant.
+        // Weights are fetched once per unit into registers: GPP all 64
+        // columns of the row (a 64-wide tile holds complete (igp, iw) triples
+        // of GPP_COLS igp), FF the warp's 16 columns (and their vcoul).
+        // Columns are fully unrolled so every register index is a compile-time
+        // constant.
         constexpr int EW = AIMG ? FF_EPI_WARPS : 1;  // warps per lane quarter
         const int q4 = warp & 3;                     // TMEM lane quarter
-        const int ej = warp < 4 ? 2 : (warp < 8 ? 0 : (warp < 12 ? 1 : 2));  // this warp's share
-        // 16-column groups of this warp: all for GPP; FF: {0, 3}, {1}, {2}
-        auto mine = [&](int grp) { return EW == 1 || (ej == 0 ? (grp == 0 || grp == 3) : grp == ej); };
+        const int ej = AIMG ? (warp - 2) >> 2 : 0;   // FF: this warp's 16-column group
         const int row = q4 * 32 + lane;
         int chunk = 0;
         bool ok = true;
@@ -383,7 +382,8 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
             const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
             const int m = mt * BM + row;
             const int mc = min(m, a.M - 1);
-            float2 wreg[EPI == EPI_GPP ? GC : 1];
+            float2 wreg[EPI == EPI_GPP ? GC : 16];
+            float vreg[EPI == EPI_GPP ? 1 : 16];
             if (EPI == EPI_GPP) {
 #pragma unroll
                 for (int i = 0; i < GC; ++i) {
@@ -391,21 +391,13 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                     wreg[i] = (i < t.gpp_cols && h < a.N / 3) ? t.W1[(long)h * t.ldw + mc] : make_float2(0.f, 0.f);
                 }
             } else {
-                // each thread stages its own row of conj(aqsm) (only it reads
-                // that row, so no barrier is needed); each warp its own vcoul copy
-                __syncwarp();
-#pragma unroll 4
-                for (int c = 0; c < BN; ++c) {
-                    if (!mine(c >> 4)) continue;
-                    const int n = nt * BN + c;
-                    sW[c * BM + row] = (n < a.N && m < a.M) ? t.W2[(long)n * t.ldw + m] : make_float2(0.f, 0.f);
+                // conj(aqsm) of this thread's row and vcoul of the warp's 16 columns
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int n = nt * BN + ej * 16 + j;
+                    wreg[j] = (n < a.N && m < a.M) ? t.W2[(long)n * t.ldw + m] : make_float2(0.f, 0.f);
+                    vreg[j] = n < a.N ? t.vcol[n] : 0.f;
                 }
-                for (int c = lane; c < BN; c += 32) {
-                    if (!mine(c >> 4)) continue;
-                    const int n = nt * BN + c;
-                    sV[q4 * BN + c] = n < a.N ? t.vcol[n] : 0.f;
-                }
-                __syncwarp();
             }
             // per-unit sums as FP32 float-float pairs (TwoSum): no FP64 instruction per drain
             // (GB300's FP64 pipe takes ~16 cycles per warp instruction); widened once per unit
@@ -420,9 +412,37 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                 tc::tc_fence_after();
                 const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * C::ACC_COLS);
                 float2 gsum[GMAX] = {make_float2(0, 0), make_float2(0, 0), make_float2(0, 0)};
+                if (EPI == EPI_FF) {
+                    // the warp's 16 columns in two halves of 8 (X = [A_re B_re | A_re B_im],
+                    // Y = [A_im B_re | A_im B_im]); the group's FP32 sums go to float-float once
+                    const int c0 = ej * 16;
 #pragma unroll
-                for (int c0 = 0; c0 < BN; c0 += 16) {
-                    if (!mine(c0 >> 4)) continue;
+                    for (int hh = 0; hh < 2; ++hh) {
+                        float xr[8], xi[8], yr[8], yi[8];
+                        tc::tmem_ld8(tl + c0 + 8 * hh, xr);
+                        tc::tmem_ld8(tl + BN + c0 + 8 * hh, xi);
+                        tc::tmem_ld8(tl + 2 * BN + c0 + 8 * hh, yr);
+                        tc::tmem_ld8(tl + 3 * BN + c0 + 8 * hh, yi);
+                        tc::tmem_ld_wait();
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const float2 sv = make_float2(xr[j] - yi[j], xi[j] + yr[j]);
+                            const float2 t2 = cmulf(wreg[8 * hh + j], sv);
+                            const float v = vreg[8 * hh + j];
+                            gsum[0].x = fmaf(v, t2.x, gsum[0].x);
+                            gsum[0].y = fmaf(v, t2.y, gsum[0].y);
+                            gsum[1].x += t2.x;
+                            gsum[1].y += t2.y;
+                        }
+                    }
+                    for (int gg = 0; gg < 2; ++gg) {
+                        ff_add(accx[gg], gsum[gg].x);
+                        ff_add(accy[gg], gsum[gg].y);
+                        gsum[gg] = make_float2(0.f, 0.f);
+                    }
+                }
+#pragma unroll
+                for (int c0 = 0; c0 < BN && EPI == EPI_GPP; c0 += 16) {
                     // X = [A_re B_re | A_re B_im], Y = [A_im B_re | A_im B_im]
                     float xr[16], xi[16], yr[16], yi[16];
                     tc::tmem_ld16(tl + c0, xr);
@@ -434,26 +454,8 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                     for (int j = 0; j < 16; ++j) {
                         const int c = c0 + j;
                         const float2 sv = make_float2(xr[j] - yi[j], xi[j] + yr[j]);
-                        if (EPI == EPI_GPP) {
-                            // tile column c = 3*(igp offset) + iw; column 63 is padding
-                            if (c < 3 * GC) cfmaf(gsum[c % 3], wreg[c / 3], sv);
-                        } else {
-                            const float2 w2 = sW[c * BM + row];
-                            const float2 t2 = cmulf(w2, sv);
-                            const float v = sV[q4 * BN + c];
-                            gsum[0].x = fmaf(v, t2.x, gsum[0].x);
-                            gsum[0].y = fmaf(v, t2.y, gsum[0].y);
-                            gsum[1].x += t2.x;
-                            gsum[1].y += t2.y;
-                        }
-                    }
-                    if (EPI == EPI_FF) {
-                        // keep FP32 column sums short: fold every 16-column group into FP64
-                        for (int gg = 0; gg < 2; ++gg) {
-                            ff_add(accx[gg], gsum[gg].x);
-                            ff_add(accy[gg], gsum[gg].y);
-                            gsum[gg] = make_float2(0.f, 0.f);
-                        }
+                        // tile column c = 3*(igp offset) + iw; column 63 is padding
+                        if (c < 3 * GC) cfmaf(gsum[c % 3], wreg[c / 3], sv);
                     }
                 }
                 tc::tc_fence_before();
@@ -562,13 +564,13 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
 }
 
 template <int EPI, int BN, bool AIMG>
-__global__ void __launch_bounds__(THREADS, 1) tc_contract_kernel(const __grid_constant__ TcArgs t) {
+__global__ void __launch_bounds__(AIMG ? THREADS_FF : THREADS, 1) tc_contract_kernel(const __grid_constant__ TcArgs t) {
     tc_contract_body<EPI, BN, AIMG>(OneReq{t}, t.err);
 }
 
 // Units of several requests from a device table (the served step).
 template <int EPI, int BN, bool AIMG>
-__global__ void __launch_bounds__(THREADS, 1) tc_contract_table_kernel(const TcTable* tab, int* err) {
+__global__ void __launch_bounds__(AIMG ? THREADS_FF : THREADS, 1) tc_contract_table_kernel(const TcTable* tab, int* err) {
     tc_contract_body<EPI, BN, AIMG>(TableReqs{tab, 0}, err);
 }
 
