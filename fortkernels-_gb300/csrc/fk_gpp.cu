@@ -367,12 +367,10 @@ FK_DEV void half_flag_terms(double wxt, double2 wt, double2 eps, double2& sch, d
     }
 }
 
-// Prep of the half sum, FP64 arithmetic for both precisions: D' as FP64 rows
-// (IMG = 0) or as the pre-split BF16 image of the tensor-core contraction
-// (IMG = 1); flag bands n1base .. n1base+NVC-1 accumulate, per (iw, sch/ssx),
-// S1 = sum_ig aqsn[n1][ig] x and S2 = sum_ig aqsm[n1][ig] x (S2 without
-// ig = igp-1) over ig < brk: F[ch][n1][my_igp][12], entry ((iw*2 + kind)*2 + part).
-template <int IMG>
+// Prep of the half sum, FP64 path: D' as FP64 rows; flag bands n1base ..
+// n1base+NVC-1 accumulate, per (iw, sch/ssx), S1 = sum_ig aqsn[n1][ig] x and
+// S2 = sum_ig aqsm[n1][ig] x (S2 without ig = igp-1) over ig < brk:
+// F[ch][n1][my_igp][12], entry ((iw*2 + kind)*2 + part).
 __global__ void __launch_bounds__(PREP_THREADS) prep_half_kernel(PrepArgs p) {
     __shared__ double2 sm[8 * NVC * 12];
     const int my_igp = blockIdx.y, ch = p.ch0 + blockIdx.x, tid = threadIdx.x;
@@ -391,13 +389,7 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_half_kernel(PrepArgs p) {
             const double wxt = p.wx[iw];
             if (p.D) {
                 const double2 dv = (igp >= 0 && half_member(ig, igp)) ? half_sch(wxt, wt, ep) : make_double2(0.0, 0.0);
-                if (IMG) {
-                    const int nt = my_igp / GPP_COLS, row = (my_igp % GPP_COLS) * 3 + iw;
-                    tcx::bimg_store<64>((uint8_t*)p.D + (long)nt * p.kstages * tcx::Cfg<64>::B_BYTES, p.kstages, row,
-                                        ig, f64_to_f32_bits(dv.x), f64_to_f32_bits(dv.y));
-                } else {
-                    ((double2*)p.D)[((long)my_igp * 3 + iw) * p.nc + ig] = dv;
-                }
+                ((double2*)p.D)[((long)my_igp * 3 + iw) * p.nc + ig] = dv;
             }
             if (nflag > 0 && ig < stop) {
                 double2 sch, ssx;
@@ -426,7 +418,7 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_half_kernel(PrepArgs p) {
     }
 }
 
-// Mixed-precision prep of the half sum: the same outputs as prep_half_kernel<1>
+// Mixed-precision prep of the half sum: prep_half_kernel's outputs, D' as the pre-split image,
 // with the branch quantities in FP32 from an FP64 wx - wtilde; inside a relative
 // guard band of 1e-5 around a threshold (or outside FP32's comfortable range)
 // the FP64 sequence decides and supplies the values, so every branch is the
@@ -838,7 +830,7 @@ __global__ void rows_kernel(RowsArgs ra) {
     const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (w < (long)ra.nb * 7) rows_warp(ra, (int)(w / 7), (int)(w % 7), threadIdx.x & 31);  // w is warp-uniform
     if (!ra.counter) return;
-    // the last block to finish adds the bands (fixed order, as totals_kernel):
+    // the last block to finish adds the bands (totals_block, fixed order):
     // the barrier orders the block's row writes before thread 0's device-scope
     // fence and count, as in a grid-wide barrier
     __shared__ int last;
@@ -867,7 +859,6 @@ FK_DEV void totals_block(int nb, const double2* rows, double2* out) {
     for (int r = threadIdx.x; r < nb; r += blockDim.x) out[7 + r] = rows[(long)r * 8 + 2];  // acht_n1_loc
 }
 
-__global__ void totals_kernel(int nb, const double2* rows, double2* out) { totals_block(nb, rows, out); }
 
 struct Plan {
     int nch, tile, passes;
@@ -1364,7 +1355,7 @@ fk_status gpp_run_half(Ctx& c, const GppDev& r) {
         PrepArgs a{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, (pass == 0 && M > 0) ? D : nullptr,
                    p.kstages, F, p.nch, p.tile, pass * NVC, 0, r.aqsm, brk};
         if (p.mixed) prep_half_mixed_kernel<<<dim3(p.nch, r.ng), PREP_THREADS, 0, st>>>(a);
-        else prep_half_kernel<0><<<dim3(p.nch, r.ng), PREP_THREADS, 0, st>>>(a);
+        else prep_half_kernel<<<dim3(p.nch, r.ng), PREP_THREADS, 0, st>>>(a);
         ++c.launches;
     }
     phase_mark(c, 2);

@@ -15,11 +15,15 @@
 // so their truncation is negligible), and all four are drained into the
 // FP64 epilogue every CHUNK_STAGES*32 k-values.
 //
-// CTA organisation (one persistent CTA per SM, 448 threads):
+// CTA organisation (one persistent CTA per SM):
 //   warp 0      TMEM allocation, MMA issue (one lane)
-//   warp 1      bulk copies of the pre-split B tiles (one lane)
-//   warps 4..7  epilogue: TMEM lanes 0..127 = tile rows, weighted sums
-//   warps 2,3,8..13  converters: FP64 A rows -> swizzled BF16 pieces in smem
+//   warp 1      copies: pre-split B tiles (and FF's pre-split A tiles) by bulk
+//               copy, GPP's FP64 A rows by tensor-map TMA (one lane issues)
+//   GPP, 448 threads: warps 4..7 epilogue (TMEM lanes 0..127 = tile rows,
+//               weighted sums), warps 2,3,8..13 converters (FP64 A rows ->
+//               swizzled BF16 pieces in smem); two operand stages
+//   FF, 576 threads: warps 2..17 epilogue, one per (lane quarter, 16-column
+//               group), weights in registers; three operand stages
 // Work units are (m-tile, n-tile, k-slice, batch); CTA i takes units
 // i, i + gridDim.x, ...  Every wait is bounded; on timeout the CTA records
 // an error code and unwinds without further waits of unbounded length.
