@@ -425,7 +425,7 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
             if (tcx::img_needs_pad(64, r.ng, 0, r.nc))
                 tcx::img_pad_kernel<64><<<dim3(p.kstages, NTb, nb_), 256, 0, st>>>(img, NTb, p.kstages, r.ng, 0, r.nc);
             (void)img_bytes;
-            dim3 gconv(ceil_div(r.nc, 256), r.ng, nb_);
+            dim3 gconv(ceil_div(ceil_div(r.nc, 8), 256), r.ng, nb_);  // 8 k-values per thread
             tcx::bimg_convert_kernel<64><<<gconv, 256, 0, st>>>(eps, a.bstride, r.ng, r.nc, pls, p.kstages, img);
             tcx::TcArgs t{};
             t.c = a;

@@ -601,16 +601,44 @@ static __global__ void weight_table_kernel(int M, int m0, int ncols, const doubl
 }
 
 // FP64 planes [plane][rows][K] -> pre-split B images [plane][nt][kstage][NSUB][BN][64 B].
+// Each thread converts 8 consecutive k-values of one row: 128 contiguous
+// bytes in, one 16-byte swizzle chunk of each of the six pieces out (the
+// swizzle permutes whole 16-byte chunks).  Grid (ceil(K/8 / blockDim), rows, planes).
 template <int BN>
 __global__ void bimg_convert_kernel(const double2* src, long plane_stride, int rows, int K, const int* planes,
                                     int kstages, uint8_t* img) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x, n = blockIdx.y, b = blockIdx.z;
-    if (k >= K) return;
+    const int k0 = 8 * (blockIdx.x * blockDim.x + threadIdx.x), n = blockIdx.y, b = blockIdx.z;
+    if (k0 >= K) return;
     const int f = planes ? planes[b] : b;
-    const double2 v = src[(long)f * plane_stride + (long)n * K + k];
+    const double2* row = src + (long)f * plane_stride + (long)n * K;
     const int NT = (rows + BN - 1) / BN;
     uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * (long)Cfg<BN>::B_BYTES;
-    bimg_store<BN>(img_nt, kstages, n % BN, k, f64_to_f32_bits(v.x), f64_to_f32_bits(v.y));
+    if (k0 + 8 > K) {  // ragged end of the row: element by element
+        for (int k = k0; k < K; ++k)
+            bimg_store<BN>(img_nt, kstages, n % BN, k, f64_to_f32_bits(row[k].x), f64_to_f32_bits(row[k].y));
+        return;
+    }
+    uint32_t pk[6][4];  // piece (part + 2*level) x four bf16 pairs
+#pragma unroll
+    for (int j = 0; j < 8; j += 2) {
+        const double2 v0 = row[k0 + j], v1 = row[k0 + j + 1];
+        uint16_t h0, m0, l0, h1, m1, l1;
+        split3(f64_to_f32_bits(v0.x), h0, m0, l0);
+        split3(f64_to_f32_bits(v1.x), h1, m1, l1);
+        pk[0][j / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        pk[2][j / 2] = (uint32_t)m0 | ((uint32_t)m1 << 16);
+        pk[4][j / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+        split3(f64_to_f32_bits(v0.y), h0, m0, l0);
+        split3(f64_to_f32_bits(v1.y), h1, m1, l1);
+        pk[1][j / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        pk[3][j / 2] = (uint32_t)m0 | ((uint32_t)m1 << 16);
+        pk[5][j / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+    }
+    uint8_t* st = img_nt + (long)(k0 / BK) * (BN * NSUB * 64);
+    const uint32_t off = tc::sw64_offset(n % BN, k0 % BK);  // 16-byte aligned: k0 % 8 == 0
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+        *(uint4*)(st + q * BN * 64 + off) = make_uint4(pk[q][0], pk[q][1], pk[q][2], pk[q][3]);
 }
 
 // Zeros the image positions that no converter writes: rows past a tile's
