@@ -470,21 +470,16 @@ def run_ours(a, w):
     kernel_launches = kt[-1][1]
     # end to end through the C ABI with pinned host buffers
     hp = dict(p)
-    h2d = 0
     # arrays drawn on the GPU (config 4) go through host memory like the others
     keys_h = keys_c + [k for k, v in p.items() if type(v).__module__.startswith("torch")]
     for k in keys_h:
-        t = (p[k].cpu() if k not in keys_c else torch.from_numpy(np.ascontiguousarray(p[k]))).pin_memory()
-        hp[k] = t
-        n = t.numel() * t.element_size()
-        if w["kind"] == "gpp" and k == "aqsmtemp" and w["ng"] * 128 <= w["nc"] and not w.get("half"):
-            # the library reads only the ngpown igp columns of aqsmtemp (BGW-Kernels/gppKer.cpp:322-325),
-            # gathers them on the host and sends number_bands x ngpown values
-            n = w["nb"] * w["ng"] * t.element_size()
-        h2d += n
-    d2h = sum(v.numel() * v.element_size() for v in outs.values() if v is not None)
+        hp[k] = (p[k].cpu() if k not in keys_c else torch.from_numpy(np.ascontiguousarray(p[k]))).pin_memory()
     for _ in range(max(1, a.warmup)):
         host_call(prec, hp)
+    # the bytes a call moves over the host link, as the library counts them: a
+    # host array in full, except the parts the call reads (the igp columns of
+    # aqsmtemp, the FF frequency planes the request needs)
+    h2d, d2h = ctx.last_transfer()
     barrier()
     t0 = time.perf_counter()
     ke = max(3, min(a.steps, 10))

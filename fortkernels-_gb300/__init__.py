@@ -109,6 +109,12 @@ class Context:
         self._check(self.lib.fk_last_kernel_time(self.h, ctypes.byref(ms), ctypes.byref(n)), self.h)
         return float(ms.value), int(n.value)
 
+    def last_transfer(self):
+        """(host-to-device, device-to-host) bytes of the last gpp / gpp_real / ff call."""
+        h, d = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+        self._check(self.lib.fk_last_transfer(self.h, ctypes.byref(h), ctypes.byref(d)), self.h)
+        return int(h.value), int(d.value)
+
     # ------------------------------------------------------------------ GPP
     def gpp(self, p: dict, precision="fp64", flags: int = 0, out=None) -> dict:
         """GPP sum on the input dict (keys as in fortkernels_gb300.inputs)."""

@@ -24,7 +24,7 @@ FK_FF_SPLIT_ACHD = 0x4
 # Every symbol include/fk_abi.h declares.
 SYMBOLS = ("fk_create", "fk_destroy", "fk_set_stream", "fk_synchronize", "fk_reserve", "fk_strerror",
            "fk_last_error", "fk_version", "fk_gpp", "fk_ff", "fk_set_profiling", "fk_last_timings",
-           "fk_last_launches", "fk_last_kernel_time", "fk_gpp_static", "fk_gpp_real", "fk_server_create", "fk_server_destroy",
+           "fk_last_launches", "fk_last_kernel_time", "fk_last_transfer", "fk_gpp_static", "fk_gpp_real", "fk_server_create", "fk_server_destroy",
            "fk_server_resident_put", "fk_server_resident_evict", "fk_server_submit", "fk_server_wait",
            "fk_server_stats", "fk_server_tune")
 
@@ -103,6 +103,7 @@ def load(path: str = LIB_PATH):
     L.fk_last_launches.argtypes = [P]
     L.fk_last_kernel_time.restype = I
     L.fk_last_kernel_time.argtypes = [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int)]
+    L.fk_last_transfer.argtypes = [P, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong)]
     for name in SYMBOLS:
         f = getattr(L, name)
         if name not in ("fk_strerror", "fk_last_error", "fk_version"):

@@ -157,6 +157,7 @@ fk_status stage(Ctx& c, const std::vector<In*>& v) {
         cudaError_t e = cudaMemcpyAsync(d, i->user, i->bytes, i->dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                         c.stream);
         if (e != cudaSuccess) return cuda_fail(c, e, "staging copy");
+        if (!i->dev) c.h2d_bytes += i->bytes;
         i->d = d;
     }
     return FK_OK;
@@ -165,7 +166,10 @@ fk_status stage(Ctx& c, const std::vector<In*>& v) {
 // Copies out[off..off+n) to a caller pointer (host or device).
 fk_status deliver(Ctx& c, void* dst, const double2* out, size_t off, size_t n, bool& host_out) {
     if (!dst || n == 0) return FK_OK;
-    if (!is_device_ptr(dst)) host_out = true;
+    if (!is_device_ptr(dst)) {
+        host_out = true;
+        c.d2h_bytes += n * sizeof(double2);
+    }
     cudaError_t e = cudaMemcpyAsync(dst, out + off, n * sizeof(double2), cudaMemcpyDefault, c.stream);
     return e == cudaSuccess ? FK_OK : cuda_fail(c, e, "output copy");
 }
@@ -333,6 +337,13 @@ fk_status fk_last_timings(fk_ctx_t c, float ms[4]) {
 
 int fk_last_launches(fk_ctx_t c) { return c ? c->launches : -1; }
 
+fk_status fk_last_transfer(fk_ctx_t c, unsigned long long* h2d, unsigned long long* d2h) {
+    if (!c) return FK_EINVAL;
+    if (h2d) *h2d = c->h2d_bytes;
+    if (d2h) *d2h = c->d2h_bytes;
+    return FK_OK;
+}
+
 fk_status fk_last_kernel_time(fk_ctx_t c, float* ms, int* launches) {
     if (!c || !ms || !launches) return FK_EINVAL;
     *ms = c->kernel_ms;
@@ -407,17 +418,21 @@ fk_status gpp_host_pipelined(Ctx& x, GppDev r, const fk_c128* aqsmtemp, const fk
     phase_mark(x, 0);
     uint8_t* pb = (uint8_t*)pinned_buffer(x, pinned_bytes);  // waits until the last call's outputs were read
     if (!pb) return fail(x, FK_ENOMEM, "gpp: pinned staging");
-    if ((st = gpp_pipe_begin(x)) != FK_OK) return st;
+    if ((st = pipe_begin(x)) != FK_OK) return st;
     cudaStream_t cs = x.copy_stream;
     // 1. small inputs
     for (auto& q : sm)
-        if (!q.dev) std::memcpy(pb + q.off, q.user, q.bytes);
+        if (!q.dev) {
+            std::memcpy(pb + q.off, q.user, q.bytes);
+            x.h2d_bytes += q.bytes;
+        }
     if (packed && cudaMemcpyAsync(small_d, pb, packed, cudaMemcpyHostToDevice, cs) != cudaSuccess)
         return cuda_fail(x, cudaGetLastError(), "gpp: small inputs");
     // 2. eps and wtilde
     if (cudaMemcpyAsync(pipe.eps_d, I_eps_array, col, cudaMemcpyHostToDevice, cs) != cudaSuccess ||
         cudaMemcpyAsync(pipe.wt_d, wtilde_array, col, cudaMemcpyHostToDevice, cs) != cudaSuccess)
         return cuda_fail(x, cudaGetLastError(), "gpp: eps / wtilde");
+    x.h2d_bytes += 2 * col;
     // 3. aqsmtemp: its igp columns gathered on the host meanwhile (or the whole array)
     if (compact) {
         std::vector<int> invh, indh;
@@ -450,12 +465,14 @@ fk_status gpp_host_pipelined(Ctx& x, GppDev r, const fk_c128* aqsmtemp, const fk
         }
         if (cudaMemcpyAsync(small_d + aqm_off, pb + aqm_off, aqm_bytes, cudaMemcpyHostToDevice, cs) != cudaSuccess)
             return cuda_fail(x, cudaGetLastError(), "gpp: aqsmtemp columns");
+        x.h2d_bytes += aqm_bytes;
         r.aqsm = (const double2*)(small_d + aqm_off);
     } else if (aqm_dev) {
         r.aqsm = (const double2*)aqsmtemp;
     } else {
         if (cudaMemcpyAsync(aqsm_full, aqsmtemp, band, cudaMemcpyHostToDevice, cs) != cudaSuccess)
             return cuda_fail(x, cudaGetLastError(), "gpp: staging aqsmtemp");
+        x.h2d_bytes += band;
         r.aqsm = aqsm_full;
     }
     if (cudaEventRecord(x.pipe_ev[PIPE_READY], cs) != cudaSuccess)
@@ -471,6 +488,7 @@ fk_status gpp_host_pipelined(Ctx& x, GppDev r, const fk_c128* aqsmtemp, const fk
     // outputs through pinned memory
     double2* po = (double2*)(pb + out_off);
     cudaError_t e = cudaMemcpyAsync(po, out, outn * e16, cudaMemcpyDeviceToHost, x.stream);
+    x.d2h_bytes += outn * e16;
     if (e == cudaSuccess) e = cudaEventRecord(x.pinned_ev, x.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(x.stream);
     if (e != cudaSuccess) return cuda_fail(x, e, "gpp: synchronize");
@@ -501,6 +519,7 @@ fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsm
                  unsigned flags, fk_c128* achtemp, fk_c128* asxtemp, fk_c128* acht_n1_loc, fk_c128* achstemp) {
     if (!c) return FK_EINVAL;
     Ctx& x = *c;
+    x.h2d_bytes = x.d2h_bytes = 0;
     if (nb <= 0 || nc <= 0 || ng <= 0 || nv < 0 || nv > nb)
         return fk::fail(x, FK_EINVAL, "gpp: need number_bands, ncouls, ngpown > 0 and 0 <= nvband <= number_bands");
     if (!aqsmtemp || !aqsntemp || !I_eps_array || !wtilde_array || !vcoul || !inv_igp_index || !indinv ||
@@ -600,6 +619,7 @@ fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsm
     }
     auto enqueue = [&]() -> fk_status {
         x.ws.reset();
+        x.h2d_bytes = x.d2h_bytes = 0;
         double2* out = (double2*)x.ws.take(outn * sizeof(double2));
         fk::phase_mark(x, 0);
         fk_status st = fk::stage(x, ins);
@@ -651,6 +671,7 @@ fk_status fk_gpp_real(fk_ctx_t c, int nb, int nv, int nc, int ng, const double* 
                       unsigned flags, double* achtemp, double* asxtemp, double* acht_n1_loc) {
     if (!c) return FK_EINVAL;
     Ctx& x = *c;
+    x.h2d_bytes = x.d2h_bytes = 0;
     if (nb <= 0 || nc <= 0 || ng <= 0 || nv < 0 || nv > nb)
         return fk::fail(x, FK_EINVAL, "gpp_real: need number_bands, ncouls, ngpown > 0 and 0 <= nvband <= number_bands");
     if (!aqsmtemp || !aqsntemp || !I_eps_array || !wtilde_array || !vcoul || !inv_igp_index || !indinv ||
@@ -697,6 +718,7 @@ fk_status fk_gpp_real(fk_ctx_t c, int nb, int nv, int nc, int ng, const double* 
         if (e == cudaSuccess && (nc & 1))
             e = cudaMemset2DAsync(d + nc, lda * sizeof(double), 0, sizeof(double), nb, x.stream);
         if (e != cudaSuccess) return fk::cuda_fail(x, e, "gpp_real: staging aqsntemp");
+        if (!aqn_dev) x.h2d_bytes += (size_t)nb * nc * sizeof(double);
         r.aqsn = d;
     }
     r.aqsm = (const double*)aqm.d; r.eps = (const double*)eps.d; r.wt = (const double*)wt.d;
@@ -710,7 +732,10 @@ fk_status fk_gpp_real(fk_ctx_t c, int nb, int nv, int nc, int ng, const double* 
     } outs[3] = {{achtemp, 0, 3}, {asxtemp, 3, 3}, {acht_n1_loc, 6, (size_t)nb}};
     for (const Out& o : outs) {
         if (!o.dst) continue;
-        host_out = host_out || !fk::is_device_ptr(o.dst);
+        if (!fk::is_device_ptr(o.dst)) {
+            host_out = true;
+            x.d2h_bytes += o.n * sizeof(double);
+        }
         cudaError_t e = cudaMemcpyAsync(o.dst, out + o.off, o.n * sizeof(double), cudaMemcpyDefault, x.stream);
         if (e != cudaSuccess) return fk::cuda_fail(x, e, "gpp_real: output copy");
     }
@@ -732,6 +757,7 @@ fk_status fk_ff(fk_ctx_t c, int nb, int nv, int nc, int ng, int nf, int ne, cons
                 fk_c128* ach2Dtemp, fk_c128* schDt_matrix) {
     if (!c) return FK_EINVAL;
     Ctx& x = *c;
+    x.h2d_bytes = x.d2h_bytes = 0;
     if (nb <= 0 || nc <= 0 || ng <= 0 || nv < 0 || nv > nb || nf < 2 || ne < 1)
         return fk::fail(x, FK_EINVAL, "ff: need sizes > 0, nFreq >= 2, 0 <= nvband <= number_bands");
     if (ng > nc) return fk::fail(x, FK_EINVAL, "ff: ngpown cannot be greater than ncouls");
@@ -757,21 +783,90 @@ fk_status fk_ff(fk_ctx_t c, int nb, int nv, int nc, int ng, int nf, int ne, cons
     r.pref_zb = pref_zb; r.fmin = freqevalmin; r.fstep = freqevalstep; r.occ = occ;
     r.prec = precision; r.flags = flags;
     r.ekq = ekq; r.grid = dFreqGrid;  // host or device; only read by the planner
-    const size_t wsb = fk::ff_workspace(x, r);
+    // host I_epsR / I_epsA of a large request: streamed in plane groups while
+    // the groups already copied are being computed (fk::FfPipe)
+    const bool pipelined = !er.dev && !ea.dev && planes >= ((size_t)64 << 20) && !fk::capturing(x.stream);
+    const size_t wsb = fk::ff_workspace(x, r, pipelined);
     if (wsb == (size_t)-1) return fk::fail(x, FK_ECUDA, "ff: reading ekq/dFreqGrid");
     const size_t outn = 1 + 4 * (size_t)ne + (size_t)nb * nf;
-    const size_t need = fk::staged_bytes(ins) + wsb + outn * sizeof(double2) + 4096;
+    auto r256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    std::vector<fk::In*> small{&vc, &inv, &ind, &ek, &gr, &br, &pr}, bands{&aqm, &aqn};
+    size_t packed = 0;
+    for (auto* i : small)
+        if (!fk::in_place(i)) packed += r256(i->bytes);
+    const size_t need = (pipelined ? fk::staged_bytes(bands) + 2 * r256(planes) + r256(packed) : fk::staged_bytes(ins)) +
+                        wsb + outn * sizeof(double2) + 4096;
     fk_status s = fk::ensure_workspace(x, need);
     if (s != FK_OK) return s;
     x.ws.reset();
     double2* out = (double2*)x.ws.take(outn * sizeof(double2));
     fk::phase_mark(x, 0);
-    if ((s = fk::stage(x, ins)) != FK_OK) return s;
+    fk::FfPipe pipe{};
+    std::vector<double> ekq_h, grid_h;
+    if (!pipelined) {
+        if ((s = fk::stage(x, ins)) != FK_OK) return s;
+    } else {
+        // small inputs packed into pinned memory, then aqsmtemp and aqsntemp, on
+        // the copy stream ahead of the planes; the planner reads ekq and dFreqGrid on the host
+        pipe.ekq_h = ekq;
+        pipe.grid_h = dFreqGrid;
+        if (ek.dev || gr.dev) {
+            ekq_h.resize(nb);
+            grid_h.resize(nf);
+            if (cudaMemcpy(ekq_h.data(), ekq, nb * sizeof(double), cudaMemcpyDefault) != cudaSuccess ||
+                cudaMemcpy(grid_h.data(), dFreqGrid, nf * sizeof(double), cudaMemcpyDefault) != cudaSuccess)
+                return fk::cuda_fail(x, cudaGetLastError(), "ff: reading ekq/dFreqGrid");
+            pipe.ekq_h = ekq_h.data();
+            pipe.grid_h = grid_h.data();
+        }
+        pipe.epsR = (const double2*)I_epsR_array;
+        pipe.epsA = (const double2*)I_epsA_array;
+        pipe.epsR_d = (double2*)x.ws.take(planes);
+        pipe.epsA_d = (double2*)x.ws.take(planes);
+        uint8_t* small_d = packed ? (uint8_t*)x.ws.take(packed) : nullptr;
+        if (!out || !pipe.epsR_d || !pipe.epsA_d || (packed && !small_d)) return fk::fail(x, FK_ENOMEM, "workspace: pipeline");
+        uint8_t* pb = packed ? (uint8_t*)fk::pinned_buffer(x, packed) : nullptr;  // free once its last copy is done
+        if (packed && !pb) return fk::fail(x, FK_ENOMEM, "ff: pinned staging");
+        if ((s = fk::pipe_begin(x)) != FK_OK) return s;
+        cudaStream_t cs = x.copy_stream;
+        size_t off = 0;
+        for (auto* i : small) {
+            if (fk::in_place(i)) {
+                i->d = i->user;
+                continue;
+            }
+            std::memcpy(pb + off, i->user, i->bytes);
+            x.h2d_bytes += i->bytes;
+            i->d = small_d + off;
+            off += r256(i->bytes);
+        }
+        cudaError_t e = cudaSuccess;
+        if (packed) {
+            e = cudaMemcpyAsync(small_d, pb, packed, cudaMemcpyHostToDevice, cs);
+            if (e == cudaSuccess) e = cudaEventRecord(x.pinned_ev, cs);
+        }
+        for (auto* i : bands) {
+            if (e != cudaSuccess) break;
+            if (fk::in_place(i)) {
+                i->d = i->user;
+                continue;
+            }
+            void* d = x.ws.take(i->bytes);
+            if (!d) return fk::fail(x, FK_ENOMEM, "workspace: staging");
+            e = cudaMemcpyAsync(d, i->user, i->bytes, i->dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, cs);
+            if (!i->dev) x.h2d_bytes += i->bytes;
+            i->d = d;
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(x.pipe_ev[fk::PIPE_READY], cs);
+        if (e != cudaSuccess) return fk::cuda_fail(x, e, "ff: staging copies");
+        er.d = pipe.epsR_d;
+        ea.d = pipe.epsA_d;
+    }
     r.aqsm = (const double2*)aqm.d; r.aqsn = (const double2*)aqn.d;
     r.epsR = (const double2*)er.d; r.epsA = (const double2*)ea.d; r.brd = (const double2*)br.d;
     r.vcoul = (const double*)vc.d; r.ekq = (const double*)ek.d; r.grid = (const double*)gr.d;
     r.pref = (const double*)pr.d; r.inv = (const int*)inv.d; r.indinv = (const int*)ind.d; r.out = out;
-    if ((s = fk::ff_run(x, r)) != FK_OK) return s;
+    if ((s = fk::ff_run(x, r, pipelined ? &pipe : nullptr)) != FK_OK) return s;
     bool host_out = false;
     if ((s = fk::deliver(x, achsDtemp, out, 0, 1, host_out)) != FK_OK) return s;
     if ((s = fk::deliver(x, asxDtemp, out, 1, ne, host_out)) != FK_OK) return s;

@@ -266,6 +266,7 @@ void compute_fact(double wx, int nFreq, const double* g, double& fact1, double& 
 struct FfPlan {
     std::vector<FactRow> fact;
     std::vector<int> planesR, planesA;
+    int groupR, groupA;           // planes per copy group (pipelined requests; else all planes in one)
     int MT, NT, KS, kchunk;
     int BN, kstages;              // tensor-core path (mixed)
     bool mixed;
@@ -289,7 +290,9 @@ void ff_pick_split_tc(long tiles, int K, int sms, int& KS, int& kchunk) {
     KS = (K + kchunk - 1) / kchunk;
 }
 
-FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double* grid_h) {
+constexpr int FF_PIPE_GROUPS = 8;  // copy groups of a pipelined request at most (events 0..7 of Ctx::pipe_ev)
+
+FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double* grid_h, bool pipelined) {
     FfPlan p;
     p.mixed = r.prec == FK_MIXED;
     p.fact.resize(r.nb);
@@ -314,7 +317,20 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
         if (all || needR[f]) p.planesR.push_back(f);
         if (needA[f]) p.planesA.push_back(f);
     }
-    const int nplanes = std::max<int>(1, (int)p.planesR.size());
+    // copy groups: the R and A planes share FF_PIPE_GROUPS groups in proportion
+    // to their counts; each group is one contraction launch, so the k-split is
+    // chosen for a group's planes
+    const int nR = (int)p.planesR.size(), nA = (int)p.planesA.size();
+    p.groupR = std::max(nR, 1);
+    p.groupA = std::max(nA, 1);
+    if (pipelined) {
+        int gR = nR ? std::max(1, std::min(nR, (FF_PIPE_GROUPS * nR + (nR + nA) / 2) / (nR + nA))) : 0;
+        const int gA = nA ? std::max(1, std::min(nA, FF_PIPE_GROUPS - gR)) : 0;
+        gR = std::min(gR, FF_PIPE_GROUPS - gA);
+        if (nR) p.groupR = ceil_div(nR, gR);
+        if (nA) p.groupA = ceil_div(nA, gA);
+    }
+    const int nplanes = pipelined ? std::max(nR ? p.groupR : 1, nA ? p.groupA : 1) : std::max(nR, 1);
     p.bytesImgR = p.bytesImgA = p.bytesW = p.bytesAimg = 0;
     if (p.mixed) {
         p.BN = 64;
@@ -348,21 +364,28 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
 
 }  // namespace
 
-size_t ff_workspace(const Ctx& c, const FfDev& r) {
+size_t ff_workspace(const Ctx& c, const FfDev& r, bool pipelined) {
     std::vector<double> ekq(r.nb), grid(r.nf);
     if (cudaMemcpy(ekq.data(), r.ekq, r.nb * sizeof(double), cudaMemcpyDefault) != cudaSuccess ||
         cudaMemcpy(grid.data(), r.grid, r.nf * sizeof(double), cudaMemcpyDefault) != cudaSuccess)
         return (size_t)-1;
-    return make_plan(c, r, ekq.data(), grid.data()).bytes;
+    return make_plan(c, r, ekq.data(), grid.data(), pipelined).bytes;
 }
 
-fk_status ff_run(Ctx& c, const FfDev& r) {
-    std::vector<double> ekq(r.nb), grid(r.nf);
-    cudaError_t e = cudaMemcpyAsync(ekq.data(), r.ekq, r.nb * sizeof(double), cudaMemcpyDefault, c.stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(grid.data(), r.grid, r.nf * sizeof(double), cudaMemcpyDefault, c.stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
-    if (e != cudaSuccess) return cuda_fail(c, e, "ff: reading ekq/dFreqGrid");
-    const FfPlan p = make_plan(c, r, ekq.data(), grid.data());
+fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
+    std::vector<double> ekq, grid;
+    cudaError_t e = cudaSuccess;
+    if (!pipe) {
+        ekq.resize(r.nb);
+        grid.resize(r.nf);
+        e = cudaMemcpyAsync(ekq.data(), r.ekq, r.nb * sizeof(double), cudaMemcpyDefault, c.stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(grid.data(), r.grid, r.nf * sizeof(double), cudaMemcpyDefault, c.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "ff: reading ekq/dFreqGrid");
+    }
+    const FfPlan p = pipe ? make_plan(c, r, pipe->ekq_h, pipe->grid_h, true)
+                          : make_plan(c, r, ekq.data(), grid.data(), false);
     cudaStream_t st = c.stream;
     const int nR = (int)p.planesR.size(), nA = (int)p.planesA.size();
     const size_t slots = (size_t)p.KS * p.NT * (p.mixed ? tcx::FF_EPI_WARPS : 1);  // partial slots per plane
@@ -396,6 +419,33 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
     if (e == cudaSuccess) e = cudaMemsetAsync(tabs, 0, 3 * (size_t)r.nb * r.nf * sizeof(double2), st);
     if (e != cudaSuccess) return cuda_fail(c, e, "ff: tables");
     c.launches = 0;
+    // pipelined request: the planes each group reads, in runs of consecutive
+    // planes, on the copy stream; group q is followed by pipe_ev[q]
+    const int gR = nR ? ceil_div(nR, p.groupR) : 0, gA = nA ? ceil_div(nA, p.groupA) : 0;
+    if (pipe) {
+        const size_t plane = (size_t)r.ng * r.nc;
+        auto copy_group = [&](const std::vector<int>& pls, int i0, int i1, const double2* src, double2* dst, int q) {
+            cudaError_t ce = cudaSuccess;
+            for (int i = i0; i < i1 && ce == cudaSuccess;) {
+                int j = i + 1;
+                while (j < i1 && pls[j] == pls[j - 1] + 1) ++j;
+                const size_t off = (size_t)pls[i] * plane;
+                ce = cudaMemcpyAsync(dst + off, src + off, (size_t)(j - i) * plane * sizeof(double2),
+                                     cudaMemcpyHostToDevice, c.copy_stream);
+                c.h2d_bytes += (size_t)(j - i) * plane * sizeof(double2);
+                i = j;
+            }
+            if (ce == cudaSuccess) ce = cudaEventRecord(c.pipe_ev[q], c.copy_stream);
+            return ce;
+        };
+        for (int q = 0; q < gR && e == cudaSuccess; ++q)
+            e = copy_group(p.planesR, q * p.groupR, std::min(nR, (q + 1) * p.groupR), pipe->epsR, pipe->epsR_d, q);
+        for (int q = 0; q < gA && e == cudaSuccess; ++q)
+            e = copy_group(p.planesA, q * p.groupA, std::min(nA, (q + 1) * p.groupA), pipe->epsA, pipe->epsA_d,
+                           gR + q);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, c.pipe_ev[PIPE_READY], 0);
+        if (e != cudaSuccess) return cuda_fail(c, e, "ff: plane copies");
+    }
 
     phase_mark(c, 1);
     ff_igp_kernel<<<ceil_div(r.ng, 128), 128, 0, st>>>(r.ng, r.nc, r.inv, r.indinv, igp);
@@ -407,8 +457,10 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
                                                                                 (float*)(W + 2 * (size_t)r.nb * r.ng));
         // aqsntemp is reused by every (plane, n-tile): split it to BF16 pieces once
         const int MTa = ceil_div(r.nb, tcx::BM);
-        if (tcx::img_needs_pad(tcx::BM, r.nb, 0, r.nc))
+        if (tcx::img_needs_pad(tcx::BM, r.nb, 0, r.nc)) {
             tcx::img_pad_kernel<tcx::BM><<<dim3(p.kstages, MTa, 1), 256, 0, st>>>(Aimg, MTa, p.kstages, r.nb, 0, r.nc);
+            ++c.launches;
+        }
         tcx::aimg_convert_kernel<<<dim3(ceil_div(r.nc, 256), r.nb), 256, 0, st>>>(r.aqsn, r.nb, r.nc, p.kstages, Aimg);
         c.launches += 2;
         cudaMemsetAsync(c.errword, 0, sizeof(int), st);
@@ -422,8 +474,10 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
         if (p.mixed) {
             // pre-split B planes (bf16 x 3), then the tensor-core contraction
             const int NTb = ceil_div(r.ng, 64);
-            if (tcx::img_needs_pad(64, r.ng, 0, r.nc))
+            if (tcx::img_needs_pad(64, r.ng, 0, r.nc)) {
                 tcx::img_pad_kernel<64><<<dim3(p.kstages, NTb, nb_), 256, 0, st>>>(img, NTb, p.kstages, r.ng, 0, r.nc);
+                ++c.launches;
+            }
             (void)img_bytes;
             dim3 gconv(ceil_div(ceil_div(r.nc, 8), 256), r.ng, nb_);  // 8 k-values per thread
             tcx::bimg_convert_kernel<64><<<gconv, 256, 0, st>>>(eps, a.bstride, r.ng, r.nc, pls, p.kstages, img);
@@ -454,8 +508,24 @@ fk_status ff_run(Ctx& c, const FfDev& r) {
             ++c.launches;
         }
     };
-    if (nR) contract(r.epsR, planes, nR, PR, imgR, p.bytesImgR);
-    if (nA) contract(r.epsA, planes + nR, nA, PA, imgA, p.bytesImgA);
+    if (!pipe) {
+        if (nR) contract(r.epsR, planes, nR, PR, imgR, p.bytesImgR);
+        if (nA) contract(r.epsA, planes + nR, nA, PA, imgA, p.bytesImgA);
+    } else {
+        // one launch pair per copy group, each after its planes have landed;
+        // a group's partials and pre-split image sit at its batch offset
+        const size_t pslab = slots * r.nb * 2, islab = (size_t)p.NT * p.kstages * tcx::Cfg<64>::B_BYTES;
+        for (int q = 0; q < gR + gA; ++q) {
+            const bool isR = q < gR;
+            const int g0 = isR ? q * p.groupR : (q - gR) * p.groupA;
+            const int n = isR ? std::min(nR - g0, p.groupR) : std::min(nA - g0, p.groupA);
+            if (cudaStreamWaitEvent(st, c.pipe_ev[q], 0) != cudaSuccess)
+                return cuda_fail(c, cudaGetLastError(), "ff: pipeline wait");
+            uint8_t* img = isR ? imgR : imgA;
+            contract(isR ? r.epsR : r.epsA, planes + (isR ? 0 : nR) + g0, n, (isR ? PR : PA) + g0 * pslab,
+                     img ? img + g0 * islab : nullptr, 0);
+        }
+    }
     phase_mark(c, 3);
     if (nR) {
         ff_rows_kernel<<<dim3(ceil_div(r.nb, 128), nR), 128, 0, st>>>(r.nb, r.nf, nR, (int)slots, planes, PR, RW, RS);

@@ -1285,16 +1285,16 @@ size_t gpp_workspace(const Ctx& c, const GppDev& r, bool pipelined) {
 
 int gpp_pipe_chunks(const Ctx& c, const GppDev& r) { return make_plan(c, r, 0, true).pipe_chunks; }
 
-fk_status gpp_pipe_begin(Ctx& c) {
+fk_status pipe_begin(Ctx& c) {
     if (!c.copy_stream && cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking) != cudaSuccess)
-        return cuda_fail(c, cudaGetLastError(), "gpp: copy stream");
+        return cuda_fail(c, cudaGetLastError(), "pipeline: copy stream");
     for (auto& e : c.pipe_ev)
         if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
-            return cuda_fail(c, cudaGetLastError(), "gpp: pipeline events");
+            return cuda_fail(c, cudaGetLastError(), "pipeline: events");
     // the destinations are free once the work queued before this call is done
     cudaError_t e = cudaEventRecord(c.pipe_ev[PIPE_FREE], c.stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c.copy_stream, c.pipe_ev[PIPE_FREE], 0);
-    return e == cudaSuccess ? FK_OK : cuda_fail(c, e, "gpp: pipeline start");
+    return e == cudaSuccess ? FK_OK : cuda_fail(c, e, "pipeline: start");
 }
 
 fk_status gpp_pipe_copy(Ctx& c, const GppDev& r, const GppPipe* pipe, int q0, int q1) {
@@ -1308,6 +1308,7 @@ fk_status gpp_pipe_copy(Ctx& c, const GppDev& r, const GppPipe* pipe, int q0, in
                                         cudaMemcpyHostToDevice, c.copy_stream);
         if (e == cudaSuccess) e = cudaEventRecord(c.pipe_ev[q], c.copy_stream);
         if (e != cudaSuccess) return cuda_fail(c, e, "gpp: block copy");
+        c.h2d_bytes += (size_t)(r1 - r0) * rowb;
     }
     return FK_OK;
 }

@@ -44,6 +44,8 @@ struct Ctx {
     int nk = 0;                 // launches bracketed in the current call
     float kernel_ms = 0.f;      // their summed device time in the last profiled call
     int kernel_launches = 0;
+    // host-link bytes of the last fk_gpp / fk_gpp_real / fk_ff call
+    unsigned long long h2d_bytes = 0, d2h_bytes = 0;
     int* errword = nullptr;      // device error word of the tensor-core kernels (bounded waits)
     // Graphs of repeated fully device-resident calls: key -> (times seen, executable graph).
     struct GraphEntry {
@@ -86,13 +88,13 @@ struct GppPipe {
 size_t gpp_workspace(const Ctx& c, const GppDev& r, bool pipelined = false);
 // Pipelined calls: aqsntemp moves in row blocks (chunk 0: the flag bands and the
 // first block of m-tiles; then one block per chunk); gpp_pipe_chunks gives their
-// number; gpp_pipe_begin makes c.copy_stream wait for the work already queued on
+// number; pipe_begin makes c.copy_stream wait for the work already queued on
 // c.stream (the destinations' last users); gpp_pipe_copy queues the row blocks
 // [q0, q1) on c.copy_stream, each followed by its event.  The caller copies
 // eps, wtilde and the small inputs first and records pipe_ev[PIPE_READY].
 constexpr int PIPE_FREE = 8, PIPE_READY = 9;
 int gpp_pipe_chunks(const Ctx& c, const GppDev& r);
-fk_status gpp_pipe_begin(Ctx& c);
+fk_status pipe_begin(Ctx& c);
 fk_status gpp_pipe_copy(Ctx& c, const GppDev& r, const GppPipe* pipe, int q0, int q1);
 fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe = nullptr);
 
@@ -154,8 +156,19 @@ struct FfDev {
     // outputs (device): [achsDtemp | asx[ne] | achD[ne] | cor[ne] | a2[ne] | schDt[nb*nf]]
     double2* out;
 };
-size_t ff_workspace(const Ctx& c, const FfDev& r);
-fk_status ff_run(Ctx& c, const FfDev& r);
+// Host I_epsR / I_epsA arrays of an FF request streamed to the device in plane
+// groups on c.copy_stream, each group followed by its event (pipe_ev[0..7]);
+// the compute stream waits for pipe_ev[PIPE_READY] (the caller's copies of
+// aqsmtemp, aqsntemp and the small inputs) and then runs each group's
+// conversion and contraction as soon as that group has landed.  The device
+// arrays hold all nFreq planes; only the planes the request reads are copied.
+struct FfPipe {
+    const double2 *epsR, *epsA;      // host sources [nFreq][ngpown][ncouls]
+    double2 *epsR_d, *epsA_d;        // device destinations (r.epsR, r.epsA point at them)
+    const double *ekq_h, *grid_h;    // host copies of ekq and dFreqGrid (the planner reads them)
+};
+size_t ff_workspace(const Ctx& c, const FfDev& r, bool pipelined = false);
+fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe = nullptr);
 
 // Phase timing helpers (no-ops unless profiling is on).
 void phase_mark(Ctx& c, int i);

@@ -306,6 +306,12 @@ int fk_last_launches(fk_ctx_t ctx);
  * the milliseconds summed over its launches (CUDA events recorded on the
  * launch stream right before and after each launch) and their count. */
 fk_status fk_last_kernel_time(fk_ctx_t ctx, float* ms, int* launches);
+/* Bytes the most recent fk_gpp / fk_gpp_real / fk_ff call moved over the host
+ * link: its host inputs copied to the device (a host array is sent in full,
+ * except where the call reads a part of it: the igp columns of aqsmtemp,
+ * the frequency planes of I_epsR/I_epsA the request reads) and its outputs
+ * copied to host arrays.  Device arrays move nothing. */
+fk_status fk_last_transfer(fk_ctx_t ctx, unsigned long long* h2d, unsigned long long* d2h);
 
 #ifdef __cplusplus
 }

@@ -123,3 +123,28 @@ def test_ff_sigma_epilogue_at_scale(ctx, fk):
     torch.cuda.empty_cache()
     errs = {k: rel(res[k], ref[k]) for k in KEYS if np.max(np.abs(ref[k])) > 0}
     assert "achDtemp" in errs and all(e <= TOLMX for e in errs.values()), errs
+
+
+@pytest.mark.parametrize("flags", [0, 5], ids=["needed-planes", "schdt-split"])
+def test_ff_host_planes_streamed(ctx, fk, orc, flags):
+    """Host I_epsR / I_epsA of 168 MB each take the streamed path (plane groups
+    copied while earlier groups are contracted, only the planes the request
+    reads); the same inputs as device arrays take the staged path.  FP64: the
+    two within 1e-12 (the k-split differs, so the summation order does);
+    mixed streamed within 1e-6 of FP64."""
+    import torch
+    p = fk.inputs.ff_synthetic(96, 2, 4096, 256, 10, 6, seed=21)
+    assert p["I_epsR_array"].nbytes >= 64 << 20
+    d = dict(p)
+    for k in ("aqsmtemp", "aqsntemp", "I_epsR_array", "I_epsA_array"):
+        d[k] = torch.from_numpy(p[k]).cuda()
+    ref = ctx.ff(d, "fp64", flags)
+    check(ctx.ff(p, "fp64", flags), ref, TOL64)
+    sc = ff_scales(p, orc)
+    res = ctx.ff(p, "mixed", flags)
+    errs = {k: scaled_err(res[k], ref[k], sc[k]) for k in KEYS if k != "schDt_matrix" or flags & 1}
+    assert all(e <= TOLMX for e in errs.values()), errs
+    # repeated streamed calls give the same bits
+    again = ctx.ff(p, "mixed", flags)
+    for k in KEYS:
+        np.testing.assert_array_equal(again[k], res[k])
