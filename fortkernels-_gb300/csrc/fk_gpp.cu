@@ -822,41 +822,182 @@ FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
     const bool empty = (c == 6 && !S) || (n1 >= nv && c >= 3 && c < 6);
     if (!empty) v = warp_tree(v);
     if (lane == 0) rows[(long)n1 * 8 + c] = v;
+    if (lane == 0 && c == 2 && ra.out) ra.out[7 + n1] = v;  // acht_n1_loc
 }
 
-FK_DEV void totals_block(int nb, const double2* rows, double2* out);
+// Bands n1 >= nvband, one warp per band.  GB300's FP64 pipe retires one warp
+// instruction per 64 cycles on each SM sub-partition, whatever the
+// instruction-level parallelism, so the sums are laid out to need few FP64
+// warp instructions per warp: lane 5p + s (p < 6: component p/2, real or
+// imaginary part p%2; s < 5) adds slots s, s+5, s+10, .. of its part, and
+// four shuffles add the five splits; lanes 30 and 31 add the static
+// remainder's parts.  Blocks are four warps (four bands, one per
+// sub-partition); warp 0 then writes the block's partial totals (eight
+// parts: components 0..2 and 6), so the totals read one value per four bands.
+// The rows buffer is [nb][8] band rows, then [band blocks][8] partials.
+constexpr int ROWS_THREADS = 128;
+__host__ __device__ inline int rows_flag_blocks(int nv) { return (nv * 7 + 3) / 4; }
+__host__ __device__ inline int rows_band_blocks(int nb, int nv) { return (nb - nv + 3) / 4; }
+__host__ __device__ inline int rows_blocks(int nb, int nv) { return rows_flag_blocks(nv) + rows_band_blocks(nb, nv); }
+__host__ __device__ inline size_t rows_bytes(int nb) {
+    return ((size_t)nb * 8 + 4 * (size_t)((nb + 3) / 4)) * sizeof(double2);
+}
 
-__global__ void rows_kernel(RowsArgs ra) {
-    const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (w < (long)ra.nb * 7) rows_warp(ra, (int)(w / 7), (int)(w % 7), threadIdx.x & 31);  // w is warp-uniform
+FK_DEV double part_of(double2 v, int im) { return im ? v.y : v.x; }
+
+// sum over slots k = s, s+5, .. < nslots (ascending) of part im of P[k][m][c]
+FK_DEV double split_sum(const double2* P, long M, long m, int c, int im, int nslots, int s) {
+    double v = 0.0;
+    for (int k0 = s; k0 < nslots; k0 += 5 * 8) {
+        double a[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int k = k0 + 5 * i;
+            a[i] = k < nslots ? part_of(P[((long)k * M + m) * 3 + c], im) : 0.0;
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            if (k0 + 5 * i >= nslots) break;
+            v = __dadd_rn(v, a[i]);
+        }
+    }
+    return v;
+}
+
+FK_DEV void rows_band_warp(const RowsArgs& ra, int n1, int lane, double* parts) {
+    const long M = ra.nb - ra.nv, m = n1 - ra.nv;
+    const int p = lane / 5, s = lane % 5, c = p >> 1, im = p & 1;
+    double a = 0.0, b = 0.0, d = 0.0;  // this split's contraction sum, A = aqsmtemp sum, diagonal terms
+    if (lane < 30) {
+        if (!(ra.re_only && im)) a = split_sum(ra.P, M, m, c, im, ra.nslots, s);
+        if (ra.P2) {
+            // half sum: the A = aqsmtemp contraction and the diagonal terms of the
+            // columns on 512-wide block edges (split s: columns s, s+5, ..)
+            b = split_sum(ra.P2, M, m, c, im, ra.nslots, s);
+            for (int h = s; h < ra.ng; h += 5) {
+                const int g = ra.igp[h];
+                if (g <= 0 || (g & 511)) continue;
+                const double2 am = cmul(cconj(ra.aqsm[(long)n1 * ra.ldm + ra.acol[h]]), ra.aqsn[(long)n1 * ra.nc + g]);
+                d = __dadd_rn(d, part_of(cscale(cmul(am, ra.schd[h * 3 + c]), 0.5 * ra.vcoul[g]), im));
+            }
+        }
+    } else if (ra.S) {
+        // static remainder: lane 30 the real, lane 31 the imaginary part
+        for (int k = 0; k < ra.nslots_s; ++k) a = __dadd_rn(a, part_of(ra.S[(long)k * ra.nb + n1], lane - 30));
+    }
+    // lane 5p adds the other four splits of part p, in split order (the
+    // shuffles read the unmodified split sums a0, b0, d0)
+    const int base = (lane < 30 ? p : 0) * 5;
+    const double a0 = a, b0 = b, d0 = d;
+#pragma unroll
+    for (int i = 1; i < 5; ++i) {
+        const double ai = __shfl_sync(0xffffffffu, a0, base + i);
+        const double bi = __shfl_sync(0xffffffffu, b0, base + i);
+        const double di = __shfl_sync(0xffffffffu, d0, base + i);
+        if (lane < 30 && s == 0) {
+            a = __dadd_rn(a, ai);
+            if (ra.P2) {
+                b = __dadd_rn(b, bi);
+                d = __dadd_rn(d, di);
+            }
+        }
+    }
+    double* row = (double*)(ra.rows + (long)n1 * 8);
+    if (lane < 30 && s == 0) {
+        double v = a;
+        if (ra.P2) v = __dadd_rn(__dadd_rn(v, im ? -b : b), d);  // + conj(A = aqsmtemp sum) + diagonal
+        row[2 * c + im] = v;
+        parts[p] = v;
+        if (c == 2 && ra.out) ((double*)(ra.out + 7 + n1))[im] = v;  // acht_n1_loc
+    }
+    if (lane >= 30) {
+        row[12 + lane - 30] = a;  // component 6
+        parts[6 + lane - 30] = a;
+    }
+    if (lane < 6) row[6 + lane] = 0.0;  // ssx (3..5): occupied bands only
+}
+
+// Block task i of a request's rows: flag blocks (four occupied-band
+// components each, rows_warp), then band blocks (four bands each).  Every
+// thread of the block calls it with the same i.
+FK_DEV void rows_block(const RowsArgs& ra, int i, int tid) {
+    const int warp = tid >> 5, lane = tid & 31, nfb = rows_flag_blocks(ra.nv);
+    if (i < nfb) {
+        const int t = i * 4 + warp;
+        if (t < ra.nv * 7) rows_warp(ra, t / 7, t % 7, lane);
+        return;
+    }
+    const int bb = i - nfb, n0 = ra.nv + bb * 4;
+    __shared__ double parts[4][8];  // the block's bands' values of the eight parts
+    if (n0 + warp < ra.nb) rows_band_warp(ra, n0 + warp, lane, parts[warp]);
+    __syncthreads();
+    if (tid < 8) {
+        // the four bands' partial totals of part tid (component tid/2 for tid < 6, else 6)
+        double v = 0.0;
+        for (int b = 0; b < 4 && n0 + b < ra.nb; ++b) v = __dadd_rn(v, parts[b][tid]);
+        ((double*)(ra.rows + (long)ra.nb * 8 + (long)bb * 4))[tid] = v;
+    }
+    __syncthreads();  // parts is reused by the block's next task
+}
+
+// Totals by one block of ROWS_THREADS: thread 16q + s (q < 8: part q of
+// components 0..2 and 6) adds items s, s+16, .. of the part's list -- the
+// occupied bands' rows, then the band blocks' partials -- and four shuffles
+// add the sixteen splits; the ssx parts (occupied bands only) by threads 0..5.
+// out = [achtemp 3 | asxtemp 3 | achstemp | acht_n1_loc nb] (acht_n1_loc is
+// written by the band warps).
+FK_DEV void totals_block(int nb, int nv, const double2* rows, double2* out) {
+    constexpr int B = 12;  // items in flight per thread: one round trip up to 16*B items
+    const int t = threadIdx.x, q = t >> 4, s = t & 15;
+    const int c = q < 6 ? q >> 1 : 6, im = q & 1;
+    const long items = nv + rows_band_blocks(nb, nv);
+    const double* part = (const double*)(rows + (long)nb * 8);
+    // ssx (components 3..5, occupied bands only): threads 0..5, loaded with the first batch
+    const int nx = t < 6 ? nv : 0;
+    double v = 0.0, w = 0.0;
+    for (long i0 = s, x0 = 0; i0 < items || x0 < nx; i0 += 16 * B, x0 += B) {
+        double a[B], x[B];
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            const long i = i0 + 16 * j, n1 = x0 + j;
+            a[j] = i >= items ? 0.0 : i < nv ? part_of(rows[i * 8 + c], im) : part[(i - nv) * 8 + q];
+            x[j] = n1 < nx ? part_of(rows[n1 * 8 + 3 + (t >> 1)], t & 1) : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            if (i0 + 16 * j >= items) break;
+            v = __dadd_rn(v, a[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            if (x0 + j >= nx) break;
+            w = __dadd_rn(w, x[j]);
+        }
+    }
+#pragma unroll
+    for (int off = 8; off > 0; off >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, off));
+    double* o = (double*)out;
+    if (s == 0) o[2 * c + im] = v;
+    if (t < 6) o[6 + t] = w;
+}
+
+__global__ void __launch_bounds__(ROWS_THREADS) rows_kernel(RowsArgs ra) {
+    rows_block(ra, blockIdx.x, threadIdx.x);
     if (!ra.counter) return;
-    // the last block to finish adds the bands (totals_block, fixed order):
-    // the barrier orders the block's row writes before thread 0's device-scope
-    // fence and count, as in a grid-wide barrier
+    // the last block to finish adds the bands (totals_block, fixed order): the
+    // barrier orders the block's row writes before thread 0's count, a
+    // device-scope release; the last block's count also acquires the others'
     __shared__ int last;
     __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
-        last = atomicAdd(ra.counter, 1) == (int)gridDim.x - 1;
+        int old;
+        asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(ra.counter) : "memory");
+        last = old == (int)gridDim.x - 1;
     }
     __syncthreads();
     if (!last) return;
-    __threadfence();
-    totals_block(ra.nb, ra.rows, ra.out);
+    totals_block(ra.nb, ra.nv, ra.rows, ra.out);
     if (threadIdx.x == 0) *ra.counter = 0;
-}
-
-// Totals over bands, one warp per component (same split and tree), and the
-// per-band sch at iw = 2.  out = [achtemp 3 | asxtemp 3 | achstemp | acht_n1_loc nb].
-FK_DEV void totals_block(int nb, const double2* rows, double2* out) {
-    const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
-    if (c < 7) {
-        double2 v = lane < nb ? ordered_sum(rows + (long)lane * 8 + c, 32L * 8, (nb - lane + 31) / 32)
-                              : make_double2(0.0, 0.0);
-        v = warp_tree(v);
-        if (lane == 0) out[c] = v;
-    }
-    for (int r = threadIdx.x; r < nb; r += blockDim.x) out[7 + r] = rows[(long)r * 8 + 2];  // acht_n1_loc
 }
 
 
@@ -964,7 +1105,7 @@ Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0, bool pipeline
     p.bytesF = (size_t)p.nch * std::max(r.nv, 1) * r.ng * (half ? 12 : 6) * sizeof(double2);
     p.bytesP = M > 0 ? (size_t)p.KS * p.NT * M * 3 * sizeof(double2) : 0;
     p.bytesS = (r.flags & FK_GPP_ACHSTEMP) ? (size_t)p.KSs * p.NTs * r.nb * sizeof(double2) : 0;
-    p.bytesRows = (size_t)r.nb * 8 * sizeof(double2);
+    p.bytesRows = rows_bytes(r.nb);
     p.bytesIgp = 2 * (size_t)r.ng * sizeof(int);  // igp, acol
     return p;
 }
@@ -1400,7 +1541,7 @@ fk_status gpp_run_half(Ctx& c, const GppDev& r) {
     ra.nc = r.nc;
     ra.counter = counter;  // the last block also writes the totals
     ra.out = r.out;
-    rows_kernel<<<ceil_div(r.nb * 7, 8), 256, 0, st>>>(ra);
+    rows_kernel<<<rows_blocks(r.nb, r.nv), ROWS_THREADS, 0, st>>>(ra);
     ++c.launches;
     phase_mark(c, 4);
     cudaError_t e = cudaGetLastError();
@@ -1564,7 +1705,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
     ra.counter = counter;  // the last block also writes the totals
     ra.out = r.out;
     ra.wf = wf;
-    rows_kernel<<<ceil_div(r.nb * 7, 8), 256, 0, st>>>(ra);
+    rows_kernel<<<rows_blocks(r.nb, r.nv), ROWS_THREADS, 0, st>>>(ra);
     ++c.launches;
     phase_mark(c, 4);
     cudaError_t e = cudaGetLastError();
@@ -1604,7 +1745,7 @@ struct StepTable {
     int first[STEP_MAX], last[STEP_MAX];
     long setup_start[STEP_MAX + 1];  // threads: ng (index map) + M*ng (weights) per first-step request
     int prep_start[STEP_MAX + 1];    // blocks: passes*nch*ng per first-step request
-    long rows_start[STEP_MAX + 1];   // warps: nb*7 per last-step request
+    long rows_start[STEP_MAX + 1];   // rows block tasks (rows_blocks) per last-step request
 };
 
 template <class T>
@@ -1659,21 +1800,19 @@ __global__ void __launch_bounds__(PREP_THREADS, 2) prep_table_kernel(const StepT
     }
 }
 
-__global__ void rows_table_kernel(const StepTable* T) {
+__global__ void __launch_bounds__(ROWS_THREADS) rows_table_kernel(const StepTable* T) {
     const long total = T->rows_start[T->nlast];
-    const long nw = (long)gridDim.x * blockDim.x / 32;
-    for (long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total; w += nw) {
-        const int l = find_range(T->rows_start, T->nlast, w);
+    for (long i = blockIdx.x; i < total; i += gridDim.x) {  // block-uniform
+        const int l = find_range(T->rows_start, T->nlast, i);
         const StepReq& q = T->req[T->last[l]];
-        const long i = w - T->rows_start[l];
-        rows_warp(q.rows, (int)(i / 7), (int)(i % 7), threadIdx.x & 31);
+        rows_block(q.rows, (int)(i - T->rows_start[l]), threadIdx.x);
     }
 }
 
 __global__ void totals_table_kernel(const StepTable* T) {
     for (int l = blockIdx.x; l < T->nlast; l += gridDim.x) {
         const StepReq& q = T->req[T->last[l]];
-        totals_block(q.nb, q.rows.rows, q.out);
+        totals_block(q.nb, q.nv, q.rows.rows, q.out);
     }
 }
 
@@ -1750,6 +1889,7 @@ GppJob* gpp_job_create(Ctx& c, const GppDev& r0, int ks, void* ws, size_t bytes,
     q.prep = PrepArgs{r.nb, r.nv, r.nc, r.ng, r.aqsn, r.eps, r.wt, r.wx, igp, D, p.kstages, F, p.nch, p.tile, 0, 0};
     q.rows = RowsArgs{r.nb, r.nv, r.ng, p.KS * p.NT, P, 0, nullptr, p.nch, F, r.ldm, r.aqsm, r.vcoul, igp, acol, rows};
     q.out = out;
+    q.rows.out = out;  // the band rows write acht_n1_loc
     if (M > 0) {
         ContractArgs a{};
         a.A = r.aqsn; a.lda = r.nc; a.m0 = r.nv; a.M = M;
@@ -1813,8 +1953,8 @@ GppStep* gpp_step_create(Ctx& c, fk_status* st) {
     step_setup_kernel<<<c.sms * 4, 256, 0, str>>>(s->dev);
     prep_table_kernel<64><<<c.sms * prep_per_sm, PREP_THREADS, 0, str>>>(s->dev);
     tck<<<c.sms, tcx::THREADS, tcx::Cfg<64>::SMEM, str>>>(&s->dev->tc, c.errword);
-    rows_table_kernel<<<c.sms * 4, 256, 0, str>>>(s->dev);
-    totals_table_kernel<<<STEP_MAX, 256, 0, str>>>(s->dev);
+    rows_table_kernel<<<c.sms * 4, ROWS_THREADS, 0, str>>>(s->dev);
+    totals_table_kernel<<<STEP_MAX, ROWS_THREADS, 0, str>>>(s->dev);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(str, &g);
     if (e != cudaSuccess || !g) return bad(FK_ECUDA);
@@ -1864,7 +2004,7 @@ fk_status gpp_step_launch(Ctx& c, GppStep* s, const GppStepItem* items, int n) {
         if (items[i].last) {
             const int l = T.nlast++;
             T.last[l] = i;
-            T.rows_start[l + 1] = T.rows_start[l] + (long)j->r.nb * 7;
+            T.rows_start[l + 1] = T.rows_start[l] + rows_blocks(j->r.nb, j->r.nv);
         }
     }
     T.tc.ustart[n] = units;
@@ -2044,7 +2184,7 @@ fk_status gpp_real_run(Ctx& c, const GppRealDev& r) {
     ra.re_only = true;
     ra.counter = counter;  // the last block also writes the totals
     ra.out = outc;
-    rows_kernel<<<ceil_div(r.nb * 7, 8), 256, 0, st>>>(ra);
+    rows_kernel<<<rows_blocks(r.nb, r.nv), ROWS_THREADS, 0, st>>>(ra);
     real_out_kernel<<<std::max(1, std::min(ceil_div(6 + r.nb, 256), 64)), 256, 0, st>>>(r.nb, outc, r.out);
     c.launches += 2;
     phase_mark(c, 4);
