@@ -138,8 +138,19 @@ def test_ff_host_planes_streamed(ctx, fk, orc, flags):
     d = dict(p)
     for k in ("aqsmtemp", "aqsntemp", "I_epsR_array", "I_epsA_array"):
         d[k] = torch.from_numpy(p[k]).cuda()
+    small = sum(np.asarray(p[k]).nbytes for k in ("vcoul", "inv_igp_index", "indinv", "ekq", "dFreqGrid",
+                                                   "dFreqBrd", "pref"))
     ref = ctx.ff(d, "fp64", flags)
+    assert ctx.last_transfer()[0] == small  # the large arrays are on the device: only the small ones move
     check(ctx.ff(p, "fp64", flags), ref, TOL64)
+    h2d, d2h = ctx.last_transfer()
+    plane = p["I_epsR_array"][0].nbytes
+    moved = h2d - p["aqsmtemp"].nbytes - p["aqsntemp"].nbytes - small
+    # whole planes only, fewer than the 2 x nFreq of the arrays unless every plane is read
+    assert moved % plane == 0 and 0 < moved // plane <= 2 * p["nFreq"], (h2d, plane)
+    if not flags & 1:
+        assert moved // plane < 2 * p["nFreq"]
+    assert d2h == sum(v.nbytes for v in ref.values())
     sc = ff_scales(p, orc)
     res = ctx.ff(p, "mixed", flags)
     errs = {k: scaled_err(res[k], ref[k], sc[k]) for k in KEYS if k != "schDt_matrix" or flags & 1}
