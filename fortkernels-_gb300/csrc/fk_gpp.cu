@@ -59,7 +59,7 @@ struct PrepArgs {
     int kstages; // mixed: k-stages per n-tile in the image
     double2* F;  // [nch][nv][ng][3][2]  (sch, ssx) flag-band sums over the chunk
     int nch;
-    int tile;    // mixed: plane waves per chunk (a multiple of PREP_THREADS)
+    int tile;    // plane waves per chunk (mixed: a multiple of the 32-wide k-stage)
     int n1base;  // first flag band handled by this pass
     int ch0;     // first chunk of this launch (blockIdx.x counts from it)
     // half-sum mode (FK_GPP_HALF_SUM)
@@ -106,11 +106,15 @@ FK_DEV int prep_setup(const PrepArgs& p, int ch, int my_igp) {
                 p.wf[((long)n1 * p.ng + my_igp) * 2 + 0] = a;
                 p.wf[((long)n1 * p.ng + my_igp) * 2 + 1] = b;
             }
-        if (p.W)
-            for (int m = threadIdx.x; m < p.M; m += blockDim.x)
-                p.W[(long)my_igp * p.M + m] =
-                    igp >= 0 ? tcx::weight_w1(p.aqsm[(long)(p.nv + m) * p.ldm + acol], 0.5 * p.vcoul[igp])
-                             : make_float2(0.f, 0.f);
+    }
+    if (p.W) {
+        // the column's epilogue weights, rows split evenly over its chunks
+        const int acol = igp < 0 ? -1 : (p.compact ? my_igp : igp);
+        const int m0 = (int)((long)p.M * ch / p.nch), m1 = (int)((long)p.M * (ch + 1) / p.nch);
+        for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x)
+            p.W[(long)my_igp * p.M + m] =
+                igp >= 0 ? tcx::weight_w1(p.aqsm[(long)(p.nv + m) * p.ldm + acol], 0.5 * p.vcoul[igp])
+                         : make_float2(0.f, 0.f);
     }
     return igp;
 }
@@ -675,16 +679,20 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
     }
     if (p.setup && D) {
         // zeros of the image that no column writes: the padding rows of this
-        // column's tile (written by the tile's last column) and, in the last
-        // chunk, k from ncouls to the end of the last k-stage
+        // column's tile (the chunk's k-range split evenly over the tile's
+        // columns) and, in the last chunk, k from ncouls to the end of the last
+        // k-stage
         const int c = my_igp % GPP_COLS, nt = my_igp / GPP_COLS;
         const bool lastcol = c == GPP_COLS - 1 || my_igp == p.ng - 1;
-        const int r0 = lastcol ? 3 * (c + 1) : 3 * c + 3;  // first padding row (none unless lastcol)
+        const int ncols = min(GPP_COLS, p.ng - nt * GPP_COLS), rp = 3 * ncols;  // first padding row
         uint8_t* tile = D + (long)nt * p.kstages * tcx::Cfg<BN>::B_BYTES;
         const int kend = p.kstages * tcx::BK;
-        if (lastcol)
-            for (int k = ch * p.tile + tid; k < min(p.nc, (ch + 1) * p.tile); k += PREP_THREADS)
-                for (int r = r0; r < BN; ++r) tcx::bimg_store<BN>(tile, p.kstages, r, k, 0.f, 0.f);
+        if (rp < BN) {
+            const int k0 = ch * p.tile, k1 = min(p.nc, (ch + 1) * p.tile);
+            const int ka = k0 + (int)((long)(k1 - k0) * c / ncols), kb = k0 + (int)((long)(k1 - k0) * (c + 1) / ncols);
+            for (int k = ka + tid; k < kb; k += PREP_THREADS)
+                for (int r = rp; r < BN; ++r) tcx::bimg_store<BN>(tile, p.kstages, r, k, 0.f, 0.f);
+        }
         if ((ch + 1) * p.tile >= p.nc)
             for (int k = p.nc + tid; k < kend; k += PREP_THREADS)
                 for (int r = 3 * c; r < (lastcol ? BN : 3 * c + 3); ++r) tcx::bimg_store<BN>(tile, p.kstages, r, k, 0.f, 0.f);
@@ -1049,8 +1057,10 @@ Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0, bool pipeline
                 cudaSuccess ||
             per_sm < 1)
             per_sm = 1;
+        // chunks in whole k-stages (a warp's 32 plane waves fill whole image rows),
+        // so that the last chunk is not much shorter than the others
         const int nch = std::max(1, per_sm * c.sms / r.ng);
-        p.tile = ceil_div(ceil_div(r.nc, nch), PREP_THREADS) * PREP_THREADS;
+        p.tile = ceil_div(ceil_div(r.nc, nch), tcx::BK) * tcx::BK;
         p.nch = ceil_div(r.nc, p.tile);
     } else {
         p.tile = PREP_TILE;
