@@ -60,50 +60,28 @@ FK_DEV double f32_to_f64_bits(float f) {
         (long long)(s | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29)));
 }
 
-// x[0] + x[stride] + ... + x[(n-1)*stride], added left to right; the loads
-// are issued in groups of eight ahead of the adds, so a long sum waits for
-// memory once per group instead of once per term.
-FK_DEV double2 ordered_sum(const double2* x, long stride, int n) {
+// x[0] + x[stride] + ... + x[(n-1)*stride], added left to right.  The loads
+// of a group are issued together ahead of the adds, so a long sum waits for
+// memory once per group.  Every load reads a valid address (the index is
+// clamped) and every add is unconditional (+0.0 for the indices past n, which
+// leaves a sum that starts at +0.0 unchanged): an add guarded by a branch lets
+// the compiler move each load next to its add, and the group's loads then wait
+// for memory one after another (measured: 3.5x slower on GB300).
+template <int G>
+FK_DEV double2 ordered_sum_g(const double2* x, long stride, int n) {
     double2 s = make_double2(0.0, 0.0);
-    int i0 = 0;
-    for (; i0 + 8 <= n; i0 += 8) {
-        double2 v[8];
+    for (int i0 = 0; i0 < n; i0 += G) {
+        double2 v[G];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) v[j] = x[(long)(i0 + j) * stride];
+        for (int j = 0; j < G; ++j) v[j] = x[(long)min(i0 + j, n - 1) * stride];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) s = cadd(s, v[j]);
-    }
-    // tail: loads still issued together, adds only for the terms that exist
-    // (predicated-off FP64 adds would still occupy the narrow FP64 pipe)
-    if (i0 < n) {
-        double2 v[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) v[j] = i0 + j < n ? x[(long)(i0 + j) * stride] : make_double2(0.0, 0.0);
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            if (i0 + j >= n) break;
-            s = cadd(s, v[j]);
-        }
+        for (int j = 0; j < G; ++j) s = cadd(s, i0 + j < n ? v[j] : make_double2(0.0, 0.0));
     }
     return s;
 }
-
-// The same left-to-right sum with every load of up to 16 terms issued before
-// the first add (one memory round trip for short sums).
-FK_DEV double2 ordered_sum16(const double2* x, long stride, int n) {
-    double2 s = make_double2(0.0, 0.0);
-    for (int i0 = 0; i0 < n; i0 += 16) {
-        double2 v[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) v[j] = i0 + j < n ? x[(long)(i0 + j) * stride] : make_double2(0.0, 0.0);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            if (i0 + j >= n) break;
-            s = cadd(s, v[j]);
-        }
-    }
-    return s;
-}
+FK_DEV double2 ordered_sum(const double2* x, long stride, int n) { return ordered_sum_g<8>(x, stride, n); }
+// The same with the loads of up to 16 terms in flight.
+FK_DEV double2 ordered_sum16(const double2* x, long stride, int n) { return ordered_sum_g<16>(x, stride, n); }
 
 // --------------------------------------------- compensated FP32 accumulation
 // float-float (hi, lo) accumulator updated with Knuth's TwoSum: exact sum of

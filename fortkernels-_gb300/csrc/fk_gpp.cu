@@ -859,15 +859,9 @@ FK_DEV double split_sum(const double2* P, long M, long m, int c, int im, int nsl
     for (int k0 = s; k0 < nslots; k0 += 5 * 8) {
         double a[8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int k = k0 + 5 * i;
-            a[i] = k < nslots ? part_of(P[((long)k * M + m) * 3 + c], im) : 0.0;
-        }
+        for (int i = 0; i < 8; ++i) a[i] = part_of(P[((long)min(k0 + 5 * i, nslots - 1) * M + m) * 3 + c], im);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            if (k0 + 5 * i >= nslots) break;
-            v = __dadd_rn(v, a[i]);
-        }
+        for (int i = 0; i < 8; ++i) v = __dadd_rn(v, k0 + 5 * i < nslots ? a[i] : 0.0);  // unconditional: see ordered_sum
     }
     return v;
 }
@@ -966,21 +960,18 @@ FK_DEV void totals_block(int nb, int nv, const double2* rows, double2* out) {
     for (long i0 = s, x0 = 0; i0 < items || x0 < nx; i0 += 16 * B, x0 += B) {
         double a[B], x[B];
 #pragma unroll
-        for (int j = 0; j < B; ++j) {
-            const long i = i0 + 16 * j, n1 = x0 + j;
-            a[j] = i >= items ? 0.0 : i < nv ? part_of(rows[i * 8 + c], im) : part[(i - nv) * 8 + q];
-            x[j] = n1 < nx ? part_of(rows[n1 * 8 + 3 + (t >> 1)], t & 1) : 0.0;
+        for (int j = 0; j < B; ++j) {  // clamped indices: every load reads a valid address
+            const long i = min(i0 + 16 * j, items - 1);
+            a[j] = *(i < nv ? (const double*)(rows + i * 8 + c) + im : part + (i - nv) * 8 + q);
         }
+        if (nx)  // threads 0..5 only (their component 3 + t/2 exists in every row)
 #pragma unroll
-        for (int j = 0; j < B; ++j) {
-            if (i0 + 16 * j >= items) break;
-            v = __dadd_rn(v, a[j]);
-        }
+            for (int j = 0; j < B; ++j) x[j] = part_of(rows[min(x0 + j, (long)nx - 1) * 8 + 3 + (t >> 1)], t & 1);
 #pragma unroll
-        for (int j = 0; j < B; ++j) {
-            if (x0 + j >= nx) break;
-            w = __dadd_rn(w, x[j]);
-        }
+        for (int j = 0; j < B; ++j) v = __dadd_rn(v, i0 + 16 * j < items ? a[j] : 0.0);  // unconditional: see ordered_sum
+        if (nx)
+#pragma unroll
+            for (int j = 0; j < B; ++j) w = __dadd_rn(w, x0 + j < nx ? x[j] : 0.0);
     }
 #pragma unroll
     for (int off = 8; off > 0; off >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, off));
