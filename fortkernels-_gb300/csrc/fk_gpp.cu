@@ -737,14 +737,15 @@ FK_DEV double2 warp_tree(double2 v) {
     return v;
 }
 
-// Per-band sums, one warp per (band n1, component c of 7); the lanes split the
-// partials, so every load of a sum is in flight at once, and a fixed shuffle
-// tree adds them (deterministic).  rows[n1][8] = {sch iw0..2, ssx iw0..2, stat, 0}.
-//   n1 >= nvband, c < 3: the contraction's k-slice partials P[slot][m][3];
-//   n1 <  nvband, c < 6: over columns my_igp, the chunk partials of the prep
-//     F[ch][n1][my_igp][6] times the reference's weight (sch: 0.5*vcoul*conj(aqsm),
-//     BGW-Kernels/gppKer.cpp:346,421; ssx: occ*vcoul*conj(aqsm), :419);
-//   c == 6: the static-remainder partials S[slot][n1].
+// Per-band sums into rows[n1][8] = {sch iw0..2, ssx iw0..2, stat, 0}.  Bands
+// n1 >= nvband add the contraction's k-slice partials P[slot][m][3]
+// (rows_band_warp, below).  Occupied bands n1 < nvband, one warp per (band,
+// component c of 7; rows_warp): for c < 6, over columns my_igp, the chunk
+// partials of the prep F[ch][n1][my_igp][6] times the reference's weight
+// (sch: 0.5*vcoul*conj(aqsm), BGW-Kernels/gppKer.cpp:346,421; ssx:
+// occ*vcoul*conj(aqsm), :419), the lanes taking columns and a fixed shuffle
+// tree adding them (deterministic); c == 6: the static-remainder partials
+// S[slot][n1].
 struct RowsArgs {
     int nb, nv, ng, nslots;
     const double2* P;
@@ -770,8 +771,8 @@ struct RowsArgs {
 };
 
 FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
-    const int nb = ra.nb, nv = ra.nv, ng = ra.ng, nslots = ra.nslots, nslots_s = ra.nslots_s, nch = ra.nch;
-    const double2 *P = ra.P, *S = ra.S, *F = ra.F, *aqsm = ra.aqsm;
+    const int nb = ra.nb, nv = ra.nv, ng = ra.ng, nslots_s = ra.nslots_s, nch = ra.nch;
+    const double2 *S = ra.S, *F = ra.F, *aqsm = ra.aqsm;
     const long ldm = ra.ldm;
     const double* vcoul = ra.vcoul;
     const int *igp = ra.igp, *acol = ra.acol;
@@ -779,22 +780,6 @@ FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
     double2 v = make_double2(0.0, 0.0);
     if (c == 6) {
         if (S && lane < nslots_s) v = ordered_sum(S + (long)lane * nb + n1, 32L * nb, (nslots_s - lane + 31) / 32);
-    } else if (n1 >= nv) {
-        const long M = nb - nv, m = n1 - nv;
-        if (c < 3 && lane < nslots) v = ordered_sum(P + ((long)lane * M + m) * 3 + c, 32 * M * 3, (nslots - lane + 31) / 32);
-        if (ra.re_only) v.y = 0.0;
-        if (c < 3 && ra.P2) {
-            // half sum: + conj(A = aqsmtemp contraction) + diagonal terms on block edges
-            if (lane < nslots)
-                v = cadd(v, cconj(ordered_sum(ra.P2 + ((long)lane * M + m) * 3 + c, 32 * M * 3, (nslots - lane + 31) / 32)));
-            for (int h = lane; h < ng; h += 32) {
-                const int g = igp[h];
-                if (g <= 0 || (g & 511)) continue;
-                const double2 t = cmul(cmul(cconj(aqsm[(long)n1 * ldm + acol[h]]), ra.aqsn[(long)n1 * ra.nc + g]),
-                                       ra.schd[h * 3 + c]);
-                v = cadd(v, cscale(t, 0.5 * vcoul[g]));
-            }
-        }
     } else if (ra.P2) {
         // half sum, occupied band: weight * (cm S1 + conj(cm S2)) per column
         const int kind = c / 3, r = ((c % 3) * 2 + kind) * 2;
@@ -826,8 +811,8 @@ FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
             v = cadd(v, cscale(cmul(cm, sum), kind ? occ * vcoul[g] : 0.5 * vcoul[g]));
         }
     }
-    // components with no terms (ssx of bands >= nvband, stat without S) skip the tree
-    const bool empty = (c == 6 && !S) || (n1 >= nv && c >= 3 && c < 6);
+    // a component with no terms (stat without S) skips the tree
+    const bool empty = c == 6 && !S;
     if (!empty) v = warp_tree(v);
     if (lane == 0) rows[(long)n1 * 8 + c] = v;
     if (lane == 0 && c == 2 && ra.out) ra.out[7 + n1] = v;  // acht_n1_loc
