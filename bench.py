@@ -197,22 +197,29 @@ class NvmlSampler:
         v = ctypes.c_uint()
         self.max_mhz = float(v.value) if self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(v)) == 0 else None
 
-    def _sample(self):
+    def _read(self):
         ct, L = self.ct, self.lib
         clk, pw, rs = ct.c_uint(), ct.c_uint(), ct.c_ulonglong()
+        if L.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(clk)) == 0:
+            L.nvmlDeviceGetPowerUsage(self.h, ct.byref(pw))
+            r = rs.value if L.nvmlDeviceGetCurrentClocksEventReasons(self.h, ct.byref(rs)) == 0 else 0
+            self.rows.append((float(clk.value), pw.value / 1000.0, r))
+
+    def _sample(self):
         while not self.stop.is_set():
-            if L.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(clk)) == 0:
-                L.nvmlDeviceGetPowerUsage(self.h, ct.byref(pw))
-                r = rs.value if L.nvmlDeviceGetCurrentClocksEventReasons(self.h, ct.byref(rs)) == 0 else 0
-                self.rows.append((float(clk.value), pw.value / 1000.0, r))
+            self._read()
             time.sleep(0.0005)
 
     def __enter__(self):
+        # one reading as the region starts and one as it ends, so that even a
+        # region of a few milliseconds is bracketed; the thread reads in between
+        self._read()
         self.t = threading.Thread(target=self._sample, daemon=True)
         self.t.start()
         return self
 
     def __exit__(self, *a):
+        self._read()
         self.stop.set()
         self.t.join(timeout=2)
 
