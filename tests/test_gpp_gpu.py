@@ -196,9 +196,16 @@ def test_gpp_full_size_benchmark_config(ctx, fk, orc):
     """number_bands=512, nvband=2, ncouls=32768, ngpown=20 (the benchmark
     workload): FP64 against the oracle, mixed against FP64."""
     p = fk.inputs.gpp_synthetic(512, 2, 32768, 20, seed=2024, dist="uniform")
+    # host bytes the call reads: all of aqsntemp, eps and wtilde, the small arrays, and only
+    # the ngpown igp columns of aqsmtemp (gathered on the host)
+    small = sum(np.asarray(p[k]).nbytes for k in ("vcoul", "inv_igp_index", "indinv", "wx_array"))
+    expect = p["aqsntemp"].nbytes + p["I_eps_array"].nbytes + p["wtilde_array"].nbytes + 512 * 20 * 16 + small
     r64 = ctx.gpp(p, "fp64")
+    assert ctx.last_transfer() == (expect, sum(v.nbytes for v in r64.values() if v is not None))
     check(r64, orc.gpp(p), TOL64)
-    check(ctx.gpp(p, "mixed"), r64, TOLMX)   # plain relative error at the benchmark size
+    rmx = ctx.gpp(p, "mixed")  # large host arrays: the pipelined path (row blocks on a copy stream)
+    assert ctx.last_transfer() == (expect, (7 + 512) * 16)  # outputs come back as one pinned block
+    check(rmx, r64, TOLMX)   # plain relative error at the benchmark size
 
 
 def test_gpp_full_size_reference_run(ctx, fk):

@@ -99,6 +99,10 @@ def test_real_benchmark_size(ctx, fk, orc):
     """512 x 2 x 32768 x 20: FP64 against the oracle, mixed against FP64."""
     p = fk.inputs.gpp_real_synthetic(512, 2, 32768, 20, seed=88, dist="branch", wx="baseline")
     r64 = ctx.gpp_real(p, "fp64")
+    # every host input is staged whole; the three outputs come back
+    sent = sum(np.asarray(p[k]).nbytes for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array", "vcoul",
+                                                  "inv_igp_index", "indinv", "wx_array"))
+    assert ctx.last_transfer() == (sent, (3 + 3 + 512) * 8)
     ref = orc.gpp_real(p)
     for k in KEYS:
         assert rel(r64[k], ref[k]) <= TOL64, k
