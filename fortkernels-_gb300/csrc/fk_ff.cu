@@ -266,7 +266,8 @@ void compute_fact(double wx, int nFreq, const double* g, double& fact1, double& 
 struct FfPlan {
     std::vector<FactRow> fact;
     std::vector<int> planesR, planesA;
-    int groupR, groupA;           // planes per copy group (pipelined requests; else all planes in one)
+    std::vector<int> groups;      // pipelined requests: copy group q = R planes (q < ngR) or A planes, of the
+    int ngR;                      // combined list [planesR | planesA], is [groups[q], groups[q+1])
     int MT, NT, KS, kchunk;
     int BN, kstages;              // tensor-core path (mixed)
     bool mixed;
@@ -318,19 +319,41 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
         if (needA[f]) p.planesA.push_back(f);
     }
     // copy groups: the R and A planes share FF_PIPE_GROUPS groups in proportion
-    // to their counts; each group is one contraction launch, so the k-split is
-    // chosen for a group's planes
+    // to their counts.  The first group (computing cannot start before it has
+    // landed) and the last (computed after the last copy) are one plane each;
+    // the others split the rest evenly.  Each group is one contraction launch,
+    // so the k-split is chosen for the largest group.
     const int nR = (int)p.planesR.size(), nA = (int)p.planesA.size();
-    p.groupR = std::max(nR, 1);
-    p.groupA = std::max(nA, 1);
+    p.ngR = 0;
+    int gmax = std::max(nR, 1);
     if (pipelined) {
         int gR = nR ? std::max(1, std::min(nR, (FF_PIPE_GROUPS * nR + (nR + nA) / 2) / (nR + nA))) : 0;
         const int gA = nA ? std::max(1, std::min(nA, FF_PIPE_GROUPS - gR)) : 0;
         gR = std::min(gR, FF_PIPE_GROUPS - gA);
-        if (nR) p.groupR = ceil_div(nR, gR);
-        if (nA) p.groupA = ceil_div(nA, gA);
+        // sizes of n planes in g groups, with a one-plane group at the front (first) or back (last)
+        auto split = [](int n, int g, bool one_first, bool one_last, std::vector<int>& out) {
+            std::vector<int> sz;
+            int lead = 0, tail = 0;
+            if (one_first && g >= 2 && n >= 2) { sz.push_back(1); lead = 1; --g; }
+            if (one_last && g >= 2 && n - lead >= 2) tail = 1, --g;
+            const int rest = n - lead - tail;
+            for (int i = 0; i < g; ++i) sz.push_back(rest / g + (i < rest % g ? 1 : 0));
+            if (tail) sz.push_back(1);
+            for (int s : sz)
+                if (s > 0) out.push_back(s);
+        };
+        std::vector<int> szR, szA;
+        split(nR, gR, true, nA == 0, szR);
+        split(nA, gA, nR == 0, true, szA);
+        p.groups.push_back(0);
+        for (int s : szR) p.groups.push_back(p.groups.back() + s);
+        p.ngR = (int)szR.size();
+        for (int s : szA) p.groups.push_back(p.groups.back() + s);
+        gmax = 1;
+        for (int s : szR) gmax = std::max(gmax, s);
+        for (int s : szA) gmax = std::max(gmax, s);
     }
-    const int nplanes = pipelined ? std::max(nR ? p.groupR : 1, nA ? p.groupA : 1) : std::max(nR, 1);
+    const int nplanes = gmax;
     p.bytesImgR = p.bytesImgA = p.bytesW = p.bytesAimg = 0;
     if (p.mixed) {
         p.BN = 64;
@@ -421,7 +444,7 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
     c.launches = 0;
     // pipelined request: the planes each group reads, in runs of consecutive
     // planes, on the copy stream; group q is followed by pipe_ev[q]
-    const int gR = nR ? ceil_div(nR, p.groupR) : 0, gA = nA ? ceil_div(nA, p.groupA) : 0;
+    const int ngroups = pipe ? (int)p.groups.size() - 1 : 0;
     if (pipe) {
         const size_t plane = (size_t)r.ng * r.nc;
         auto copy_group = [&](const std::vector<int>& pls, int i0, int i1, const double2* src, double2* dst, int q) {
@@ -438,11 +461,12 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
             if (ce == cudaSuccess) ce = cudaEventRecord(c.pipe_ev[q], c.copy_stream);
             return ce;
         };
-        for (int q = 0; q < gR && e == cudaSuccess; ++q)
-            e = copy_group(p.planesR, q * p.groupR, std::min(nR, (q + 1) * p.groupR), pipe->epsR, pipe->epsR_d, q);
-        for (int q = 0; q < gA && e == cudaSuccess; ++q)
-            e = copy_group(p.planesA, q * p.groupA, std::min(nA, (q + 1) * p.groupA), pipe->epsA, pipe->epsA_d,
-                           gR + q);
+        for (int q = 0; q < ngroups && e == cudaSuccess; ++q) {
+            const bool isR = q < p.ngR;
+            const int off = isR ? 0 : nR;  // group bounds count R planes, then A planes
+            e = copy_group(isR ? p.planesR : p.planesA, p.groups[q] - off, p.groups[q + 1] - off,
+                           isR ? pipe->epsR : pipe->epsA, isR ? pipe->epsR_d : pipe->epsA_d, q);
+        }
         if (e == cudaSuccess) e = cudaStreamWaitEvent(st, c.pipe_ev[PIPE_READY], 0);
         if (e != cudaSuccess) return cuda_fail(c, e, "ff: plane copies");
     }
@@ -515,10 +539,9 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
         // one launch pair per copy group, each after its planes have landed;
         // a group's partials and pre-split image sit at its batch offset
         const size_t pslab = slots * r.nb * 2, islab = (size_t)p.NT * p.kstages * tcx::Cfg<64>::B_BYTES;
-        for (int q = 0; q < gR + gA; ++q) {
-            const bool isR = q < gR;
-            const int g0 = isR ? q * p.groupR : (q - gR) * p.groupA;
-            const int n = isR ? std::min(nR - g0, p.groupR) : std::min(nA - g0, p.groupA);
+        for (int q = 0; q < ngroups; ++q) {
+            const bool isR = q < p.ngR;
+            const int g0 = p.groups[q] - (isR ? 0 : nR), n = p.groups[q + 1] - p.groups[q];
             if (cudaStreamWaitEvent(st, c.pipe_ev[q], 0) != cudaSuccess)
                 return cuda_fail(c, cudaGetLastError(), "ff: pipeline wait");
             uint8_t* img = isR ? imgR : imgA;
