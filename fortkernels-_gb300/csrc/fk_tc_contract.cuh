@@ -273,13 +273,16 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                             break;
                         }
                         tc::tc_fence_after();
-                        const uint32_t sa = tc::smem_u32(base + s * C::STAGE_BYTES);
-                        const uint32_t sb = sa + C::A_BYTES;
+                        // the descriptor's start-address field is address / 16 in its low 14 bits and
+                        // shared addresses stay below 2^18, so every operand's descriptor is the stage's
+                        // base descriptor plus a constant: one add per MMA for the single issuing thread
+                        const uint64_t dA = tc::sdesc_sw64(tc::smem_u32(base + s * C::STAGE_BYTES));
+                        const uint64_t dB = dA + (C::A_BYTES >> 4);
 #pragma unroll
                         for (int kk = 0; kk < 2; ++kk) {
                             // A sub-tile (re h,m,l, im h,m,l) and paired B piece [re|im], k offset kk*16
-                            auto ad = [&](int sub) { return tc::sdesc_sw64(sa + sub * BM * 64) + 2 * kk; };
-                            auto bd = [&](int piece) { return tc::sdesc_sw64(sb + piece * 2 * BN * 64) + 2 * kk; };
+                            auto ad = [&](int sub) { return dA + (uint64_t)((sub * BM * 64) >> 4) + 2 * kk; };
+                            auto bd = [&](int piece) { return dB + (uint64_t)((piece * 2 * BN * 64) >> 4) + 2 * kk; };
                             const uint32_t acc0 = (st > st0 || kk > 0) ? 1u : 0u;
                             // piece products (a, b): the five small ones (mm, lh, hl, mh, hm), then hh;
                             // X += A_re,a x [B_re|B_im]_b, Y += A_im,a x [B_re|B_im]_b
