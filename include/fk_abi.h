@@ -53,7 +53,7 @@ typedef enum {
     FK_ECUDA = 3,     /* a CUDA call failed (no device, launch error, ...)    */
     FK_ETIMEOUT = 4,  /* a bounded device-side wait gave up                   */
     FK_EBUSY = 5,     /* admission refused (serving: over the memory budget)  */
-    FK_ENOTSUP = 6    /* valid request this build does not support           */
+    FK_ENOTSUP = 6    /* valid request the library does not support          */
 } fk_status;
 
 typedef enum {
