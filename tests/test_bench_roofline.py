@@ -1,0 +1,64 @@
+"""CPU tests of bench.py's roofline arithmetic: the term counts, the
+algorithmic bytes and flops of the dominant kernel, and the choice of bound."""
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+PEAKS = {"hbm_gbs": 6786.2, "bf16_tflops": 1900.0}
+
+
+@pytest.fixture(scope="module")
+def bench():
+    import bench as b
+    return b
+
+
+def test_gpp_default_workload_is_hbm_bound(bench):
+    w = dict(bench.WORKLOADS["gpp"], name="gpp")
+    assert bench.terms(w) == 512 * 20 * 32768 * 3
+    byts, flops = bench.algorithmic(w)
+    # aqsntemp rows n1 >= nvband once (16 B per complex) and the D image (8 B per complex)
+    assert byts == 16 * 510 * 32768 + 8 * 60 * 32768 == 283115520
+    assert flops == 8 * 510 * 60 * 32768
+    r = bench.roofline(w, "mixed", byts, flops, 0.070, 1, PEAKS)
+    assert r["bound"] == "hbm" and r["unit"] == "GB/s" and r["peak"] == PEAKS["hbm_gbs"]
+    assert r["achieved"] == pytest.approx(byts / 70e-6 / 1e9)
+    assert r["frac"] == pytest.approx(r["achieved"] / PEAKS["hbm_gbs"])
+    assert 0.5 < r["frac"] < 0.7
+
+
+def test_half_sum_counts_both_contractions(bench):
+    w = dict(bench.WORKLOADS["gpphalf"], name="gpphalf")
+    full = dict(w, half=False)
+    assert bench.algorithmic(w) == tuple(2 * x for x in bench.algorithmic(full))
+    # ig < igp for the baseline columns igp = i * ncouls / ngpown: about half the full sum
+    assert 0.4 < bench.terms(w) / bench.terms(full) < 0.5
+
+
+def test_ff_config_is_tensor_bound(bench):
+    w = dict(bench.WORKLOADS["ff"], name="ff")
+    byts, flops = bench.algorithmic(w)
+    assert flops == 8 * 15 * 512 * 512 * 4096
+    r = bench.roofline(w, "mixed", byts, flops, 1.204, 2, PEAKS)
+    assert r["bound"] == "tensor" and r["unit"] == "TFLOP/s"
+    assert r["duration_ms"] == pytest.approx(0.602)
+    assert r["frac"] == pytest.approx(flops / 1.204e-3 / 1e12 / PEAKS["bf16_tflops"])
+    assert r["executed_bf16_tflops"] == pytest.approx(6 * r["achieved"])
+
+
+def test_fp64_precision_is_reported_against_hbm_and_without_traffic(bench):
+    w = dict(bench.WORKLOADS["ff"], name="ff")
+    byts, flops = bench.algorithmic(w)
+    r = bench.roofline(w, "fp64", byts, flops, 100.0, 2, PEAKS)
+    assert r["bound"] == "hbm" and r["traffic"] is None
+
+
+def test_fallback_peaks_are_named(bench):
+    w = dict(bench.WORKLOADS["gpp"], name="gpp")
+    byts, flops = bench.algorithmic(w)
+    r = bench.roofline(w, "mixed", byts, flops, 0.070, 1, {})
+    assert r["peak_source"] == "fallback" and r["peak"] == 6800.0
