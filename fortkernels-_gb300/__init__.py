@@ -22,10 +22,10 @@ import numpy as np
 
 from . import _native
 from ._native import (FK_FF_PHYSICS, FK_FF_SCHDT_GEMM, FK_FF_SPLIT_ACHD, FK_FP64, FK_GPP_ACHSTEMP,
-                      FK_GPP_HALF_SUM, FK_GPP_REAL_ZERO_MASKED, FK_GPP_ROOT_QUIRKS, FK_MIXED, FKError)
+                      FK_GPP_HALF_SUM, FK_GPP_PHYSICS, FK_GPP_REAL_ZERO_MASKED, FK_GPP_ROOT_QUIRKS, FK_MIXED, FKError)
 
 __all__ = ["Context", "Server", "gppKer", "ffKernel", "FKError", "FK_FP64", "FK_MIXED", "FK_GPP_ROOT_QUIRKS",
-           "FK_GPP_ACHSTEMP", "FK_GPP_HALF_SUM", "FK_GPP_REAL_ZERO_MASKED", "FK_FF_SCHDT_GEMM", "FK_FF_PHYSICS", "FK_FF_SPLIT_ACHD", "precision_code"]
+           "FK_GPP_ACHSTEMP", "FK_GPP_HALF_SUM", "FK_GPP_PHYSICS", "FK_GPP_REAL_ZERO_MASKED", "FK_FF_SCHDT_GEMM", "FK_FF_PHYSICS", "FK_FF_SPLIT_ACHD", "precision_code"]
 
 
 def precision_code(p) -> int:
@@ -108,6 +108,16 @@ class Context:
         ms, n = ctypes.c_float(), ctypes.c_int()
         self._check(self.lib.fk_last_kernel_time(self.h, ctypes.byref(ms), ctypes.byref(n)), self.h)
         return float(ms.value), int(n.value)
+
+    def set_wait_limit(self, cycles: int):
+        """Bound (SM clock cycles) of the tensor-core kernels' waits; negative: the default.
+        Lowering it is a test hook for the timeout path."""
+        self._check(self.lib.fk_set_wait_limit(self.h, int(cycles)), self.h)
+
+    def selftest_timeout(self, cycles: int) -> int:
+        """Status of a one-warp kernel whose bounded wait on a barrier nothing
+        arrives on gives up after `cycles` cycles (FK_ETIMEOUT expected)."""
+        return int(self.lib.fk_selftest_timeout(self.h, int(cycles)))
 
     def last_transfer(self):
         """(host-to-device, device-to-host) bytes of the last gpp / gpp_real / ff call."""
@@ -269,6 +279,11 @@ class Server:
             self._pending.pop(ticket, None)
         self._check(st, "fk_server_wait")
         return out, lat.value
+
+    def cancel(self, ticket: int) -> int:
+        """Cancel a request still waiting for admission; returns the status
+        (FK_OK: cancelled, its wait gives FK_ECANCELED; FK_EBUSY: already admitted)."""
+        return int(self.lib.fk_server_cancel(self.h, ticket))
 
     def tune(self, number_bands: int, nvband: int, ncouls: int, ngpown: int, flags: int = 0) -> int:
         """Autotune the plan of a request shape (server idle); returns the chosen k-slice count."""

@@ -11,11 +11,12 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libfk_gb300.so")
 
-FK_OK, FK_EINVAL, FK_ENOMEM, FK_ECUDA, FK_ETIMEOUT, FK_EBUSY, FK_ENOTSUP = range(7)
+FK_OK, FK_EINVAL, FK_ENOMEM, FK_ECUDA, FK_ETIMEOUT, FK_EBUSY, FK_ENOTSUP, FK_ECANCELED = range(8)
 FK_FP64, FK_MIXED = 0, 1
 FK_GPP_ROOT_QUIRKS = 0x1
 FK_GPP_ACHSTEMP = 0x2
 FK_GPP_HALF_SUM = 0x4
+FK_GPP_PHYSICS = 0x8
 FK_GPP_REAL_ZERO_MASKED = 0x10
 FK_FF_SCHDT_GEMM = 0x1
 FK_FF_PHYSICS = 0x2
@@ -26,7 +27,7 @@ SYMBOLS = ("fk_create", "fk_destroy", "fk_set_stream", "fk_synchronize", "fk_res
            "fk_last_error", "fk_version", "fk_gpp", "fk_ff", "fk_set_profiling", "fk_last_timings",
            "fk_last_launches", "fk_last_kernel_time", "fk_last_transfer", "fk_gpp_static", "fk_gpp_real", "fk_server_create", "fk_server_destroy",
            "fk_server_resident_put", "fk_server_resident_evict", "fk_server_submit", "fk_server_wait",
-           "fk_server_stats", "fk_server_tune")
+           "fk_server_stats", "fk_server_tune", "fk_set_wait_limit", "fk_selftest_timeout", "fk_wait_error_status", "fk_server_cancel")
 
 
 class ServerConfig(ctypes.Structure):
@@ -97,6 +98,7 @@ def load(path: str = LIB_PATH):
     L.fk_server_submit.argtypes = [P, ctypes.POINTER(GppRequest), ctypes.POINTER(UL)]
     L.fk_server_wait.argtypes = [P, UL, D, ctypes.POINTER(D)]
     L.fk_server_stats.argtypes = [P, ctypes.POINTER(ServerInfo)]
+    L.fk_server_cancel.argtypes = [P, UL]
     L.fk_server_tune.argtypes = [P, I, I, I, I, U, ctypes.POINTER(I)]
     L.fk_set_profiling.argtypes = [P, I]
     L.fk_last_timings.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
@@ -104,6 +106,9 @@ def load(path: str = LIB_PATH):
     L.fk_last_kernel_time.restype = I
     L.fk_last_kernel_time.argtypes = [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int)]
     L.fk_last_transfer.argtypes = [P, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong)]
+    L.fk_set_wait_limit.argtypes = [P, ctypes.c_longlong]
+    L.fk_selftest_timeout.argtypes = [P, ctypes.c_longlong]
+    L.fk_wait_error_status.argtypes = [I, ctypes.c_char_p, ctypes.c_size_t]
     for name in SYMBOLS:
         f = getattr(L, name)
         if name not in ("fk_strerror", "fk_last_error", "fk_version"):

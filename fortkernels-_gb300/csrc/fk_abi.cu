@@ -11,8 +11,7 @@
 #include <vector>
 
 #include "fk_internal.h"
-
-
+#include "fk_tc.cuh"
 
 namespace fk {
 
@@ -193,18 +192,31 @@ void* pinned_buffer(Ctx& c, size_t bytes) {
 }
 
 // After a synchronize: a nonzero error word means a bounded device-side wait
-// of the tensor-core kernels gave up.
+// of the tensor-core kernels gave up (fk_wait_error_status decodes it).
 fk_status check_errword(Ctx& c) {
     int w = 0;
     cudaError_t e = cudaMemcpy(&w, c.errword, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(c, e, "reading the device error word");
     if (w != 0) {
         cudaMemset(c.errword, 0, sizeof(int));
-        char buf[96];
-        std::snprintf(buf, sizeof buf, "a device-side wait timed out (code 0x%x)", w);
-        return fail(c, FK_ETIMEOUT, buf);
+        char buf[512];
+        const fk_status s = fk_wait_error_status(w, buf, sizeof buf);
+        return fail(c, s, buf);
     }
     return FK_OK;
+}
+
+// One thread initialises an mbarrier that expects one arrival, which never
+// comes, and waits on it with the bounded wait of the tensor-core kernels; the
+// wait gives up after `limit` cycles and the thread records code 0x100 in the
+// error word, as a timed-out wait of those kernels does.  No copy or MMA is
+// in flight, so giving up is always safe.
+__global__ void selftest_wait_kernel(int* err, long long limit) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    tc::mbar_init(&bar, 1);
+    tc::fence_barrier_init();
+    if (!tc::mbar_wait(&bar, 0, limit)) atomicOr(err, 0x100);
 }
 
 }  // namespace
@@ -225,11 +237,47 @@ const char* fk_strerror(fk_status s) {
         case FK_ETIMEOUT: return "device wait timed out";
         case FK_EBUSY: return "busy: request not admitted";
         case FK_ENOTSUP: return "not supported";
+        case FK_ECANCELED: return "cancelled";
     }
     return "unknown status";
 }
 
 const char* fk_last_error(fk_ctx_t ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+fk_status fk_wait_error_status(int word, char* msg, size_t msg_len) {
+    // the bits the kernels set (fk_tc_contract.cuh, selftest_wait_kernel)
+    static const struct {
+        int bit;
+        const char* what;
+    } roles[] = {{0x1, "MMA issuer waiting for a free accumulator buffer"},
+                 {0x2, "MMA issuer waiting for an operand stage"},
+                 {0x4, "MMA issuer waiting for its last MMAs"},
+                 {0x8, "copy warp waiting for a free operand stage"},
+                 {0x10, "epilogue waiting for an accumulator"},
+                 {0x20, "converter warps waiting for operand rows"},
+                 {0x40, "copy warp waiting for a free staging half"},
+                 {0x80, "copy warp waiting for its last copies"},
+                 {0x100, "self-test wait"}};
+    std::string m;
+    if (word == 0) {
+        m = "no device-side wait gave up";
+    } else {
+        char head[64];
+        std::snprintf(head, sizeof head, "a device-side wait timed out (code 0x%x):", (unsigned)word);
+        m = head;
+        int known = 0;
+        for (const auto& r : roles)
+            if (word & r.bit) {
+                m += std::string(known++ ? "; " : " ") + r.what;
+            }
+        if (word & ~0x1FF) m += std::string(known ? "; " : " ") + "unknown bits";
+    }
+    if (msg && msg_len) {
+        std::strncpy(msg, m.c_str(), msg_len - 1);
+        msg[msg_len - 1] = '\0';
+    }
+    return word == 0 ? FK_OK : FK_ETIMEOUT;
+}
 
 fk_status fk_create(int device, fk_ctx_t* out) {
     if (!out) return FK_EINVAL;
@@ -321,6 +369,34 @@ fk_status fk_reserve(fk_ctx_t c, size_t bytes) {
     if (!c) return FK_EINVAL;
     fk::DeviceGuard g(c->device);
     return fk::ensure_workspace(*c, bytes);
+}
+
+fk_status fk_set_wait_limit(fk_ctx_t c, long long cycles) {
+    if (!c) return FK_EINVAL;
+    const long long v = cycles < 0 ? 4000000000LL : cycles;
+    if (v != c->wait_limit) {
+        fk::DeviceGuard g(c->device);
+        if (c->stream) cudaStreamSynchronize(c->stream);
+        fk::drop_graphs(*c);  // captured launches carry the old bound
+        c->wait_limit = v;
+    }
+    return FK_OK;
+}
+
+fk_status fk_selftest_timeout(fk_ctx_t c, long long cycles) {
+    if (!c) return FK_EINVAL;
+    if (cycles < 0 || cycles > 4000000000LL)
+        return fk::fail(*c, FK_EINVAL, "selftest_timeout: cycles must lie in [0, 4e9]");
+    fk::DeviceGuard g(c->device);
+    if (!g.ok) return fk::fail(*c, FK_ECUDA, "selftest_timeout: cannot select device");
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->errword, 0, sizeof(int), c->stream);
+    if (e != cudaSuccess) return fk::cuda_fail(*c, e, "selftest_timeout");
+    fk::selftest_wait_kernel<<<1, 32, 0, c->stream>>>(c->errword, cycles);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return fk::cuda_fail(*c, e, "selftest_timeout: kernel");
+    return fk::check_errword(*c);
 }
 
 fk_status fk_set_profiling(fk_ctx_t c, int enable) {
@@ -526,8 +602,10 @@ fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsm
         !wx_array || !achtemp || !asxtemp)
         return fk::fail(x, FK_EINVAL, "gpp: null required pointer");
     if (precision != FK_FP64 && precision != FK_MIXED) return fk::fail(x, FK_EINVAL, "gpp: bad precision");
-    if (flags & ~(FK_GPP_ROOT_QUIRKS | FK_GPP_ACHSTEMP | FK_GPP_HALF_SUM))
+    if (flags & ~(FK_GPP_ROOT_QUIRKS | FK_GPP_ACHSTEMP | FK_GPP_HALF_SUM | FK_GPP_PHYSICS))
         return fk::fail(x, FK_EINVAL, "gpp: unknown flag");
+    if ((flags & FK_GPP_PHYSICS) && (flags & (FK_GPP_ROOT_QUIRKS | FK_GPP_HALF_SUM)))
+        return fk::fail(x, FK_EINVAL, "gpp: FK_GPP_PHYSICS follows the Fortran source, not the root or half-sum drivers");
     if ((flags & FK_GPP_HALF_SUM) && (flags & FK_GPP_ROOT_QUIRKS))
         return fk::fail(x, FK_EINVAL, "gpp: FK_GPP_HALF_SUM and FK_GPP_ROOT_QUIRKS are different drivers");
     if ((flags & FK_GPP_HALF_SUM) && (flags & FK_GPP_ACHSTEMP))

@@ -514,6 +514,7 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
             t.kstages_total = p.kstages;
             t.MT = p.MT; t.NT = p.NT; t.units = p.MT * p.NT * p.KS * nb_;
             t.err = c.errword;
+            t.wait_limit = c.wait_limit;
             const int grid1 = std::min(t.units, c.sms);
             auto k = tcx::tc_contract_kernel<EPI_FF, 64, true>;
             constexpr size_t smem = tcx::Cfg<64, true>::SMEM;

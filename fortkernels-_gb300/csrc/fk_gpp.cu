@@ -81,6 +81,7 @@ struct PrepArgs {
     int M;
     int* counter;
     double2* wf;          // [nv][ng][2] flag-band weights (sch: 0.5*vcoul*conj(aqsm), ssx: occ*vcoul*conj(aqsm)), or nullptr
+    int asx_neg;          // physics mode: the ssx weight is -occ*vcoul*conj(aqsm) (asxtemp subtracted)
 };
 
 // The set-up work of block (ch, my_igp) other than the image padding.
@@ -99,7 +100,9 @@ FK_DEV int prep_setup(const PrepArgs& p, int ch, int my_igp) {
                 double2 a = make_double2(0.0, 0.0), b = a;
                 if (igp >= 0) {
                     const double2 cm = cconj(p.aqsm[(long)n1 * p.ldm + acol]);
-                    const double occ = 1.0;
+                    // asxtemp += ssx*occ*vcoul (BGW-Kernels/gppKer.cpp:419); the Fortran
+                    // subtracts it (gppkernel.deslippe.09.30.2014.f90:393)
+                    const double occ = p.asx_neg ? -1.0 : 1.0;
                     a = cscale(cm, 0.5 * p.vcoul[igp]);
                     b = cscale(cm, occ * p.vcoul[igp]);
                 }
@@ -138,8 +141,14 @@ FK_DEV Branch64 branch64(double wxt, double2 wt) {
     b.B = delwr > TO1;
     return b;
 }
-// ssx of ssxt_scht_solver, BGW-Kernels/gppKer.cpp:38-58.
-FK_DEV double2 ssx64(const Branch64& b, double wxt, double2 wt2, double2 Omega2) {
+// ssx of ssxt_scht_solver, BGW-Kernels/gppKer.cpp:38-58.  phys: the Fortran
+// branch A, cden = wxt**2 - wtilde2 (gppkernel.deslippe.09.30.2014.f90:302-305).
+FK_DEV double2 ssx64(const Branch64& b, double wxt, double2 wt2, double2 Omega2, bool phys = false) {
+    if (b.A && phys) {
+        const double2 cd = make_double2(__dsub_rn(__dmul_rn(wxt, wxt), wt2.x), __dsub_rn(0.0, wt2.y));
+        const double rd = __ddiv_rn(1.0, cnorm2(cd));
+        return cscale(cmul(Omega2, cconj(cd)), rd);
+    }
     if (b.A) {
         double w2 = __dmul_rn(wxt, wxt);
         double rd = __ddiv_rn(1.0, __dmul_rn(w2, w2));
@@ -154,6 +163,12 @@ FK_DEV double2 ssx64(const Branch64& b, double wxt, double2 wt2, double2 Omega2)
         return cmul(cscale(cmul(negO, cconj(c)), rd), b.delw);
     }
     return make_double2(0.0, 0.0);
+}
+// The Fortran sexcut test (gppkernel.deslippe.09.30.2014.f90:319-320): ssx is
+// dropped when wxt < 0 and |ssx| > sexcut*|I_eps| (the C++ test, abs(wxt) < 0 at
+// BGW-Kernels/gppKer.cpp:60-61, never fires).
+FK_DEV double2 sexcut64(double2 ssx, double wxt, double2 ep) {
+    return (wxt < 0.0 && hypot(ssx.x, ssx.y) > 4.0 * hypot(ep.x, ep.y)) ? make_double2(0.0, 0.0) : ssx;
 }
 
 // Fixed-order block sum of NV values per thread; thread v < NV of the block
@@ -225,7 +240,9 @@ FK_DEV void block_sum_ff(float2 (&v)[NV], double2* sm /* [8][NV] */, double2 (&o
     }
 }
 
-template <int Q>  // Q = 1: root gppKer.cpp semantics
+// Q = 0: BGW-Kernels/gppKer.cpp; 1: root gppKer.cpp semantics; 2: the Fortran
+// source's (physics mode)
+template <int Q>
 __global__ void __launch_bounds__(PREP_THREADS) prep64_kernel(PrepArgs p) {
     __shared__ double2 sm[8 * NVC * 6];
     const int my_igp = blockIdx.y, ch = blockIdx.x, tid = threadIdx.x;
@@ -245,19 +262,20 @@ __global__ void __launch_bounds__(PREP_THREADS) prep64_kernel(PrepArgs p) {
         if (nflag > 0) {
             wt2 = cmul(wt, wt);
             Om = cmul(wt2, ep);
-            if (Q) eq = p.eps[(long)my_igp * p.ng + ig];  // gppKer.cpp:139
+            if (Q == 1) eq = p.eps[(long)my_igp * p.ng + ig];  // gppKer.cpp:139
         }
 #pragma unroll
         for (int iw = 0; iw < 3; ++iw) {
             const double wxt = p.wx[iw];
             Branch64 b = branch64(wxt, wt);
             if (D) {
-                double2 dv = (igp >= 0 && (Q || b.A)) ? cmul(b.delw, ep) : make_double2(0.0, 0.0);
+                double2 dv = (igp >= 0 && (Q == 1 || b.A)) ? cmul(b.delw, ep) : make_double2(0.0, 0.0);
                 D[((long)my_igp * 3 + iw) * p.nc + ig] = dv;
             }
             if (nflag > 0 && igp >= 0) {
                 double2 sch = b.A ? cmul(b.delw, eq) : make_double2(0.0, 0.0);
-                double2 ssx = ssx64(b, wxt, wt2, Om);
+                double2 ssx = ssx64(b, wxt, wt2, Om, Q == 2);
+                if (Q == 2) ssx = sexcut64(ssx, wxt, ep);
 #pragma unroll
                 for (int j = 0; j < NVC; ++j)
                     if (j < nflag) {
@@ -553,7 +571,8 @@ struct Exact {
     float2 dv, sch, ssx;
     int A, B;
 };
-__device__ __noinline__ Exact exact_element(double wxt, double2 wt64, double2 ep64, double2 eq64, int need_ssx) {
+__device__ __noinline__ Exact exact_element(double wxt, double2 wt64, double2 ep64, double2 eq64, int need_ssx,
+                                            int phys) {
     const Branch64 b = branch64(wxt, wt64);
     Exact r;
     r.A = b.A;
@@ -563,7 +582,9 @@ __device__ __noinline__ Exact exact_element(double wxt, double2 wt64, double2 ep
     r.ssx = make_float2(0.f, 0.f);
     if (need_ssx) {
         const double2 wt2d = cmul(wt64, wt64);
-        r.ssx = c64_to_f32(ssx64(b, wxt, wt2d, cmul(wt2d, ep64)));
+        double2 x = ssx64(b, wxt, wt2d, cmul(wt2d, ep64), phys != 0);
+        if (phys) x = sexcut64(x, wxt, ep64);
+        r.ssx = c64_to_f32(x);
     }
     return r;
 }
@@ -619,7 +640,7 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
         if (nflag > 0) {
             wt2 = cmulf(wt, wt);
             Om = cmulf(wt2, ep);
-            if (Q) {
+            if (Q == 1) {
                 eq64 = p.eps[(long)my_igp * p.ng + ig];
                 eq = c64_to_f32(eq64);
             }
@@ -639,9 +660,13 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
             const bool amb = !(wdiffr > 1e-30f) || !(delwr < 1e30f) ||
                              fabsf(wdiffr - limittwo) <= limittwo * GUARD ||
                              fabsf(delwr - limitone) <= limitone * GUARD || fabsf(delwr - to1) <= to1 * GUARD;
+            // physics mode: elements whose Fortran quantities are ill-conditioned in
+            // FP32 (wx^2 - wtilde^2 near 0) or whose sexcut test lies within the guard
+            // band go to the exact sequence as well
+            bool amb2 = false;
             if (__any_sync(__activemask(), amb) && amb) {
                 // exact FP64 sequence for this element (rare)
-                const Exact x = exact_element(wx64[iw], wt64, ep64, eq64, nflag > 0);
+                const Exact x = exact_element(wx64[iw], wt64, ep64, eq64, nflag > 0, Q == 2);
                 A = x.A != 0;
                 B = x.B != 0;
                 dv = x.dv;
@@ -652,7 +677,17 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
                 B = delwr > to1;
                 dv = cmulf(delw, ep);
                 sch = A ? cmulf(delw, eq) : make_float2(0.f, 0.f);
-                if (A) {
+                if (A && Q == 2) {
+                    // cden = wx^2 - wtilde^2 = (wx - wtilde)(wx + wtilde), each factor from an
+                    // FP64 subtraction / addition (gppkernel.deslippe.09.30.2014.f90:302-305)
+                    const float wsr = f64_to_f32_bits(__dadd_rn(wx64[iw], wt64.x));
+                    const float2 cd = cmulf(make_float2(wdr, wdi), make_float2(wsr, wt.y));
+                    const float cd2 = cd.x * cd.x + cd.y * cd.y;
+                    amb2 = !(cd2 > 1e-30f);
+                    const float rd = __frcp_rn(cd2);
+                    const float2 t = cmulf(Om, make_float2(cd.x, -cd.y));
+                    ssx = make_float2(t.x * rd, t.y * rd);
+                } else if (A) {
                     ssx = make_float2(Om.x * iw2[iw], Om.y * iw2[iw]);
                 } else if (B) {
                     float2 c = cmulf(make_float2(4.f * wt2.x, 4.f * wt2.y), make_float2(delw.x + 0.5f, delw.y));
@@ -662,10 +697,25 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
                 } else {
                     ssx = make_float2(0.f, 0.f);
                 }
+                if (Q == 2 && wx64[iw] < 0.0) {
+                    // the Fortran sexcut test, |ssx| > 4|I_eps| (f90:319-320), in squares
+                    const float a2 = ssx.x * ssx.x + ssx.y * ssx.y, c2 = 16.f * (ep.x * ep.x + ep.y * ep.y);
+                    const bool near = !(a2 < 1e30f) || fabsf(a2 - c2) <= c2 * (4.f * GUARD);
+                    amb2 = amb2 || near;
+                    if (!near && a2 > c2) ssx = make_float2(0.f, 0.f);
+                }
+            }
+            if (Q == 2 && nflag > 0 && __any_sync(__activemask(), amb2) && amb2) {
+                const Exact x = exact_element(wx64[iw], wt64, ep64, eq64, nflag > 0, 1);
+                A = x.A != 0;
+                B = x.B != 0;
+                dv = x.dv;
+                sch = x.sch;
+                ssx = x.ssx;
             }
             if (D) {
                 // every element of the image is written (zero where the term is masked)
-                const bool keep = igp >= 0 && (Q || A);
+                const bool keep = igp >= 0 && (Q == 1 || A);
                 const int nt = my_igp / GPP_COLS, row = (my_igp % GPP_COLS) * 3 + iw;
                 tcx::bimg_store<BN>(D + (long)nt * p.kstages * tcx::Cfg<BN>::B_BYTES, p.kstages, row, ig,
                                     keep ? dv.x : 0.f, keep ? dv.y : 0.f);
@@ -1503,6 +1553,7 @@ fk_status gpp_run_half(Ctx& c, const GppDev& r) {
             t.kstages_total = p.kstages;
             t.MT = p.MT; t.NT = p.NT; t.units = p.units;
             t.err = c.errword;
+            t.wait_limit = c.wait_limit;
             if (tcx::encode_rows_map(&t.amap, A, r.nc, r.nc, r.nb) != cudaSuccess)
                 return fail(c, FK_ECUDA, "gpp: cannot describe an input as a tensor map (needs a 16-byte aligned array)");
             auto k = tcx::tc_contract_kernel<EPI_GPP, 64, false>;
@@ -1556,7 +1607,8 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
         cudaError_t e = cudaMemsetAsync(c.errword, 0, sizeof(int), st);  // bounded-wait status
         if (e != cudaSuccess) return cuda_fail(c, e, "gpp: error word");
     }
-    const bool Q = (r.flags & FK_GPP_ROOT_QUIRKS) != 0;
+    // prep variant: 0 = BGW-Kernels/gppKer.cpp, 1 = root gppKer.cpp, 2 = the Fortran source
+    const int Q = (r.flags & FK_GPP_ROOT_QUIRKS) ? 1 : (r.flags & FK_GPP_PHYSICS) ? 2 : 0;
     const int M = r.nb - r.nv;
     c.launches = 0;
     // the first prep pass also maps the columns, writes the epilogue weights and
@@ -1574,8 +1626,21 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
             a.M = M;
             a.counter = counter;
             a.wf = wf;
+            a.asx_neg = Q == 2;
         }
         return a;
+    };
+    auto launch_prep = [&](const PrepArgs& a, dim3 grid) {
+        if (p.mixed) {
+            if (Q == 1) prep_mixed_kernel<1, 64><<<grid, PREP_THREADS, 0, st>>>(a);
+            else if (Q == 2) prep_mixed_kernel<2, 64><<<grid, PREP_THREADS, 0, st>>>(a);
+            else prep_mixed_kernel<0, 64><<<grid, PREP_THREADS, 0, st>>>(a);
+        } else {
+            if (Q == 1) prep64_kernel<1><<<grid, PREP_THREADS, 0, st>>>(a);
+            else if (Q == 2) prep64_kernel<2><<<grid, PREP_THREADS, 0, st>>>(a);
+            else prep64_kernel<0><<<grid, PREP_THREADS, 0, st>>>(a);
+        }
+        ++c.launches;
     };
 
     phase_mark(c, 1);
@@ -1586,12 +1651,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
     if (pipe) {
         if (cudaStreamWaitEvent(st, c.pipe_ev[0], 0) != cudaSuccess)
             return cuda_fail(c, cudaGetLastError(), "gpp: waiting for a block");
-        for (int pass = 0; pass < p.passes; ++pass) {
-            const PrepArgs a = prep_args(pass);
-            if (Q) prep_mixed_kernel<1, 64><<<dim3(p.nch, r.ng), PREP_THREADS, 0, st>>>(a);
-            else prep_mixed_kernel<0, 64><<<dim3(p.nch, r.ng), PREP_THREADS, 0, st>>>(a);
-            ++c.launches;
-        }
+        for (int pass = 0; pass < p.passes; ++pass) launch_prep(prep_args(pass), dim3(p.nch, r.ng));
         if (p.mixed && M > 0) {
             ContractArgs a{};
             a.A = r.aqsn; a.lda = r.nc; a.m0 = r.nv; a.M = M;
@@ -1606,6 +1666,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
             t.kstages_total = p.kstages;
             t.NT = p.NT;
             t.err = c.errword;
+            t.wait_limit = c.wait_limit;
             if (tcx::encode_rows_map(&t.amap, r.aqsn, r.nc, r.nc, r.nb) != cudaSuccess)
                 return fail(c, FK_ECUDA, "gpp: cannot describe aqsntemp as a tensor map");
             set_smem(tcx::tc_contract_kernel<EPI_GPP, 64, false>, tcx::Cfg<64>::SMEM);
@@ -1623,18 +1684,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
             }
         }
     }
-    for (int pass = 0; pass < p.passes && !pipe; ++pass) {
-        const PrepArgs a = prep_args(pass);
-        dim3 grid(p.nch, r.ng);
-        if (p.mixed) {
-            if (Q) prep_mixed_kernel<1, 64><<<grid, PREP_THREADS, 0, st>>>(a);
-            else prep_mixed_kernel<0, 64><<<grid, PREP_THREADS, 0, st>>>(a);
-        } else {
-            if (Q) prep64_kernel<1><<<grid, PREP_THREADS, 0, st>>>(a);
-            else prep64_kernel<0><<<grid, PREP_THREADS, 0, st>>>(a);
-        }
-        ++c.launches;
-    }
+    for (int pass = 0; pass < p.passes && !pipe; ++pass) launch_prep(prep_args(pass), dim3(p.nch, r.ng));
     phase_mark(c, 2);
     if (M > 0 && !pipe) {
         ContractArgs a{};
@@ -1651,6 +1701,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
             t.kstages_total = p.kstages;
             t.MT = p.MT; t.NT = p.NT; t.units = p.units;
             t.err = c.errword;
+            t.wait_limit = c.wait_limit;
             if (tcx::encode_rows_map(&t.amap, r.aqsn, r.nc, r.nc, r.nb) != cudaSuccess)
                 return fail(c, FK_ECUDA, "gpp: cannot describe aqsntemp as a tensor map (needs a 16-byte aligned array)");
             const int grid1 = std::min(p.units, c.sms);
@@ -1889,6 +1940,7 @@ GppJob* gpp_job_create(Ctx& c, const GppDev& r0, int ks, void* ws, size_t bytes,
         t.kstages_total = p.kstages;
         t.MT = p.MT; t.NT = p.NT; t.units = p.units;
         t.err = c.errword;
+        t.wait_limit = c.wait_limit;
         if (tcx::encode_rows_map(&t.amap, r.aqsn, r.nc, r.nc, r.nb) != cudaSuccess) {
             delete j;
             *st = FK_ECUDA;
@@ -1938,7 +1990,7 @@ GppStep* gpp_step_create(Ctx& c, fk_status* st) {
     cudaMemsetAsync(c.errword, 0, sizeof(int), str);
     step_setup_kernel<<<c.sms * 4, 256, 0, str>>>(s->dev);
     prep_table_kernel<64><<<c.sms * prep_per_sm, PREP_THREADS, 0, str>>>(s->dev);
-    tck<<<c.sms, tcx::THREADS, tcx::Cfg<64>::SMEM, str>>>(&s->dev->tc, c.errword);
+    tck<<<c.sms, tcx::THREADS, tcx::Cfg<64>::SMEM, str>>>(&s->dev->tc, c.errword, c.wait_limit);
     rows_table_kernel<<<c.sms * 4, ROWS_THREADS, 0, str>>>(s->dev);
     totals_table_kernel<<<STEP_MAX, ROWS_THREADS, 0, str>>>(s->dev);
     cudaGraph_t g = nullptr;
@@ -2149,6 +2201,7 @@ fk_status gpp_real_run(Ctx& c, const GppRealDev& r) {
             t.kstages_total = p.kstages;
             t.MT = p.MT; t.NT = p.NT; t.units = p.units;
             t.err = c.errword;
+            t.wait_limit = c.wait_limit;
             if (tcx::encode_rows_map(&t.amap, a.A, a.lda, a.K, r.nb) != cudaSuccess)
                 return fail(c, FK_ECUDA, "gpp_real: cannot describe aqsntemp as a tensor map");
             auto k = tcx::tc_contract_kernel<EPI_GPP, 64, false>;

@@ -47,6 +47,7 @@ struct Ctx {
     // host-link bytes of the last fk_gpp / fk_gpp_real / fk_ff call
     unsigned long long h2d_bytes = 0, d2h_bytes = 0;
     int* errword = nullptr;      // device error word of the tensor-core kernels (bounded waits)
+    long long wait_limit = 4000000000LL;  // bound of their waits between roles, SM clock cycles (~2 s)
     // Graphs of repeated fully device-resident calls: key -> (times seen, executable graph).
     struct GraphEntry {
         int seen = 0;

@@ -579,6 +579,24 @@ fk_status fk_server_wait(fk_server_t s, unsigned long long ticket, double timeou
     return st;
 }
 
+fk_status fk_server_cancel(fk_server_t s, unsigned long long ticket) {
+    if (!s) return FK_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return FK_EINVAL;
+    fk::Request* r = it->second;
+    if (r->state != 0) return FK_EBUSY;  // admitted (or finished): it completes as usual
+    auto w = std::find(s->waiting.begin(), s->waiting.end(), r);
+    if (w == s->waiting.end()) return FK_EBUSY;
+    s->waiting.erase(w);
+    s->release(r);  // drops its resident references (it holds no memory yet)
+    r->status = FK_ECANCELED;
+    r->state = 2;
+    r->t_done = fk::now_s();
+    s->done_cv.notify_all();
+    return FK_OK;
+}
+
 fk_status fk_server_tune(fk_server_t s, int nb, int nv, int nc, int ng, unsigned flags, int* chosen_ks) {
     if (!s || nb <= 0 || nc <= 0 || ng <= 0 || nv < 0 || nv > nb || ng > 65535) return FK_EINVAL;
     if (flags & ~(unsigned)FK_GPP_ROOT_QUIRKS) return FK_EINVAL;

@@ -15,17 +15,22 @@ namespace {
 // All intermediates of one call: branch-resolved factors, chunk and slice
 // partial sums, per-band rows and the output block.  Module data of this
 // translation unit: the CUDA runtime reserves it on a GPU when it loads the
-// module there (at the first call's symbol lookup).
+// module there.  Under lazy module loading (the default since CUDA 12.2) that
+// happens at the first call's symbol lookup; with CUDA_MODULE_LOADING=EAGER
+// every context that loads the library reserves it at once, whether or not it
+// ever calls fk_gpp_static.
 __device__ __align__(256) unsigned char g_gpp_scratch[FK_GPP_STATIC_SCRATCH_BYTES];
 
 constexpr int MAX_DEVICES = 64;
+// The scratch address and SM count of each device, found by the first call
+// that succeeds there (base == nullptr: not set up yet).  A failed set-up is
+// not kept: the next call on that device tries again.
 struct DevScratch {
     void* base = nullptr;
     int sms = 0;
-    cudaError_t status = cudaSuccess;
 };
 DevScratch g_scratch[MAX_DEVICES];
-std::once_flag g_setup[MAX_DEVICES];
+std::mutex g_setup_mu;
 
 // Device (or managed) memory that a kernel may read where it lies: the
 // kernels move rows with 16-byte and bulk copies, so it must start on a
@@ -73,15 +78,27 @@ extern "C" fk_status fk_gpp_static(void* stream, int nb, int nv, int nc, int ng,
         cudaGetLastError();
         return FK_ECUDA;
     }
-    // set-up, once per device: the scratch array's address and the SM count
-    std::call_once(g_setup[dev], [dev]() {
-        DevScratch& s = g_scratch[dev];
-        s.status = cudaGetSymbolAddress(&s.base, g_gpp_scratch);
-        if (s.status == cudaSuccess) s.status = cudaDeviceGetAttribute(&s.sms, cudaDevAttrMultiProcessorCount, dev);
-        if (s.status != cudaSuccess) cudaGetLastError();
-    });
-    const DevScratch& s = g_scratch[dev];
-    if (s.status != cudaSuccess || !s.base) return FK_ECUDA;
+    // set-up, once per device (until it succeeds): the scratch array's address
+    // and the SM count.  The address stays valid for the life of the primary
+    // context; a cudaDeviceReset after the first call is not supported.
+    DevScratch s;
+    {
+        std::lock_guard<std::mutex> lk(g_setup_mu);
+        DevScratch& g = g_scratch[dev];
+        if (!g.base) {
+            void* base = nullptr;
+            int sms = 0;
+            cudaError_t e = cudaGetSymbolAddress(&base, g_gpp_scratch);
+            if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess || !base) {
+                cudaGetLastError();
+                return FK_ECUDA;
+            }
+            g.sms = sms;
+            g.base = base;
+        }
+        s = g;
+    }
 
     fk::Ctx c;
     c.device = dev;

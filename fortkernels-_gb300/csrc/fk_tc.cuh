@@ -52,6 +52,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long l
     return true;
 }
 
+// The warp-uniform outcome of a condition every lane evaluates (all 32 lanes
+// must call it).  A bounded wait inside a warp whose lanes then execute warp-
+// collective instructions (shuffles, __syncwarp, tcgen05.ld.sync.aligned) must
+// give up in all lanes or in none: each lane waits, and the vote makes the
+// decision common, so that a lane that timed out never leaves the others
+// behind at a collective.
+__device__ __forceinline__ bool warp_all(bool v) { return __all_sync(0xffffffffu, v); }
+
 // Make generic-proxy writes to shared memory visible to the async proxy
 // (tensor-core operand reads, bulk copies).
 __device__ __forceinline__ void fence_proxy_async_smem() {

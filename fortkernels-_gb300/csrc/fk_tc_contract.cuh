@@ -49,7 +49,13 @@ constexpr int THREADS_FF = 576;  // FF: MMA, producer, 16 epilogue warps
 // quarter, all columns.
 constexpr int FF_EPI_WARPS = 4;
 constexpr int NCONV = 8;          // converter warps
-constexpr long long WAIT_LIMIT = 4000000000LL;  // ~2 s at 2 GHz
+// Default bound of every wait on another role of the CTA (SM clock cycles,
+// ~2 s at 2 GHz); a launch may pass a different one (TcArgs::wait_limit).
+constexpr long long WAIT_LIMIT = 4000000000LL;
+// Bound of the waits at the end of a CTA for its own asynchronous work (bulk
+// copies still landing, issued MMAs): these always run to completion, so they
+// keep the default bound whatever limit the launch passes.
+constexpr long long DRAIN_LIMIT = 4000000000LL;
 
 template <int BN, bool WSMEM = false>
 struct Cfg {
@@ -86,6 +92,8 @@ struct TcArgs {
     int MT, NT, units;
     int mt0;              // first m-tile of the launch (its units cover m-tiles mt0 .. mt0+MT-1)
     int* err;             // device error word (nonzero: a wait timed out)
+    long long wait_limit; // bound of the waits between roles, cycles (0 is allowed: any wait that
+                          // is not satisfied on its first test gives up)
 };
 
 // Split an FP32 value into three BF16 pieces (exact: 8+8+8 significand bits).
@@ -178,7 +186,7 @@ struct TableReqs {
 };
 
 template <int EPI, int BN, bool AIMG, class Src>
-__device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
+__device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long long wait_limit) {
     using C = Cfg<BN, EPI == EPI_FF>;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-aligned operand area
@@ -260,14 +268,14 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                 const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
                 for (int st0 = 0; st0 < nst && ok; st0 += C::CHUNK_STAGES, ++chunk) {
                     const int b = chunk & 1;
-                    if (!tc::mbar_wait(&accEmpty[b], ((chunk >> 1) & 1) ^ 1, WAIT_LIMIT)) { fail(1); ok = false; break; }
+                    if (!tc::mbar_wait(&accEmpty[b], ((chunk >> 1) & 1) ^ 1, wait_limit)) { fail(1); ok = false; break; }
                     tc::tc_fence_after();
                     const uint32_t dX = tmem + (uint32_t)(b * C::ACC_COLS), dY = dX + 2 * BN;
                     const int st1 = min(nst, st0 + C::CHUNK_STAGES);
                     for (int st = st0; st < st1; ++st, ++g) {
                         const int s = g % C::STAGES;
                         const uint32_t par = (g / C::STAGES) & 1;
-                        if (!tc::mbar_wait(&fullA[s], par, WAIT_LIMIT) || !tc::mbar_wait(&fullB[s], par, WAIT_LIMIT)) {
+                        if (!tc::mbar_wait(&fullA[s], par, wait_limit) || !tc::mbar_wait(&fullB[s], par, wait_limit)) {
                             fail(2);
                             ok = false;
                             break;
@@ -303,7 +311,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
             }
             // drain: every issued MMA has completed before TMEM is released
             tc::mma_commit(done);
-            if (!tc::mbar_wait(done, 0, WAIT_LIMIT)) fail(4);
+            if (!tc::mbar_wait(done, 0, DRAIN_LIMIT)) fail(4);
         }
     } else if (warp == 1) {
         // ------------------------------------------------ bulk copies
@@ -311,6 +319,11 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
         // all lanes (GPP): the next stage's FP64 A rows into the staging buffer.
         int g = 0;
         bool ok = true;
+        // the last copy issued into each stage / staging half (-1: none), so
+        // that the CTA can wait for every copy it started before it exits
+        int last_st[C::STAGES], last_f[2] = {-1, -1};
+#pragma unroll
+        for (int s = 0; s < C::STAGES; ++s) last_st[s] = -1;
         for (int u = blockIdx.x; u < src.units() && ok; u += gridDim.x) {
             int lu;
             const TcArgs& t = src.at(u, lu);
@@ -332,7 +345,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                     // FP64 rows in two halves of BK/2 k-values, each into its own half of the
                     // staging buffer as soon as the converters have read that half of the last stage
                     for (int h = 0; h < 2 && ok; ++h) {
-                        if (!tc::mbar_wait(&fEmpty[h], (g & 1) ^ 1, WAIT_LIMIT) || s_abort) {
+                        if (!tc::warp_all(tc::mbar_wait(&fEmpty[h], (g & 1) ^ 1, wait_limit) && !s_abort)) {
                             fail(64);
                             ok = false;
                             break;
@@ -341,12 +354,13 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                             tc::mbar_arrive_expect_tx(&fFull[h], C::F64_BYTES / 2);
                             tc::tma_load_2d(sF + h * (BM * BK / 2), &t.amap, 2 * (k0 + st * BK + h * (BK / 2)),
                                             a.m0 + mt * BM, &fFull[h]);
+                            last_f[h] = g;
                         }
                     }
                     if (!ok) break;
                 }
                 if (lane == 0) {
-                    if (!tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, WAIT_LIMIT) || s_abort) {
+                    if (!tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, wait_limit) || s_abort) {
                         fail(8);
                         ok = false;
                     } else {
@@ -359,11 +373,30 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                             tc::mbar_arrive_expect_tx(&fullA[s], C::A_BYTES);
                             tc::bulk_g2s(base + s * C::STAGE_BYTES, asrc, C::A_BYTES, &fullA[s]);
                         }
+                        last_st[s] = g;
                     }
                 }
                 ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
                 if (!ok) break;
             }
+        }
+        // Every copy this warp started lands before the CTA exits (after a
+        // timed-out wait elsewhere, the consumers may never have waited for
+        // them).  A stage's copies start only after its previous phase was
+        // consumed, so each barrier owes at most its last issued phase.
+        if (lane == 0) {
+            bool drained = true;
+#pragma unroll
+            for (int s = 0; s < C::STAGES; ++s)
+                if (last_st[s] >= 0) {
+                    const uint32_t par = (uint32_t)(last_st[s] / C::STAGES) & 1u;
+                    drained = tc::mbar_wait(&fullB[s], par, DRAIN_LIMIT) && drained;
+                    if (AIMG) drained = tc::mbar_wait(&fullA[s], par, DRAIN_LIMIT) && drained;
+                }
+            if (!AIMG)
+                for (int h = 0; h < 2; ++h)
+                    if (last_f[h] >= 0) drained = tc::mbar_wait(&fFull[h], (uint32_t)last_f[h] & 1u, DRAIN_LIMIT) && drained;
+            if (!drained) fail(128);
         }
     } else if ((warp >= 4 && warp < 8) || AIMG) {
         // ------------------------------------------------------- epilogue
@@ -411,7 +444,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
             ff32 accx[GMAX] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, accy[GMAX] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
             for (int st0 = 0; st0 < nst; st0 += C::CHUNK_STAGES, ++chunk) {
                 const int b = chunk & 1;
-                if (!tc::mbar_wait(&accFull[b], (chunk >> 1) & 1, WAIT_LIMIT) || s_abort) {
+                if (!tc::warp_all(tc::mbar_wait(&accFull[b], (chunk >> 1) & 1, wait_limit) && !s_abort)) {
                     fail(16);
                     ok = false;
                     break;
@@ -507,7 +540,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                 const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
                 for (int st = 0; st < nst; ++st, ++g) {
                     const int s = g % C::STAGES;
-                    if (!tc::mbar_wait(&fFull[0], g & 1, WAIT_LIMIT) || s_abort) {
+                    if (!tc::warp_all(tc::mbar_wait(&fFull[0], g & 1, wait_limit) && !s_abort)) {
                         fail(32);
                         ok = false;
                         break;
@@ -517,7 +550,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                     const int kk = lane & 15, rr = lane >> 4;
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
-                        if (h == 1 && (!tc::mbar_wait(&fFull[1], g & 1, WAIT_LIMIT) || s_abort)) {
+                        if (h == 1 && !tc::warp_all(tc::mbar_wait(&fFull[1], g & 1, wait_limit) && !s_abort)) {
                             fail(32);
                             ok = false;
                             break;
@@ -533,7 +566,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
                         if (lane == 0) tc::mbar_arrive(&fEmpty[h]);
                     }
                     if (!ok) break;
-                    if (!tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, WAIT_LIMIT) || s_abort) {
+                    if (!tc::warp_all(tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, wait_limit) && !s_abort)) {
                         fail(32);
                         ok = false;
                         break;
@@ -572,13 +605,13 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err) {
 
 template <int EPI, int BN, bool AIMG>
 __global__ void __launch_bounds__(AIMG ? THREADS_FF : THREADS, 1) tc_contract_kernel(const __grid_constant__ TcArgs t) {
-    tc_contract_body<EPI, BN, AIMG>(OneReq{t}, t.err);
+    tc_contract_body<EPI, BN, AIMG>(OneReq{t}, t.err, t.wait_limit);
 }
 
 // Units of several requests from a device table (the served step).
 template <int EPI, int BN, bool AIMG>
-__global__ void __launch_bounds__(AIMG ? THREADS_FF : THREADS, 1) tc_contract_table_kernel(const TcTable* tab, int* err) {
-    tc_contract_body<EPI, BN, AIMG>(TableReqs{tab, 0}, err);
+__global__ void __launch_bounds__(AIMG ? THREADS_FF : THREADS, 1) tc_contract_table_kernel(const TcTable* tab, int* err, long long wait_limit) {
+    tc_contract_body<EPI, BN, AIMG>(TableReqs{tab, 0}, err, wait_limit);
 }
 
 // Epilogue weight tables in FP32, column-major (row m contiguous):

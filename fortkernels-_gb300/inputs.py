@@ -97,13 +97,15 @@ def gpp_synthetic(number_bands: int, nvband: int, ncouls: int, ngpown: int, seed
            "reference" e_lk - e_n1kq + dw*(iw-1) = {3,4,5}
            "stress"    {0.4, 3, 5}: a frequency below 0.5 makes the third branch
                        (neither sch nor ssx, |delw|^2 <= 1e-6) reachable
+           "negative"  {-1.2, -0.7, 1.1}: frequencies below zero, where the Fortran
+                       source's sexcut test applies (FK_GPP_PHYSICS)
     """
     rng = np.random.default_rng(seed)
     aqsm = _cu(rng, (number_bands, ncouls))
     aqsn = _cu(rng, (number_bands, ncouls))
     eps = _cu(rng, (ngpown, ncouls))
     wxa = {"baseline": np.array([9.0, 10.0, 11.0]), "reference": gpp_wx(),
-           "stress": np.array([0.4, 3.0, 5.0])}[wx]
+           "stress": np.array([0.4, 3.0, 5.0]), "negative": np.array([-1.2, -0.7, 1.1])}[wx]
     if dist == "uniform":
         wt = rng.uniform(0.5, 2.0, (ngpown, ncouls)) + 1j * rng.uniform(-0.05, 0.05, (ngpown, ncouls))
     elif dist == "branch":

@@ -53,7 +53,8 @@ typedef enum {
     FK_ECUDA = 3,     /* a CUDA call failed (no device, launch error, ...)    */
     FK_ETIMEOUT = 4,  /* a bounded device-side wait gave up                   */
     FK_EBUSY = 5,     /* admission refused (serving: over the memory budget)  */
-    FK_ENOTSUP = 6    /* valid request the library does not support          */
+    FK_ENOTSUP = 6,   /* valid request the library does not support          */
+    FK_ECANCELED = 7  /* serving: the request was cancelled before it ran     */
 } fk_status;
 
 typedef enum {
@@ -98,6 +99,15 @@ const char* fk_version(void);
                                    conjugate pair (noflagOCC_solver :206-242 with the
                                    driver's 512-wide blocks :430-447, flagOCC_solver
                                    :90-139); not with FK_GPP_ROOT_QUIRKS or FK_GPP_ACHSTEMP */
+#define FK_GPP_PHYSICS     0x8u /* the Fortran source of the kernel where it differs from
+                                   the C++ ("physics" mode; the default is the C++):
+                                   branch-A ssx with cden = wx**2 - wtilde**2
+                                   (gppkernel.deslippe.09.30.2014.f90:302-305, C++:
+                                   pow(wx,2), BGW-Kernels/gppKer.cpp:41-44), the sexcut
+                                   test applied when wx < 0 (f90:319-320; the C++ test
+                                   abs(wx) < 0 never fires), and asxtemp subtracted
+                                   (f90:393; C++ adds, :419); not with
+                                   FK_GPP_ROOT_QUIRKS or FK_GPP_HALF_SUM */
 #define FK_GPP_REAL_ZERO_MASKED 0x10u /* fk_gpp_real only: a masked noflag term
                                    contributes 0 (the else left commented out at
                                    gppKer_real.cpp:371-372) instead of the value the
@@ -161,9 +171,18 @@ fk_status fk_gpp_real(fk_ctx_t ctx, int number_bands, int nvband, int ncouls, in
  * to start at zero: every value a call reads was written earlier in the same
  * call.
  *
+ * When the memory is taken: under lazy module loading (CUDA's default since
+ * 12.2) the array is reserved on a GPU when the first fk_gpp_static call
+ * there looks it up; with CUDA_MODULE_LOADING=EAGER every process that loads
+ * the library reserves 64 MiB on each GPU it uses, even if it never calls
+ * fk_gpp_static.
+ *
  * Set-up: the first call on each device looks up the array's address
  * (cudaGetSymbolAddress), which may load that part of the library onto the
- * GPU; make the first call on a device before any stream capture.
+ * GPU; make the first call on a device before any stream capture.  A set-up
+ * that fails returns FK_ECUDA and is tried again by the next call.  The
+ * address is kept for the life of the process: calling cudaDeviceReset on a
+ * device after its first fk_gpp_static call is not supported.
  *
  * Concurrency: all calls on one GPU share the one array.  Calls whose work
  * overlaps in time (from different threads, or on different streams without
@@ -283,6 +302,12 @@ fk_status fk_server_submit(fk_server_t srv, const fk_gpp_request* req, unsigned 
  * returns its status; latency_s (may be NULL) gets submit-to-completion time.
  * The ticket is consumed when the request has completed. */
 fk_status fk_server_wait(fk_server_t srv, unsigned long long ticket, double timeout_s, double* latency_s);
+/* Cancels a request that is still waiting for admission: it leaves the queue
+ * without running (its outputs are not written), its references to resident
+ * arrays are dropped, and fk_server_wait on its ticket returns FK_ECANCELED
+ * at once.  A request already admitted runs to completion: FK_EBUSY (wait for
+ * it as usual).  FK_EINVAL for an unknown ticket. */
+fk_status fk_server_cancel(fk_server_t srv, unsigned long long ticket);
 fk_status fk_server_stats(fk_server_t srv, fk_server_info* out);
 /* Autotunes the plan of one request shape (while the server is idle, else
  * FK_EBUSY): runs the shape with synthetic inputs through the server's steps
@@ -312,6 +337,31 @@ fk_status fk_last_kernel_time(fk_ctx_t ctx, float* ms, int* launches);
  * the frequency planes of I_epsR/I_epsA the request reads) and its outputs
  * copied to host arrays.  Device arrays move nothing. */
 fk_status fk_last_transfer(fk_ctx_t ctx, unsigned long long* h2d, unsigned long long* d2h);
+
+/* ------------------------------------------------------------ diagnostics */
+
+/* Bound, in SM clock cycles, of every wait between the warp roles of the
+ * tensor-core kernels (default 4e9, about 2 s at 2 GHz; a negative value
+ * restores the default).  A wait that runs out makes its kernel record a
+ * code in the context's error word, let the copies and MMAs it has already
+ * started finish, and return; the call then returns FK_ETIMEOUT and clears
+ * the error word, so the context stays usable.  Lowering the bound is a test
+ * hook: with 0 cycles any wait not satisfied on its first test gives up.  No
+ * counterpart in the reference (its loops never wait on another part of the
+ * GPU). */
+fk_status fk_set_wait_limit(fk_ctx_t ctx, long long cycles);
+/* Runs a one-warp kernel that waits, through the same bounded wait, on a
+ * barrier that nothing arrives on, giving up after `cycles` (0 .. 4e9)
+ * cycles: returns FK_ETIMEOUT through the same error-word path as a
+ * timed-out contraction and leaves the context usable.  No counterpart in the
+ * reference. */
+fk_status fk_selftest_timeout(fk_ctx_t ctx, long long cycles);
+/* Decodes a device error word of the tensor-core kernels: FK_OK for 0, else
+ * FK_ETIMEOUT, with a description naming each kind of wait that gave up
+ * written to msg (msg_len bytes, NUL-terminated; msg may be NULL).  Calls
+ * that see a nonzero word return this status and keep this description as
+ * their fk_last_error.  No GPU needed.  No counterpart in the reference. */
+fk_status fk_wait_error_status(int word, char* msg, size_t msg_len);
 
 #ifdef __cplusplus
 }

@@ -70,9 +70,11 @@ static int gpp_igp(int my_igp, int nc, const int* inv_igp_index,
 }
 
 /* ssxt_scht_solver, BGW-Kernels/gppKer.cpp:19-65.  ieps_s is the I_eps value
- * the caller passes as I_eps_array_igp_myIgp. */
+ * the caller passes as I_eps_array_igp_myIgp.  physics != 0: the Fortran
+ * form of the same block, gppkernel.deslippe.09.30.2014.f90:288-320 (branch-A
+ * cden = wxt**2 - wtilde2, and the sexcut test with wxt < 0). */
 static inline void gpp_solver(double wxt, cx wtilde, cx wtilde2, cx Omega2,
-                              cx matngmatmgp, cx ieps_s, cx* ssxa, cx* scha) {
+                              cx matngmatmgp, cx ieps_s, cx* ssxa, cx* scha, int physics) {
     const double to1 = 1e-6;
     const double limitone = 1.0 / (to1 * 4.0);
     const double limittwo = 0.5 * 0.5;
@@ -85,11 +87,18 @@ static inline void gpp_solver(double wxt, cx wtilde, cx wtilde2, cx Omega2,
     double wdiffr = cx_norm2(wdiff);
     if ((wdiffr > limittwo) && (delwr < limitone)) {
         sch = cx_mul(delw, ieps_s);
-        double w2 = wxt * wxt;               /* pow(wxt,2) */
-        double rd = 1.00 / (w2 * w2);        /* real(cden*conj(cden)) */
-        /* Omega2 * conj(cden) with cden = (w2, 0) */
-        cx t = cx_make(Omega2.re * w2 - Omega2.im * (-0.0), Omega2.re * (-0.0) + Omega2.im * w2);
-        ssx = cx_scale(t, rd);
+        if (physics) {
+            /* cden = wxt**2 - wtilde2; rden = 1/(cden*conj(cden)); ssx = Omega2*conj(cden)*rden */
+            cx cd = cx_make(wxt * wxt - wtilde2.re, 0.0 - wtilde2.im);
+            double rd = 1.0 / cx_norm2(cd);
+            ssx = cx_scale(cx_mul(Omega2, cx_conj(cd)), rd);
+        } else {
+            double w2 = wxt * wxt;               /* pow(wxt,2) */
+            double rd = 1.00 / (w2 * w2);        /* real(cden*conj(cden)) */
+            /* Omega2 * conj(cden) with cden = (w2, 0) */
+            cx t = cx_make(Omega2.re * w2 - Omega2.im * (-0.0), Omega2.re * (-0.0) + Omega2.im * w2);
+            ssx = cx_scale(t, rd);
+        }
     } else if (delwr > to1) {
         sch = cx_make(0.0, 0.0);
         cx c = cx_mul(cx_scale(wtilde2, 4.00), cx_make(delw.re + 0.50, delw.im));
@@ -100,7 +109,10 @@ static inline void gpp_solver(double wxt, cx wtilde, cx wtilde2, cx Omega2,
         sch = cx_make(0.0, 0.0);
         ssx = cx_make(0.0, 0.0);
     }
-    /* the sexcut test (:60-61) requires abs(wxt) < 0 and never fires */
+    /* the C++ sexcut test (:60-61) requires abs(wxt) < 0 and never fires; the
+     * Fortran one (:319-320) zeroes ssx when wxt < 0 and |ssx| > sexcut*|I_eps| */
+    if (physics && wxt < 0.0 && hypot(ssx.re, ssx.im) > 4.0 * hypot(ieps_s.re, ieps_s.im))
+        ssx = cx_make(0.0, 0.0);
     *ssxa = cx_mul(matngmatmgp, ssx);
     *scha = cx_mul(matngmatmgp, sch);
 }
@@ -217,7 +229,9 @@ int orc_gpp(int nb, int nv, int nc, int ng,
             double* achstemp, double* sch_out, double* ssx_out) {
     if (nb <= 0 || nc <= 0 || ng <= 0 || nv < 0 || nv > nb) return -1;
     const int quirk = (flags & ORC_GPP_ROOT_QUIRKS) != 0;
+    const int physics = (flags & ORC_GPP_PHYSICS) != 0;
     if (quirk && (long)(ng - 1) * ng + nc > (long)ng * nc) return -1;
+    if (physics && (flags & (ORC_GPP_ROOT_QUIRKS | ORC_GPP_HALF_SUM))) return -1;
     set_threads(nthreads);
     const double limitone = 1.0 / (1e-6 * 4.0);
     const double limittwo = 0.5 * 0.5;
@@ -258,7 +272,7 @@ int orc_gpp(int nb, int nv, int nc, int ng,
                         cx matngmatmgp = cx_mul(cx_ld(nrow, ig), mygpvar1);
                         cx ieps_s = quirk ? cx_ld(I_eps, (long)my_igp * ng + ig) : cx_ld(erow, ig);
                         cx ssxa, scha;
-                        gpp_solver(wxt, wt, wt2, Omega2, matngmatmgp, ieps_s, &ssxa, &scha);
+                        gpp_solver(wxt, wt, wt2, Omega2, matngmatmgp, ieps_s, &ssxa, &scha, physics);
                         ssxt = cx_add(ssxt, ssxa);
                         scht = cx_add(scht, scha);
                     }
@@ -310,7 +324,8 @@ int orc_gpp(int nb, int nv, int nc, int ng,
     kcx acc[3] = {KCX_ZERO, KCX_ZERO, KCX_ZERO};
     kcx asx[3] = {KCX_ZERO, KCX_ZERO, KCX_ZERO};
     kcx st = KCX_ZERO;
-    const double occ = 1.0;
+    /* asxtemp += ssx*occ*vcoul (BGW-Kernels/gppKer.cpp:419); the Fortran subtracts it (f90:393) */
+    const double occ = physics ? -1.0 : 1.0;
     for (int n1 = 0; n1 < nb; ++n1) {
         kcx n1loc = KCX_ZERO;
         for (int my_igp = 0; my_igp < ng; ++my_igp) {

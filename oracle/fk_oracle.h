@@ -32,6 +32,13 @@ extern "C" {
                                      I_eps[my_igp*ngpown+ig] (gppKer.cpp:139) */
 #define ORC_GPP_ACHSTEMP    0x2u  /* compute the static-CH remainder achstemp
                                      as in gppkernel.deslippe.09.30.2014.f90:195-229 */
+#define ORC_GPP_PHYSICS     0x8u  /* the Fortran source of the kernel
+                                     (gppkernel.deslippe.09.30.2014.f90) where it
+                                     differs from the C++: branch-A ssx with
+                                     cden = wx**2 - wtilde**2 (:302-305), the sexcut
+                                     test applied when wx < 0 (:319-320), and asxtemp
+                                     subtracted (:393).  Parity unpinned: no Fortran
+                                     compiler was available to run the source. */
 #define ORC_GPP_HALF_SUM    0x4u  /* gppsum == 1 of gppKerSeq.cpp: the sum over ig
                                      runs below igp with the conjugate pair term
                                      (flagOCC_solver :90-139, noflagOCC_solver

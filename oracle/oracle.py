@@ -23,6 +23,7 @@ REF_DIR = os.path.join(HERE, "_ref")
 ORC_GPP_ROOT_QUIRKS = 0x1
 ORC_GPP_ACHSTEMP = 0x2
 ORC_GPP_HALF_SUM = 0x4
+ORC_GPP_PHYSICS = 0x8
 ORC_GPP_REAL_ZERO_MASKED = 0x10
 ORC_FF_SCHDT_GEMM = 0x1
 ORC_FF_PHYSICS = 0x2
@@ -32,11 +33,13 @@ _lib = None
 
 
 def build(quiet: bool = True) -> None:
-    """Compile liboracle.so (and oracle/_ref/ when the reference is present)."""
+    """Compile liboracle.so (and oracle/_ref/ when the reference sources are at hand:
+    FK_REFERENCE_DIR, or their copy in oracle/_ref/src/)."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"], stdout=out)
-    if os.path.isdir("/root/reference"):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref"], stdout=out)
+    ref = os.environ.get("FK_REFERENCE_DIR")
+    if (ref and os.path.isdir(ref)) or os.path.isdir(os.path.join(REF_DIR, "src")):
+        subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "ref"], stdout=out)
 
 
 def lib():

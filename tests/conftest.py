@@ -60,6 +60,23 @@ def scaled_err(res, ref, scale):
     return float(np.max(np.abs(res - ref) / den))
 
 
+def mixed_gate(res, ref, scales, tol=1e-6, kappa_max=4.0, keys=None):
+    """The mixed-precision gate.  Plain relative error (rel: max |res - ref| /
+    max |ref| over each output) is asserted for every output that is not a
+    cancellation, i.e. whose contributions' root-sum-square is at most
+    kappa_max times its magnitude; an output that cancels more is gated by its
+    error at the natural scale (scaled_err), with the plain relative error
+    recorded beside it.  Returns {output: {rel, scaled, kappa}}."""
+    import numpy as np
+    errs = {}
+    for k in (keys or scales):
+        kappa = float(np.max(scales[k])) / max(float(np.max(np.abs(ref[k]))), 1e-300)
+        e_rel, e_sc = rel(res[k], ref[k]), scaled_err(res[k], ref[k], scales[k])
+        errs[k] = {"rel": e_rel, "scaled": e_sc, "kappa": kappa}
+        assert (e_rel if kappa <= kappa_max else e_sc) <= tol, (k, errs[k])
+    return errs
+
+
 def gpp_igp(p):
     import numpy as np
     nc = p["ncouls"]

@@ -1,7 +1,8 @@
 """Regenerate the golden fixtures of tests/golden/ from the reference.
 
-Needs the reference tree (its drivers and harnesses are compiled into
-oracle/_ref/ by `make -C oracle ref`).  It runs:
+Needs the reference tree, named by the FK_REFERENCE_DIR environment variable
+(its drivers and harnesses are compiled into oracle/_ref/ by
+`make -C oracle ref-src ref`).  It runs:
   * the unmodified reference drivers (BGW-Kernels/gppKer.cpp, repo-root
     gppKer.cpp, gppKer_orig.cpp, gppKerSeq.cpp, gppKer_real.cpp,
     FFKer_cori/ffKernel.cpp) with their own constant inputs, recording what

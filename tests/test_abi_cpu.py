@@ -42,7 +42,7 @@ def test_abi_has_no_torch_dependency(fk):
 def test_version_and_strerror(fk):
     lib = fk._native.load()
     assert lib.fk_version().decode().startswith("fk_gb300")
-    for code in range(7):
+    for code in range(8):
         assert lib.fk_strerror(code).decode()
     assert lib.fk_strerror(99).decode() == "unknown status"
 
@@ -87,3 +87,25 @@ def test_python_argument_checks(fk):
     assert fk.precision_code("mixed") == fk.FK_MIXED and fk.precision_code("fp64") == fk.FK_FP64
     with pytest.raises(ValueError):
         fk.precision_code("fp8")
+
+
+def test_wait_error_word_maps_to_timeout(fk):
+    """The device error word of the tensor-core kernels (set when a bounded
+    wait gives up) maps to FK_ETIMEOUT with a message naming the waits; 0 is
+    FK_OK.  Host logic only: no GPU."""
+    lib = fk._native.load()
+    buf = ctypes.create_string_buffer(512)
+    assert lib.fk_wait_error_status(0, buf, 512) == fk._native.FK_OK
+    assert lib.fk_wait_error_status(0x10, buf, 512) == fk._native.FK_ETIMEOUT
+    assert b"epilogue" in buf.value and b"0x10" in buf.value
+    assert lib.fk_wait_error_status(0x2 | 0x20 | 0x80, buf, 512) == fk._native.FK_ETIMEOUT
+    msg = buf.value.decode()
+    assert "operand stage" in msg and "converter" in msg and "last copies" in msg
+    assert lib.fk_wait_error_status(0x100, buf, 512) == fk._native.FK_ETIMEOUT
+    assert "self-test" in buf.value.decode()
+    assert lib.fk_wait_error_status(0x4000, buf, 512) == fk._native.FK_ETIMEOUT
+    assert "unknown" in buf.value.decode()
+    small = ctypes.create_string_buffer(8)
+    assert lib.fk_wait_error_status(0x1, small, 8) == fk._native.FK_ETIMEOUT
+    assert len(small.value) == 7  # truncated, NUL-terminated
+    assert lib.fk_wait_error_status(0x1, None, 0) == fk._native.FK_ETIMEOUT

@@ -10,7 +10,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import gpp_scales, rel, scaled_err
+from conftest import gpp_scales, mixed_gate, rel
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
@@ -44,9 +44,7 @@ def test_gpp_fp64_matches_oracle(ctx, fk, orc, case):
 
 
 def check_mixed(res, ref, scales, tol=TOLMX):
-    errs = {k: scaled_err(res[k], ref[k], scales[k]) for k in scales}
-    assert all(e <= tol for e in errs.values()), errs
-    return errs
+    return mixed_gate(res, ref, scales, tol)
 
 
 @pytest.mark.parametrize("case", CASES, ids=lambda c: "x".join(map(str, c[:4])) + "-" + c[4])
@@ -264,3 +262,39 @@ def test_profiling_times_the_contraction_kernel(ctx, fk, prec):
         assert n2 == 2 and ms2 > 0
     finally:
         ctx.set_profiling(False)
+
+
+PHYS_CASES = [
+    # (nb, nv, nc, ng, dist, index, wx)
+    (512, 2, 2048, 64, "uniform", "baseline", "baseline"),
+    (64, 2, 777, 7, "branch", "reference", "stress"),
+    (33, 5, 1000, 13, "branch", "baseline", "negative"),   # sexcut test of the Fortran source
+    (40, 2, 2048, 16, "uniform", "baseline", "negative"),
+]
+
+
+@pytest.mark.parametrize("case", PHYS_CASES, ids=lambda c: "x".join(map(str, c[:4])) + "-" + c[6])
+def test_gpp_physics_fp64_matches_oracle(ctx, fk, orc, case):
+    """FK_GPP_PHYSICS (the Fortran source's ssx, sexcut test and asxtemp sign)
+    against the oracle's physics mode; parity unpinned against the Fortran
+    itself, which no compiler here can build."""
+    nb, nv, nc, ng, dist, index, wx = case
+    p = fk.inputs.gpp_synthetic(nb, nv, nc, ng, seed=nb + nc + 1, dist=dist, index=index, wx=wx)
+    ref = orc.gpp(p, flags=orc.ORC_GPP_PHYSICS)
+    check(ctx.gpp(p, "fp64", fk.FK_GPP_PHYSICS), ref, TOL64)
+
+
+@pytest.mark.parametrize("case", PHYS_CASES, ids=lambda c: "x".join(map(str, c[:4])) + "-" + c[6])
+def test_gpp_physics_mixed_within_1e6(ctx, fk, orc, case):
+    nb, nv, nc, ng, dist, index, wx = case
+    p = fk.inputs.gpp_synthetic(nb, nv, nc, ng, seed=nb + nc + 1, dist=dist, index=index, wx=wx)
+    ref = ctx.gpp(p, "fp64", fk.FK_GPP_PHYSICS)
+    check_mixed(ctx.gpp(p, "mixed", fk.FK_GPP_PHYSICS), ref, gpp_scales(p, orc, orc.ORC_GPP_PHYSICS))
+
+
+def test_gpp_physics_rejects_other_drivers(ctx, fk):
+    p = fk.inputs.gpp_synthetic(8, 2, 256, 4, seed=1)
+    for extra in (fk.FK_GPP_ROOT_QUIRKS, fk.FK_GPP_HALF_SUM):
+        with pytest.raises(fk.FKError) as e:
+            ctx.gpp(p, "fp64", fk.FK_GPP_PHYSICS | extra)
+        assert e.value.status == fk._native.FK_EINVAL

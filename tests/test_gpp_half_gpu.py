@@ -16,7 +16,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import gpp_scales, rel, scaled_err
+from conftest import gpp_scales, mixed_gate, rel
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
@@ -69,8 +69,7 @@ def test_half_sum_mixed_within_1e6(ctx, fk, orc, case):
     ref = ctx.gpp(p, "fp64", fk.FK_GPP_HALF_SUM)
     res = ctx.gpp(p, "mixed", fk.FK_GPP_HALF_SUM)
     scales = gpp_scales(p, orc, orc.ORC_GPP_HALF_SUM)
-    errs = {k: scaled_err(res[k], ref[k], scales[k]) for k in scales}
-    assert all(e <= TOLMX for e in errs.values()), errs
+    mixed_gate(res, ref, scales, TOLMX)
 
 
 def seq_entries():

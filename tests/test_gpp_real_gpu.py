@@ -18,7 +18,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import rel, scaled_err
+from conftest import mixed_gate, rel
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
@@ -77,8 +77,7 @@ def test_real_mixed_within_1e6(ctx, fk, orc, case, zero_masked):
     ref = ctx.gpp_real(p, "fp64", flags)
     res = ctx.gpp_real(p, "mixed", flags)
     scales = real_scales(p, orc, orc.ORC_GPP_REAL_ZERO_MASKED if zero_masked else 0)
-    errs = {k: scaled_err(res[k], ref[k], scales[k]) for k in scales}
-    assert all(e <= TOLMX for e in errs.values()), errs
+    mixed_gate(res, ref, scales, TOLMX)
 
 
 def real_entries():

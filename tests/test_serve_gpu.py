@@ -138,3 +138,46 @@ def test_autotuned_plan(fk, reqs, ref64):
     for k in KEYS:
         assert rel(alone[k], ref64[2][k]) <= TOL, k
         np.testing.assert_array_equal(mixed[2][k], alone[k])
+
+
+def test_served_config3_request_shapes(fk, ctx):
+    """The served stream's request shapes at their real sizes: every
+    number_bands value of the stream (128, 256, 512, 1024) at both ends of
+    its ncouls range (2048 and 32768), ngpown = ncouls / 64, nvband 2, the
+    benchmark distributions, epsilon and wtilde resident.  Each result is
+    within plain relative error 1e-6 of fk_gpp's FP64 path, and the same bits
+    alone and in the mix."""
+    import torch
+    shapes = [(nb, nc) for nc in (2048, 32768) for nb in (128, 256, 512, 1024)]
+    pools = {nc: fk.inputs.gpp_synthetic(1024, 2, nc, nc // 64, seed=nc) for nc in (2048, 32768)}
+    dev = {nc: {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() if isinstance(v, np.ndarray) else v
+                for k, v in q.items()} for nc, q in pools.items()}
+
+    def request(nb, nc):
+        q = dict(dev[nc])
+        q["number_bands"] = nb
+        q["aqsmtemp"], q["aqsntemp"] = q["aqsmtemp"][:nb], q["aqsntemp"][:nb]
+        return q
+
+    want = {s: ctx.gpp(request(*s), "fp64") for s in shapes}  # host outputs: the call waits for its stream
+    srv = fk.Server(hbm_bytes=12 << 30, max_active=16, step_stages=32)
+    try:
+        for i, nc in enumerate((2048, 32768)):
+            srv.resident_put(10 + 2 * i, dev[nc]["I_eps_array"])
+            srv.resident_put(11 + 2 * i, dev[nc]["wtilde_array"])
+        keys = {2048: (10, 11), 32768: (12, 13)}
+
+        def submit(nb, nc):
+            return srv.submit(request(nb, nc), eps_key=keys[nc][0], wtilde_key=keys[nc][1])
+
+        alone = {s: srv.wait(submit(*s))[0] for s in shapes}
+        tickets = {s: submit(*s) for s in shapes}
+        mixed = {s: srv.wait(t)[0] for s, t in tickets.items()}
+        info = srv.stats()
+    finally:
+        srv.close()
+    assert info["mean_active"] > 1.0
+    for s in shapes:
+        for k in KEYS:
+            assert rel(alone[s][k], want[s][k]) <= TOL, (s, k, rel(alone[s][k], want[s][k]))
+            np.testing.assert_array_equal(mixed[s][k], alone[s][k])

@@ -104,3 +104,39 @@ def test_static_scratch_rejects_what_it_cannot_hold(ctx, fk):
     h["inv_igp_index"] = np.ascontiguousarray(q["inv_igp_index"], np.int32)
     h["indinv"] = np.ascontiguousarray(q["indinv"], np.int32)
     assert call_static(lib, h, 8, 2, 64, 4, 0, out) == fk._native.FK_EINVAL
+
+
+def test_static_calls_allocate_no_device_memory(ctx, fk):
+    """The property the entry point exists for: after a first call (which may
+    load the library's scratch array onto the GPU), further calls -- device
+    and host outputs, with and without achstemp -- leave the device's free
+    memory unchanged."""
+    import torch
+    nb, nv, nc, ng = 128, 2, 4096, 24
+    p = fk.inputs.gpp_synthetic(nb, nv, nc, ng, seed=35, dist="branch", wx="stress")
+    d = device_inputs(p)
+    lib = fk._native.load()
+    stream = torch.cuda.Stream()
+    dev_out = {k: torch.zeros(n, dtype=torch.complex128, device="cuda")
+               for k, n in (("achtemp", 3), ("asxtemp", 3), ("acht_n1_loc", nb), ("achstemp", 1))}
+    host_out = {"achtemp": np.zeros(3, np.complex128), "asxtemp": np.zeros(3, np.complex128),
+                "acht_n1_loc": np.zeros(nb, np.complex128), "achstemp": np.zeros(1, np.complex128)}
+    P = ctypes.c_void_p
+    ins = [P(d[k].data_ptr()) for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array", "vcoul",
+                                        "inv_igp_index", "indinv", "wx_array")]
+    assert call_static(lib, d, nb, nv, nc, ng, 0, dev_out, stream.cuda_stream) == fk._native.FK_OK
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for flags in (0, fk.FK_GPP_ACHSTEMP):
+        for _ in range(2):
+            o = dict(dev_out)
+            if not flags:
+                o["achstemp"] = None
+            assert call_static(lib, d, nb, nv, nc, ng, flags, o, stream.cuda_stream) == fk._native.FK_OK
+            ho = [P(host_out[k].ctypes.data) for k in OUTS[:3]] + [P(host_out["achstemp"].ctypes.data) if flags else None]
+            assert lib.fk_gpp_static(P(stream.cuda_stream), nb, nv, nc, ng, *ins, flags, *ho) == fk._native.FK_OK
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    want = ctx.gpp(p, "fp64", fk.FK_GPP_ACHSTEMP)
+    for k in OUTS:
+        assert rel(host_out[k], want[k]) <= TOL, k
