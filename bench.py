@@ -277,10 +277,64 @@ def dist_setup():
     return world, rank, local
 
 
+REF_GPP = os.path.join(ROOT, "oracle", "_ref", "gppKer_bgw")
+
+
+def reference_gpp_binary(w, runs, warmup=1):
+    """Seconds per run of the reference's own GPP driver, BGW-Kernels/gppKer.cpp
+    built unmodified from its sources (oracle/Makefile, target ref), as its own
+    chrono line reports them (the loop nest alone, :301,441-446), on all host
+    cores: `gppKer_bgw nb nvband ncouls nodes_per_group`, nodes_per_group =
+    ncouls / ngpown so that the driver's ngpown (:175-176) is the workload's.
+    None when the binary was not built on this machine or the shape cannot be
+    expressed that way.  The driver fills its own constant inputs."""
+    if w["kind"] != "gpp" or w.get("half") or w.get("real") or not os.access(REF_GPP, os.X_OK):
+        return None
+    npg = w["nc"] // w["ng"]
+    if npg < 1 or w["nc"] // npg != w["ng"]:
+        return None
+    cores = os.cpu_count() or 1
+    env = dict(os.environ, OMP_NUM_THREADS=str(cores))
+    times = []
+    for i in range(warmup + runs):
+        out = subprocess.run([REF_GPP, str(w["nb"]), str(w["nv"]), str(w["nc"]), str(npg)], capture_output=True,
+                             text=True, env=env, timeout=600)
+        if out.returncode != 0:
+            return None
+        t = [float(x.split("=")[1].split()[0]) for x in out.stdout.splitlines() if "Chrono Time Taken" in x]
+        if not t:
+            return None
+        if i >= warmup:
+            times.append(t[0])
+    return {"times": times, "cores": cores, "args": [w["nb"], w["nv"], w["nc"], npg]}
+
+
 def run_reference(a, w):
-    """CPU restatement of the reference loop nest (oracle/) on all host cores."""
+    """The reference's own CPU implementation of the path on all host cores:
+    its GPP driver when it was built here (reference_gpp_binary), else the CPU
+    restatement of its loop nest (oracle/)."""
     world, rank, _ = dist_setup()
     if rank != 0:
+        return
+    ref = reference_gpp_binary(w, a.steps, warmup=a.warmup)
+    if ref is not None:
+        times = ref["times"]
+        tot = sum(times)
+        val = terms(w) * len(times) / tot
+        sample = ("the reference's GPP driver BGW-Kernels/gppKer.cpp built unmodified with g++ -O3 -fopenmp, "
+                  "`gppKer %s` (ngpown %d), its own constant inputs, its own chrono time of the loop nest; "
+                  "one full run (%.3g terms) per step, OpenMP %d threads"
+                  % (" ".join(map(str, ref["args"])), w["ng"], terms(w), ref["cores"]))
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": val, "unit": "terms/s", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * tot / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "the reference driver's constant inputs",
+            "config": workload_config(a, w),
+            "cpu_baseline": {"value": val, "unit": "terms/s", "cores": ref["cores"], "kind": "reference",
+                             "sample": sample},
+            "e2e": {"value": val, "unit": "terms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "latency_ms": {"p50": 1e3 * statistics.median(times), "p99": 1e3 * float(np.percentile(times, 99))},
+        }), flush=True)
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
@@ -390,15 +444,13 @@ def rel(a, b):
     return float(np.max(np.abs(a - b))) / d if d > 0 else float(np.max(np.abs(a)))
 
 
-def run_ours(a, w):
+def measure_ours(a, w, fk, world, rank, local, sub=False):
+    """One workload through the library on this rank's GPU; returns the JSON
+    line's fields (rank 0) or None.  sub: a sub-block of the default line --
+    fewer steps, the FP64 path run once (for its error and its time), no CPU
+    baseline."""
     import torch
-    world, rank, local = dist_setup()
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    import __graft_entry__
-    fk = __graft_entry__.load_package()
+    steps = min(a.steps, w.get("sub_steps", 10)) if sub else a.steps
     ctx = fk.Context(local)
     stream = torch.cuda.Stream(local)
     ctx.set_stream(stream.cuda_stream)
@@ -441,12 +493,18 @@ def run_ours(a, w):
         torch.cuda.synchronize()
         return {k: (v.cpu().numpy().copy() if v is not None else None) for k, v in r.items()}
 
-    ref64 = fetch(call("fp64"))
-    resm = fetch(call("mixed"))
-    errs = {k: rel(resm[k], ref64[k]) for k in ref64 if ref64[k] is not None and np.max(np.abs(ref64[k])) > 0}
-
     prec = a.precision
     other = "fp64" if prec == "mixed" else "mixed"
+    if sub:
+        # the FP64 call once, timed by the library's own events
+        ctx.set_profiling(True)
+        ref64 = fetch(call("fp64"))
+        ms_fp64 = sum(ctx.last_timings())
+        ctx.set_profiling(False)
+    else:
+        ref64 = fetch(call("fp64"))
+    resm = fetch(call("mixed"))
+    errs = {k: rel(resm[k], ref64[k]) for k in ref64 if ref64[k] is not None and np.max(np.abs(ref64[k])) > 0}
     barrier()
     for _ in range(a.warmup):
         call(prec)
@@ -454,20 +512,23 @@ def run_ours(a, w):
     with clock_sampler(local) as clk:
         barrier()
         torch.cuda.nvtx.range_push("timed")
-        per = timed(torch, stream, lambda: call(prec), a.steps, 0, per_step=False)
+        per = timed(torch, stream, lambda: call(prec), steps, 0, per_step=False)
         torch.cuda.nvtx.range_pop()
         barrier()
     ms = max_over_ranks(per[0], f"cuda:{local}")
     launches = ctx.last_launches()
     # per-step latency distribution (events around each call)
-    lat = timed(torch, stream, lambda: call(prec), a.steps, 1, per_step=True)
+    lat = timed(torch, stream, lambda: call(prec), steps, 1, per_step=True)
     # the other precision, for the mixed-vs-FP64 ratio
-    k_other = max(3, min(a.steps, 10))
-    ms_other = statistics.mean(timed(torch, stream, lambda: call(other), k_other, 1, per_step=True))
+    if sub and prec == "mixed":
+        ms_other = ms_fp64
+    else:
+        k_other = max(3, min(steps, 10))
+        ms_other = statistics.mean(timed(torch, stream, lambda: call(other), k_other, 1, per_step=True))
     # dominant-kernel duration from the library's events on its stream
     ctx.set_profiling(True)
     ph, kt = [], []
-    for _ in range(max(3, min(a.steps, 10))):
+    for _ in range(max(3, min(steps, 10))):
         call(prec)
         ph.append(ctx.last_timings())
         kt.append(ctx.last_kernel_time())
@@ -481,7 +542,7 @@ def run_ours(a, w):
     keys_h = keys_c + [k for k, v in p.items() if type(v).__module__.startswith("torch")]
     for k in keys_h:
         hp[k] = (p[k].cpu() if k not in keys_c else torch.from_numpy(np.ascontiguousarray(p[k]))).pin_memory()
-    for _ in range(max(1, a.warmup)):
+    for _ in range(1 if sub else max(1, a.warmup)):
         host_call(prec, hp)
     # the bytes a call moves over the host link, as the library counts them: a
     # host array in full, except the parts the call reads (the igp columns of
@@ -489,52 +550,87 @@ def run_ours(a, w):
     h2d, d2h = ctx.last_transfer()
     barrier()
     t0 = time.perf_counter()
-    ke = max(3, min(a.steps, 10))
+    ke = 3 if sub else max(3, min(steps, 10))
     for _ in range(ke):
         host_call(prec, hp)
     torch.cuda.synchronize()
     e2e_s = max_over_ranks((time.perf_counter() - t0) / ke, f"cuda:{local}")
     cpu = None
-    if rank == 0 and world == 1 and not a.no_cpu:
+    if rank == 0 and world == 1 and not a.no_cpu and not sub:
         cpu = cpu_baseline(fk, w, p)
-    if rank == 0:
-        peaks = {}
-        try:
-            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-                peaks = json.load(f)
-        except OSError:
-            pass
-        byts, flops = algorithmic(w)
-        kms = kernel_ms
-        T = terms(w)
-        line = {
-            "metric": METRIC, "value": job_value(world, T, ms * 1e-3), "unit": "terms/s", "n_gpus": world,
-            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64 in / fp32 bulk + fp64 branch/reductions" if prec == "mixed" else "f64",
-            "data": "synthetic (seeded, benchmark value distributions)", "config": workload_config(a, w),
-            "precision": prec,
-            "fp64_value" if prec == "mixed" else "mixed_value": job_value(world, T, ms_other * 1e-3),
-            "mixed_vs_fp64": (ms_other / ms) if prec == "mixed" else (ms / ms_other),
-            "rel_err_mixed_vs_fp64": errs,
-            "latency_ms": {"p50": statistics.median(lat), "p99": float(np.percentile(lat, 99))},
-            "phase_ms": {"staging": phase[0], "prep": phase[1], "contraction": phase[2], "reduction": phase[3]},
-            "roofline": roofline(w, prec, byts, flops, kms, kernel_launches, peaks),
-            "e2e": {"value": job_value(world, T, e2e_s), "unit": "terms/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
-            "gpu_launches": launches * a.steps,
-            "clocks": clk.summary(),
-        }
-        if cpu:
-            line["cpu_baseline"] = cpu
-        print(json.dumps(line), flush=True)
     ctx.close()
+    del d, hp, outs, p
+    torch.cuda.empty_cache()
+    if rank != 0:
+        return None
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    byts, flops = algorithmic(w)
+    T = terms(w)
+    line = {
+        "metric": METRIC, "value": job_value(world, T, ms * 1e-3), "unit": "terms/s", "n_gpus": world,
+        "steps": steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 in / fp32 bulk + fp64 branch/reductions" if prec == "mixed" else "f64",
+        "data": "synthetic (seeded, benchmark value distributions)", "config": workload_config(a, w),
+        "precision": prec,
+        "fp64_value" if prec == "mixed" else "mixed_value": job_value(world, T, ms_other * 1e-3),
+        "mixed_vs_fp64": (ms_other / ms) if prec == "mixed" else (ms / ms_other),
+        "rel_err_mixed_vs_fp64": errs,
+        "latency_ms": {"p50": statistics.median(lat), "p99": float(np.percentile(lat, 99))},
+        "phase_ms": {"staging": phase[0], "prep": phase[1], "contraction": phase[2], "reduction": phase[3]},
+        "roofline": roofline(w, prec, byts, flops, kernel_ms, kernel_launches, peaks),
+        "e2e": {"value": job_value(world, T, e2e_s), "unit": "terms/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": launches * steps,
+        "clocks": clk.summary(),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    return line
+
+
+# The default line's sub-blocks: the metric's other workloads, each measured
+# after the headline (config 1) with a few steps.
+SUB_BLOCKS = ("gpp1638", "ff", "serve", "ff4")
+
+
+def run_ours(a, w):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import __graft_entry__
+    fk = __graft_entry__.load_package()
+    line = measure_ours(a, w, fk, world, rank, local)
+    # the default workload carries the metric's other configurations as
+    # sub-blocks of the same line (one GPU: the replicas run only the headline)
+    if line is not None and world == 1 and a.workload == "gpp" and not a.headline_only:
+        for name in SUB_BLOCKS:
+            sw = dict(WORKLOADS[name], name=name)
+            t0 = time.perf_counter()
+            blk = measure_serve(a, sw, fk, sub=True) if sw["kind"] == "serve" else \
+                measure_ours(a, sw, fk, world, rank, local, sub=True)
+            for k in ("metric", "n_gpus", "higher_is_better", "scaling", "vs_baseline", "data", "warmup"):
+                blk.pop(k, None)
+            blk["wall_s"] = time.perf_counter() - t0
+            line[name] = blk
+    if line is not None:
+        print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
 def cpu_baseline(fk, w, p):
-    """Oracle (CPU restatement of the reference loop nest) on the host cores,
-    on a bounded sample of the same workload."""
+    """The reference's own GPP driver on the host cores when it was built here
+    (kind "reference"; the CPU restatement's rate beside it), else the CPU
+    restatement of the reference loop nest (oracle/, kind "port"), on a
+    bounded sample of the same workload."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     cores = os.cpu_count() or 1
@@ -545,8 +641,17 @@ def cpu_baseline(fk, w, p):
         else:
             oracle.gpp(p, flags=oracle.ORC_GPP_HALF_SUM if w.get("half") else 0, nthreads=cores)
         dt = time.perf_counter() - t0
-        return {"value": terms(w) / dt, "unit": "terms/s", "cores": cores, "kind": "port",
-                "sample": f"one full call ({terms(w):.3g} terms)"}
+        port = {"value": terms(w) / dt, "unit": "terms/s", "cores": cores, "kind": "port",
+                "sample": f"one full call of the CPU restatement on the seeded inputs ({terms(w):.3g} terms)"}
+        ref = reference_gpp_binary(w, runs=3)
+        if ref is None:
+            return port
+        return {"value": terms(w) * len(ref["times"]) / sum(ref["times"]), "unit": "terms/s", "cores": ref["cores"],
+                "kind": "reference",
+                "sample": ("the reference's GPP driver BGW-Kernels/gppKer.cpp built unmodified (g++ -O3 -fopenmp), "
+                           "`gppKer %s`, its constant inputs, its chrono time of the loop nest, mean of %d runs "
+                           "(%.3g terms each)" % (" ".join(map(str, ref["args"])), len(ref["times"]), terms(w))),
+                "port_value": port["value"], "port_sample": port["sample"]}
     q = dict(p)
     big = w["ng"] * w["nc"] * w["nf"] > 1e9
     nbs, nfs = (8, 4) if big else (64, w["nf"])
@@ -576,13 +681,12 @@ def serve_stream(w, seed=2024):
     return levels, reqs, rng.exponential(1.0, w["requests"])
 
 
-def run_serve(a, w):
-    """BASELINE config 3: the request server (fk_server_*) on a stream of GPP
-    requests of uneven size.  First a burst (all requests at once: saturation
-    throughput), then Poisson arrivals at `load` x that rate (latency)."""
+def measure_serve(a, w, fk, sub=False):
+    """The served GPP stream: the request server (fk_server_*) on a stream of
+    GPP requests of uneven size.  First a burst (all requests at once:
+    saturation throughput), then Poisson arrivals at `load` x that rate
+    (latency).  Returns the line's fields (rank 0) or None."""
     import torch
-    import __graft_entry__
-    fk = __graft_entry__.load_package()
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
     levels, reqs, gaps = serve_stream(w, seed=2024 + rank)
@@ -649,8 +753,10 @@ def run_serve(a, w):
     pois_s = time.perf_counter() - t0
     info = srv.stats()
     srv.close()
+    pools.clear()
+    torch.cuda.empty_cache()
     cpu = None
-    if rank == 0 and not a.no_cpu:
+    if rank == 0 and not a.no_cpu and not sub:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle
         cores = os.cpu_count() or 1
@@ -691,6 +797,14 @@ def run_serve(a, w):
         }
         if cpu:
             line["cpu_baseline"] = cpu
+        return line
+    return None
+
+
+def run_serve(a, w):
+    import __graft_entry__
+    line = measure_serve(a, w, __graft_entry__.load_package())
+    if line is not None:
         print(json.dumps(line), flush=True)
 
 
@@ -703,6 +817,8 @@ def main():
     ap.add_argument("--workload", default="gpp", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="default workload: skip the sub-blocks of the metric's other configurations")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     w = dict(WORKLOADS[a.workload], name=a.workload)

@@ -10,7 +10,7 @@ only on its own shape).
 import numpy as np
 import pytest
 
-from conftest import rel
+from conftest import gpp_scales_torch, mixed_gate, rel
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-6
@@ -178,6 +178,7 @@ def test_served_config3_request_shapes(fk, ctx):
         srv.close()
     assert info["mean_active"] > 1.0
     for s in shapes:
+        # plain relative error, except for outputs that cancel (see mixed_gate)
+        mixed_gate(alone[s], want[s], gpp_scales_torch(request(*s)), TOL, keys=KEYS)
         for k in KEYS:
-            assert rel(alone[s][k], want[s][k]) <= TOL, (s, k, rel(alone[s][k], want[s][k]))
             np.testing.assert_array_equal(mixed[s][k], alone[s][k])
