@@ -109,15 +109,22 @@ def gpp_scales_torch(p):
     return {"achtemp": np.array(ach), "asxtemp": np.array(ach), "acht_n1_loc": n1loc}
 
 
+def host(x):
+    """numpy view of an array that may be a torch tensor (copied to the host)."""
+    import numpy as np
+    return x.detach().cpu().numpy() if type(x).__module__.startswith("torch") else np.asarray(x)
+
+
 def gpp_igp(p):
     import numpy as np
     nc = p["ncouls"]
     out = []
-    for i in np.asarray(p["inv_igp_index"]):
+    indinv = host(p["indinv"])
+    for i in host(p["inv_igp_index"]):
         if i == nc:
             out.append(nc - 1)
         elif 0 <= i < nc:
-            g = int(p["indinv"][i])
+            g = int(indinv[i])
             out.append(g if 0 <= g < nc else -1)
         else:
             out.append(-1)
