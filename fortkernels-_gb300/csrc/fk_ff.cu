@@ -356,16 +356,18 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
     const int nplanes = gmax;
     p.bytesImgR = p.bytesImgA = p.bytesW = p.bytesAimg = 0;
     if (p.mixed) {
+        // the contraction runs on CTA pairs: units of 256 bands (p.MT counts them),
+        // over an A image of an even number of 128-row tiles
         p.BN = 64;
         p.kstages = ceil_div(r.nc, tcx::BK);
-        p.MT = ceil_div(r.nb, tcx::BM);
+        p.MT = ceil_div(r.nb, 2 * tcx::BM);
         p.NT = ceil_div(r.ng, p.BN);
-        ff_pick_split_tc((long)p.MT * p.NT * nplanes, r.nc, c.sms, p.KS, p.kchunk);
+        ff_pick_split_tc((long)p.MT * p.NT * nplanes, r.nc, c.sms / 2, p.KS, p.kchunk);
         const size_t bb = tcx::Cfg<64>::B_BYTES;
         p.bytesImgR = p.planesR.size() * (size_t)p.NT * p.kstages * bb;
         p.bytesImgA = p.planesA.size() * (size_t)p.NT * p.kstages * bb;
         p.bytesW = 2 * (size_t)r.nb * r.ng * sizeof(float2) + (size_t)r.ng * sizeof(float) + 256;
-        p.bytesAimg = (size_t)p.MT * p.kstages * tcx::Cfg<64>::A_BYTES;
+        p.bytesAimg = (size_t)2 * p.MT * p.kstages * tcx::Cfg<64>::A_BYTES;
     } else {
         p.BN = d64::BN;
         p.kstages = 0;
@@ -480,8 +482,9 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
                                                                                 igp, igp, 1.0, W, W + (size_t)r.nb * r.ng,
                                                                                 (float*)(W + 2 * (size_t)r.nb * r.ng));
         // aqsntemp is reused by every (plane, n-tile): split it to BF16 pieces once
-        const int MTa = ceil_div(r.nb, tcx::BM);
-        if (tcx::img_needs_pad(tcx::BM, r.nb, 0, r.nc)) {
+        // (an even number of 128-row tiles: rows past number_bands are zeros)
+        const int MTa = 2 * p.MT;
+        if (tcx::img_needs_pad(tcx::BM, r.nb, 0, r.nc) || MTa * tcx::BM > r.nb) {
             tcx::img_pad_kernel<tcx::BM><<<dim3(p.kstages, MTa, 1), 256, 0, st>>>(Aimg, MTa, p.kstages, r.nb, 0, r.nc);
             ++c.launches;
         }
@@ -515,9 +518,10 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
             t.MT = p.MT; t.NT = p.NT; t.units = p.MT * p.NT * p.KS * nb_;
             t.err = c.errword;
             t.wait_limit = c.wait_limit;
-            const int grid1 = std::min(t.units, c.sms);
-            auto k = tcx::tc_contract_kernel<EPI_FF, 64, true>;
-            constexpr size_t smem = tcx::Cfg<64, true>::SMEM;
+            auto k = tcx::tc_contract_pair_kernel<EPI_FF, 64, true>;
+            constexpr size_t smem = tcx::Cfg<64, true, true>::SMEM;
+            static const int pairs = tcx::resident_pairs(k, smem, tcx::THREADS_FF, c.sms / 2);
+            const int grid1 = 2 * std::min(t.units, pairs);
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             kernel_begin(c);
             k<<<grid1, tcx::THREADS_FF, smem, st>>>(t);

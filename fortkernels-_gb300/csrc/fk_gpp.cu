@@ -1035,6 +1035,13 @@ __global__ void __launch_bounds__(ROWS_THREADS) rows_kernel(RowsArgs ra) {
 }
 
 
+// The mixed-precision contraction of fk_gpp runs on CTA pairs, except in the
+// pipelined host path (one launch per row block), the half sum, the served
+// steps and the real-valued sum, which keep the single-CTA kernel.
+inline bool gpp_pair(const GppDev& r, bool pipelined) {
+    return r.prec == FK_MIXED && !pipelined && !(r.flags & FK_GPP_HALF_SUM);
+}
+
 struct Plan {
     int nch, tile, passes;
     int pipe_sub, pipe_chunks;   // pipelined host path: prep chunks (= k-slices) per k-chunk, k-chunks
@@ -1072,7 +1079,9 @@ void pick_split(int tiles, int K, int target, int& KS, int& kchunk) {
 
 constexpr int PIPE_CHUNKS = 8;  // row blocks of the pipelined host path at most (events 0..7 of Ctx::pipe_ev)
 
-Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0, bool pipelined = false) {
+// pair: the contraction runs on CTA pairs (tc_contract_pair_kernel): MT counts
+// 256-row tiles and the k-split fills the SM pairs
+Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0, bool pipelined = false, bool pair = false) {
     Plan p{};
     p.mixed = r.prec == FK_MIXED;
     p.pipe_sub = p.pipe_chunks = 0;
@@ -1106,9 +1115,9 @@ Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0, bool pipeline
     if (p.mixed) {
         p.BN = 64;
         p.kstages = ceil_div(r.nc, tcx::BK);
-        p.MT = ceil_div(std::max(M, 1), tcx::BM);
+        p.MT = ceil_div(std::max(M, 1), (pair ? 2 : 1) * tcx::BM);
         p.NT = ceil_div(r.ng, GPP_COLS);
-        pick_split_tc(p.MT * p.NT, r.nc, c.sms, p.KS, p.kchunk);
+        pick_split_tc(p.MT * p.NT, r.nc, pair ? c.sms / 2 : c.sms, p.KS, p.kchunk);
         if (ks_override > 0) {
             const int ks = std::min(ks_override, std::max(1, ceil_div(r.nc, tcx::BK)));
             p.kchunk = ceil_div(ceil_div(r.nc, ks), tcx::BK) * tcx::BK;
@@ -1454,7 +1463,7 @@ __global__ void real_out_kernel(int nb, const double2* outc, double* out) {
 }  // namespace
 
 size_t gpp_workspace(const Ctx& c, const GppDev& r, bool pipelined) {
-    Plan p = make_plan(c, r, 0, pipelined);
+    Plan p = make_plan(c, r, 0, pipelined, gpp_pair(r, pipelined));
     const size_t half = (r.flags & FK_GPP_HALF_SUM) ? p.bytesP + (size_t)r.ng * (4 + 3 * sizeof(double2)) + 768 : 0;
     const size_t wf = (size_t)r.nv * r.ng * 2 * sizeof(double2);
     return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesRows + p.bytesIgp + p.bytesW + half + wf + 12 * 256;
@@ -1587,7 +1596,7 @@ fk_status gpp_run_half(Ctx& c, const GppDev& r) {
 
 fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
     if (r.flags & FK_GPP_HALF_SUM) return pipe ? fail(c, FK_EINVAL, "gpp: no pipelined half sum") : gpp_run_half(c, r);
-    const Plan p = make_plan(c, r, 0, pipe != nullptr);
+    const Plan p = make_plan(c, r, 0, pipe != nullptr, gpp_pair(r, pipe != nullptr));
     if (pipe && !p.pipe_chunks) return fail(c, FK_EINVAL, "gpp: pipelined staging needs the mixed path");
     cudaStream_t st = c.stream;
     int* igp = (int*)c.ws.take(p.bytesIgp);
@@ -1704,11 +1713,13 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
             t.wait_limit = c.wait_limit;
             if (tcx::encode_rows_map(&t.amap, r.aqsn, r.nc, r.nc, r.nb) != cudaSuccess)
                 return fail(c, FK_ECUDA, "gpp: cannot describe aqsntemp as a tensor map (needs a 16-byte aligned array)");
-            const int grid1 = std::min(p.units, c.sms);
-            auto k = tcx::tc_contract_kernel<EPI_GPP, 64, false>;
-            set_smem(k, tcx::Cfg<64>::SMEM);
+            auto k = tcx::tc_contract_pair_kernel<EPI_GPP, 64, false>;
+            constexpr size_t smem = tcx::Cfg<64, false, true>::SMEM;
+            static const int pairs = tcx::resident_pairs(k, smem, tcx::THREADS, c.sms / 2);
+            const int grid1 = 2 * std::min(p.units, pairs);
+            set_smem(k, smem);
             kernel_begin(c);
-            k<<<grid1, tcx::THREADS, tcx::Cfg<64>::SMEM, st>>>(t);
+            k<<<grid1, tcx::THREADS, smem, st>>>(t);
             kernel_end(c);
         } else {
             auto k = d64::contract_kernel<EPI_GPP>;

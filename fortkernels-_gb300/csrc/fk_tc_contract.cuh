@@ -29,6 +29,8 @@
 // an error code and unwinds without further waits of unbounded length.
 #pragma once
 #include <cuda.h>
+
+#include <algorithm>
 #include <cuda_bf16.h>
 
 #include "fk_gemm.cuh"
@@ -57,7 +59,7 @@ constexpr long long WAIT_LIMIT = 4000000000LL;
 // keep the default bound whatever limit the launch passes.
 constexpr long long DRAIN_LIMIT = 4000000000LL;
 
-template <int BN, bool WSMEM = false>
+template <int BN, bool WSMEM = false, bool PAIR = false>
 struct Cfg {
     static_assert(BN == 64, "four accumulators x two buffers fill the 512 TMEM columns at BN = 64");
     // Operand stages: FF three (its epilogue keeps the per-unit weights in
@@ -69,8 +71,11 @@ struct Cfg {
     static constexpr int STAGES = WSMEM ? 3 : 2;
     static constexpr int CHUNK_STAGES = 1;  // k-values per TMEM accumulation = 32
     static constexpr uint32_t A_BYTES = NSUB * BM * 64;
-    static constexpr uint32_t B_BYTES = NSUB * BN * 64;
-    static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+    static constexpr uint32_t B_BYTES = NSUB * BN * 64;  // one k-stage of an n-tile in the pre-split B image
+    // B in one CTA's stage: all six pieces, or, for a CTA pair, the real (even
+    // CTA) or imaginary (odd CTA) half of each piece's [B_re | B_im]
+    static constexpr uint32_t B_SMEM = PAIR ? NSPLIT * BN * 64 : B_BYTES;
+    static constexpr uint32_t STAGE_BYTES = A_BYTES + B_SMEM;
     static constexpr uint32_t ACC_COLS = 4 * BN;       // X = A_re x [B_re|B_im], Y = A_im x [B_re|B_im]
     static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;  // double buffered
     static constexpr uint32_t W_BYTES = 0u;
@@ -185,9 +190,14 @@ struct TableReqs {
     static constexpr bool kTable = true;
 };
 
-template <int EPI, int BN, bool AIMG, class Src>
+// PAIR: a cluster of two CTAs computes M = 256 rows per unit (128 per CTA)
+// with MMAs the even CTA issues for both (see fk_tc.cuh): each CTA loads its
+// own A rows and its half of B; the odd CTA's "stage landed" and "accumulator
+// drained" signals go to the even CTA's barriers (a relay thread and remote
+// arrivals); the MMA commits reach both CTAs' barriers.
+template <int EPI, int BN, bool AIMG, bool PAIR, class Src>
 __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long long wait_limit) {
-    using C = Cfg<BN, EPI == EPI_FF>;
+    using C = Cfg<BN, EPI == EPI_FF, PAIR>;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-aligned operand area
     uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -201,11 +211,17 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
     uint64_t* done = accEmpty + 2;
     uint64_t* fFull = done + 1;    // [2] GPP: FP64 staging half filled (tx bytes)
     uint64_t* fEmpty = done + 3;   // [2] GPP: FP64 staging half read by all converter warps
-    uint32_t* tslot = (uint32_t*)(done + 5);
+    uint64_t* peerFull = done + 5; // [STAGES] PAIR, even CTA: the odd CTA's half of the stage has landed
+    uint32_t* tslot = (uint32_t*)(done + 5 + C::STAGES);
     __shared__ int s_abort_flag;
     volatile int& s_abort = s_abort_flag;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // a CTA pair takes units together: pair id, pair count, rank in the pair
+    const uint32_t rank = PAIR ? tc::cluster_rank() : 0u;
+    const int pid = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+    const int npairs = PAIR ? (int)(gridDim.x >> 1) : (int)gridDim.x;
+    constexpr int EPI_WARPS = AIMG ? 4 * FF_EPI_WARPS : 4;
 
     if (tid == 0) {
         for (int s = 0; s < C::STAGES; ++s) {
@@ -215,8 +231,9 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&accFull[b], 1);
-            tc::mbar_init(&accEmpty[b], AIMG ? 4 * FF_EPI_WARPS : 4);
+            tc::mbar_init(&accEmpty[b], PAIR ? 2 * EPI_WARPS : EPI_WARPS);  // both CTAs' epilogues drain
         }
+        for (int s = 0; s < C::STAGES; ++s) tc::mbar_init(&peerFull[s], 1);
         tc::mbar_init(done, 1);
         for (int h = 0; h < 2; ++h) {
             tc::mbar_init(&fFull[h], 1);
@@ -226,17 +243,25 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
         s_abort = 0;
     }
     if (warp == 0) {
-        tc::tmem_alloc(tslot, C::TMEM_COLS);
-        tc::tmem_relinquish();
+        if constexpr (PAIR) {
+            tc::tmem_alloc_pair(tslot, C::TMEM_COLS);
+            tc::tmem_relinquish_pair();
+        } else {
+            tc::tmem_alloc(tslot, C::TMEM_COLS);
+            tc::tmem_relinquish();
+        }
     }
     tc::tc_fence_before();
     __syncthreads();
+    if constexpr (PAIR) tc::cluster_sync();  // both CTAs' barriers and TMEM exist before any MMA
     tc::tc_fence_after();
     const uint32_t tmem = *tslot;
 
     // local unit -> (m-tile, n-tile, k-slice, batch) and the slice's k range
+    // (PAIR: MT counts 256-row tiles; mt is this CTA's 128-row tile)
     auto unit_coords = [&](const TcArgs& t, int u, int& mt, int& nt, int& ks, int& batch) {
         mt = t.mt0 + u % t.MT;
+        if (PAIR) mt = 2 * mt + (int)rank;
         int r = u / t.MT;
         nt = r % t.NT;
         r /= t.NT;
@@ -254,12 +279,36 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
 
     Src src = src0;  // per-role cursor
     if (warp == 0) {
-        // ------------------------------------------------------------ MMA
-        if (lane == 0) {
+        if (PAIR && rank == 1 && lane == 0) {
+            // ------------------------------------------------- relay (odd CTA)
+            // each stage's operands of this CTA have landed -> the even CTA's peerFull
+            int g = 0;
+            bool ok = true;
+            for (int u = pid; u < src.units() && ok; u += npairs) {
+                int lu;
+                const TcArgs& t = src.at(u, lu);
+                int mt, nt, ks, batch, k0, k1;
+                unit_coords(t, lu, mt, nt, ks, batch);
+                krange(t, ks, k0, k1);
+                const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
+                for (int st = 0; st < nst; ++st, ++g) {
+                    const int s = g % C::STAGES;
+                    const uint32_t par = (g / C::STAGES) & 1;
+                    if (!tc::mbar_wait(&fullA[s], par, wait_limit) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
+                        s_abort) {
+                        fail(2);
+                        ok = false;
+                        break;
+                    }
+                    tc::mbar_arrive_remote(&peerFull[s], 0);
+                }
+            }
+        } else if (lane == 0 && (!PAIR || rank == 0)) {
+            // ------------------------------------------------------------ MMA
             int g = 0, chunk = 0;
             bool ok = true;
-            const uint32_t idp = tc::idesc_bf16(BM, 2 * BN, false);
-            for (int u = blockIdx.x; u < src.units() && ok; u += gridDim.x) {
+            const uint32_t idp = tc::idesc_bf16(PAIR ? 2 * BM : BM, 2 * BN, false);
+            for (int u = pid; u < src.units() && ok; u += npairs) {
                 int lu;
                 const TcArgs& t = src.at(u, lu);
                 int mt, nt, ks, batch, k0, k1;
@@ -268,14 +317,17 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                 const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
                 for (int st0 = 0; st0 < nst && ok; st0 += C::CHUNK_STAGES, ++chunk) {
                     const int b = chunk & 1;
-                    if (!tc::mbar_wait(&accEmpty[b], ((chunk >> 1) & 1) ^ 1, wait_limit)) { fail(1); ok = false; break; }
+                    const bool freed = PAIR ? tc::mbar_wait_cluster(&accEmpty[b], ((chunk >> 1) & 1) ^ 1, wait_limit)
+                                            : tc::mbar_wait(&accEmpty[b], ((chunk >> 1) & 1) ^ 1, wait_limit);
+                    if (!freed) { fail(1); ok = false; break; }
                     tc::tc_fence_after();
                     const uint32_t dX = tmem + (uint32_t)(b * C::ACC_COLS), dY = dX + 2 * BN;
                     const int st1 = min(nst, st0 + C::CHUNK_STAGES);
                     for (int st = st0; st < st1; ++st, ++g) {
                         const int s = g % C::STAGES;
                         const uint32_t par = (g / C::STAGES) & 1;
-                        if (!tc::mbar_wait(&fullA[s], par, wait_limit) || !tc::mbar_wait(&fullB[s], par, wait_limit)) {
+                        if (!tc::mbar_wait(&fullA[s], par, wait_limit) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
+                            (PAIR && !tc::mbar_wait_cluster(&peerFull[s], par, wait_limit))) {
                             fail(2);
                             ok = false;
                             break;
@@ -290,7 +342,10 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         for (int kk = 0; kk < 2; ++kk) {
                             // A sub-tile (re h,m,l, im h,m,l) and paired B piece [re|im], k offset kk*16
                             auto ad = [&](int sub) { return dA + (uint64_t)((sub * BM * 64) >> 4) + 2 * kk; };
-                            auto bd = [&](int piece) { return dB + (uint64_t)((piece * 2 * BN * 64) >> 4) + 2 * kk; };
+                            // (PAIR: each CTA holds its half [B_re] or [B_im] of a piece, BN rows)
+                            auto bd = [&](int piece) {
+                                return dB + (uint64_t)((piece * (PAIR ? 1 : 2) * BN * 64) >> 4) + 2 * kk;
+                            };
                             const uint32_t acc0 = (st > st0 || kk > 0) ? 1u : 0u;
                             // piece products (a, b): the five small ones (mm, lh, hl, mh, hm), then hh;
                             // X += A_re,a x [B_re|B_im]_b, Y += A_im,a x [B_re|B_im]_b
@@ -299,18 +354,26 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
 #pragma unroll
                             for (int q = 0; q < 6; ++q) {
                                 const uint32_t first = (q == 0) ? acc0 : 1u;
-                                tc::mma_bf16(dX, ad(PA[q]), bd(PB[q]), idp, first);
-                                tc::mma_bf16(dY, ad(3 + PA[q]), bd(PB[q]), idp, first);
+                                if constexpr (PAIR) {
+                                    tc::mma_bf16_pair(dX, ad(PA[q]), bd(PB[q]), idp, first);
+                                    tc::mma_bf16_pair(dY, ad(3 + PA[q]), bd(PB[q]), idp, first);
+                                } else {
+                                    tc::mma_bf16(dX, ad(PA[q]), bd(PB[q]), idp, first);
+                                    tc::mma_bf16(dY, ad(3 + PA[q]), bd(PB[q]), idp, first);
+                                }
                             }
                         }
-                        tc::mma_commit(&empty[s]);
+                        if constexpr (PAIR) tc::mma_commit_pair(&empty[s], 3);  // frees the stage in both CTAs
+                        else tc::mma_commit(&empty[s]);
                     }
                     if (!ok) break;
-                    tc::mma_commit(&accFull[b]);
+                    if constexpr (PAIR) tc::mma_commit_pair(&accFull[b], 3);  // both CTAs' epilogues
+                    else tc::mma_commit(&accFull[b]);
                 }
             }
             // drain: every issued MMA has completed before TMEM is released
-            tc::mma_commit(done);
+            if constexpr (PAIR) tc::mma_commit_pair(done, 1);
+            else tc::mma_commit(done);
             if (!tc::mbar_wait(done, 0, DRAIN_LIMIT)) fail(4);
         }
     } else if (warp == 1) {
@@ -324,7 +387,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
         int last_st[C::STAGES], last_f[2] = {-1, -1};
 #pragma unroll
         for (int s = 0; s < C::STAGES; ++s) last_st[s] = -1;
-        for (int u = blockIdx.x; u < src.units() && ok; u += gridDim.x) {
+        for (int u = pid; u < src.units() && ok; u += npairs) {
             int lu;
             const TcArgs& t = src.at(u, lu);
             const ContractArgs& a = t.c;
@@ -366,8 +429,16 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                     } else {
                         const uint8_t* src =
                             t.Bimg + (((long)plane * t.NT + nt) * t.kstages_total + kst) * (long)C::B_BYTES;
-                        tc::mbar_arrive_expect_tx(&fullB[s], C::B_BYTES);
-                        tc::bulk_g2s(base + s * C::STAGE_BYTES + C::A_BYTES, src, C::B_BYTES, &fullB[s]);
+                        tc::mbar_arrive_expect_tx(&fullB[s], C::B_SMEM);
+                        if constexpr (PAIR) {
+                            // the even CTA's B_re, the odd CTA's B_im of each piece (paired image layout:
+                            // re h, im h, re m, im m, re l, im l), BN rows each
+                            for (int pc = 0; pc < NSPLIT; ++pc)
+                                tc::bulk_g2s(base + s * C::STAGE_BYTES + C::A_BYTES + pc * BN * 64,
+                                             src + (2 * pc + (int)rank) * BN * 64, BN * 64, &fullB[s]);
+                        } else {
+                            tc::bulk_g2s(base + s * C::STAGE_BYTES + C::A_BYTES, src, C::B_BYTES, &fullB[s]);
+                        }
                         if (AIMG) {
                             const uint8_t* asrc = t.Aimg + ((long)mt * t.kstages_total + kst) * (long)C::A_BYTES;
                             tc::mbar_arrive_expect_tx(&fullA[s], C::A_BYTES);
@@ -412,7 +483,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
         int chunk = 0;
         bool ok = true;
         constexpr int GC = BN / 3;  // 21 igp per GPP tile
-        for (int u = blockIdx.x; u < src.units() && ok; u += gridDim.x) {
+        for (int u = pid; u < src.units() && ok; u += npairs) {
             int lu;
             const TcArgs& t = src.at(u, lu);
             const ContractArgs& a = t.c;
@@ -500,7 +571,10 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                 }
                 tc::tc_fence_before();
                 __syncwarp();
-                if (lane == 0) tc::mbar_arrive(&accEmpty[b]);
+                if (lane == 0) {
+                    if (PAIR && rank == 1) tc::mbar_arrive_remote(&accEmpty[b], 0);  // the MMA issuer's barrier
+                    else tc::mbar_arrive(&accEmpty[b]);
+                }
                 if (EPI == EPI_GPP) {
 #pragma unroll
                     for (int gg = 0; gg < 3; ++gg) {
@@ -530,7 +604,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             constexpr int RPW = BM / NCONV;                  // rows per converter warp
             int g = 0;
             bool ok = true;
-            for (int u = blockIdx.x; u < src.units() && ok; u += gridDim.x) {
+            for (int u = pid; u < src.units() && ok; u += npairs) {
                 int lu;
                 const TcArgs& t = src.at(u, lu);
                 const ContractArgs& a = t.c;
@@ -597,21 +671,33 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
 
     tc::tc_fence_before();
     __syncthreads();
+    // PAIR: the even CTA's MMAs read this CTA's shared memory and write its
+    // TMEM; neither CTA releases either before both are done
+    if constexpr (PAIR) tc::cluster_sync();
     if (warp == 0) {
         __syncwarp();
-        tc::tmem_dealloc(tmem, C::TMEM_COLS);
+        if constexpr (PAIR) tc::tmem_dealloc_pair(tmem, C::TMEM_COLS);
+        else tc::tmem_dealloc(tmem, C::TMEM_COLS);
     }
 }
 
 template <int EPI, int BN, bool AIMG>
 __global__ void __launch_bounds__(AIMG ? THREADS_FF : THREADS, 1) tc_contract_kernel(const __grid_constant__ TcArgs t) {
-    tc_contract_body<EPI, BN, AIMG>(OneReq{t}, t.err, t.wait_limit);
+    tc_contract_body<EPI, BN, AIMG, false>(OneReq{t}, t.err, t.wait_limit);
+}
+
+// The same over CTA pairs (M = 256 per unit; t.MT counts 256-row tiles and
+// the grid is an even number of CTAs).
+template <int EPI, int BN, bool AIMG>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(AIMG ? THREADS_FF : THREADS, 1)
+    tc_contract_pair_kernel(const __grid_constant__ TcArgs t) {
+    tc_contract_body<EPI, BN, AIMG, true>(OneReq{t}, t.err, t.wait_limit);
 }
 
 // Units of several requests from a device table (the served step).
 template <int EPI, int BN, bool AIMG>
 __global__ void __launch_bounds__(AIMG ? THREADS_FF : THREADS, 1) tc_contract_table_kernel(const TcTable* tab, int* err, long long wait_limit) {
-    tc_contract_body<EPI, BN, AIMG>(TableReqs{tab, 0}, err, wait_limit);
+    tc_contract_body<EPI, BN, AIMG, false>(TableReqs{tab, 0}, err, wait_limit);
 }
 
 // Epilogue weight tables in FP32, column-major (row m contiguous):
@@ -710,6 +796,25 @@ static __global__ void aimg_convert_kernel(const double2* src, int rows, int K, 
     const double2 v = src[(long)m * K + k];
     uint8_t* tile = img + ((long)(m / BM) * kstages) * (long)(BM * NSUB * 64);
     img_store<BM>(tile, m % BM, k, f64_to_f32_bits(v.x), f64_to_f32_bits(v.y));
+}
+
+// Host: how many CTA pairs of a pair kernel can be resident at once with
+// `smem` bytes of dynamic shared memory (at most `cap`), so that a persistent
+// launch never leaves pairs waiting for a second wave.  (Callers keep the
+// answer: it depends only on the kernel and the device.)
+template <class K>
+inline int resident_pairs(K kernel, size_t smem, int threads, int cap) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * (unsigned)cap);
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    int m = 0;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveClusters(&m, (const void*)kernel, &cfg) != cudaSuccess || m <= 0) {
+        cudaGetLastError();
+        m = cap;
+    }
+    return std::max(1, std::min(m, cap));
 }
 
 // Host: A (rows of complex FP64, row stride lda complex elements) as a 2-D FP64
