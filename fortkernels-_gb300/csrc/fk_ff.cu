@@ -20,6 +20,7 @@
 #include "fk_gemm.cuh"
 #include "fk_internal.h"
 #include "fk_tc_contract.cuh"
+#include <cstdlib>
 
 namespace fk {
 namespace {
@@ -492,7 +493,8 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
         c.launches += 2;
         cudaMemsetAsync(c.errword, 0, sizeof(int), st);
     }
-    auto contract = [&](const double2* eps, const int* pls, int nb_, double2* P, uint8_t* img, size_t img_bytes) {
+    auto contract = [&](const double2* eps, const int* pls, int nb_, double2* P, uint8_t* img, size_t img_bytes,
+                        bool need_rs) {
         ContractArgs a{};
         a.A = r.aqsn; a.lda = r.nc; a.m0 = 0; a.M = r.nb;
         a.B = eps; a.ldb = r.nc; a.bstride = (long)r.ng * r.nc; a.N = r.ng; a.K = r.nc;
@@ -518,6 +520,8 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
             t.MT = p.MT; t.NT = p.NT; t.units = p.MT * p.NT * p.KS * nb_;
             t.err = c.errword;
             t.wait_limit = c.wait_limit;
+            t.ff_no_rs = need_rs ? 0 : 1;
+            t.chunk_stages = getenv("FK_TC_CHUNK") ? atoi(getenv("FK_TC_CHUNK")) : 1;
             auto k = tcx::tc_contract_pair_kernel<EPI_FF, 64, true>;
             constexpr size_t smem = tcx::Cfg<64, true, true>::SMEM;
             static const int pairs = tcx::resident_pairs(k, smem, tcx::THREADS_FF, c.sms / 2);
@@ -538,8 +542,8 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
         }
     };
     if (!pipe) {
-        if (nR) contract(r.epsR, planes, nR, PR, imgR, p.bytesImgR);
-        if (nA) contract(r.epsA, planes + nR, nA, PA, imgA, p.bytesImgA);
+        if (nR) contract(r.epsR, planes, nR, PR, imgR, p.bytesImgR, true);
+        if (nA) contract(r.epsA, planes + nR, nA, PA, imgA, p.bytesImgA, false);  // A planes: AW only
     } else {
         // one launch pair per copy group, each after its planes have landed;
         // a group's partials and pre-split image sit at its batch offset
@@ -551,7 +555,7 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
                 return cuda_fail(c, cudaGetLastError(), "ff: pipeline wait");
             uint8_t* img = isR ? imgR : imgA;
             contract(isR ? r.epsR : r.epsA, planes + (isR ? 0 : nR) + g0, n, (isR ? PR : PA) + g0 * pslab,
-                     img ? img + g0 * islab : nullptr, 0);
+                     img ? img + g0 * islab : nullptr, 0, isR);
         }
     }
     phase_mark(c, 3);

@@ -24,6 +24,7 @@
 // decisions remain those of the FP64 sequence; the bulk products run in FP32
 // with compensated accumulation.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -1039,7 +1040,8 @@ __global__ void __launch_bounds__(ROWS_THREADS) rows_kernel(RowsArgs ra) {
 // pipelined host path (one launch per row block), the half sum, the served
 // steps and the real-valued sum, which keep the single-CTA kernel.
 inline bool gpp_pair(const GppDev& r, bool pipelined) {
-    return r.prec == FK_MIXED && !pipelined && !(r.flags & FK_GPP_HALF_SUM);
+    static const bool on = getenv("FK_GPP_PAIR") ? atoi(getenv("FK_GPP_PAIR")) != 0 : true;
+    return on && r.prec == FK_MIXED && !pipelined && !(r.flags & FK_GPP_HALF_SUM);
 }
 
 struct Plan {
@@ -1713,14 +1715,23 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
             t.wait_limit = c.wait_limit;
             if (tcx::encode_rows_map(&t.amap, r.aqsn, r.nc, r.nc, r.nb) != cudaSuccess)
                 return fail(c, FK_ECUDA, "gpp: cannot describe aqsntemp as a tensor map (needs a 16-byte aligned array)");
-            auto k = tcx::tc_contract_pair_kernel<EPI_GPP, 64, false>;
-            constexpr size_t smem = tcx::Cfg<64, false, true>::SMEM;
-            static const int pairs = tcx::resident_pairs(k, smem, tcx::THREADS, c.sms / 2);
-            const int grid1 = 2 * std::min(p.units, pairs);
-            set_smem(k, smem);
-            kernel_begin(c);
-            k<<<grid1, tcx::THREADS, smem, st>>>(t);
-            kernel_end(c);
+            t.chunk_stages = getenv("FK_TC_CHUNK") ? atoi(getenv("FK_TC_CHUNK")) : 1;
+            if (gpp_pair(r, false)) {
+                auto k = tcx::tc_contract_pair_kernel<EPI_GPP, 64, false>;
+                constexpr size_t smem = tcx::Cfg<64, false, true>::SMEM;
+                static const int pairs = tcx::resident_pairs(k, smem, tcx::THREADS, c.sms / 2);
+                const int grid1 = 2 * std::min(p.units, pairs);
+                set_smem(k, smem);
+                kernel_begin(c);
+                k<<<grid1, tcx::THREADS, smem, st>>>(t);
+                kernel_end(c);
+            } else {
+                auto k = tcx::tc_contract_kernel<EPI_GPP, 64, false>;
+                set_smem(k, tcx::Cfg<64>::SMEM);
+                kernel_begin(c);
+                k<<<std::min(p.units, c.sms), tcx::THREADS, tcx::Cfg<64>::SMEM, st>>>(t);
+                kernel_end(c);
+            }
         } else {
             auto k = d64::contract_kernel<EPI_GPP>;
             set_smem(k, d64::SMEM);

@@ -99,6 +99,8 @@ struct TcArgs {
     int* err;             // device error word (nonzero: a wait timed out)
     long long wait_limit; // bound of the waits between roles, cycles (0 is allowed: any wait that
                           // is not satisfied on its first test gives up)
+    int chunk_stages;     // k-stages accumulated in TMEM between drains (0: 1)
+    int ff_no_rs;         // FF: the unweighted sum (partial 1) is not needed; only the vcoul-weighted one
 };
 
 // Split an FP32 value into three BF16 pieces (exact: 8+8+8 significand bits).
@@ -315,14 +317,15 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                 unit_coords(t, lu, mt, nt, ks, batch);
                 krange(t, ks, k0, k1);
                 const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
-                for (int st0 = 0; st0 < nst && ok; st0 += C::CHUNK_STAGES, ++chunk) {
+                const int CH = t.chunk_stages > 0 ? t.chunk_stages : 1;
+                for (int st0 = 0; st0 < nst && ok; st0 += CH, ++chunk) {
                     const int b = chunk & 1;
                     const bool freed = PAIR ? tc::mbar_wait_cluster(&accEmpty[b], ((chunk >> 1) & 1) ^ 1, wait_limit)
                                             : tc::mbar_wait(&accEmpty[b], ((chunk >> 1) & 1) ^ 1, wait_limit);
                     if (!freed) { fail(1); ok = false; break; }
                     tc::tc_fence_after();
                     const uint32_t dX = tmem + (uint32_t)(b * C::ACC_COLS), dY = dX + 2 * BN;
-                    const int st1 = min(nst, st0 + C::CHUNK_STAGES);
+                    const int st1 = min(nst, st0 + CH);
                     for (int st = st0; st < st1; ++st, ++g) {
                         const int s = g % C::STAGES;
                         const uint32_t par = (g / C::STAGES) & 1;
@@ -513,7 +516,9 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             // per-unit sums as FP32 float-float pairs (TwoSum): no FP64 instruction per drain
             // (GB300's FP64 pipe takes ~16 cycles per warp instruction); widened once per unit
             ff32 accx[GMAX] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, accy[GMAX] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-            for (int st0 = 0; st0 < nst; st0 += C::CHUNK_STAGES, ++chunk) {
+            const int CH = t.chunk_stages > 0 ? t.chunk_stages : 1;
+            const bool rs = !t.ff_no_rs;
+            for (int st0 = 0; st0 < nst; st0 += CH, ++chunk) {
                 const int b = chunk & 1;
                 if (!tc::warp_all(tc::mbar_wait(&accFull[b], (chunk >> 1) & 1, wait_limit) && !s_abort)) {
                     fail(16);
@@ -523,6 +528,16 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                 tc::tc_fence_after();
                 const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * C::ACC_COLS);
                 float2 gsum[GMAX] = {make_float2(0, 0), make_float2(0, 0), make_float2(0, 0)};
+                // the buffer goes back to the MMA issuer as soon as this warp's last
+                // TMEM load of it has landed, before the arithmetic on those values
+                auto release = [&]() {
+                    tc::tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) {
+                        if (PAIR && rank == 1) tc::mbar_arrive_remote(&accEmpty[b], 0);  // the MMA issuer's barrier
+                        else tc::mbar_arrive(&accEmpty[b]);
+                    }
+                };
                 if (EPI == EPI_FF) {
                     // the warp's 16 columns in two halves of 8 (X = [A_re B_re | A_re B_im],
                     // Y = [A_im B_re | A_im B_im]); the group's FP32 sums go to float-float once
@@ -535,6 +550,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         tc::tmem_ld8(tl + 2 * BN + c0 + 8 * hh, yr);
                         tc::tmem_ld8(tl + 3 * BN + c0 + 8 * hh, yi);
                         tc::tmem_ld_wait();
+                        if (hh == 1) release();
 #pragma unroll
                         for (int j = 0; j < 8; ++j) {
                             const float2 sv = make_float2(xr[j] - yi[j], xi[j] + yr[j]);
@@ -542,8 +558,10 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                             const float v = vreg[8 * hh + j];
                             gsum[0].x = fmaf(v, t2.x, gsum[0].x);
                             gsum[0].y = fmaf(v, t2.y, gsum[0].y);
-                            gsum[1].x += t2.x;
-                            gsum[1].y += t2.y;
+                            if (rs) {
+                                gsum[1].x += t2.x;
+                                gsum[1].y += t2.y;
+                            }
                         }
                     }
                     for (int gg = 0; gg < 2; ++gg) {
@@ -561,6 +579,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                     tc::tmem_ld16(tl + 2 * BN + c0, yr);
                     tc::tmem_ld16(tl + 3 * BN + c0, yi);
                     tc::tmem_ld_wait();
+                    if (c0 + 16 >= BN) release();
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         const int c = c0 + j;
@@ -568,12 +587,6 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         // tile column c = 3*(igp offset) + iw; column 63 is padding
                         if (c < 3 * GC) cfmaf(gsum[c % 3], wreg[c / 3], sv);
                     }
-                }
-                tc::tc_fence_before();
-                __syncwarp();
-                if (lane == 0) {
-                    if (PAIR && rank == 1) tc::mbar_arrive_remote(&accEmpty[b], 0);  // the MMA issuer's barrier
-                    else tc::mbar_arrive(&accEmpty[b]);
                 }
                 if (EPI == EPI_GPP) {
 #pragma unroll
