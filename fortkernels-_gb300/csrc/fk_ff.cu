@@ -521,7 +521,6 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
             t.err = c.errword;
             t.wait_limit = c.wait_limit;
             t.ff_no_rs = need_rs ? 0 : 1;
-            t.chunk_stages = getenv("FK_TC_CHUNK") ? atoi(getenv("FK_TC_CHUNK")) : 1;
             auto k = tcx::tc_contract_pair_kernel<EPI_FF, 64, true>;
             constexpr size_t smem = tcx::Cfg<64, true, true>::SMEM;
             static const int pairs = tcx::resident_pairs(k, smem, tcx::THREADS_FF, c.sms / 2);

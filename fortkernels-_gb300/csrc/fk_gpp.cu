@@ -1039,9 +1039,11 @@ __global__ void __launch_bounds__(ROWS_THREADS) rows_kernel(RowsArgs ra) {
 // The mixed-precision contraction of fk_gpp runs on CTA pairs, except in the
 // pipelined host path (one launch per row block), the half sum, the served
 // steps and the real-valued sum, which keep the single-CTA kernel.
+// A request with one n-tile of columns (ngpown <= 21) streams aqsntemp once at
+// the HBM rate, where the single-CTA kernel is the faster one (measured: 73 vs
+// 79 us at 512 x 2 x 32768 x 20); with more n-tiles the tensor work dominates.
 inline bool gpp_pair(const GppDev& r, bool pipelined) {
-    static const bool on = getenv("FK_GPP_PAIR") ? atoi(getenv("FK_GPP_PAIR")) != 0 : true;
-    return on && r.prec == FK_MIXED && !pipelined && !(r.flags & FK_GPP_HALF_SUM);
+    return r.prec == FK_MIXED && !pipelined && !(r.flags & FK_GPP_HALF_SUM) && r.ng > 21;
 }
 
 struct Plan {
@@ -1715,7 +1717,6 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
             t.wait_limit = c.wait_limit;
             if (tcx::encode_rows_map(&t.amap, r.aqsn, r.nc, r.nc, r.nb) != cudaSuccess)
                 return fail(c, FK_ECUDA, "gpp: cannot describe aqsntemp as a tensor map (needs a 16-byte aligned array)");
-            t.chunk_stages = getenv("FK_TC_CHUNK") ? atoi(getenv("FK_TC_CHUNK")) : 1;
             if (gpp_pair(r, false)) {
                 auto k = tcx::tc_contract_pair_kernel<EPI_GPP, 64, false>;
                 constexpr size_t smem = tcx::Cfg<64, false, true>::SMEM;

@@ -341,31 +341,34 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         // base descriptor plus a constant: one add per MMA for the single issuing thread
                         const uint64_t dA = tc::sdesc_sw64(tc::smem_u32(base + s * C::STAGE_BYTES));
                         const uint64_t dB = dA + (C::A_BYTES >> 4);
-#pragma unroll
-                        for (int kk = 0; kk < 2; ++kk) {
-                            // A sub-tile (re h,m,l, im h,m,l) and paired B piece [re|im], k offset kk*16
-                            auto ad = [&](int sub) { return dA + (uint64_t)((sub * BM * 64) >> 4) + 2 * kk; };
-                            // (PAIR: each CTA holds its half [B_re] or [B_im] of a piece, BN rows)
-                            auto bd = [&](int piece) {
-                                return dB + (uint64_t)((piece * (PAIR ? 1 : 2) * BN * 64) >> 4) + 2 * kk;
-                            };
-                            const uint32_t acc0 = (st > st0 || kk > 0) ? 1u : 0u;
-                            // piece products (a, b): the five small ones (mm, lh, hl, mh, hm), then hh;
-                            // X += A_re,a x [B_re|B_im]_b, Y += A_im,a x [B_re|B_im]_b
-                            const int PA[6] = {1, 2, 0, 1, 0, 0};
-                            const int PB[6] = {1, 0, 2, 0, 1, 0};
-#pragma unroll
-                            for (int q = 0; q < 6; ++q) {
-                                const uint32_t first = (q == 0) ? acc0 : 1u;
-                                if constexpr (PAIR) {
-                                    tc::mma_bf16_pair(dX, ad(PA[q]), bd(PB[q]), idp, first);
-                                    tc::mma_bf16_pair(dY, ad(3 + PA[q]), bd(PB[q]), idp, first);
-                                } else {
-                                    tc::mma_bf16(dX, ad(PA[q]), bd(PB[q]), idp, first);
-                                    tc::mma_bf16(dY, ad(3 + PA[q]), bd(PB[q]), idp, first);
-                                }
+                        // A sub-tile (re h,m,l, im h,m,l) and paired B piece [re|im], k offset kk*16
+                        // (PAIR: each CTA holds its half [B_re] or [B_im] of a piece, BN rows)
+                        auto ad = [&](int sub, int kk) { return dA + (uint64_t)((sub * BM * 64) >> 4) + 2 * kk; };
+                        auto bd = [&](int piece, int kk) {
+                            return dB + (uint64_t)((piece * (PAIR ? 1 : 2) * BN * 64) >> 4) + 2 * kk;
+                        };
+                        auto mma2 = [&](int pa, int pb, int kk, uint32_t accumulate) {
+                            // X += A_re,pa x [B_re|B_im]_pb, Y += A_im,pa x [B_re|B_im]_pb
+                            if constexpr (PAIR) {
+                                tc::mma_bf16_pair(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
+                                tc::mma_bf16_pair(dY, ad(3 + pa, kk), bd(pb, kk), idp, accumulate);
+                            } else {
+                                tc::mma_bf16(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
+                                tc::mma_bf16(dY, ad(3 + pa, kk), bd(pb, kk), idp, accumulate);
                             }
-                        }
+                        };
+                        // The accumulators truncate each addition to FP32 at the magnitude they
+                        // hold, so the five small piece products (mm, lh, hl, mh, hm; 2^-8 and
+                        // below of the sum) of both k-steps go in first, while the accumulator is
+                        // small, and the two hh products last: two full-scale roundings per stage.
+                        const int PA[5] = {1, 2, 0, 1, 0};
+                        const int PB[5] = {1, 0, 2, 0, 1};
+#pragma unroll
+                        for (int kk = 0; kk < 2; ++kk)
+#pragma unroll
+                            for (int q = 0; q < 5; ++q) mma2(PA[q], PB[q], kk, (st > st0 || kk > 0 || q > 0) ? 1u : 0u);
+                        mma2(0, 0, 0, 1u);
+                        mma2(0, 0, 1, 1u);
                         if constexpr (PAIR) tc::mma_commit_pair(&empty[s], 3);  // frees the stage in both CTAs
                         else tc::mma_commit(&empty[s]);
                     }
