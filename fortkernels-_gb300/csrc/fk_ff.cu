@@ -33,15 +33,17 @@ __global__ void ff_igp_kernel(int ng, int nc, const int* inv, const int* indinv,
     igp[i] = (g >= 0 && g < nc) ? g : -1;
 }
 
-// Sum the (KS x NT) partial slots of each (batch, n1, group) and scatter into
-// the per-plane tables RW/RS [nb][nf].
+// Sum the (KS x NT) partial slots of each (batch, row, group) and scatter into
+// the per-plane tables RW/RS [nb][nf]; partial row i belongs to band order[i]
+// (or i).
 __global__ void ff_rows_kernel(int nb, int nf, int batches, int slots_per_batch, const int* planes,
-                               const double2* P, double2* RW, double2* RS) {
-    const int n1 = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
-    if (n1 >= nb || b >= batches) return;
-    const double2* q = P + ((long)b * slots_per_batch * nb + n1) * 2;
+                               const double2* P, double2* RW, double2* RS, const int* order) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (i >= nb || b >= batches) return;
+    const double2* q = P + ((long)b * slots_per_batch * nb + i) * 2;
     const double2 s0 = ordered_sum(q, 2L * nb, slots_per_batch);
     const double2 s1 = RS ? ordered_sum(q + 1, 2L * nb, slots_per_batch) : make_double2(0.0, 0.0);
+    const int n1 = order ? order[i] : i;
     const int f = planes[b];
     RW[(long)n1 * nf + f] = s0;
     if (RS) RS[(long)n1 * nf + f] = s1;
@@ -271,6 +273,12 @@ struct FfPlan {
     int ngR;                      // combined list [planesR | planesA], is [groups[q], groups[q+1])
     int MT, NT, KS, kchunk;
     int BN, kstages;              // tensor-core path (mixed)
+    // Mixed path: bands in the order of the A image and the partial sums --
+    // those with a correction term grouped by its bracket plane, then the
+    // others -- and for each A plane the rows [aLo, aHi) of the bands that read
+    // it, contracted with KSa k-slices of kchunka.
+    std::vector<int> order, aLo, aHi;
+    int KSa = 0, kchunka = 0;
     bool mixed;
     size_t bytes, bytesImgR, bytesImgA, bytesW, bytesAimg;
 };
@@ -379,11 +387,44 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
         p.kchunk = ((r.nc + p.KS - 1) / p.KS + 15) / 16 * 16;
         p.KS = (r.nc + p.kchunk - 1) / p.kchunk;
     }
+    if (p.mixed) {
+        // the correction term of band n1 reads the A planes ifq_c and ifq_c + 1 only
+        // (achDtemp_cor_Kernel, FFKer_cori/ffKernel.cpp:212-246): sort the bands by that
+        // bracket so that each A plane is contracted over the row tiles of its bands only
+        p.order.resize(r.nb);
+        for (int i = 0; i < r.nb; ++i) p.order[i] = i;
+        std::stable_sort(p.order.begin(), p.order.end(), [&](int a, int b) {
+            const int ka = p.fact[a].kind ? p.fact[a].ifq_c : 1 << 30, kb = p.fact[b].kind ? p.fact[b].ifq_c : 1 << 30;
+            return ka < kb;
+        });
+        long tiles = 0;
+        for (int f : p.planesA) {
+            int lo = -1, hi = -1;
+            for (int i = 0; i < r.nb; ++i) {
+                const FactRow& fr = p.fact[p.order[i]];
+                if (fr.kind && (fr.ifq_c == f || fr.ifq_c + 1 == f)) {
+                    if (lo < 0) lo = i;
+                    hi = i + 1;
+                }
+            }
+            if (lo < 0) lo = hi = 0;
+            p.aLo.push_back(lo);
+            p.aHi.push_back(hi);
+            tiles += hi > lo ? (hi - 1) / tcx::BM - lo / tcx::BM + 1 : 0;
+        }
+        // k-slices so that one plane's launch (its row tiles x n-tiles) fills the SMs
+        const double per_plane = p.planesA.empty() ? 1.0 : std::max(1.0, (double)tiles / p.planesA.size()) * p.NT;
+        p.KSa = std::max(1, std::min(std::min(64, std::max(1, r.nc / 256)), (int)std::lround(c.sms / per_plane)));
+        p.kchunka = ((r.nc + p.KSa - 1) / p.KSa + tcx::BK - 1) / tcx::BK * tcx::BK;
+        p.KSa = (r.nc + p.kchunka - 1) / p.kchunka;
+    }
     const size_t slots = (size_t)p.KS * p.NT * (p.mixed ? tcx::FF_EPI_WARPS : 1);  // partial slots per plane
-    p.bytes = (slots * (p.planesR.size() + p.planesA.size()) * r.nb * 2 + 3 * (size_t)r.nb * r.nf +
+    const size_t slotsA = p.mixed ? (size_t)p.KSa * p.NT * tcx::FF_EPI_WARPS : slots;
+    p.bytes = ((slots * p.planesR.size() + slotsA * p.planesA.size()) * r.nb * 2 + 3 * (size_t)r.nb * r.nf +
                (size_t)r.ne * r.nb + (size_t)r.nb * r.nf + r.nf) * sizeof(double2) +
               (p.mixed ? (size_t)r.nb * r.nf * sizeof(float4) + r.nf * sizeof(float2) : 0) + 4 * 256 +
               r.nb * sizeof(FactRow) + (p.planesR.size() + p.planesA.size()) * sizeof(int) + r.ng * sizeof(int) +
+              r.nb * sizeof(int) +
               p.bytesImgR + p.bytesImgA + p.bytesW + p.bytesAimg + 20 * 256;
     return p;
 }
@@ -415,11 +456,13 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
     cudaStream_t st = c.stream;
     const int nR = (int)p.planesR.size(), nA = (int)p.planesA.size();
     const size_t slots = (size_t)p.KS * p.NT * (p.mixed ? tcx::FF_EPI_WARPS : 1);  // partial slots per plane
+    const size_t slotsA = p.mixed ? (size_t)p.KSa * p.NT * tcx::FF_EPI_WARPS : slots;
     int* igp = (int*)c.ws.take(r.ng * sizeof(int));
+    int* order = p.mixed ? (int*)c.ws.take(r.nb * sizeof(int)) : nullptr;
     int* planes = (int*)c.ws.take((nR + nA) * sizeof(int));
     FactRow* fact = (FactRow*)c.ws.take(r.nb * sizeof(FactRow));
     double2* PR = (double2*)c.ws.take(slots * std::max(nR, 1) * r.nb * 2 * sizeof(double2));
-    double2* PA = nA ? (double2*)c.ws.take(slots * nA * r.nb * 2 * sizeof(double2)) : nullptr;
+    double2* PA = nA ? (double2*)c.ws.take(slotsA * nA * r.nb * 2 * sizeof(double2)) : nullptr;
     double2* tabs = (double2*)c.ws.take(3 * (size_t)r.nb * r.nf * sizeof(double2));
     double2* SD = (double2*)c.ws.take((size_t)r.ne * r.nb * sizeof(double2));
     SchdiTab stab{};
@@ -433,7 +476,7 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
     uint8_t* imgA = p.bytesImgA ? (uint8_t*)c.ws.take(p.bytesImgA) : nullptr;
     float2* W = p.bytesW ? (float2*)c.ws.take(p.bytesW) : nullptr;
     uint8_t* Aimg = p.bytesAimg ? (uint8_t*)c.ws.take(p.bytesAimg) : nullptr;
-    if (!igp || !planes || !fact || !PR || (nA && !PA) || !tabs || !SD || (p.bytesImgR && !imgR) ||
+    if (!igp || (p.mixed && !order) || !planes || !fact || !PR || (nA && !PA) || !tabs || !SD || (p.bytesImgR && !imgR) ||
         (p.bytesImgA && !imgA) || (p.bytesW && !W) || (p.bytesAimg && !Aimg))
         return fail(c, FK_ENOMEM, "workspace too small for FF request");
     double2 *RW = tabs, *RS = tabs + (size_t)r.nb * r.nf, *AW = tabs + 2 * (size_t)r.nb * r.nf;
@@ -442,6 +485,8 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
     pl.insert(pl.end(), p.planesA.begin(), p.planesA.end());
     e = cudaMemcpyAsync(planes, pl.data(), pl.size() * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(fact, p.fact.data(), r.nb * sizeof(FactRow), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && order)
+        e = cudaMemcpyAsync(order, p.order.data(), r.nb * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(tabs, 0, 3 * (size_t)r.nb * r.nf * sizeof(double2), st);
     if (e != cudaSuccess) return cuda_fail(c, e, "ff: tables");
     c.launches = 0;
@@ -481,7 +526,7 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
     if (p.mixed) {
         tcx::weight_table_kernel<<<dim3(ceil_div(r.nb, 128), r.ng), 128, 0, st>>>(r.nb, 0, r.ng, r.aqsm, r.nc, r.vcoul,
                                                                                 igp, igp, 1.0, W, W + (size_t)r.nb * r.ng,
-                                                                                (float*)(W + 2 * (size_t)r.nb * r.ng));
+                                                                                (float*)(W + 2 * (size_t)r.nb * r.ng), order);
         // aqsntemp is reused by every (plane, n-tile): split it to BF16 pieces once
         // (an even number of 128-row tiles: rows past number_bands are zeros)
         const int MTa = 2 * p.MT;
@@ -489,12 +534,15 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
             tcx::img_pad_kernel<tcx::BM><<<dim3(p.kstages, MTa, 1), 256, 0, st>>>(Aimg, MTa, p.kstages, r.nb, 0, r.nc);
             ++c.launches;
         }
-        tcx::aimg_convert_kernel<<<dim3(ceil_div(r.nc, 256), r.nb), 256, 0, st>>>(r.aqsn, r.nb, r.nc, p.kstages, Aimg);
+        tcx::aimg_convert_kernel<<<dim3(ceil_div(r.nc, 256), r.nb), 256, 0, st>>>(r.aqsn, r.nb, r.nc, p.kstages, Aimg,
+                                                                                order);
         c.launches += 2;
         cudaMemsetAsync(c.errword, 0, sizeof(int), st);
     }
+    // a0 < 0: R planes, all bands on CTA pairs; a0 >= 0: the A planes a0 .. a0+nb_-1
+    // of planesA, each over the row tiles of the bands that read it
     auto contract = [&](const double2* eps, const int* pls, int nb_, double2* P, uint8_t* img, size_t img_bytes,
-                        bool need_rs) {
+                        int a0) {
         ContractArgs a{};
         a.A = r.aqsn; a.lda = r.nc; a.m0 = 0; a.M = r.nb;
         a.B = eps; a.ldb = r.nc; a.bstride = (long)r.ng * r.nc; a.N = r.ng; a.K = r.nc;
@@ -520,7 +568,34 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
             t.MT = p.MT; t.NT = p.NT; t.units = p.MT * p.NT * p.KS * nb_;
             t.err = c.errword;
             t.wait_limit = c.wait_limit;
-            t.ff_no_rs = need_rs ? 0 : 1;
+            if (a0 >= 0) {
+                // one single-CTA launch per A plane: its rows' tiles, the A k-split, and only
+                // the vcoul-weighted sum (AW)
+                t.ff_no_rs = 1;
+                t.c.batches = 1;
+                t.c.KS = p.KSa;
+                t.c.kchunk = p.kchunka;
+                const size_t islab = (size_t)p.NT * p.kstages * tcx::Cfg<64>::B_BYTES;
+                const size_t pslabA = slotsA * r.nb * 2;
+                auto k = tcx::tc_contract_kernel<EPI_FF, 64, true>;
+                constexpr size_t smem = tcx::Cfg<64, true>::SMEM;
+                cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                for (int j = 0; j < nb_; ++j) {
+                    const int lo = p.aLo[a0 + j], hi = p.aHi[a0 + j];
+                    if (hi <= lo) continue;
+                    t.mt0 = lo / tcx::BM;
+                    t.MT = (hi - 1) / tcx::BM - t.mt0 + 1;
+                    t.units = t.MT * p.NT * p.KSa;
+                    t.Bimg = img + j * islab;
+                    t.c.P = P + j * pslabA;
+                    kernel_begin(c);
+                    k<<<std::min(t.units, c.sms), tcx::THREADS_FF, smem, st>>>(t);
+                    kernel_end(c);
+                    ++c.launches;
+                }
+                ++c.launches;  // the conversion
+                return;
+            }
             auto k = tcx::tc_contract_pair_kernel<EPI_FF, 64, true>;
             constexpr size_t smem = tcx::Cfg<64, true, true>::SMEM;
             static const int pairs = tcx::resident_pairs(k, smem, tcx::THREADS_FF, c.sms / 2);
@@ -541,30 +616,33 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
         }
     };
     if (!pipe) {
-        if (nR) contract(r.epsR, planes, nR, PR, imgR, p.bytesImgR, true);
-        if (nA) contract(r.epsA, planes + nR, nA, PA, imgA, p.bytesImgA, false);  // A planes: AW only
+        if (nR) contract(r.epsR, planes, nR, PR, imgR, p.bytesImgR, -1);
+        if (nA) contract(r.epsA, planes + nR, nA, PA, imgA, p.bytesImgA, 0);  // A planes: AW only
     } else {
         // one launch pair per copy group, each after its planes have landed;
         // a group's partials and pre-split image sit at its batch offset
-        const size_t pslab = slots * r.nb * 2, islab = (size_t)p.NT * p.kstages * tcx::Cfg<64>::B_BYTES;
+        const size_t pslab = slots * r.nb * 2, pslabA = slotsA * r.nb * 2;
+        const size_t islab = (size_t)p.NT * p.kstages * tcx::Cfg<64>::B_BYTES;
         for (int q = 0; q < ngroups; ++q) {
             const bool isR = q < p.ngR;
             const int g0 = p.groups[q] - (isR ? 0 : nR), n = p.groups[q + 1] - p.groups[q];
             if (cudaStreamWaitEvent(st, c.pipe_ev[q], 0) != cudaSuccess)
                 return cuda_fail(c, cudaGetLastError(), "ff: pipeline wait");
             uint8_t* img = isR ? imgR : imgA;
-            contract(isR ? r.epsR : r.epsA, planes + (isR ? 0 : nR) + g0, n, (isR ? PR : PA) + g0 * pslab,
-                     img ? img + g0 * islab : nullptr, 0, isR);
+            contract(isR ? r.epsR : r.epsA, planes + (isR ? 0 : nR) + g0, n, isR ? PR + g0 * pslab : PA + g0 * pslabA,
+                     img ? img + g0 * islab : nullptr, 0, isR ? -1 : g0);
         }
     }
     phase_mark(c, 3);
     if (nR) {
-        ff_rows_kernel<<<dim3(ceil_div(r.nb, 128), nR), 128, 0, st>>>(r.nb, r.nf, nR, (int)slots, planes, PR, RW, RS);
+        ff_rows_kernel<<<dim3(ceil_div(r.nb, 128), nR), 128, 0, st>>>(r.nb, r.nf, nR, (int)slots, planes, PR, RW, RS,
+                                                                     order);
         ++c.launches;
     }
     if (nA) {
-        ff_rows_kernel<<<dim3(ceil_div(r.nb, 128), nA), 128, 0, st>>>(r.nb, r.nf, nA, (int)slots, planes + nR, PA, AW,
-                                                                     nullptr);
+        // (rows outside a plane's tiles give values no band reads)
+        ff_rows_kernel<<<dim3(ceil_div(r.nb, 128), nA), 128, 0, st>>>(r.nb, r.nf, nA, (int)slotsA, planes + nR, PA, AW,
+                                                                     nullptr, order);
         ++c.launches;
     }
     EpiArgs ea{};

@@ -717,19 +717,20 @@ __global__ void __launch_bounds__(AIMG ? THREADS_FF : THREADS, 1) tc_contract_ta
 }
 
 // Epilogue weight tables in FP32, column-major (row m contiguous):
-// W1[h][m] = wscale*vcoul[igp]*conj(aqsm[m0+m][igp]), W2[h][m] = conj(aqsm[m0+m][igp]).
+// W1[h][m] = wscale*vcoul[igp]*conj(aqsm[r][igp]), W2[h][m] = conj(aqsm[r][igp]),
+// r = m0 + m, or rowmap[m] when the rows are in another order.
 __device__ __forceinline__ float2 weight_w1(const double2 am, double s) {
     return make_float2(f64_to_f32_bits(am.x * s), f64_to_f32_bits(-am.y * s));
 }
 static __global__ void weight_table_kernel(int M, int m0, int ncols, const double2* aqsm, long ldm, const double* vcoul,
                                     const int* igp, const int* acol, double wscale, float2* W1, float2* W2,
-                                    float* vcol) {
+                                    float* vcol, const int* rowmap = nullptr) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x, h = blockIdx.y;
     if (h >= ncols || m >= M) return;
     const int g = igp[h];
     float2 w1 = make_float2(0.f, 0.f), w2 = w1;
     if (g >= 0) {
-        const double2 am = aqsm[(long)(m0 + m) * ldm + acol[h]];
+        const double2 am = aqsm[(long)(rowmap ? rowmap[m] : m0 + m) * ldm + acol[h]];
         w1 = weight_w1(am, wscale * vcoul[g]);
         w2 = make_float2(f64_to_f32_bits(am.x), f64_to_f32_bits(-am.y));
     }
@@ -805,11 +806,13 @@ inline bool img_needs_pad(int rows_per_tile, int cols, int gpp_cols, int K) {
     return cols % rows_per_tile != 0;
 }
 
-// FP64 rows [rows][K] -> pre-split A image [mt][kstage][NSUB][BM][64 B].
-static __global__ void aimg_convert_kernel(const double2* src, int rows, int K, int kstages, uint8_t* img) {
+// FP64 rows [rows][K] -> pre-split A image [mt][kstage][NSUB][BM][64 B]; image
+// row m holds source row rowmap[m] (or m).
+static __global__ void aimg_convert_kernel(const double2* src, int rows, int K, int kstages, uint8_t* img,
+                                           const int* rowmap = nullptr) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
     if (k >= K || m >= rows) return;
-    const double2 v = src[(long)m * K + k];
+    const double2 v = src[(long)(rowmap ? rowmap[m] : m) * K + k];
     uint8_t* tile = img + ((long)(m / BM) * kstages) * (long)(BM * NSUB * 64);
     img_store<BM>(tile, m % BM, k, f64_to_f32_bits(v.x), f64_to_f32_bits(v.y));
 }
