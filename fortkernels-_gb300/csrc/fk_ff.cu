@@ -35,14 +35,25 @@ __global__ void ff_igp_kernel(int ng, int nc, const int* inv, const int* indinv,
 
 // Sum the (KS x NT) partial slots of each (batch, row, group) and scatter into
 // the per-plane tables RW/RS [nb][nf]; partial row i belongs to band order[i]
-// (or i).
+// (or i).  One warp per (row, batch): lane l adds slots l, l+32, .. in order,
+// then a fixed shuffle tree adds the lanes (deterministic), so a row's slots
+// are loaded in a few round trips rather than one after another.
 __global__ void ff_rows_kernel(int nb, int nf, int batches, int slots_per_batch, const int* planes,
                                const double2* P, double2* RW, double2* RS, const int* order) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
-    if (i >= nb || b >= batches) return;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), b = blockIdx.y, lane = threadIdx.x & 31;
+    if (i >= nb || b >= batches) return;  // warp-uniform
     const double2* q = P + ((long)b * slots_per_batch * nb + i) * 2;
-    const double2 s0 = ordered_sum(q, 2L * nb, slots_per_batch);
-    const double2 s1 = RS ? ordered_sum(q + 1, 2L * nb, slots_per_batch) : make_double2(0.0, 0.0);
+    const int n = slots_per_batch > lane ? (slots_per_batch - lane + 31) / 32 : 0;
+    double2 s0 = ordered_sum(q + (long)lane * 2 * nb, 64L * nb, n);
+    double2 s1 = RS ? ordered_sum(q + 1 + (long)lane * 2 * nb, 64L * nb, n) : make_double2(0.0, 0.0);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        s0.x = __dadd_rn(s0.x, __shfl_xor_sync(0xffffffffu, s0.x, off));
+        s0.y = __dadd_rn(s0.y, __shfl_xor_sync(0xffffffffu, s0.y, off));
+        s1.x = __dadd_rn(s1.x, __shfl_xor_sync(0xffffffffu, s1.x, off));
+        s1.y = __dadd_rn(s1.y, __shfl_xor_sync(0xffffffffu, s1.y, off));
+    }
+    if (lane) return;
     const int n1 = order ? order[i] : i;
     const int f = planes[b];
     RW[(long)n1 * nf + f] = s0;
@@ -412,11 +423,8 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
             p.aHi.push_back(hi);
             tiles += hi > lo ? (hi - 1) / tcx::BM - lo / tcx::BM + 1 : 0;
         }
-        // k-slices so that one plane's launch (its row tiles x n-tiles) fills the SMs
-        const double per_plane = p.planesA.empty() ? 1.0 : std::max(1.0, (double)tiles / p.planesA.size()) * p.NT;
-        p.KSa = std::max(1, std::min(std::min(64, std::max(1, r.nc / 256)), (int)std::lround(c.sms / per_plane)));
-        p.kchunka = ((r.nc + p.KSa - 1) / p.KSa + tcx::BK - 1) / tcx::BK * tcx::BK;
-        p.KSa = (r.nc + p.kchunka - 1) / p.kchunka;
+        // k-slices for the one launch over all A planes' (row tile, n-tile) pairs
+        ff_pick_split_tc(std::max(1L, tiles) * p.NT, r.nc, c.sms, p.KSa, p.kchunka);
     }
     const size_t slots = (size_t)p.KS * p.NT * (p.mixed ? tcx::FF_EPI_WARPS : 1);  // partial slots per plane
     const size_t slotsA = p.mixed ? (size_t)p.KSa * p.NT * tcx::FF_EPI_WARPS : slots;
@@ -569,28 +577,32 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
             t.err = c.errword;
             t.wait_limit = c.wait_limit;
             if (a0 >= 0) {
-                // one single-CTA launch per A plane: its rows' tiles, the A k-split, and only
-                // the vcoul-weighted sum (AW)
+                // the A planes in one persistent launch (up to 64 planes each): every plane over
+                // the row tiles of the bands that read it, with the A k-split, and only the
+                // vcoul-weighted sum (AW).  Not bracketed by the kernel timer: the timed launches
+                // are the R-plane contraction, whose algorithmic flops the caller counts.
                 t.ff_no_rs = 1;
                 t.c.batches = 1;
                 t.c.KS = p.KSa;
                 t.c.kchunk = p.kchunka;
-                const size_t islab = (size_t)p.NT * p.kstages * tcx::Cfg<64>::B_BYTES;
-                const size_t pslabA = slotsA * r.nb * 2;
-                auto k = tcx::tc_contract_kernel<EPI_FF, 64, true>;
+                auto k = tcx::tc_contract_planes_kernel<EPI_FF, 64, true>;
                 constexpr size_t smem = tcx::Cfg<64, true>::SMEM;
                 cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                for (int j = 0; j < nb_; ++j) {
-                    const int lo = p.aLo[a0 + j], hi = p.aHi[a0 + j];
-                    if (hi <= lo) continue;
-                    t.mt0 = lo / tcx::BM;
-                    t.MT = (hi - 1) / tcx::BM - t.mt0 + 1;
-                    t.units = t.MT * p.NT * p.KSa;
-                    t.Bimg = img + j * islab;
-                    t.c.P = P + j * pslabA;
-                    // (not bracketed by the kernel timer: the timed launches are the R-plane
-                    // contraction whose algorithmic flops the caller counts)
-                    k<<<std::min(t.units, c.sms), tcx::THREADS_FF, smem, st>>>(t);
+                for (int j0 = 0; j0 < nb_; j0 += tcx::TC_MAXPL) {
+                    tcx::PlaneTab pt{};
+                    pt.islab = (long)p.NT * p.kstages * tcx::Cfg<64>::B_BYTES;
+                    pt.pslab = (long)slotsA * r.nb * 2;
+                    pt.u0[0] = 0;
+                    for (int j = j0; j < std::min(nb_, j0 + tcx::TC_MAXPL); ++j) {
+                        const int lo = p.aLo[a0 + j], hi = p.aHi[a0 + j], q = pt.n++;
+                        pt.mt0[q] = hi > lo ? lo / tcx::BM : 0;
+                        pt.MT[q] = hi > lo ? (hi - 1) / tcx::BM - pt.mt0[q] + 1 : 0;
+                        pt.u0[q + 1] = pt.u0[q] + pt.MT[q] * p.NT * p.KSa;
+                    }
+                    if (pt.u0[pt.n] == 0) continue;
+                    t.Bimg = img + (long)j0 * pt.islab;
+                    t.c.P = P + (long)j0 * pt.pslab;
+                    k<<<std::min(pt.u0[pt.n], c.sms), tcx::THREADS_FF, smem, st>>>(t, pt);
                     ++c.launches;
                 }
                 ++c.launches;  // the conversion
@@ -635,13 +647,13 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
     }
     phase_mark(c, 3);
     if (nR) {
-        ff_rows_kernel<<<dim3(ceil_div(r.nb, 128), nR), 128, 0, st>>>(r.nb, r.nf, nR, (int)slots, planes, PR, RW, RS,
+        ff_rows_kernel<<<dim3(ceil_div(r.nb, 4), nR), 128, 0, st>>>(r.nb, r.nf, nR, (int)slots, planes, PR, RW, RS,
                                                                      order);
         ++c.launches;
     }
     if (nA) {
         // (rows outside a plane's tiles give values no band reads)
-        ff_rows_kernel<<<dim3(ceil_div(r.nb, 128), nA), 128, 0, st>>>(r.nb, r.nf, nA, (int)slotsA, planes + nR, PA, AW,
+        ff_rows_kernel<<<dim3(ceil_div(r.nb, 4), nA), 128, 0, st>>>(r.nb, r.nf, nA, (int)slotsA, planes + nR, PA, AW,
                                                                      nullptr, order);
         ++c.launches;
     }

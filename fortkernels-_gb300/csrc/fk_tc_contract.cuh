@@ -197,6 +197,40 @@ struct TableReqs {
 // own A rows and its half of B; the odd CTA's "stage landed" and "accumulator
 // drained" signals go to the even CTA's barriers (a relay thread and remote
 // arrivals); the MMA commits reach both CTAs' barriers.
+// Units of several batches (FF frequency planes) with their own row-tile
+// ranges in one launch: plane r owns units [u0[r], u0[r+1]) over row tiles
+// [mt0[r], mt0[r] + MT[r]); its B image and partial sums sit islab / pslab
+// bytes / elements after the previous plane's.  Each warp role keeps a copy
+// of the current plane's arguments, updated when it moves to the next plane.
+constexpr int TC_MAXPL = 64;
+struct PlaneTab {
+    int n;
+    int u0[TC_MAXPL + 1], mt0[TC_MAXPL], MT[TC_MAXPL];
+    long islab, pslab;
+};
+struct PlaneSeq {
+    const TcArgs* base;
+    const PlaneTab* tab;
+    TcArgs cur;
+    int r;
+    __device__ int units() const { return tab->u0[tab->n]; }
+    __device__ const TcArgs& at(int u, int& lu) {
+        if (r < 0 || u >= tab->u0[r + 1]) {
+            if (r < 0) r = 0;
+            while (r + 1 < tab->n && u >= tab->u0[r + 1]) ++r;
+            cur = *base;
+            cur.mt0 = tab->mt0[r];
+            cur.MT = tab->MT[r];
+            cur.units = tab->u0[r + 1] - tab->u0[r];
+            cur.Bimg = base->Bimg + (long)r * tab->islab;
+            cur.c.P = base->c.P + (long)r * tab->pslab;
+        }
+        lu = u - tab->u0[r];
+        return cur;
+    }
+    static constexpr bool kTable = false;
+};
+
 template <int EPI, int BN, bool AIMG, bool PAIR, class Src>
 __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long long wait_limit) {
     using C = Cfg<BN, EPI == EPI_FF, PAIR>;
@@ -708,6 +742,13 @@ template <int EPI, int BN, bool AIMG>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(AIMG ? THREADS_FF : THREADS, 1)
     tc_contract_pair_kernel(const __grid_constant__ TcArgs t) {
     tc_contract_body<EPI, BN, AIMG, true>(OneReq{t}, t.err, t.wait_limit);
+}
+
+// The batches of a PlaneTab in one launch (single CTAs).
+template <int EPI, int BN, bool AIMG>
+__global__ void __launch_bounds__(AIMG ? THREADS_FF : THREADS, 1)
+    tc_contract_planes_kernel(const __grid_constant__ TcArgs t, const __grid_constant__ PlaneTab pt) {
+    tc_contract_body<EPI, BN, AIMG, false>(PlaneSeq{&t, &pt, t, -1}, t.err, t.wait_limit);
 }
 
 // Units of several requests from a device table (the served step).
