@@ -383,7 +383,7 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
         p.MT = ceil_div(r.nb, 2 * tcx::BM);
         p.NT = ceil_div(r.ng, p.BN);
         ff_pick_split_tc((long)p.MT * p.NT * nplanes, r.nc, c.sms / 2, p.KS, p.kchunk);
-        const size_t bb = tcx::Cfg<64>::B_BYTES;
+        const size_t bb = tcx::Cfg<64, true>::B_BYTES;
         p.bytesImgR = p.planesR.size() * (size_t)p.NT * p.kstages * bb;
         p.bytesImgA = p.planesA.size() * (size_t)p.NT * p.kstages * bb;
         p.bytesW = 2 * (size_t)r.nb * r.ng * sizeof(float2) + (size_t)r.ng * sizeof(float) + 256;
@@ -560,7 +560,7 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
             // pre-split B planes (bf16 x 3), then the tensor-core contraction
             const int NTb = ceil_div(r.ng, 64);
             if (tcx::img_needs_pad(64, r.ng, 0, r.nc)) {
-                tcx::img_pad_kernel<64><<<dim3(p.kstages, NTb, nb_), 256, 0, st>>>(img, NTb, p.kstages, r.ng, 0, r.nc);
+                tcx::img_pad_kernel<64, 9><<<dim3(p.kstages, NTb, nb_), 256, 0, st>>>(img, NTb, p.kstages, r.ng, 0, r.nc);
                 ++c.launches;
             }
             (void)img_bytes;
@@ -590,7 +590,7 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
                 cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
                 for (int j0 = 0; j0 < nb_; j0 += tcx::TC_MAXPL) {
                     tcx::PlaneTab pt{};
-                    pt.islab = (long)p.NT * p.kstages * tcx::Cfg<64>::B_BYTES;
+                    pt.islab = (long)p.NT * p.kstages * tcx::Cfg<64, true>::B_BYTES;
                     pt.pslab = (long)slotsA * r.nb * 2;
                     pt.u0[0] = 0;
                     for (int j = j0; j < std::min(nb_, j0 + tcx::TC_MAXPL); ++j) {
@@ -634,7 +634,7 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
         // one launch pair per copy group, each after its planes have landed;
         // a group's partials and pre-split image sit at its batch offset
         const size_t pslab = slots * r.nb * 2, pslabA = slotsA * r.nb * 2;
-        const size_t islab = (size_t)p.NT * p.kstages * tcx::Cfg<64>::B_BYTES;
+        const size_t islab = (size_t)p.NT * p.kstages * tcx::Cfg<64, true>::B_BYTES;
         for (int q = 0; q < ngroups; ++q) {
             const bool isR = q < p.ngR;
             const int g0 = p.groups[q] - (isR ? 0 : nR), n = p.groups[q + 1] - p.groups[q];

@@ -61,7 +61,7 @@ constexpr long long DRAIN_LIMIT = 4000000000LL;
 
 template <int BN, bool WSMEM = false, bool PAIR = false>
 struct Cfg {
-    static_assert(BN == 64, "four accumulators x two buffers fill the 512 TMEM columns at BN = 64");
+    static_assert(BN == 64, "the accumulator buffers fill the 512 TMEM columns at BN = 64");
     // Operand stages: FF three (its epilogue keeps the per-unit weights in
     // registers, so shared memory holds operands only), GPP two.  GPP: a 64 KB staging buffer receives
     // FP64 A rows by TMA in two halves of BK/2 k-values, so that one half is in
@@ -71,13 +71,23 @@ struct Cfg {
     static constexpr int STAGES = WSMEM ? 3 : 2;
     static constexpr int CHUNK_STAGES = 1;  // k-values per TMEM accumulation = 32
     static constexpr uint32_t A_BYTES = NSUB * BM * 64;
-    static constexpr uint32_t B_BYTES = NSUB * BN * 64;  // one k-stage of an n-tile in the pre-split B image
-    // B in one CTA's stage: all six pieces, or, for a CTA pair, the real (even
-    // CTA) or imaginary (odd CTA) half of each piece's [B_re | B_im]
-    static constexpr uint32_t B_SMEM = PAIR ? NSPLIT * BN * 64 : B_BYTES;
+    // The pre-split B image, one k-stage of an n-tile: GPP six sub-tiles (re h,
+    // im h, re m, im m, re l, im l); FF nine (-im, re, im of each piece h, m, l),
+    // the negated imaginary parts serving the CTA pairs' complex accumulation.
+    static constexpr bool IMG9 = WSMEM;
+    static constexpr uint32_t B_BYTES = (IMG9 ? 9 : NSUB) * BN * 64;
+    // SL (FF on CTA pairs): one accumulator D = A_re x [B_re|B_im] + A_im x
+    // [-B_im|B_re] = [S_re | S_im], 2*BN columns, in four buffers; otherwise two
+    // accumulators X = A_re x [B_re|B_im], Y = A_im x [B_re|B_im] in two buffers.
+    static constexpr bool SL = WSMEM && PAIR;
+    // B in one CTA's stage: [B_re; B_im] of each piece (single CTA); for a CTA
+    // pair the even CTA's B_re (SL: [B_re; -B_im]) and the odd CTA's B_im (SL:
+    // [B_im; B_re]) of each piece
+    static constexpr uint32_t B_SMEM = (PAIR ? (SL ? 2 : 1) : 2) * NSPLIT * BN * 64;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_SMEM;
-    static constexpr uint32_t ACC_COLS = 4 * BN;       // X = A_re x [B_re|B_im], Y = A_im x [B_re|B_im]
-    static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;  // double buffered
+    static constexpr int NBUF = SL ? 4 : 2;
+    static constexpr uint32_t ACC_COLS = SL ? 2 * BN : 4 * BN;
+    static constexpr uint32_t TMEM_COLS = NBUF * ACC_COLS;
     static constexpr uint32_t W_BYTES = 0u;
     static constexpr uint32_t F64_BYTES = WSMEM ? 0u : (uint32_t)(BM * BK * sizeof(double2));
     static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + W_BYTES + F64_BYTES + 1024 + 256;
@@ -242,9 +252,9 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
     uint64_t* fullA = bars;
     uint64_t* fullB = bars + C::STAGES;
     uint64_t* empty = bars + 2 * C::STAGES;
-    uint64_t* accFull = bars + 3 * C::STAGES;
-    uint64_t* accEmpty = accFull + 2;
-    uint64_t* done = accEmpty + 2;
+    uint64_t* accFull = bars + 3 * C::STAGES;  // [NBUF]
+    uint64_t* accEmpty = accFull + C::NBUF;    // [NBUF]
+    uint64_t* done = accEmpty + C::NBUF;
     uint64_t* fFull = done + 1;    // [2] GPP: FP64 staging half filled (tx bytes)
     uint64_t* fEmpty = done + 3;   // [2] GPP: FP64 staging half read by all converter warps
     uint64_t* peerFull = done + 5; // [STAGES] PAIR, even CTA: the odd CTA's half of the stage has landed
@@ -265,7 +275,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             tc::mbar_init(&fullB[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < C::NBUF; ++b) {
             tc::mbar_init(&accFull[b], 1);
             tc::mbar_init(&accEmpty[b], PAIR ? 2 * EPI_WARPS : EPI_WARPS);  // both CTAs' epilogues drain
         }
@@ -353,11 +363,13 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                 const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
                 const int CH = t.chunk_stages > 0 ? t.chunk_stages : 1;
                 for (int st0 = 0; st0 < nst && ok; st0 += CH, ++chunk) {
-                    const int b = chunk & 1;
-                    const bool freed = PAIR ? tc::mbar_wait_cluster(&accEmpty[b], ((chunk >> 1) & 1) ^ 1, wait_limit)
-                                            : tc::mbar_wait(&accEmpty[b], ((chunk >> 1) & 1) ^ 1, wait_limit);
+                    const int b = chunk % C::NBUF;
+                    const uint32_t bpar = ((chunk / C::NBUF) & 1) ^ 1;
+                    const bool freed = PAIR ? tc::mbar_wait_cluster(&accEmpty[b], bpar, wait_limit)
+                                            : tc::mbar_wait(&accEmpty[b], bpar, wait_limit);
                     if (!freed) { fail(1); ok = false; break; }
                     tc::tc_fence_after();
+                    // X, Y (two accumulators) or, SL, the one accumulator D = dX
                     const uint32_t dX = tmem + (uint32_t)(b * C::ACC_COLS), dY = dX + 2 * BN;
                     const int st1 = min(nst, st0 + CH);
                     for (int st = st0; st < st1; ++st, ++g) {
@@ -375,15 +387,21 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         // base descriptor plus a constant: one add per MMA for the single issuing thread
                         const uint64_t dA = tc::sdesc_sw64(tc::smem_u32(base + s * C::STAGE_BYTES));
                         const uint64_t dB = dA + (C::A_BYTES >> 4);
-                        // A sub-tile (re h,m,l, im h,m,l) and paired B piece [re|im], k offset kk*16
-                        // (PAIR: each CTA holds its half [B_re] or [B_im] of a piece, BN rows)
+                        // A sub-tile (re h,m,l, im h,m,l) and B piece, k offset kk*16.  A CTA's B
+                        // piece is 2*BN rows ([B_re; B_im], or SL [B_re; -B_im] / [B_im; B_re]),
+                        // or BN rows (pair without SL: its half [B_re] or [B_im])
                         auto ad = [&](int sub, int kk) { return dA + (uint64_t)((sub * BM * 64) >> 4) + 2 * kk; };
                         auto bd = [&](int piece, int kk) {
-                            return dB + (uint64_t)((piece * (PAIR ? 1 : 2) * BN * 64) >> 4) + 2 * kk;
+                            return dB + (uint64_t)((piece * ((PAIR && !C::SL) ? 1 : 2) * BN * 64) >> 4) + 2 * kk;
                         };
+                        constexpr uint64_t B_HALF = (uint64_t)(BN * 64) >> 4;  // SL: the piece's second BN rows
                         auto mma2 = [&](int pa, int pb, int kk, uint32_t accumulate) {
-                            // X += A_re,pa x [B_re|B_im]_pb, Y += A_im,pa x [B_re|B_im]_pb
-                            if constexpr (PAIR) {
+                            // X += A_re,pa x [B_re|B_im]_pb, Y += A_im,pa x [B_re|B_im]_pb; SL:
+                            // D += A_re,pa x [B_re|B_im]_pb + A_im,pa x [-B_im|B_re]_pb
+                            if constexpr (C::SL) {
+                                tc::mma_bf16_pair(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
+                                tc::mma_bf16_pair(dX, ad(3 + pa, kk), bd(pb, kk) + B_HALF, idp, 1u);
+                            } else if constexpr (PAIR) {
                                 tc::mma_bf16_pair(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
                                 tc::mma_bf16_pair(dY, ad(3 + pa, kk), bd(pb, kk), idp, accumulate);
                             } else {
@@ -470,12 +488,25 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         const uint8_t* src =
                             t.Bimg + (((long)plane * t.NT + nt) * t.kstages_total + kst) * (long)C::B_BYTES;
                         tc::mbar_arrive_expect_tx(&fullB[s], C::B_SMEM);
-                        if constexpr (PAIR) {
+                        uint8_t* bdst = base + s * C::STAGE_BYTES + C::A_BYTES;
+                        if constexpr (C::SL) {
+                            // image -im, re, im per piece: the even CTA takes [re; -im], the odd [im; re]
+                            for (int pc = 0; pc < NSPLIT; ++pc) {
+                                const int s0 = rank ? 2 : 1, s1 = rank ? 1 : 0;
+                                tc::bulk_g2s(bdst + (2 * pc) * BN * 64, src + (3 * pc + s0) * BN * 64, BN * 64, &fullB[s]);
+                                tc::bulk_g2s(bdst + (2 * pc + 1) * BN * 64, src + (3 * pc + s1) * BN * 64, BN * 64,
+                                             &fullB[s]);
+                            }
+                        } else if constexpr (C::IMG9) {
+                            // single CTA over the nine-sub-tile image: [re; im] of each piece, adjacent
+                            for (int pc = 0; pc < NSPLIT; ++pc)
+                                tc::bulk_g2s(bdst + (2 * pc) * BN * 64, src + (3 * pc + 1) * BN * 64, 2 * BN * 64,
+                                             &fullB[s]);
+                        } else if constexpr (PAIR) {
                             // the even CTA's B_re, the odd CTA's B_im of each piece (paired image layout:
                             // re h, im h, re m, im m, re l, im l), BN rows each
                             for (int pc = 0; pc < NSPLIT; ++pc)
-                                tc::bulk_g2s(base + s * C::STAGE_BYTES + C::A_BYTES + pc * BN * 64,
-                                             src + (2 * pc + (int)rank) * BN * 64, BN * 64, &fullB[s]);
+                                tc::bulk_g2s(bdst + pc * BN * 64, src + (2 * pc + (int)rank) * BN * 64, BN * 64, &fullB[s]);
                         } else {
                             tc::bulk_g2s(base + s * C::STAGE_BYTES + C::A_BYTES, src, C::B_BYTES, &fullB[s]);
                         }
@@ -556,8 +587,8 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             const int CH = t.chunk_stages > 0 ? t.chunk_stages : 1;
             const bool rs = !t.ff_no_rs;
             for (int st0 = 0; st0 < nst; st0 += CH, ++chunk) {
-                const int b = chunk & 1;
-                if (!tc::warp_all(tc::mbar_wait(&accFull[b], (chunk >> 1) & 1, wait_limit) && !s_abort)) {
+                const int b = chunk % C::NBUF;
+                if (!tc::warp_all(tc::mbar_wait(&accFull[b], (chunk / C::NBUF) & 1, wait_limit) && !s_abort)) {
                     fail(16);
                     ok = false;
                     break;
@@ -575,7 +606,31 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         else tc::mbar_arrive(&accEmpty[b]);
                     }
                 };
-                if (EPI == EPI_FF) {
+                if (EPI == EPI_FF && C::SL) {
+                    // the warp's 16 columns of D = [S_re | S_im]: both loads, then the buffer
+                    // goes back, then the weighted sums
+                    const int c0 = ej * 16;
+                    float sr[16], si[16];
+                    tc::tmem_ld16(tl + c0, sr);
+                    tc::tmem_ld16(tl + BN + c0, si);
+                    tc::tmem_ld_wait();
+                    release();
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const float2 t2 = cmulf(wreg[j], make_float2(sr[j], si[j]));
+                        gsum[0].x = fmaf(vreg[j], t2.x, gsum[0].x);
+                        gsum[0].y = fmaf(vreg[j], t2.y, gsum[0].y);
+                        if (rs) {
+                            gsum[1].x += t2.x;
+                            gsum[1].y += t2.y;
+                        }
+                    }
+                    for (int gg = 0; gg < 2; ++gg) {
+                        ff_add(accx[gg], gsum[gg].x);
+                        ff_add(accy[gg], gsum[gg].y);
+                        gsum[gg] = make_float2(0.f, 0.f);
+                    }
+                } else if (EPI == EPI_FF) {
                     // the warp's 16 columns in two halves of 8 (X = [A_re B_re | A_re B_im],
                     // Y = [A_im B_re | A_im B_im]); the group's FP32 sums go to float-float once
                     const int c0 = ej * 16;
@@ -780,22 +835,37 @@ static __global__ void weight_table_kernel(int M, int m0, int ncols, const doubl
     if (vcol && m == 0) vcol[h] = g >= 0 ? f64_to_f32_bits(vcoul[g]) : 0.f;
 }
 
-// FP64 planes [plane][rows][K] -> pre-split B images [plane][nt][kstage][NSUB][BN][64 B].
-// Each thread converts 8 consecutive k-values of one row: 128 contiguous
-// bytes in, one 16-byte swizzle chunk of each of the six pieces out (the
-// swizzle permutes whole 16-byte chunks).  Grid (ceil(K/8 / blockDim), rows, planes).
+// FP64 planes [plane][rows][K] -> the nine-sub-tile B images of FF
+// [plane][nt][kstage][piece h, m, l][-im, re, im][BN][64 B] (a piece of -im is
+// the piece of im with its sign flipped: the split is symmetric).  Each thread
+// converts 8 consecutive k-values of one row: 128 contiguous bytes in, one
+// 16-byte swizzle chunk of each of the nine sub-tiles out (the swizzle permutes
+// whole 16-byte chunks).  Grid (ceil(K/8 / blockDim), rows, planes).
 template <int BN>
 __global__ void bimg_convert_kernel(const double2* src, long plane_stride, int rows, int K, const int* planes,
                                     int kstages, uint8_t* img) {
+    constexpr long STAGE = 9L * BN * 64;
     const int k0 = 8 * (blockIdx.x * blockDim.x + threadIdx.x), n = blockIdx.y, b = blockIdx.z;
     if (k0 >= K) return;
     const int f = planes ? planes[b] : b;
     const double2* row = src + (long)f * plane_stride + (long)n * K;
     const int NT = (rows + BN - 1) / BN;
-    uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * (long)Cfg<BN>::B_BYTES;
+    uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * STAGE;
     if (k0 + 8 > K) {  // ragged end of the row: element by element
-        for (int k = k0; k < K; ++k)
-            bimg_store<BN>(img_nt, kstages, n % BN, k, f64_to_f32_bits(row[k].x), f64_to_f32_bits(row[k].y));
+        for (int k = k0; k < K; ++k) {
+            uint8_t* st = img_nt + (long)(k / BK) * STAGE;
+            const uint32_t off = tc::sw64_offset(n % BN, k % BK);
+            uint16_t rh, rm, rl, ih, im, il;
+            split3(f64_to_f32_bits(row[k].x), rh, rm, rl);
+            split3(f64_to_f32_bits(row[k].y), ih, im, il);
+            const uint16_t pr[3] = {rh, rm, rl}, pi[3] = {ih, im, il};
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                *(uint16_t*)(st + (3 * q + 0) * BN * 64 + off) = (uint16_t)(pi[q] ^ 0x8000u);
+                *(uint16_t*)(st + (3 * q + 1) * BN * 64 + off) = pr[q];
+                *(uint16_t*)(st + (3 * q + 2) * BN * 64 + off) = pi[q];
+            }
+        }
         return;
     }
     uint32_t pk[6][4];  // piece (part + 2*level) x four bf16 pairs
@@ -814,30 +884,37 @@ __global__ void bimg_convert_kernel(const double2* src, long plane_stride, int r
         pk[3][j / 2] = (uint32_t)m0 | ((uint32_t)m1 << 16);
         pk[5][j / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
     }
-    uint8_t* st = img_nt + (long)(k0 / BK) * (BN * NSUB * 64);
+    uint8_t* st = img_nt + (long)(k0 / BK) * STAGE;
     const uint32_t off = tc::sw64_offset(n % BN, k0 % BK);  // 16-byte aligned: k0 % 8 == 0
 #pragma unroll
-    for (int q = 0; q < 6; ++q)
-        *(uint4*)(st + q * BN * 64 + off) = make_uint4(pk[q][0], pk[q][1], pk[q][2], pk[q][3]);
+    for (int q = 0; q < 3; ++q) {  // piece level h, m, l: pk[2q] re, pk[2q+1] im
+        const uint32_t* re = pk[2 * q];
+        const uint32_t* im = pk[2 * q + 1];
+        *(uint4*)(st + (3 * q + 0) * BN * 64 + off) =
+            make_uint4(im[0] ^ 0x80008000u, im[1] ^ 0x80008000u, im[2] ^ 0x80008000u, im[3] ^ 0x80008000u);
+        *(uint4*)(st + (3 * q + 1) * BN * 64 + off) = make_uint4(re[0], re[1], re[2], re[3]);
+        *(uint4*)(st + (3 * q + 2) * BN * 64 + off) = make_uint4(im[0], im[1], im[2], im[3]);
+    }
 }
 
 // Zeros the image positions that no converter writes: rows past a tile's
 // valid rows and k-values past K.  Valid rows of tile nt: 3*min(gpp_cols,
 // cols - gpp_cols*nt) when gpp_cols > 0 (GPP: gpp_cols igp triples per tile),
-// else min(ROWS, cols - ROWS*nt).  Grid (kstages, NT, planes).
-template <int ROWS>
+// else min(ROWS, cols - ROWS*nt).  NS sub-tiles per stage (six; nine for the
+// FF B images).  Grid (kstages, NT, planes).
+template <int ROWS, int NS = NSUB>
 __global__ void img_pad_kernel(uint8_t* img, int NT, int kstages, int cols, int gpp_cols, int K) {
     const int kst = blockIdx.x, nt = blockIdx.y, pl = blockIdx.z;
     const int vr = gpp_cols > 0 ? 3 * min(gpp_cols, cols - gpp_cols * nt) : min(ROWS, cols - ROWS * nt);
     const int kv = min(BK, K - kst * BK);  // valid k-values of this stage
     if (vr >= ROWS && kv >= BK) return;
-    uint8_t* st = img + (((long)pl * NT + nt) * kstages + kst) * (long)(ROWS * NSUB * 64);
+    uint8_t* st = img + (((long)pl * NT + nt) * kstages + kst) * (long)(ROWS * NS * 64);
     for (int i = threadIdx.x; i < ROWS * BK; i += blockDim.x) {
         const int row = i / BK, k = i % BK;
         if (row < vr && k < kv) continue;
         const uint32_t off = tc::sw64_offset(row, k);
 #pragma unroll
-        for (int q = 0; q < NSUB; ++q) *(uint16_t*)(st + q * ROWS * 64 + off) = 0;
+        for (int q = 0; q < NS; ++q) *(uint16_t*)(st + q * ROWS * 64 + off) = 0;
     }
 }
 // True when some image position needs img_pad_kernel.
