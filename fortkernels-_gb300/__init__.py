@@ -114,6 +114,18 @@ class Context:
         Lowering it is a test hook for the timeout path."""
         self._check(self.lib.fk_set_wait_limit(self.h, int(cycles)), self.h)
 
+    def set_error_estimate(self, enable: bool = True):
+        """Make later mixed gpp calls also compute an a-priori error estimate
+        (one more pass over aqsntemp); read it with gpp_error_estimate()."""
+        self._check(self.lib.fk_set_error_estimate(self.h, 1 if enable else 0), self.h)
+
+    def gpp_error_estimate(self) -> dict:
+        """Estimated absolute error of the last mixed gpp call's outputs:
+        {"achtemp": max over iw, "asxtemp": max over iw, "acht_n1_loc": max over bands}."""
+        v = (ctypes.c_double * 3)()
+        self._check(self.lib.fk_gpp_error_estimate(self.h, v), self.h)
+        return {"achtemp": v[0], "asxtemp": v[1], "acht_n1_loc": v[2]}
+
     def selftest_timeout(self, cycles: int) -> int:
         """Status of a one-warp kernel whose bounded wait on a barrier nothing
         arrives on gives up after `cycles` cycles (FK_ETIMEOUT expected)."""

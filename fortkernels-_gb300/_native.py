@@ -27,7 +27,8 @@ SYMBOLS = ("fk_create", "fk_destroy", "fk_set_stream", "fk_synchronize", "fk_res
            "fk_last_error", "fk_version", "fk_gpp", "fk_ff", "fk_set_profiling", "fk_last_timings",
            "fk_last_launches", "fk_last_kernel_time", "fk_last_transfer", "fk_gpp_static", "fk_gpp_real", "fk_server_create", "fk_server_destroy",
            "fk_server_resident_put", "fk_server_resident_evict", "fk_server_submit", "fk_server_wait",
-           "fk_server_stats", "fk_server_tune", "fk_set_wait_limit", "fk_selftest_timeout", "fk_wait_error_status", "fk_server_cancel")
+           "fk_server_stats", "fk_server_tune", "fk_set_wait_limit", "fk_selftest_timeout", "fk_wait_error_status", "fk_server_cancel",
+           "fk_set_error_estimate", "fk_gpp_error_estimate")
 
 
 class ServerConfig(ctypes.Structure):
@@ -108,6 +109,8 @@ def load(path: str = LIB_PATH):
     L.fk_last_transfer.argtypes = [P, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong)]
     L.fk_set_wait_limit.argtypes = [P, ctypes.c_longlong]
     L.fk_selftest_timeout.argtypes = [P, ctypes.c_longlong]
+    L.fk_set_error_estimate.argtypes = [P, I]
+    L.fk_gpp_error_estimate.argtypes = [P, ctypes.POINTER(D)]
     L.fk_wait_error_status.argtypes = [I, ctypes.c_char_p, ctypes.c_size_t]
     for name in SYMBOLS:
         f = getattr(L, name)

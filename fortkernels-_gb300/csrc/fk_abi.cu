@@ -333,6 +333,7 @@ fk_status fk_destroy(fk_ctx_t c) {
         fk::drop_graphs(*c);
         if (c->ws.base) cudaFree(c->ws.base);
         if (c->errword) cudaFree(c->errword);
+        if (c->est_dev) cudaFree(c->est_dev);
         if (c->pinned) cudaFreeHost(c->pinned);
         if (c->pinned_ev) cudaEventDestroy(c->pinned_ev);
         for (auto& e : c->ev)
@@ -589,11 +590,11 @@ fk_status gpp_host_pipelined(Ctx& x, GppDev r, const fk_c128* aqsmtemp, const fk
 }  // namespace
 }  // namespace fk
 
-fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsmtemp, const fk_c128* aqsntemp,
-                 const fk_c128* I_eps_array, const fk_c128* wtilde_array, const double* vcoul,
-                 const int* inv_igp_index, const int* indinv, const double* wx_array, fk_precision precision,
-                 unsigned flags, fk_c128* achtemp, fk_c128* asxtemp, fk_c128* acht_n1_loc, fk_c128* achstemp) {
-    if (!c) return FK_EINVAL;
+namespace {
+fk_status gpp_call(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsmtemp, const fk_c128* aqsntemp,
+                   const fk_c128* I_eps_array, const fk_c128* wtilde_array, const double* vcoul,
+                   const int* inv_igp_index, const int* indinv, const double* wx_array, fk_precision precision,
+                   unsigned flags, fk_c128* achtemp, fk_c128* asxtemp, fk_c128* acht_n1_loc, fk_c128* achstemp) {
     Ctx& x = *c;
     x.h2d_bytes = x.d2h_bytes = 0;
     if (nb <= 0 || nc <= 0 || ng <= 0 || nv < 0 || nv > nb)
@@ -677,8 +678,8 @@ fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsm
     fk::Ctx::GraphEntry* ge = nullptr;
     if (all_dev) {
         uint64_t w[24] = {(uint64_t)nb, (uint64_t)nv, (uint64_t)nc, (uint64_t)ng, (uint64_t)precision, flags,
-                          (uint64_t)(uintptr_t)x.stream, (uint64_t)(uintptr_t)x.ws.base};
-        int n = 8;
+                          (uint64_t)(uintptr_t)x.stream, (uint64_t)(uintptr_t)x.ws.base, (uint64_t)x.est_on};
+        int n = 9;
         for (auto* i : ins) w[n++] = (uint64_t)(uintptr_t)i->user;
         for (auto* o : outs) w[n++] = (uint64_t)(uintptr_t)o;
         key = fk::fnv(w, n);
@@ -741,6 +742,56 @@ fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsm
         s = enqueue();
     }
     return s;
+}
+}  // namespace
+
+fk_status fk_gpp(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aqsmtemp, const fk_c128* aqsntemp,
+                 const fk_c128* I_eps_array, const fk_c128* wtilde_array, const double* vcoul,
+                 const int* inv_igp_index, const int* indinv, const double* wx_array, fk_precision precision,
+                 unsigned flags, fk_c128* achtemp, fk_c128* asxtemp, fk_c128* acht_n1_loc, fk_c128* achstemp) {
+    if (!c) return FK_EINVAL;
+    c->est_valid = false;
+    const fk_status s = gpp_call(c, nb, nv, nc, ng, aqsmtemp, aqsntemp, I_eps_array, wtilde_array, vcoul,
+                                 inv_igp_index, indinv, wx_array, precision, flags, achtemp, asxtemp, acht_n1_loc,
+                                 achstemp);
+    // the mixed sums other than the half sum carry the estimate (fk_gpp_error_estimate)
+    c->est_valid = s == FK_OK && c->est_on && c->est_dev && precision == FK_MIXED && !(flags & FK_GPP_HALF_SUM);
+    return s;
+}
+
+fk_status fk_set_error_estimate(fk_ctx_t c, int enable) {
+    if (!c) return FK_EINVAL;
+    c->est_valid = false;
+    if (enable && !c->est_dev) {
+        fk::DeviceGuard g(c->device);
+        if (!g.ok) return fk::fail(*c, FK_ECUDA, "set_error_estimate: cannot select device");
+        if (cudaMalloc(&c->est_dev, 4 * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            c->est_dev = nullptr;
+            return fk::fail(*c, FK_ENOMEM, "set_error_estimate: cannot allocate the estimate's result");
+        }
+    }
+    c->est_on = enable != 0;
+    return FK_OK;
+}
+
+fk_status fk_gpp_error_estimate(fk_ctx_t c, double* max_err_est) {
+    if (!c) return FK_EINVAL;
+    if (!max_err_est) return fk::fail(*c, FK_EINVAL, "gpp_error_estimate: null max_err_est");
+    if (!c->est_valid)
+        return fk::fail(*c, FK_ENOTSUP, "gpp_error_estimate: the last fk_gpp call on this context was not a "
+                                        "mixed-precision call made with fk_set_error_estimate(ctx, 1) (the half "
+                                        "sum has no estimate)");
+    fk::DeviceGuard g(c->device);
+    if (!g.ok) return fk::fail(*c, FK_ECUDA, "gpp_error_estimate: cannot select device");
+    double h[3];
+    cudaError_t e = cudaMemcpyAsync(h, c->est_dev, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return fk::cuda_fail(*c, e, "gpp_error_estimate");
+    fk_status st = fk::check_errword(*c);
+    if (st != FK_OK) return st;
+    for (int i = 0; i < 3; ++i) max_err_est[i] = h[i];
+    return FK_OK;
 }
 
 fk_status fk_gpp_real(fk_ctx_t c, int nb, int nv, int nc, int ng, const double* aqsmtemp, const double* aqsntemp,

@@ -42,6 +42,10 @@ constexpr int NVC = 2;  // flag bands contracted per prep pass
 constexpr double TO1 = 1e-6;
 constexpr float GUARD = 1e-5f;  // relative guard band of the FP32 branch tests
 constexpr int GPP_COLS = 21;    // igp columns per 64-wide tensor-core n-tile (63 used)
+// error estimate of the mixed path: C of C * 2^-24 * sqrt(sum |term|^2), set
+// above the largest ratio |mixed - FP64| / (2^-24 * bound) measured over the
+// GPU tests' inputs with a margin (est_* kernels)
+constexpr double GPP_EST_C = 64.0;
 
 __global__ void igp_map_kernel(int ng, int nc, const int* inv, const int* indinv, int compact, int* igp, int* acol) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -83,6 +87,7 @@ struct PrepArgs {
     int* counter;
     double2* wf;          // [nv][ng][2] flag-band weights (sch: 0.5*vcoul*conj(aqsm), ssx: occ*vcoul*conj(aqsm)), or nullptr
     int asx_neg;          // physics mode: the ssx weight is -occ*vcoul*conj(aqsm) (asxtemp subtracted)
+    float* est;           // error estimate (EST prep): [nch][ng][3][6] magnitudes of the chunk's values
 };
 
 // The set-up work of block (ch, my_igp) other than the image padding.
@@ -596,7 +601,10 @@ __device__ __noinline__ Exact exact_element(double wxt, double2 wt64, double2 ep
 // inputs already loading while the current one is evaluated.
 // Writes D straight into the pre-split BF16 image consumed by the tensor-core
 // contraction (column j = my_igp*3 + iw lives in n-tile j / GPP_COLS).
-template <int Q, int BN>
+// EST: also the magnitudes the error estimate needs, per frequency iw over the
+// block's elements: sum and max of |D|^2 (the image values), |sch|^2 and
+// |ssx|^2 (the flag-band factors), written to p.est[ch][my_igp][iw][6].
+template <int Q, int BN, bool EST = false>
 FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) {
     const int tid = threadIdx.x;
     const int nflag = min(NVC, p.nv - p.n1base);
@@ -618,6 +626,9 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
     float2 acc[NVC * 6];
 #pragma unroll
     for (int i = 0; i < NVC * 6; ++i) acc[i] = make_float2(0.f, 0.f);
+    float es[EST ? 18 : 1];
+#pragma unroll
+    for (int i = 0; i < (EST ? 18 : 1); ++i) es[i] = 0.f;
     // inputs of the next element
     double2 wt_n = make_double2(0.0, 0.0), ep_n = wt_n, an_n[NVC];
     auto load = [&](int ig) {
@@ -714,6 +725,20 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
                 sch = x.sch;
                 ssx = x.ssx;
             }
+            if constexpr (EST) {
+                if (igp >= 0) {
+                    const float d2 = (Q == 1 || A) ? dv.x * dv.x + dv.y * dv.y : 0.f;
+                    const float c2 = sch.x * sch.x + sch.y * sch.y, x2 = ssx.x * ssx.x + ssx.y * ssx.y;
+                    es[iw * 6 + 0] += d2;
+                    es[iw * 6 + 1] = fmaxf(es[iw * 6 + 1], d2);
+                    if (nflag > 0) {
+                        es[iw * 6 + 2] += c2;
+                        es[iw * 6 + 3] = fmaxf(es[iw * 6 + 3], c2);
+                        es[iw * 6 + 4] += x2;
+                        es[iw * 6 + 5] = fmaxf(es[iw * 6 + 5], x2);
+                    }
+                }
+            }
             if (D) {
                 // every element of the image is written (zero where the term is masked)
                 const bool keep = igp >= 0 && (Q == 1 || A);
@@ -748,6 +773,26 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
             for (int k = p.nc + tid; k < kend; k += PREP_THREADS)
                 for (int r = 3 * c; r < (lastcol ? BN : 3 * c + 3); ++r) tcx::bimg_store<BN>(tile, p.kstages, r, k, 0.f, 0.f);
     }
+    if constexpr (EST) {
+        // sums (even q) and maxima (odd q) over the block: warps, then the eight warps in order
+        __shared__ float esm[8][18];
+#pragma unroll
+        for (int q = 0; q < 18; ++q)
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const float o = __shfl_down_sync(0xffffffffu, es[q], off);
+                es[q] = (q & 1) ? fmaxf(es[q], o) : es[q] + o;
+            }
+        if ((tid & 31) == 0)
+#pragma unroll
+            for (int q = 0; q < 18; ++q) esm[tid >> 5][q] = es[q];
+        __syncthreads();
+        if (tid < 18) {
+            float v = 0.f;
+            for (int w = 0; w < PREP_THREADS / 32; ++w) v = (tid & 1) ? fmaxf(v, esm[w][tid]) : v + esm[w][tid];
+            p.est[((long)ch * p.ng + my_igp) * 18 + tid] = v;
+        }
+    }
     if (nflag <= 0) return;
     double2 accd[NVC * 6];
     block_sum_ff<NVC * 6>(acc, sm, accd);
@@ -759,10 +804,126 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
     }
 }
 
-template <int Q, int BN>
+template <int Q, int BN, bool EST = false>
 __global__ void __launch_bounds__(PREP_THREADS, 2) prep_mixed_kernel(PrepArgs p) {
     __shared__ double2 sm[8 * NVC * 6];
-    prep_mixed_item<Q, BN>(p, p.ch0 + blockIdx.x, blockIdx.y, sm);
+    prep_mixed_item<Q, BN, EST>(p, p.ch0 + blockIdx.x, blockIdx.y, sm);
+}
+
+// ------------------------------------------------------------ error estimate
+// A-priori estimate of the mixed path's absolute error (fk_gpp_error_estimate).
+// Each output is a sum of terms w * a * x (w the band-column weight, a an
+// aqsntemp element, x a D / sch / ssx value).  Every term carries a few FP32
+// roundings (operands, the FP32 branch factors, the tensor cores' truncating
+// FP32 accumulation, the FP32 epilogue) of random sign, so the error is about
+// C * 2^-24 * sqrt(sum of |term|^2).  The sum over ig of |a|^2 |x|^2 is bounded
+// by min(|a_n|_2^2 |x_j|_inf^2, |a_n|_inf^2 |x_j|_2^2) for band n and column
+// j = (my_igp, iw), which needs only the row norms below and the prep's column
+// magnitudes; the estimate is therefore at least C * 2^-24 * rss.
+
+// an[n] = (sum_ig |aqsn[n][ig]|^2, max_ig |aqsn[n][ig]|^2), one block per band.
+__global__ void __launch_bounds__(256) est_rows_kernel(int nc, const double2* aqsn, float2* an) {
+    const double2* row = aqsn + (long)blockIdx.x * nc;
+    float s = 0.f, m = 0.f;
+    for (int ig = threadIdx.x; ig < nc; ig += 256) {
+        const float2 a = c64_to_f32(row[ig]);
+        const float a2 = a.x * a.x + a.y * a.y;
+        s += a2;
+        m = fmaxf(m, a2);
+    }
+    __shared__ float sm[8][2];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, off);
+        m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sm[threadIdx.x >> 5][0] = s;
+        sm[threadIdx.x >> 5][1] = m;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < 8; ++w) {
+            s += sm[w][0];
+            m = fmaxf(m, sm[w][1]);
+        }
+        an[blockIdx.x] = make_float2(s, m);
+    }
+}
+
+// Per band n, per iw: the bound of sum |term|^2 of its achtemp terms (bands
+// n >= nvband: D columns; occupied bands: sch) and, occupied bands, of its
+// asxtemp terms (ssx), into eb[n][6].  One block of 128 threads per band, the
+// threads taking columns; the column magnitudes are first reduced over the
+// prep's chunks.
+__global__ void __launch_bounds__(128) est_bands_kernel(int nv, int ng, int nch, const float* est, const float2* an,
+                                                        const double2* aqsm, long ldm, const int* igp,
+                                                        const int* acol, const double* vcoul, double* eb) {
+    const int n = blockIdx.x;
+    const float2 a = an[n];
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    for (int h = threadIdx.x; h < ng; h += 128) {
+        const int g = igp[h];
+        if (g < 0) continue;
+        const double2 am = aqsm[(long)n * ldm + acol[h]];
+        const double w2 = (am.x * am.x + am.y * am.y) * vcoul[g] * vcoul[g];
+#pragma unroll
+        for (int iw = 0; iw < 3; ++iw) {
+            float c[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            for (int ch = 0; ch < nch; ++ch) {
+                const float* e = est + ((long)ch * ng + h) * 18 + iw * 6;
+#pragma unroll
+                for (int q = 0; q < 6; ++q) c[q] = (q & 1) ? fmaxf(c[q], e[q]) : c[q] + e[q];
+            }
+            const int o = n < nv ? 2 : 0;  // occupied bands: sch; the others: the image values
+            const double t = fmin((double)a.x * c[o + 1], (double)a.y * c[o]);
+            v[iw] += 0.25 * w2 * t;  // achtemp weight 0.5 vcoul conj(aqsm)
+            if (n < nv) v[3 + iw] += w2 * fmin((double)a.x * c[5], (double)a.y * c[4]);  // asxtemp: vcoul conj(aqsm)
+        }
+    }
+    __shared__ double sm[4][6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], off);
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) sm[threadIdx.x >> 5][q] = v[q];
+    __syncthreads();
+    if (threadIdx.x < 6) eb[(long)n * 6 + threadIdx.x] = sm[0][threadIdx.x] + sm[1][threadIdx.x] + sm[2][threadIdx.x] + sm[3][threadIdx.x];
+}
+
+// out[0] = achtemp, out[1] = asxtemp (max over iw), out[2] = acht_n1_loc (max
+// over bands; its component is iw = 2): scale * sqrt(bound), bands added in a
+// fixed order.  One block of 256 threads.
+__global__ void __launch_bounds__(256) est_total_kernel(int nb, const double* eb, double scale, double* out) {
+    double v[6] = {0, 0, 0, 0, 0, 0}, mx = 0.0;
+    for (int n = threadIdx.x; n < nb; n += 256) {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) v[q] += eb[(long)n * 6 + q];
+        mx = fmax(mx, eb[(long)n * 6 + 2]);
+    }
+    __shared__ double sm[8][7];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) v[q] += __shfl_down_sync(0xffffffffu, v[q], off);
+        mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) sm[threadIdx.x >> 5][q] = v[q];
+        sm[threadIdx.x >> 5][6] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t[7] = {0, 0, 0, 0, 0, 0, 0};
+        for (int w = 0; w < 8; ++w)
+            for (int q = 0; q < 7; ++q) t[q] = q == 6 ? fmax(t[q], sm[w][q]) : t[q] + sm[w][q];
+        out[0] = scale * sqrt(fmax(fmax(t[0], t[1]), t[2]));
+        out[1] = scale * sqrt(fmax(fmax(t[3], t[4]), t[5]));
+        out[2] = scale * sqrt(t[6]);
+    }
 }
 
 // ------------------------------------------------------------------ finalize
@@ -1613,8 +1774,13 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
     float2* W = p.bytesW ? (float2*)c.ws.take(p.bytesW) : nullptr;
     int* counter = (int*)c.ws.take(sizeof(int));
     double2* wf = r.nv > 0 ? (double2*)c.ws.take((size_t)r.nv * r.ng * 2 * sizeof(double2)) : nullptr;
+    // error estimate: the prep's column magnitudes, the bands' row norms and bounds
+    const bool est = c.est_on && p.mixed && c.est_dev;
+    float* estE = est ? (float*)c.ws.take((size_t)p.nch * r.ng * 18 * sizeof(float)) : nullptr;
+    float2* estA = est ? (float2*)c.ws.take((size_t)r.nb * sizeof(float2)) : nullptr;
+    double* estB = est ? (double*)c.ws.take((size_t)r.nb * 6 * sizeof(double)) : nullptr;
     if (!igp || !F || !rows || !counter || (p.bytesD && !D) || (p.bytesP && !P) || (p.bytesS && !S) ||
-        (p.bytesW && !W) || (r.nv > 0 && !wf))
+        (p.bytesW && !W) || (r.nv > 0 && !wf) || (est && (!estE || !estA || !estB)))
         return fail(c, FK_ENOMEM, "workspace too small for GPP request");
     if (p.mixed && D) {
         cudaError_t e = cudaMemsetAsync(c.errword, 0, sizeof(int), st);  // bounded-wait status
@@ -1640,11 +1806,16 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
             a.counter = counter;
             a.wf = wf;
             a.asx_neg = Q == 2;
+            a.est = estE;
         }
         return a;
     };
     auto launch_prep = [&](const PrepArgs& a, dim3 grid) {
-        if (p.mixed) {
+        if (p.mixed && a.est) {
+            if (Q == 1) prep_mixed_kernel<1, 64, true><<<grid, PREP_THREADS, 0, st>>>(a);
+            else if (Q == 2) prep_mixed_kernel<2, 64, true><<<grid, PREP_THREADS, 0, st>>>(a);
+            else prep_mixed_kernel<0, 64, true><<<grid, PREP_THREADS, 0, st>>>(a);
+        } else if (p.mixed) {
             if (Q == 1) prep_mixed_kernel<1, 64><<<grid, PREP_THREADS, 0, st>>>(a);
             else if (Q == 2) prep_mixed_kernel<2, 64><<<grid, PREP_THREADS, 0, st>>>(a);
             else prep_mixed_kernel<0, 64><<<grid, PREP_THREADS, 0, st>>>(a);
@@ -1767,6 +1938,13 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
     ra.wf = wf;
     rows_kernel<<<rows_blocks(r.nb, r.nv), ROWS_THREADS, 0, st>>>(ra);
     ++c.launches;
+    if (est) {
+        // every row block of a pipelined call has landed: the contractions waited for them
+        est_rows_kernel<<<r.nb, 256, 0, st>>>(r.nc, r.aqsn, estA);
+        est_bands_kernel<<<r.nb, 128, 0, st>>>(r.nv, r.ng, p.nch, estE, estA, r.aqsm, r.ldm, igp, acol, r.vcoul, estB);
+        est_total_kernel<<<1, 256, 0, st>>>(r.nb, estB, GPP_EST_C * 0x1p-24, c.est_dev);
+        c.launches += 3;
+    }
     phase_mark(c, 4);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "gpp kernels");

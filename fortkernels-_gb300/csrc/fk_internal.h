@@ -48,6 +48,11 @@ struct Ctx {
     unsigned long long h2d_bytes = 0, d2h_bytes = 0;
     int* errword = nullptr;      // device error word of the tensor-core kernels (bounded waits)
     long long wait_limit = 4000000000LL;  // bound of their waits between roles, SM clock cycles (~2 s)
+    // a-priori error estimate of mixed fk_gpp calls (fk_set_error_estimate): on/off,
+    // its device result [3], and whether the last fk_gpp call on the context made one
+    bool est_on = false;
+    double* est_dev = nullptr;
+    bool est_valid = false;
     // Graphs of repeated fully device-resident calls: key -> (times seen, executable graph).
     struct GraphEntry {
         int seen = 0;

@@ -168,6 +168,16 @@ __device__ __forceinline__ void mbar_arrive_remote(uint64_t* bar, uint32_t rank)
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(smem_u32(bar)), "r"(rank));
     asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(a) : "memory");
 }
+// Arrive on the barrier at the same offset in CTA `rank` of the cluster with
+// the default semantics (release at CTA scope): it orders only this thread's
+// own earlier operations, without the cluster-wide fence of
+// mbar_arrive_remote.  Enough where the arrive reports work that has already
+// completed in the registers (a TMEM buffer whose loads were waited for).
+__device__ __forceinline__ void mbar_arrive_peer(uint64_t* bar, uint32_t rank) {
+    uint32_t a;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(smem_u32(bar)), "r"(rank));
+    asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(a) : "memory");
+}
 // Bounded wait with cluster-scope acquire, for barriers the peer CTA arrives on.
 __device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* bar, uint32_t parity) {
     uint32_t ok;

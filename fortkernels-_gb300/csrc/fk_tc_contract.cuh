@@ -586,35 +586,65 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             ff32 accx[GMAX] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, accy[GMAX] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
             const int CH = t.chunk_stages > 0 ? t.chunk_stages : 1;
             const bool rs = !t.ff_no_rs;
-            for (int st0 = 0; st0 < nst; st0 += CH, ++chunk) {
-                const int b = chunk % C::NBUF;
-                if (!tc::warp_all(tc::mbar_wait(&accFull[b], (chunk / C::NBUF) & 1, wait_limit) && !s_abort)) {
+            // SL (FF on CTA pairs): a pass drains two accumulator buffers (consecutive
+            // chunks) and adds them in registers, one round-to-nearest FP32 addition,
+            // before the weighted sums: half the arithmetic, waits and returns per chunk
+            constexpr int PASS = (EPI == EPI_FF && C::SL) ? 2 : 1;
+            for (int st0 = 0; st0 < nst;) {
+                const int npass = (PASS == 2 && st0 + CH < nst) ? 2 : 1;
+                const int b = chunk % C::NBUF, b2 = (chunk + 1) % C::NBUF;
+                bool full = tc::mbar_wait(&accFull[b], (chunk / C::NBUF) & 1, wait_limit);
+                if (npass == 2) full = full && tc::mbar_wait(&accFull[b2], ((chunk + 1) / C::NBUF) & 1, wait_limit);
+                if (!tc::warp_all(full && !s_abort)) {
                     fail(16);
                     ok = false;
                     break;
                 }
+                st0 += npass * CH;
+                chunk += npass;
                 tc::tc_fence_after();
                 const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * C::ACC_COLS);
+                const uint32_t tl2 = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b2 * C::ACC_COLS);
                 float2 gsum[GMAX] = {make_float2(0, 0), make_float2(0, 0), make_float2(0, 0)};
-                // the buffer goes back to the MMA issuer as soon as this warp's last
-                // TMEM load of it has landed, before the arithmetic on those values
+                // the pass's buffers go back to the MMA issuer as soon as this warp's
+                // last TMEM load of them has landed, before the arithmetic on those values
                 auto release = [&]() {
                     tc::tc_fence_before();
                     __syncwarp();
-                    if (lane == 0) {
-                        if (PAIR && rank == 1) tc::mbar_arrive_remote(&accEmpty[b], 0);  // the MMA issuer's barrier
-                        else tc::mbar_arrive(&accEmpty[b]);
-                    }
+                    if (lane == 0)
+                        for (int i = 0; i < npass; ++i) {
+                            // the MMA issuer's barrier; the loads of the buffer have completed, so
+                            // no cluster-wide release is needed (it cost ~2000 cycles per drain)
+                            uint64_t* bar = &accEmpty[i ? b2 : b];
+                            if (PAIR && rank == 1) tc::mbar_arrive_peer(bar, 0);
+                            else tc::mbar_arrive(bar);
+                        }
                 };
                 if (EPI == EPI_FF && C::SL) {
-                    // the warp's 16 columns of D = [S_re | S_im]: both loads, then the buffer
-                    // goes back, then the weighted sums
+                    // the warp's 16 columns of D = [S_re | S_im] of each buffer (the real
+                    // parts of both, added, then the imaginary parts: 48 registers of
+                    // values live instead of 64), the buffers go back, then the weighted sums
                     const int c0 = ej * 16;
                     float sr[16], si[16];
-                    tc::tmem_ld16(tl + c0, sr);
-                    tc::tmem_ld16(tl + BN + c0, si);
-                    tc::tmem_ld_wait();
-                    release();
+                    if (npass == 2) {
+                        float tx[16];
+                        tc::tmem_ld16(tl + c0, sr);
+                        tc::tmem_ld16(tl2 + c0, tx);
+                        tc::tmem_ld_wait();
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) sr[j] += tx[j];
+                        tc::tmem_ld16(tl + BN + c0, si);
+                        tc::tmem_ld16(tl2 + BN + c0, tx);
+                        tc::tmem_ld_wait();
+                        release();
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) si[j] += tx[j];
+                    } else {
+                        tc::tmem_ld16(tl + c0, sr);
+                        tc::tmem_ld16(tl + BN + c0, si);
+                        tc::tmem_ld_wait();
+                        release();
+                    }
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         const float2 t2 = cmulf(wreg[j], make_float2(sr[j], si[j]));

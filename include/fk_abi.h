@@ -133,6 +133,28 @@ fk_status fk_gpp(fk_ctx_t ctx, int number_bands, int nvband, int ncouls, int ngp
                  fk_c128* achtemp, fk_c128* asxtemp, fk_c128* acht_n1_loc, fk_c128* achstemp);
 
 /*
+ * A-priori error estimate of the mixed path (no counterpart in the reference,
+ * whose sums are FP64).  fk_set_error_estimate(ctx, 1) makes every later
+ * mixed-precision fk_gpp call on ctx (not the half sum) also compute, on the
+ * device, an estimate of the absolute error of its outputs against exact
+ * arithmetic; the cost is one more pass over aqsntemp and a few small
+ * kernels (off by default).  fk_gpp_error_estimate then returns, for the last
+ * fk_gpp call on ctx, max_err_est[0] for achtemp (the largest over the three
+ * frequencies), [1] for asxtemp and [2] for acht_n1_loc (the largest over the
+ * bands).  The model: every term w*a*x of a sum (w the band-column weight, a
+ * an aqsntemp element, x the branch factor) carries a few FP32 roundings of
+ * random sign, so the error is about C * 2^-24 * sqrt(sum |w a x|^2); the sum
+ * of squares is bounded from the row norms of aqsntemp and the column norms
+ * of the branch factors (so the estimate is at least the model's value), and
+ * C = 64 lies above every ratio measured in the tests.  achstemp
+ * (FK_GPP_ACHSTEMP) is not covered.  FK_ENOTSUP when the last fk_gpp call on
+ * ctx failed, was FP64 or the half sum, or ran with the estimate off.
+ * fk_gpp_error_estimate waits for the context's stream.
+ */
+fk_status fk_set_error_estimate(fk_ctx_t ctx, int enable);
+fk_status fk_gpp_error_estimate(fk_ctx_t ctx, double* max_err_est /* [3] */);
+
+/*
  * Real-valued GPP sum (gppKer_real.cpp:297-412): the same loop nest on double
  * arrays, aqsmtemp/aqsntemp [number_bands][ncouls], I_eps_array/wtilde_array
  * [ngpown][ncouls], with the index map and frequencies of fk_gpp.  As in the
