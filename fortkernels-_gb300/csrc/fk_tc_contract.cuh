@@ -86,6 +86,11 @@ struct Cfg {
     static constexpr uint32_t B_SMEM = (PAIR ? (SL ? 2 : 1) : 2) * NSPLIT * BN * 64;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_SMEM;
     static constexpr int NBUF = SL ? 4 : 2;
+    // SL: the accumulator buffers are handed over in groups of two (consecutive
+    // chunks), one full and one empty barrier per group: the MMA issuer waits,
+    // fences and commits once per group, the epilogue drains a group in one pass
+    static constexpr int GRP = SL ? 2 : 1;
+    static constexpr int NSLOT = NBUF / GRP;
     static constexpr uint32_t ACC_COLS = SL ? 2 * BN : 4 * BN;
     static constexpr uint32_t TMEM_COLS = NBUF * ACC_COLS;
     static constexpr uint32_t W_BYTES = 0u;
@@ -340,7 +345,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                 for (int st = 0; st < nst; ++st, ++g) {
                     const int s = g % C::STAGES;
                     const uint32_t par = (g / C::STAGES) & 1;
-                    if (!tc::mbar_wait(&fullA[s], par, wait_limit) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
+                    if ((!AIMG && !tc::mbar_wait(&fullA[s], par, wait_limit)) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
                         s_abort) {
                         fail(2);
                         ok = false;
@@ -351,7 +356,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             }
         } else if (lane == 0 && (!PAIR || rank == 0)) {
             // ------------------------------------------------------------ MMA
-            int g = 0, chunk = 0;
+            int g = 0, grp = 0;
             bool ok = true;
             const uint32_t idp = tc::idesc_bf16(PAIR ? 2 * BM : BM, 2 * BN, false);
             for (int u = pid; u < src.units() && ok; u += npairs) {
@@ -362,71 +367,77 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                 krange(t, ks, k0, k1);
                 const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
                 const int CH = t.chunk_stages > 0 ? t.chunk_stages : 1;
-                for (int st0 = 0; st0 < nst && ok; st0 += CH, ++chunk) {
-                    const int b = chunk % C::NBUF;
-                    const uint32_t bpar = ((chunk / C::NBUF) & 1) ^ 1;
-                    const bool freed = PAIR ? tc::mbar_wait_cluster(&accEmpty[b], bpar, wait_limit)
-                                            : tc::mbar_wait(&accEmpty[b], bpar, wait_limit);
+                for (int sg0 = 0; sg0 < nst && ok; sg0 += C::GRP * CH, ++grp) {
+                    // a group: up to GRP chunks of CH stages, each into its own buffer of the slot
+                    const int slot = grp % C::NSLOT;
+                    const uint32_t bpar = ((grp / C::NSLOT) & 1) ^ 1;
+                    const bool freed = PAIR ? tc::mbar_wait_cluster(&accEmpty[slot], bpar, wait_limit)
+                                            : tc::mbar_wait(&accEmpty[slot], bpar, wait_limit);
                     if (!freed) { fail(1); ok = false; break; }
                     tc::tc_fence_after();
-                    // X, Y (two accumulators) or, SL, the one accumulator D = dX
-                    const uint32_t dX = tmem + (uint32_t)(b * C::ACC_COLS), dY = dX + 2 * BN;
-                    const int st1 = min(nst, st0 + CH);
-                    for (int st = st0; st < st1; ++st, ++g) {
-                        const int s = g % C::STAGES;
-                        const uint32_t par = (g / C::STAGES) & 1;
-                        if (!tc::mbar_wait(&fullA[s], par, wait_limit) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
-                            (PAIR && !tc::mbar_wait_cluster(&peerFull[s], par, wait_limit))) {
-                            fail(2);
-                            ok = false;
-                            break;
-                        }
-                        tc::tc_fence_after();
-                        // the descriptor's start-address field is address / 16 in its low 14 bits and
-                        // shared addresses stay below 2^18, so every operand's descriptor is the stage's
-                        // base descriptor plus a constant: one add per MMA for the single issuing thread
-                        const uint64_t dA = tc::sdesc_sw64(tc::smem_u32(base + s * C::STAGE_BYTES));
-                        const uint64_t dB = dA + (C::A_BYTES >> 4);
-                        // A sub-tile (re h,m,l, im h,m,l) and B piece, k offset kk*16.  A CTA's B
-                        // piece is 2*BN rows ([B_re; B_im], or SL [B_re; -B_im] / [B_im; B_re]),
-                        // or BN rows (pair without SL: its half [B_re] or [B_im])
-                        auto ad = [&](int sub, int kk) { return dA + (uint64_t)((sub * BM * 64) >> 4) + 2 * kk; };
-                        auto bd = [&](int piece, int kk) {
-                            return dB + (uint64_t)((piece * ((PAIR && !C::SL) ? 1 : 2) * BN * 64) >> 4) + 2 * kk;
-                        };
-                        constexpr uint64_t B_HALF = (uint64_t)(BN * 64) >> 4;  // SL: the piece's second BN rows
-                        auto mma2 = [&](int pa, int pb, int kk, uint32_t accumulate) {
-                            // X += A_re,pa x [B_re|B_im]_pb, Y += A_im,pa x [B_re|B_im]_pb; SL:
-                            // D += A_re,pa x [B_re|B_im]_pb + A_im,pa x [-B_im|B_re]_pb
-                            if constexpr (C::SL) {
-                                tc::mma_bf16_pair(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
-                                tc::mma_bf16_pair(dX, ad(3 + pa, kk), bd(pb, kk) + B_HALF, idp, 1u);
-                            } else if constexpr (PAIR) {
-                                tc::mma_bf16_pair(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
-                                tc::mma_bf16_pair(dY, ad(3 + pa, kk), bd(pb, kk), idp, accumulate);
-                            } else {
-                                tc::mma_bf16(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
-                                tc::mma_bf16(dY, ad(3 + pa, kk), bd(pb, kk), idp, accumulate);
+                    const int sg1 = min(nst, sg0 + C::GRP * CH);
+                    for (int st0 = sg0, b = slot * C::GRP; st0 < sg1 && ok; st0 += CH, ++b) {
+                        // X, Y (two accumulators) or, SL, the one accumulator D = dX
+                        const uint32_t dX = tmem + (uint32_t)(b * C::ACC_COLS), dY = dX + 2 * BN;
+                        const int st1 = min(nst, st0 + CH);
+                        for (int st = st0; st < st1; ++st, ++g) {
+                            const int s = g % C::STAGES;
+                            const uint32_t par = (g / C::STAGES) & 1;
+                            // AIMG: the A image lands on fullB too (one barrier per stage)
+                            if ((!AIMG && !tc::mbar_wait(&fullA[s], par, wait_limit)) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
+                                (PAIR && !tc::mbar_wait_cluster(&peerFull[s], par, wait_limit))) {
+                                fail(2);
+                                ok = false;
+                                break;
                             }
-                        };
-                        // The accumulators truncate each addition to FP32 at the magnitude they
-                        // hold, so the five small piece products (mm, lh, hl, mh, hm; 2^-8 and
-                        // below of the sum) of both k-steps go in first, while the accumulator is
-                        // small, and the two hh products last: two full-scale roundings per stage.
-                        const int PA[5] = {1, 2, 0, 1, 0};
-                        const int PB[5] = {1, 0, 2, 0, 1};
-#pragma unroll
-                        for (int kk = 0; kk < 2; ++kk)
-#pragma unroll
-                            for (int q = 0; q < 5; ++q) mma2(PA[q], PB[q], kk, (st > st0 || kk > 0 || q > 0) ? 1u : 0u);
-                        mma2(0, 0, 0, 1u);
-                        mma2(0, 0, 1, 1u);
-                        if constexpr (PAIR) tc::mma_commit_pair(&empty[s], 3);  // frees the stage in both CTAs
-                        else tc::mma_commit(&empty[s]);
+                            tc::tc_fence_after();
+                            // the descriptor's start-address field is address / 16 in its low 14 bits and
+                            // shared addresses stay below 2^18, so every operand's descriptor is the stage's
+                            // base descriptor plus a constant: one add per MMA for the single issuing thread
+                            const uint64_t dA = tc::sdesc_sw64(tc::smem_u32(base + s * C::STAGE_BYTES));
+                            const uint64_t dB = dA + (C::A_BYTES >> 4);
+                            // A sub-tile (re h,m,l, im h,m,l) and B piece, k offset kk*16.  A CTA's B
+                            // piece is 2*BN rows ([B_re; B_im], or SL [B_re; -B_im] / [B_im; B_re]),
+                            // or BN rows (pair without SL: its half [B_re] or [B_im])
+                            auto ad = [&](int sub, int kk) { return dA + (uint64_t)((sub * BM * 64) >> 4) + 2 * kk; };
+                            auto bd = [&](int piece, int kk) {
+                                return dB + (uint64_t)((piece * ((PAIR && !C::SL) ? 1 : 2) * BN * 64) >> 4) + 2 * kk;
+                            };
+                            constexpr uint64_t B_HALF = (uint64_t)(BN * 64) >> 4;  // SL: the piece's second BN rows
+                            auto mma2 = [&](int pa, int pb, int kk, uint32_t accumulate) {
+                                // X += A_re,pa x [B_re|B_im]_pb, Y += A_im,pa x [B_re|B_im]_pb; SL:
+                                // D += A_re,pa x [B_re|B_im]_pb + A_im,pa x [-B_im|B_re]_pb
+                                if constexpr (C::SL) {
+                                    tc::mma_bf16_pair(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
+                                    tc::mma_bf16_pair(dX, ad(3 + pa, kk), bd(pb, kk) + B_HALF, idp, 1u);
+                                } else if constexpr (PAIR) {
+                                    tc::mma_bf16_pair(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
+                                    tc::mma_bf16_pair(dY, ad(3 + pa, kk), bd(pb, kk), idp, accumulate);
+                                } else {
+                                    tc::mma_bf16(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
+                                    tc::mma_bf16(dY, ad(3 + pa, kk), bd(pb, kk), idp, accumulate);
+                                }
+                            };
+                            // The accumulators truncate each addition to FP32 at the magnitude they
+                            // hold, so the five small piece products (mm, lh, hl, mh, hm; 2^-8 and
+                            // below of the sum) of both k-steps go in first, while the accumulator is
+                            // small, and the two hh products last: two full-scale roundings per stage.
+                            const int PA[5] = {1, 2, 0, 1, 0};
+                            const int PB[5] = {1, 0, 2, 0, 1};
+    #pragma unroll
+                            for (int kk = 0; kk < 2; ++kk)
+    #pragma unroll
+                                for (int q = 0; q < 5; ++q) mma2(PA[q], PB[q], kk, (st > st0 || kk > 0 || q > 0) ? 1u : 0u);
+                            mma2(0, 0, 0, 1u);
+                            mma2(0, 0, 1, 1u);
+                            if constexpr (PAIR) tc::mma_commit_pair(&empty[s], 3);  // frees the stage in both CTAs
+                            else tc::mma_commit(&empty[s]);
+                        }
                     }
                     if (!ok) break;
-                    if constexpr (PAIR) tc::mma_commit_pair(&accFull[b], 3);  // both CTAs' epilogues
-                    else tc::mma_commit(&accFull[b]);
+                    // one commit tracks every earlier MMA of this thread: the whole group
+                    if constexpr (PAIR) tc::mma_commit_pair(&accFull[slot], 3);  // both CTAs' epilogues
+                    else tc::mma_commit(&accFull[slot]);
                 }
             }
             // drain: every issued MMA has completed before TMEM is released
@@ -487,7 +498,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                     } else {
                         const uint8_t* src =
                             t.Bimg + (((long)plane * t.NT + nt) * t.kstages_total + kst) * (long)C::B_BYTES;
-                        tc::mbar_arrive_expect_tx(&fullB[s], C::B_SMEM);
+                        tc::mbar_arrive_expect_tx(&fullB[s], C::B_SMEM + (AIMG ? C::A_BYTES : 0u));
                         uint8_t* bdst = base + s * C::STAGE_BYTES + C::A_BYTES;
                         if constexpr (C::SL) {
                             // image -im, re, im per piece: the even CTA takes [re; -im], the odd [im; re]
@@ -512,8 +523,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         }
                         if (AIMG) {
                             const uint8_t* asrc = t.Aimg + ((long)mt * t.kstages_total + kst) * (long)C::A_BYTES;
-                            tc::mbar_arrive_expect_tx(&fullA[s], C::A_BYTES);
-                            tc::bulk_g2s(base + s * C::STAGE_BYTES, asrc, C::A_BYTES, &fullA[s]);
+                            tc::bulk_g2s(base + s * C::STAGE_BYTES, asrc, C::A_BYTES, &fullB[s]);
                         }
                         last_st[s] = g;
                     }
@@ -532,8 +542,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             for (int s = 0; s < C::STAGES; ++s)
                 if (last_st[s] >= 0) {
                     const uint32_t par = (uint32_t)(last_st[s] / C::STAGES) & 1u;
-                    drained = tc::mbar_wait(&fullB[s], par, DRAIN_LIMIT) && drained;
-                    if (AIMG) drained = tc::mbar_wait(&fullA[s], par, DRAIN_LIMIT) && drained;
+                    drained = tc::mbar_wait(&fullB[s], par, DRAIN_LIMIT) && drained;  // AIMG: the A image too
                 }
             if (!AIMG)
                 for (int h = 0; h < 2; ++h)
@@ -551,7 +560,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
         const int q4 = warp & 3;                     // TMEM lane quarter
         const int ej = AIMG ? (warp - 2) >> 2 : 0;   // FF: this warp's 16-column group
         const int row = q4 * 32 + lane;
-        int chunk = 0;
+        int grp = 0;
         bool ok = true;
         constexpr int GC = BN / 3;  // 21 igp per GPP tile
         for (int u = pid; u < src.units() && ok; u += npairs) {
@@ -586,22 +595,19 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             ff32 accx[GMAX] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, accy[GMAX] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
             const int CH = t.chunk_stages > 0 ? t.chunk_stages : 1;
             const bool rs = !t.ff_no_rs;
-            // SL (FF on CTA pairs): a pass drains two accumulator buffers (consecutive
-            // chunks) and adds them in registers, one round-to-nearest FP32 addition,
-            // before the weighted sums: half the arithmetic, waits and returns per chunk
-            constexpr int PASS = (EPI == EPI_FF && C::SL) ? 2 : 1;
-            for (int st0 = 0; st0 < nst;) {
-                const int npass = (PASS == 2 && st0 + CH < nst) ? 2 : 1;
-                const int b = chunk % C::NBUF, b2 = (chunk + 1) % C::NBUF;
-                bool full = tc::mbar_wait(&accFull[b], (chunk / C::NBUF) & 1, wait_limit);
-                if (npass == 2) full = full && tc::mbar_wait(&accFull[b2], ((chunk + 1) / C::NBUF) & 1, wait_limit);
-                if (!tc::warp_all(full && !s_abort)) {
+            // a pass drains one group of accumulator buffers (SL: two consecutive chunks,
+            // added in registers with one round-to-nearest FP32 addition before the
+            // weighted sums: half the arithmetic, waits and returns per chunk)
+            for (int st0 = 0; st0 < nst; ++grp) {
+                const int npass = min(C::GRP, (nst - st0 + CH - 1) / CH);  // chunks in the group
+                const int slot = grp % C::NSLOT;
+                const int b = slot * C::GRP, b2 = b + 1;
+                if (!tc::warp_all(tc::mbar_wait(&accFull[slot], (grp / C::NSLOT) & 1, wait_limit) && !s_abort)) {
                     fail(16);
                     ok = false;
                     break;
                 }
                 st0 += npass * CH;
-                chunk += npass;
                 tc::tc_fence_after();
                 const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * C::ACC_COLS);
                 const uint32_t tl2 = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b2 * C::ACC_COLS);
@@ -611,14 +617,12 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                 auto release = [&]() {
                     tc::tc_fence_before();
                     __syncwarp();
-                    if (lane == 0)
-                        for (int i = 0; i < npass; ++i) {
-                            // the MMA issuer's barrier; the loads of the buffer have completed, so
-                            // no cluster-wide release is needed (it cost ~2000 cycles per drain)
-                            uint64_t* bar = &accEmpty[i ? b2 : b];
-                            if (PAIR && rank == 1) tc::mbar_arrive_peer(bar, 0);
-                            else tc::mbar_arrive(bar);
-                        }
+                    if (lane == 0) {
+                        // the MMA issuer's barrier; the loads of the group have completed, so
+                        // no cluster-wide release is needed (it cost ~2000 cycles per drain)
+                        if (PAIR && rank == 1) tc::mbar_arrive_peer(&accEmpty[slot], 0);
+                        else tc::mbar_arrive(&accEmpty[slot]);
+                    }
                 };
                 if (EPI == EPI_FF && C::SL) {
                     // the warp's 16 columns of D = [S_re | S_im] of each buffer (the real
