@@ -292,6 +292,7 @@ struct FfPlan {
     int KSa = 0, kchunka = 0;
     bool mixed;
     size_t bytes, bytesImgR, bytesImgA, bytesW, bytesAimg;
+    size_t bytesScale;  // mixed: 2^-k of every A image row and of every row of the converted planes
 };
 
 // k-slices for the persistent tensor-core kernel (see fk_gpp.cu)
@@ -374,7 +375,7 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
         for (int s : szA) gmax = std::max(gmax, s);
     }
     const int nplanes = gmax;
-    p.bytesImgR = p.bytesImgA = p.bytesW = p.bytesAimg = 0;
+    p.bytesImgR = p.bytesImgA = p.bytesW = p.bytesAimg = p.bytesScale = 0;
     if (p.mixed) {
         // the contraction runs on CTA pairs: units of 256 bands (p.MT counts them),
         // over an A image of an even number of 128-row tiles
@@ -387,7 +388,8 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
         p.bytesImgR = p.planesR.size() * (size_t)p.NT * p.kstages * bb;
         p.bytesImgA = p.planesA.size() * (size_t)p.NT * p.kstages * bb;
         p.bytesW = 2 * (size_t)r.nb * r.ng * sizeof(float2) + (size_t)r.ng * sizeof(float) + 256;
-        p.bytesAimg = (size_t)2 * p.MT * p.kstages * tcx::Cfg<64>::A_BYTES;
+        p.bytesAimg = (size_t)2 * p.MT * p.kstages * tcx::Cfg<64, true>::A_BYTES;
+        p.bytesScale = ((size_t)r.nb + (p.planesR.size() + p.planesA.size()) * (size_t)r.ng) * sizeof(float);
     } else {
         p.BN = d64::BN;
         p.kstages = 0;
@@ -433,7 +435,7 @@ FfPlan make_plan(const Ctx& c, const FfDev& r, const double* ekq_h, const double
               (p.mixed ? (size_t)r.nb * r.nf * sizeof(float4) + r.nf * sizeof(float2) : 0) + 4 * 256 +
               r.nb * sizeof(FactRow) + (p.planesR.size() + p.planesA.size()) * sizeof(int) + r.ng * sizeof(int) +
               r.nb * sizeof(int) +
-              p.bytesImgR + p.bytesImgA + p.bytesW + p.bytesAimg + 20 * 256;
+              p.bytesImgR + p.bytesImgA + p.bytesW + p.bytesAimg + p.bytesScale + 20 * 256;
     return p;
 }
 
@@ -484,8 +486,12 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
     uint8_t* imgA = p.bytesImgA ? (uint8_t*)c.ws.take(p.bytesImgA) : nullptr;
     float2* W = p.bytesW ? (float2*)c.ws.take(p.bytesW) : nullptr;
     uint8_t* Aimg = p.bytesAimg ? (uint8_t*)c.ws.take(p.bytesAimg) : nullptr;
+    float* scales = p.bytesScale ? (float*)c.ws.take(p.bytesScale) : nullptr;
+    float* ascale = scales;                                              // [nb], image row order
+    float* bscaleR = scales ? scales + r.nb : nullptr;                   // [nR][ng]
+    float* bscaleA = scales ? bscaleR + (size_t)nR * r.ng : nullptr;     // [nA][ng]
     if (!igp || (p.mixed && !order) || !planes || !fact || !PR || (nA && !PA) || !tabs || !SD || (p.bytesImgR && !imgR) ||
-        (p.bytesImgA && !imgA) || (p.bytesW && !W) || (p.bytesAimg && !Aimg))
+        (p.bytesImgA && !imgA) || (p.bytesW && !W) || (p.bytesAimg && !Aimg) || (p.bytesScale && !scales))
         return fail(c, FK_ENOMEM, "workspace too small for FF request");
     double2 *RW = tabs, *RS = tabs + (size_t)r.nb * r.nf, *AW = tabs + 2 * (size_t)r.nb * r.nf;
     // host tables -> device (pageable source; the copy completes before return of the call's sync)
@@ -535,21 +541,20 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
         tcx::weight_table_kernel<<<dim3(ceil_div(r.nb, 128), r.ng), 128, 0, st>>>(r.nb, 0, r.ng, r.aqsm, r.nc, r.vcoul,
                                                                                 igp, igp, 1.0, W, W + (size_t)r.nb * r.ng,
                                                                                 (float*)(W + 2 * (size_t)r.nb * r.ng), order);
-        // aqsntemp is reused by every (plane, n-tile): split it to BF16 pieces once
+        // aqsntemp is reused by every (plane, n-tile): split it to FP16 pieces once
         // (an even number of 128-row tiles: rows past number_bands are zeros)
         const int MTa = 2 * p.MT;
         if (tcx::img_needs_pad(tcx::BM, r.nb, 0, r.nc) || MTa * tcx::BM > r.nb) {
-            tcx::img_pad_kernel<tcx::BM><<<dim3(p.kstages, MTa, 1), 256, 0, st>>>(Aimg, MTa, p.kstages, r.nb, 0, r.nc);
+            tcx::img_pad_kernel<tcx::BM, 4><<<dim3(p.kstages, MTa, 1), 256, 0, st>>>(Aimg, MTa, p.kstages, r.nb, 0, r.nc);
             ++c.launches;
         }
-        tcx::aimg_convert_kernel<<<dim3(ceil_div(r.nc, 256), r.nb), 256, 0, st>>>(r.aqsn, r.nb, r.nc, p.kstages, Aimg,
-                                                                                order);
+        tcx::aimg_convert_kernel<<<r.nb, 256, 0, st>>>(r.aqsn, r.nb, r.nc, p.kstages, Aimg, order, ascale);
         c.launches += 2;
         cudaMemsetAsync(c.errword, 0, sizeof(int), st);
     }
     // a0 < 0: R planes, all bands on CTA pairs; a0 >= 0: the A planes a0 .. a0+nb_-1
     // of planesA, each over the row tiles of the bands that read it
-    auto contract = [&](const double2* eps, const int* pls, int nb_, double2* P, uint8_t* img, size_t img_bytes,
+    auto contract = [&](const double2* eps, const int* pls, int nb_, double2* P, uint8_t* img, float* bsc,
                         int a0) {
         ContractArgs a{};
         a.A = r.aqsn; a.lda = r.nc; a.m0 = 0; a.M = r.nb;
@@ -557,20 +562,20 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
         a.KS = p.KS; a.kchunk = p.kchunk; a.batches = nb_; a.batch_plane = pls;
         a.aqsm = r.aqsm; a.ldm = r.nc; a.vcoul = r.vcoul; a.igp = igp; a.acol = igp; a.wscale = 1.0; a.G = 2; a.P = P;
         if (p.mixed) {
-            // pre-split B planes (bf16 x 3), then the tensor-core contraction
+            // pre-split B planes (FP16 hi/lo, rows scaled), then the tensor-core contraction
             const int NTb = ceil_div(r.ng, 64);
             if (tcx::img_needs_pad(64, r.ng, 0, r.nc)) {
-                tcx::img_pad_kernel<64, 9><<<dim3(p.kstages, NTb, nb_), 256, 0, st>>>(img, NTb, p.kstages, r.ng, 0, r.nc);
+                tcx::img_pad_kernel<64, 6><<<dim3(p.kstages, NTb, nb_), 256, 0, st>>>(img, NTb, p.kstages, r.ng, 0, r.nc);
                 ++c.launches;
             }
-            (void)img_bytes;
-            dim3 gconv(ceil_div(ceil_div(r.nc, 8), 256), r.ng, nb_);  // 8 k-values per thread
-            tcx::bimg_convert_kernel<64><<<gconv, 256, 0, st>>>(eps, a.bstride, r.ng, r.nc, pls, p.kstages, img);
+            tcx::bimg_convert_kernel<64><<<dim3(r.ng, nb_), 256, 0, st>>>(eps, a.bstride, r.ng, r.nc, pls, p.kstages,
+                                                                          img, bsc);
             tcx::TcArgs t{};
             t.c = a;
             t.c.batch_plane = nullptr;  // the image is indexed by batch position
             t.Bimg = img;
             t.W1 = W; t.W2 = W + (size_t)r.nb * r.ng; t.ldw = r.nb; t.Aimg = Aimg; t.gpp_cols = 0;
+            t.ascale = ascale; t.bscale = bsc;
             t.vcol = (const float*)(W + 2 * (size_t)r.nb * r.ng);
             t.kstages_total = p.kstages;
             t.MT = p.MT; t.NT = p.NT; t.units = p.MT * p.NT * p.KS * nb_;
@@ -601,6 +606,7 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
                     }
                     if (pt.u0[pt.n] == 0) continue;
                     t.Bimg = img + (long)j0 * pt.islab;
+                    t.bscale = bsc + (long)j0 * r.ng;
                     t.c.P = P + (long)j0 * pt.pslab;
                     k<<<std::min(pt.u0[pt.n], c.sms), tcx::THREADS_FF, smem, st>>>(t, pt);
                     ++c.launches;
@@ -628,8 +634,8 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
         }
     };
     if (!pipe) {
-        if (nR) contract(r.epsR, planes, nR, PR, imgR, p.bytesImgR, -1);
-        if (nA) contract(r.epsA, planes + nR, nA, PA, imgA, p.bytesImgA, 0);  // A planes: AW only
+        if (nR) contract(r.epsR, planes, nR, PR, imgR, bscaleR, -1);
+        if (nA) contract(r.epsA, planes + nR, nA, PA, imgA, bscaleA, 0);  // A planes: AW only
     } else {
         // one launch pair per copy group, each after its planes have landed;
         // a group's partials and pre-split image sit at its batch offset
@@ -641,8 +647,9 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
             if (cudaStreamWaitEvent(st, c.pipe_ev[q], 0) != cudaSuccess)
                 return cuda_fail(c, cudaGetLastError(), "ff: pipeline wait");
             uint8_t* img = isR ? imgR : imgA;
+            float* bs = isR ? bscaleR : bscaleA;
             contract(isR ? r.epsR : r.epsA, planes + (isR ? 0 : nR) + g0, n, isR ? PR + g0 * pslab : PA + g0 * pslabA,
-                     img ? img + g0 * islab : nullptr, 0, isR ? -1 : g0);
+                     img ? img + g0 * islab : nullptr, bs ? bs + (size_t)g0 * r.ng : nullptr, isR ? -1 : g0);
         }
     }
     phase_mark(c, 3);

@@ -130,6 +130,12 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N, bool neg_a) {
            ((uint32_t)(M >> 4) << 24);
 }
 
+// The same for FP16 A and B (the format fields 0): kind::f16 takes both
+// operands of one instruction in the same type.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
 // D[tmem] (+)= A[smem] x B[smem]^T ; issued by a single thread.
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accumulate) {

@@ -32,6 +32,7 @@
 
 #include <algorithm>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "fk_gemm.cuh"
 #include "fk_tc.cuh"
@@ -68,14 +69,21 @@ struct Cfg {
     // flight while the converters read the other.  (Two full stagings do not fit
     // beside two operand stages; one operand stage with two stagings measured
     // slower: the converters then wait for each stage's MMAs.)
-    static constexpr int STAGES = WSMEM ? 3 : 2;
     static constexpr int CHUNK_STAGES = 1;  // k-values per TMEM accumulation = 32
-    static constexpr uint32_t A_BYTES = NSUB * BM * 64;
+    // FF operands are FP16 hi/lo pieces (two per real value; every row scaled by
+    // a power of two that brings its largest magnitude just below 2^15, three
+    // piece products per complex product: hh, hl, lh), GPP operands BF16
+    // hi/mid/lo pieces (three per value, six piece products)
+    static constexpr bool F16 = WSMEM;
+    static constexpr int NPIECE = F16 ? 2 : NSPLIT;
+    static constexpr int ASUB = 2 * NPIECE;  // A sub-tiles: the re pieces, then the im pieces
+    static constexpr int STAGES = WSMEM ? (F16 ? 4 : 3) : 2;
+    static constexpr uint32_t A_BYTES = ASUB * BM * 64;
     // The pre-split B image, one k-stage of an n-tile: GPP six sub-tiles (re h,
-    // im h, re m, im m, re l, im l); FF nine (-im, re, im of each piece h, m, l),
+    // im h, re m, im m, re l, im l); FF six (-im, re, im of each piece h, l),
     // the negated imaginary parts serving the CTA pairs' complex accumulation.
     static constexpr bool IMG9 = WSMEM;
-    static constexpr uint32_t B_BYTES = (IMG9 ? 9 : NSUB) * BN * 64;
+    static constexpr uint32_t B_BYTES = (IMG9 ? 3 * NPIECE : NSUB) * BN * 64;
     // SL (FF on CTA pairs): one accumulator D = A_re x [B_re|B_im] + A_im x
     // [-B_im|B_re] = [S_re | S_im], 2*BN columns, in four buffers; otherwise two
     // accumulators X = A_re x [B_re|B_im], Y = A_im x [B_re|B_im] in two buffers.
@@ -83,7 +91,7 @@ struct Cfg {
     // B in one CTA's stage: [B_re; B_im] of each piece (single CTA); for a CTA
     // pair the even CTA's B_re (SL: [B_re; -B_im]) and the odd CTA's B_im (SL:
     // [B_im; B_re]) of each piece
-    static constexpr uint32_t B_SMEM = (PAIR ? (SL ? 2 : 1) : 2) * NSPLIT * BN * 64;
+    static constexpr uint32_t B_SMEM = (PAIR ? (SL ? 2 : 1) : 2) * NPIECE * BN * 64;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_SMEM;
     static constexpr int NBUF = SL ? 4 : 2;
     // SL: the accumulator buffers are handed over in groups of two (consecutive
@@ -102,7 +110,9 @@ struct TcArgs {
     CUtensorMap amap;     // GPP: A (FP64 complex rows) as a 2-D FP64 tensor, box 32 x BM (half a stage), zero fill
     ContractArgs c;       // shapes, partial buffer (same meaning as fk_gemm.cuh)
     const uint8_t* Bimg;  // pre-split B tiles: [plane][nt][kstage][NSUB][BN rows][64 B]
-    const uint8_t* Aimg;  // pre-split A tiles [mt][kstage][NSUB][BM rows][64 B] (AIMG kernels only)
+    const uint8_t* Aimg;  // pre-split A tiles [mt][kstage][ASUB][BM rows][64 B] (AIMG kernels only)
+    const float* ascale;  // FF: 2^-k of each A image row (the row was scaled by 2^k before its split)
+    const float* bscale;  // FF: 2^-k of each B row, [batch][N]
     const float2* W1;     // epilogue weights, column-major [h][ldw] (GPP: 0.5 vcoul conj(aqsm); FF: vcoul conj(aqsm))
     const float2* W2;     // FF only: conj(aqsm), [h][ldw]
     int ldw;              // = M (rows are contiguous, so a warp's 32 rows load coalesced)
@@ -238,6 +248,7 @@ struct PlaneSeq {
             cur.MT = tab->MT[r];
             cur.units = tab->u0[r + 1] - tab->u0[r];
             cur.Bimg = base->Bimg + (long)r * tab->islab;
+            if (base->bscale) cur.bscale = base->bscale + (long)r * base->c.N;
             cur.c.P = base->c.P + (long)r * tab->pslab;
         }
         lu = u - tab->u0[r];
@@ -358,7 +369,8 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             // ------------------------------------------------------------ MMA
             int g = 0, grp = 0;
             bool ok = true;
-            const uint32_t idp = tc::idesc_bf16(PAIR ? 2 * BM : BM, 2 * BN, false);
+            const uint32_t idp = C::F16 ? tc::idesc_f16(PAIR ? 2 * BM : BM, 2 * BN)
+                                        : tc::idesc_bf16(PAIR ? 2 * BM : BM, 2 * BN, false);
             for (int u = pid; u < src.units() && ok; u += npairs) {
                 int lu;
                 const TcArgs& t = src.at(u, lu);
@@ -409,25 +421,27 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                                 // D += A_re,pa x [B_re|B_im]_pb + A_im,pa x [-B_im|B_re]_pb
                                 if constexpr (C::SL) {
                                     tc::mma_bf16_pair(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
-                                    tc::mma_bf16_pair(dX, ad(3 + pa, kk), bd(pb, kk) + B_HALF, idp, 1u);
+                                    tc::mma_bf16_pair(dX, ad(C::NPIECE + pa, kk), bd(pb, kk) + B_HALF, idp, 1u);
                                 } else if constexpr (PAIR) {
                                     tc::mma_bf16_pair(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
-                                    tc::mma_bf16_pair(dY, ad(3 + pa, kk), bd(pb, kk), idp, accumulate);
+                                    tc::mma_bf16_pair(dY, ad(C::NPIECE + pa, kk), bd(pb, kk), idp, accumulate);
                                 } else {
                                     tc::mma_bf16(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
-                                    tc::mma_bf16(dY, ad(3 + pa, kk), bd(pb, kk), idp, accumulate);
+                                    tc::mma_bf16(dY, ad(C::NPIECE + pa, kk), bd(pb, kk), idp, accumulate);
                                 }
                             };
                             // The accumulators truncate each addition to FP32 at the magnitude they
-                            // hold, so the five small piece products (mm, lh, hl, mh, hm; 2^-8 and
-                            // below of the sum) of both k-steps go in first, while the accumulator is
-                            // small, and the two hh products last: two full-scale roundings per stage.
-                            const int PA[5] = {1, 2, 0, 1, 0};
-                            const int PB[5] = {1, 0, 2, 0, 1};
-    #pragma unroll
+                            // hold, so the small piece products (BF16: mm, lh, hl, mh, hm, 2^-8 and
+                            // below of the sum; FP16: lh, hl, 2^-11) of both k-steps go in first,
+                            // while the accumulator is small, and the two hh products last: two
+                            // full-scale roundings per stage.
+                            constexpr int NQ = C::F16 ? 2 : 5;
+                            constexpr int PA[5] = {1, C::F16 ? 0 : 2, 0, 1, 0};
+                            constexpr int PB[5] = {C::F16 ? 0 : 1, C::F16 ? 1 : 0, 2, 0, 1};
+#pragma unroll
                             for (int kk = 0; kk < 2; ++kk)
-    #pragma unroll
-                                for (int q = 0; q < 5; ++q) mma2(PA[q], PB[q], kk, (st > st0 || kk > 0 || q > 0) ? 1u : 0u);
+#pragma unroll
+                                for (int q = 0; q < NQ; ++q) mma2(PA[q], PB[q], kk, (st > st0 || kk > 0 || q > 0) ? 1u : 0u);
                             mma2(0, 0, 0, 1u);
                             mma2(0, 0, 1, 1u);
                             if constexpr (PAIR) tc::mma_commit_pair(&empty[s], 3);  // frees the stage in both CTAs
@@ -502,7 +516,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         uint8_t* bdst = base + s * C::STAGE_BYTES + C::A_BYTES;
                         if constexpr (C::SL) {
                             // image -im, re, im per piece: the even CTA takes [re; -im], the odd [im; re]
-                            for (int pc = 0; pc < NSPLIT; ++pc) {
+                            for (int pc = 0; pc < C::NPIECE; ++pc) {
                                 const int s0 = rank ? 2 : 1, s1 = rank ? 1 : 0;
                                 tc::bulk_g2s(bdst + (2 * pc) * BN * 64, src + (3 * pc + s0) * BN * 64, BN * 64, &fullB[s]);
                                 tc::bulk_g2s(bdst + (2 * pc + 1) * BN * 64, src + (3 * pc + s1) * BN * 64, BN * 64,
@@ -510,7 +524,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                             }
                         } else if constexpr (C::IMG9) {
                             // single CTA over the nine-sub-tile image: [re; im] of each piece, adjacent
-                            for (int pc = 0; pc < NSPLIT; ++pc)
+                            for (int pc = 0; pc < C::NPIECE; ++pc)
                                 tc::bulk_g2s(bdst + (2 * pc) * BN * 64, src + (3 * pc + 1) * BN * 64, 2 * BN * 64,
                                              &fullB[s]);
                         } else if constexpr (PAIR) {
@@ -582,12 +596,19 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                     wreg[i] = (i < t.gpp_cols && h < a.N / 3) ? t.W1[(long)h * t.ldw + mc] : make_float2(0.f, 0.f);
                 }
             } else {
-                // conj(aqsm) of this thread's row and vcoul of the warp's 16 columns
+                // conj(aqsm) of this thread's row and vcoul of the warp's 16 columns; the
+                // weights carry 2^-k of the row's and the column's scales (powers of two: exact)
+                const float sa = (t.ascale && m < a.M) ? t.ascale[m] : 1.f;
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     const int n = nt * BN + ej * 16 + j;
                     wreg[j] = (n < a.N && m < a.M) ? t.W2[(long)n * t.ldw + m] : make_float2(0.f, 0.f);
                     vreg[j] = n < a.N ? t.vcol[n] : 0.f;
+                    if (t.bscale) {
+                        const float sc = sa * (n < a.N ? t.bscale[(long)batch * a.N + n] : 0.f);
+                        wreg[j].x *= sc;
+                        wreg[j].y *= sc;
+                    }
                 }
             }
             // per-unit sums as FP32 float-float pairs (TwoSum): no FP64 instruction per drain
@@ -869,65 +890,107 @@ static __global__ void weight_table_kernel(int M, int m0, int ncols, const doubl
     if (vcol && m == 0) vcol[h] = g >= 0 ? f64_to_f32_bits(vcoul[g]) : 0.f;
 }
 
-// FP64 planes [plane][rows][K] -> the nine-sub-tile B images of FF
-// [plane][nt][kstage][piece h, m, l][-im, re, im][BN][64 B] (a piece of -im is
-// the piece of im with its sign flipped: the split is symmetric).  Each thread
-// converts 8 consecutive k-values of one row: 128 contiguous bytes in, one
-// 16-byte swizzle chunk of each of the nine sub-tiles out (the swizzle permutes
-// whole 16-byte chunks).  Grid (ceil(K/8 / blockDim), rows, planes).
+// FF operands in FP16 pieces.  A row is scaled by 2^k, k from its largest
+// magnitude |re| or |im| (its FP64 exponent e: k = 14 - e, so the row's values
+// lie below 2^15, within FP16's range, and its largest ones use FP16's full
+// precision); a scaled FP32 value v splits into h = fp16(v) and l = fp16(v - h)
+// (v - h is exact in FP32), v = h + l to 22 bits.  k is clamped to [-126, 126]
+// (2^k and 2^-k stay normal FP32 numbers): rows whose largest magnitude lies
+// outside [2^-112, 2^140] keep fewer bits.  Rows of zeros get k = 0.
+__device__ __forceinline__ int f16_row_shift(unsigned long long maxbits) {
+    const int e = (int)((maxbits >> 52) & 0x7ff);
+    if (e == 0) return 0;
+    return min(126, max(-126, 14 - (e - 1023)));
+}
+__device__ __forceinline__ float pow2f(int k) { return __uint_as_float((uint32_t)(127 + k) << 23); }
+__device__ __forceinline__ void split_f16(float v, uint16_t& h, uint16_t& l) {
+    const __half hh = __float2half_rn(v);
+    h = __half_as_ushort(hh);
+    l = __half_as_ushort(__float2half_rn(v - __half2float(hh)));
+}
+// Largest |re| or |im| bit pattern of an FP64 complex row (integer compares:
+// the FP64 pipe is narrow on this GPU), over the block; every thread gets it.
+__device__ __forceinline__ unsigned long long row_max_bits(const double2* row, int K) {
+    unsigned long long mx = 0;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        const double2 v = row[k];
+        const unsigned long long a = (unsigned long long)__double_as_longlong(v.x) & 0x7fffffffffffffffull;
+        const unsigned long long b = (unsigned long long)__double_as_longlong(v.y) & 0x7fffffffffffffffull;
+        mx = max(mx, max(a, b));
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    __shared__ unsigned long long wm[32];
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    mx = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mx = max(mx, wm[w]);
+    return mx;
+}
+
+// FP64 planes [plane][rows][K] -> the FF B images
+// [plane][nt][kstage][piece h, l][-im, re, im][BN][64 B], each row scaled by its
+// own 2^k (scale[plane][row] = 2^-k; a piece of -im is the piece of im with its
+// sign flipped).  One block of 256 threads per (row, plane): the row's largest
+// magnitude, then its pieces, each thread converting 8 consecutive k-values
+// (128 contiguous bytes in, one 16-byte swizzle chunk of each of the six
+// sub-tiles out; the swizzle permutes whole 16-byte chunks).  Grid (rows, planes).
 template <int BN>
-__global__ void bimg_convert_kernel(const double2* src, long plane_stride, int rows, int K, const int* planes,
-                                    int kstages, uint8_t* img) {
-    constexpr long STAGE = 9L * BN * 64;
-    const int k0 = 8 * (blockIdx.x * blockDim.x + threadIdx.x), n = blockIdx.y, b = blockIdx.z;
-    if (k0 >= K) return;
+__global__ void __launch_bounds__(256) bimg_convert_kernel(const double2* src, long plane_stride, int rows, int K,
+                                                           const int* planes, int kstages, uint8_t* img,
+                                                           float* scale) {
+    constexpr long STAGE = 6L * BN * 64;
+    const int n = blockIdx.x, b = blockIdx.y;
     const int f = planes ? planes[b] : b;
     const double2* row = src + (long)f * plane_stride + (long)n * K;
+    const int k2 = f16_row_shift(row_max_bits(row, K));
+    const float s = pow2f(k2);
+    if (threadIdx.x == 0) scale[(long)b * rows + n] = pow2f(-k2);
     const int NT = (rows + BN - 1) / BN;
     uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * STAGE;
-    if (k0 + 8 > K) {  // ragged end of the row: element by element
-        for (int k = k0; k < K; ++k) {
-            uint8_t* st = img_nt + (long)(k / BK) * STAGE;
-            const uint32_t off = tc::sw64_offset(n % BN, k % BK);
-            uint16_t rh, rm, rl, ih, im, il;
-            split3(f64_to_f32_bits(row[k].x), rh, rm, rl);
-            split3(f64_to_f32_bits(row[k].y), ih, im, il);
-            const uint16_t pr[3] = {rh, rm, rl}, pi[3] = {ih, im, il};
+    for (int k0 = 8 * threadIdx.x; k0 < K; k0 += 8 * blockDim.x) {
+        if (k0 + 8 > K) {  // ragged end of the row: element by element
+            for (int k = k0; k < K; ++k) {
+                uint8_t* st = img_nt + (long)(k / BK) * STAGE;
+                const uint32_t off = tc::sw64_offset(n % BN, k % BK);
+                uint16_t rh, rl, ih, il;
+                split_f16(f64_to_f32_bits(row[k].x) * s, rh, rl);
+                split_f16(f64_to_f32_bits(row[k].y) * s, ih, il);
+                const uint16_t pr[2] = {rh, rl}, pi[2] = {ih, il};
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                *(uint16_t*)(st + (3 * q + 0) * BN * 64 + off) = (uint16_t)(pi[q] ^ 0x8000u);
-                *(uint16_t*)(st + (3 * q + 1) * BN * 64 + off) = pr[q];
-                *(uint16_t*)(st + (3 * q + 2) * BN * 64 + off) = pi[q];
+                for (int q = 0; q < 2; ++q) {
+                    *(uint16_t*)(st + (3 * q + 0) * BN * 64 + off) = (uint16_t)(pi[q] ^ 0x8000u);
+                    *(uint16_t*)(st + (3 * q + 1) * BN * 64 + off) = pr[q];
+                    *(uint16_t*)(st + (3 * q + 2) * BN * 64 + off) = pi[q];
+                }
             }
+            break;
         }
-        return;
-    }
-    uint32_t pk[6][4];  // piece (part + 2*level) x four bf16 pairs
+        uint32_t pk[4][4];  // piece (part + 2*level) x four fp16 pairs
 #pragma unroll
-    for (int j = 0; j < 8; j += 2) {
-        const double2 v0 = row[k0 + j], v1 = row[k0 + j + 1];
-        uint16_t h0, m0, l0, h1, m1, l1;
-        split3(f64_to_f32_bits(v0.x), h0, m0, l0);
-        split3(f64_to_f32_bits(v1.x), h1, m1, l1);
-        pk[0][j / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-        pk[2][j / 2] = (uint32_t)m0 | ((uint32_t)m1 << 16);
-        pk[4][j / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
-        split3(f64_to_f32_bits(v0.y), h0, m0, l0);
-        split3(f64_to_f32_bits(v1.y), h1, m1, l1);
-        pk[1][j / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-        pk[3][j / 2] = (uint32_t)m0 | ((uint32_t)m1 << 16);
-        pk[5][j / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
-    }
-    uint8_t* st = img_nt + (long)(k0 / BK) * STAGE;
-    const uint32_t off = tc::sw64_offset(n % BN, k0 % BK);  // 16-byte aligned: k0 % 8 == 0
+        for (int j = 0; j < 8; j += 2) {
+            const double2 v0 = row[k0 + j], v1 = row[k0 + j + 1];
+            uint16_t h0, l0, h1, l1;
+            split_f16(f64_to_f32_bits(v0.x) * s, h0, l0);
+            split_f16(f64_to_f32_bits(v1.x) * s, h1, l1);
+            pk[0][j / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+            pk[2][j / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+            split_f16(f64_to_f32_bits(v0.y) * s, h0, l0);
+            split_f16(f64_to_f32_bits(v1.y) * s, h1, l1);
+            pk[1][j / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+            pk[3][j / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+        }
+        uint8_t* st = img_nt + (long)(k0 / BK) * STAGE;
+        const uint32_t off = tc::sw64_offset(n % BN, k0 % BK);  // 16-byte aligned: k0 % 8 == 0
 #pragma unroll
-    for (int q = 0; q < 3; ++q) {  // piece level h, m, l: pk[2q] re, pk[2q+1] im
-        const uint32_t* re = pk[2 * q];
-        const uint32_t* im = pk[2 * q + 1];
-        *(uint4*)(st + (3 * q + 0) * BN * 64 + off) =
-            make_uint4(im[0] ^ 0x80008000u, im[1] ^ 0x80008000u, im[2] ^ 0x80008000u, im[3] ^ 0x80008000u);
-        *(uint4*)(st + (3 * q + 1) * BN * 64 + off) = make_uint4(re[0], re[1], re[2], re[3]);
-        *(uint4*)(st + (3 * q + 2) * BN * 64 + off) = make_uint4(im[0], im[1], im[2], im[3]);
+        for (int q = 0; q < 2; ++q) {  // piece level h, l: pk[2q] re, pk[2q+1] im
+            const uint32_t* re = pk[2 * q];
+            const uint32_t* im = pk[2 * q + 1];
+            *(uint4*)(st + (3 * q + 0) * BN * 64 + off) =
+                make_uint4(im[0] ^ 0x80008000u, im[1] ^ 0x80008000u, im[2] ^ 0x80008000u, im[3] ^ 0x80008000u);
+            *(uint4*)(st + (3 * q + 1) * BN * 64 + off) = make_uint4(re[0], re[1], re[2], re[3]);
+            *(uint4*)(st + (3 * q + 2) * BN * 64 + off) = make_uint4(im[0], im[1], im[2], im[3]);
+        }
     }
 }
 
@@ -958,15 +1021,29 @@ inline bool img_needs_pad(int rows_per_tile, int cols, int gpp_cols, int K) {
     return cols % rows_per_tile != 0;
 }
 
-// FP64 rows [rows][K] -> pre-split A image [mt][kstage][NSUB][BM][64 B]; image
-// row m holds source row rowmap[m] (or m).
-static __global__ void aimg_convert_kernel(const double2* src, int rows, int K, int kstages, uint8_t* img,
-                                           const int* rowmap = nullptr) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
-    if (k >= K || m >= rows) return;
-    const double2 v = src[(long)(rowmap ? rowmap[m] : m) * K + k];
-    uint8_t* tile = img + ((long)(m / BM) * kstages) * (long)(BM * NSUB * 64);
-    img_store<BM>(tile, m % BM, k, f64_to_f32_bits(v.x), f64_to_f32_bits(v.y));
+// FF: FP64 rows [rows][K] -> the A image [mt][kstage][re h, re l, im h, im l][BM][64 B],
+// image row m holding source row rowmap[m] (or m) scaled by its own 2^k
+// (scale[m] = 2^-k).  One block of 256 threads per row.
+static __global__ void __launch_bounds__(256) aimg_convert_kernel(const double2* src, int rows, int K, int kstages,
+                                                                  uint8_t* img, const int* rowmap, float* scale) {
+    const int m = blockIdx.x;
+    const double2* row = src + (long)(rowmap ? rowmap[m] : m) * K;
+    const int k2 = f16_row_shift(row_max_bits(row, K));
+    const float s = pow2f(k2);
+    if (threadIdx.x == 0) scale[m] = pow2f(-k2);
+    uint8_t* tile = img + ((long)(m / BM) * kstages) * (long)(BM * 4 * 64);
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        const double2 v = row[k];
+        uint8_t* st = tile + (long)(k / BK) * (BM * 4 * 64);
+        const uint32_t off = tc::sw64_offset(m % BM, k % BK);
+        uint16_t h, l;
+        split_f16(f64_to_f32_bits(v.x) * s, h, l);
+        *(uint16_t*)(st + 0 * BM * 64 + off) = h;
+        *(uint16_t*)(st + 1 * BM * 64 + off) = l;
+        split_f16(f64_to_f32_bits(v.y) * s, h, l);
+        *(uint16_t*)(st + 2 * BM * 64 + off) = h;
+        *(uint16_t*)(st + 3 * BM * 64 + off) = l;
+    }
 }
 
 // Host: how many CTA pairs of a pair kernel can be resident at once with
