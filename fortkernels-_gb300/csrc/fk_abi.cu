@@ -257,7 +257,8 @@ fk_status fk_wait_error_status(int word, char* msg, size_t msg_len) {
                  {0x20, "converter warps waiting for operand rows"},
                  {0x40, "copy warp waiting for a free staging half"},
                  {0x80, "copy warp waiting for its last copies"},
-                 {0x100, "self-test wait"}};
+                 {0x100, "self-test wait"},
+                 {0x200, "plane conversion waiting for its row copy"}};
     std::string m;
     if (word == 0) {
         m = "no device-side wait gave up";
@@ -270,7 +271,7 @@ fk_status fk_wait_error_status(int word, char* msg, size_t msg_len) {
             if (word & r.bit) {
                 m += std::string(known++ ? "; " : " ") + r.what;
             }
-        if (word & ~0x1FF) m += std::string(known ? "; " : " ") + "unknown bits";
+        if (word & ~0x3FF) m += std::string(known ? "; " : " ") + "unknown bits";
     }
     if (msg && msg_len) {
         std::strncpy(msg, m.c_str(), msg_len - 1);

@@ -568,8 +568,21 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
                 tcx::img_pad_kernel<64, 6><<<dim3(p.kstages, NTb, nb_), 256, 0, st>>>(img, NTb, p.kstages, r.ng, 0, r.nc);
                 ++c.launches;
             }
-            tcx::bimg_convert_kernel<64><<<dim3(r.ng, nb_), 256, 0, st>>>(eps, a.bstride, r.ng, r.nc, pls, p.kstages,
-                                                                          img, bsc);
+            // rows up to 4096 k-values through shared memory (bulk copies: the planes
+            // start on a 16-byte boundary), else held in registers up to 8192 k-values
+            // (one or two chunks of 8 per thread), else read twice
+            const dim3 gconv(r.ng, nb_);
+            if (r.nc <= tcx::FF_ROW_SMEM_K && ((uintptr_t)eps & 15) == 0) {
+                auto kc = tcx::bimg_convert_smem_kernel<64>;
+                const int sm = r.nc * 16;
+                cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, tcx::FF_ROW_SMEM_K * 16);
+                kc<<<gconv, 256, sm, st>>>(eps, a.bstride, r.ng, r.nc, pls, p.kstages, img, bsc, c.errword, c.wait_limit);
+            } else if (r.nc <= 4096)
+                tcx::bimg_convert_kernel<64, 1><<<gconv, 512, 0, st>>>(eps, a.bstride, r.ng, r.nc, pls, p.kstages, img, bsc);
+            else if (r.nc <= 8192)
+                tcx::bimg_convert_kernel<64, 2><<<gconv, 512, 0, st>>>(eps, a.bstride, r.ng, r.nc, pls, p.kstages, img, bsc);
+            else
+                tcx::bimg_convert_kernel<64, 0><<<gconv, 512, 0, st>>>(eps, a.bstride, r.ng, r.nc, pls, p.kstages, img, bsc);
             tcx::TcArgs t{};
             t.c = a;
             t.c.batch_plane = nullptr;  // the image is indexed by batch position

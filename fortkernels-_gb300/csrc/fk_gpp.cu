@@ -88,6 +88,7 @@ struct PrepArgs {
     double2* wf;          // [nv][ng][2] flag-band weights (sch: 0.5*vcoul*conj(aqsm), ssx: occ*vcoul*conj(aqsm)), or nullptr
     int asx_neg;          // physics mode: the ssx weight is -occ*vcoul*conj(aqsm) (asxtemp subtracted)
     float* est;           // error estimate (EST prep): [nch][ng][3][6] magnitudes of the chunk's values
+    int wm0 = -1;         // first band of the weight table W (-1: nvband)
 };
 
 // The set-up work of block (ch, my_igp) other than the image padding.
@@ -120,9 +121,10 @@ FK_DEV int prep_setup(const PrepArgs& p, int ch, int my_igp) {
         // the column's epilogue weights, rows split evenly over its chunks
         const int acol = igp < 0 ? -1 : (p.compact ? my_igp : igp);
         const int m0 = (int)((long)p.M * ch / p.nch), m1 = (int)((long)p.M * (ch + 1) / p.nch);
+        const int w0 = p.wm0 < 0 ? p.nv : p.wm0;
         for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x)
             p.W[(long)my_igp * p.M + m] =
-                igp >= 0 ? tcx::weight_w1(p.aqsm[(long)(p.nv + m) * p.ldm + acol], 0.5 * p.vcoul[igp])
+                igp >= 0 ? tcx::weight_w1(p.aqsm[(long)(w0 + m) * p.ldm + acol], 0.5 * p.vcoul[igp])
                          : make_float2(0.f, 0.f);
     }
     return igp;
@@ -604,8 +606,12 @@ __device__ __noinline__ Exact exact_element(double wxt, double2 wt64, double2 ep
 // EST: also the magnitudes the error estimate needs, per frequency iw over the
 // block's elements: sum and max of |D|^2 (the image values), |sch|^2 and
 // |ssx|^2 (the flag-band factors), written to p.est[ch][my_igp][iw][6].
-template <int Q, int BN, bool EST = false>
+// SCH = false: the flag bands' sch sums are left to the contraction (their
+// terms are the image's products: sch = D where the mask holds, for the C++
+// and Fortran variants), and only the ssx sums are kept (F's odd entries).
+template <int Q, int BN, bool EST = false, bool SCH = true>
 FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) {
+    constexpr int NK = SCH ? 2 : 1;  // kinds accumulated per (band, iw): sch and ssx, or ssx
     const int tid = threadIdx.x;
     const int nflag = min(NVC, p.nv - p.n1base);
     const int igp = prep_setup(p, ch, my_igp);
@@ -623,9 +629,9 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
     const double2* wrow = p.wt + (long)my_igp * p.nc;
     const double2* erow = p.eps + (long)my_igp * p.nc;
     const int ig_end = min(p.nc, (ch + 1) * p.tile);
-    float2 acc[NVC * 6];
+    float2 acc[NVC * 3 * NK];
 #pragma unroll
-    for (int i = 0; i < NVC * 6; ++i) acc[i] = make_float2(0.f, 0.f);
+    for (int i = 0; i < NVC * 3 * NK; ++i) acc[i] = make_float2(0.f, 0.f);
     float es[EST ? 18 : 1];
 #pragma unroll
     for (int i = 0; i < (EST ? 18 : 1); ++i) es[i] = 0.f;
@@ -748,8 +754,8 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
             }
 #pragma unroll
             for (int j = 0; j < NVC; ++j) {
-                cfmaf(acc[(j * 3 + iw) * 2 + 0], an[j], sch);
-                cfmaf(acc[(j * 3 + iw) * 2 + 1], an[j], ssx);
+                if (SCH) cfmaf(acc[(j * 3 + iw) * NK + 0], an[j], sch);
+                cfmaf(acc[(j * 3 + iw) * NK + NK - 1], an[j], ssx);
             }
         }
     }
@@ -794,20 +800,21 @@ FK_DEV void prep_mixed_item(const PrepArgs& p, int ch, int my_igp, double2* sm) 
         }
     }
     if (nflag <= 0) return;
-    double2 accd[NVC * 6];
-    block_sum_ff<NVC * 6>(acc, sm, accd);
-    if (tid < nflag * 6) {
-        const int j = tid / 6, r = tid % 6;
+    double2 accd[NVC * 3 * NK];
+    block_sum_ff<NVC * 3 * NK>(acc, sm, accd);
+    if (tid < nflag * 3 * NK) {
+        // F[..][iw * 2 + kind] (kind 0 sch, 1 ssx)
+        const int j = tid / (3 * NK), q = tid % (3 * NK), r = SCH ? q : 2 * q + 1;
 #pragma unroll
-        for (int i = 0; i < NVC * 6; ++i)
+        for (int i = 0; i < NVC * 3 * NK; ++i)
             if (i == tid) p.F[(((long)ch * p.nv + p.n1base + j) * p.ng + my_igp) * 6 + r] = accd[i];
     }
 }
 
-template <int Q, int BN, bool EST = false>
+template <int Q, int BN, bool EST = false, bool SCH = true>
 __global__ void __launch_bounds__(PREP_THREADS, 2) prep_mixed_kernel(PrepArgs p) {
     __shared__ double2 sm[8 * NVC * 6];
-    prep_mixed_item<Q, BN, EST>(p, p.ch0 + blockIdx.x, blockIdx.y, sm);
+    prep_mixed_item<Q, BN, EST, SCH>(p, p.ch0 + blockIdx.x, blockIdx.y, sm);
 }
 
 // ------------------------------------------------------------ error estimate
@@ -980,6 +987,8 @@ struct RowsArgs {
     int* counter;
     double2* out;
     const double2* wf;    // flag-band weights from the prep ([nv][ng][2]), or nullptr
+    int m0 = -1;          // first band of the contraction partials P (-1: nvband)
+    bool fsch = false;    // occupied bands' sch components from P (rows from m0 = 0), not from F
 };
 
 FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
@@ -992,6 +1001,11 @@ FK_DEV void rows_warp(const RowsArgs& ra, int n1, int c, int lane) {
     double2 v = make_double2(0.0, 0.0);
     if (c == 6) {
         if (S && lane < nslots_s) v = ordered_sum(S + (long)lane * nb + n1, 32L * nb, (nslots_s - lane + 31) / 32);
+    } else if (ra.fsch && c < 3) {
+        // the band's sch component from the contraction: its k-slice partials in slot order
+        const int m0 = ra.m0 < 0 ? nv : ra.m0;
+        const long M = nb - m0, m = n1 - m0;
+        if (lane < ra.nslots) v = ordered_sum(ra.P + ((long)lane * M + m) * 3 + c, 32L * M * 3, (ra.nslots - lane + 31) / 32);
     } else if (ra.P2) {
         // half sum, occupied band: weight * (cm S1 + conj(cm S2)) per column
         const int kind = c / 3, r = ((c % 3) * 2 + kind) * 2;
@@ -1064,7 +1078,8 @@ FK_DEV double split_sum(const double2* P, long M, long m, int c, int im, int nsl
 }
 
 FK_DEV void rows_band_warp(const RowsArgs& ra, int n1, int lane, double* parts) {
-    const long M = ra.nb - ra.nv, m = n1 - ra.nv;
+    const int m0 = ra.m0 < 0 ? ra.nv : ra.m0;
+    const long M = ra.nb - m0, m = n1 - m0;
     const int p = lane / 5, s = lane % 5, c = p >> 1, im = p & 1;
     double a = 0.0, b = 0.0, d = 0.0;  // this split's contraction sum, A = aqsmtemp sum, diagonal terms
     if (lane < 30) {
@@ -1214,8 +1229,17 @@ struct Plan {
     int MT, NT, KS, kchunk;      // main contraction
     int MTs, NTs, KSs, kchunks;  // static remainder contraction
     bool mixed;
+    bool fsch;  // the occupied bands' sch sums through the contraction (its rows start at band 0)
+    int m0;     // first band of the contraction: 0 with fsch, else nvband
     size_t bytesD, bytesF, bytesP, bytesS, bytesRows, bytesIgp, bytesW;
 };
+
+// fk_gpp's mixed path (not the half sum, not the root file's flag-band I_eps
+// indexing, whose sch differs from the image's values) contracts the occupied
+// bands too: their sch terms are the image's products.
+inline bool gpp_fsch(const GppDev& r) {
+    return r.prec == FK_MIXED && !(r.flags & (FK_GPP_HALF_SUM | FK_GPP_ROOT_QUIRKS));
+}
 
 // k-slice count for the persistent tensor-core kernel: the fewest slices
 // whose unit count fills the SMs evenly (tail waste <= 8%), with slices of at
@@ -1246,16 +1270,18 @@ constexpr int PIPE_CHUNKS = 8;  // row blocks of the pipelined host path at most
 
 // pair: the contraction runs on CTA pairs (tc_contract_pair_kernel): MT counts
 // 256-row tiles and the k-split fills the SM pairs
-Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0, bool pipelined = false, bool pair = false) {
+Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0, bool pipelined = false, bool pair = false,
+               bool fsch = false) {
     Plan p{};
     p.mixed = r.prec == FK_MIXED;
+    p.fsch = fsch && p.mixed;
+    p.m0 = p.fsch ? 0 : r.nv;
     p.pipe_sub = p.pipe_chunks = 0;
     if (r.prec == FK_MIXED) {
         // one wave: chunks x ngpown blocks fill the resident block slots
         int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, prep_mixed_kernel<0, 64>, PREP_THREADS, 0) !=
-                cudaSuccess ||
-            per_sm < 1)
+        void (*kprep)(PrepArgs) = p.fsch ? prep_mixed_kernel<0, 64, false, false> : prep_mixed_kernel<0, 64>;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kprep, PREP_THREADS, 0) != cudaSuccess || per_sm < 1)
             per_sm = 1;
         // chunks in whole k-stages (a warp's 32 plane waves fill whole image rows),
         // so that the last chunk is not much shorter than the others
@@ -1276,7 +1302,7 @@ Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0, bool pipeline
         p.nch = ceil_div(r.nc, p.tile);
     }
     p.passes = std::max(1, ceil_div(r.nv, NVC));
-    const int M = r.nb - r.nv, N = 3 * r.ng;
+    const int M = r.nb - p.m0, N = 3 * r.ng;
     if (p.mixed) {
         p.BN = 64;
         p.kstages = ceil_div(r.nc, tcx::BK);
@@ -1628,13 +1654,13 @@ __global__ void real_out_kernel(int nb, const double2* outc, double* out) {
 }  // namespace
 
 size_t gpp_workspace(const Ctx& c, const GppDev& r, bool pipelined) {
-    Plan p = make_plan(c, r, 0, pipelined, gpp_pair(r, pipelined));
+    Plan p = make_plan(c, r, 0, pipelined, gpp_pair(r, pipelined), gpp_fsch(r));
     const size_t half = (r.flags & FK_GPP_HALF_SUM) ? p.bytesP + (size_t)r.ng * (4 + 3 * sizeof(double2)) + 768 : 0;
     const size_t wf = (size_t)r.nv * r.ng * 2 * sizeof(double2);
     return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesRows + p.bytesIgp + p.bytesW + half + wf + 12 * 256;
 }
 
-int gpp_pipe_chunks(const Ctx& c, const GppDev& r) { return make_plan(c, r, 0, true).pipe_chunks; }
+int gpp_pipe_chunks(const Ctx& c, const GppDev& r) { return make_plan(c, r, 0, true, false, gpp_fsch(r)).pipe_chunks; }
 
 fk_status pipe_begin(Ctx& c) {
     if (!c.copy_stream && cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking) != cudaSuccess)
@@ -1649,12 +1675,12 @@ fk_status pipe_begin(Ctx& c) {
 }
 
 fk_status gpp_pipe_copy(Ctx& c, const GppDev& r, const GppPipe* pipe, int q0, int q1) {
-    const Plan p = make_plan(c, r, 0, true);
+    const Plan p = make_plan(c, r, 0, true, false, gpp_fsch(r));
     const size_t rowb = (size_t)r.nc * sizeof(double2);
     for (int q = q0; q < std::min(q1, p.pipe_chunks); ++q) {
-        // rows of m-tiles q*pipe_sub .. ; block 0 also carries the flag bands 0 .. nvband-1
-        const long r0 = q == 0 ? 0 : r.nv + (long)q * p.pipe_sub * tcx::BM;
-        const long r1 = std::min((long)r.nb, r.nv + (long)(q + 1) * p.pipe_sub * tcx::BM);
+        // rows of m-tiles q*pipe_sub .. (from band m0); block 0 also carries the flag bands 0 .. nvband-1
+        const long r0 = q == 0 ? 0 : p.m0 + (long)q * p.pipe_sub * tcx::BM;
+        const long r1 = std::min((long)r.nb, p.m0 + (long)(q + 1) * p.pipe_sub * tcx::BM);
         cudaError_t e = cudaMemcpyAsync(pipe->aqsn_d + r0 * r.nc, pipe->aqsn + r0 * r.nc, (size_t)(r1 - r0) * rowb,
                                         cudaMemcpyHostToDevice, c.copy_stream);
         if (e == cudaSuccess) e = cudaEventRecord(c.pipe_ev[q], c.copy_stream);
@@ -1761,7 +1787,7 @@ fk_status gpp_run_half(Ctx& c, const GppDev& r) {
 
 fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
     if (r.flags & FK_GPP_HALF_SUM) return pipe ? fail(c, FK_EINVAL, "gpp: no pipelined half sum") : gpp_run_half(c, r);
-    const Plan p = make_plan(c, r, 0, pipe != nullptr, gpp_pair(r, pipe != nullptr));
+    const Plan p = make_plan(c, r, 0, pipe != nullptr, gpp_pair(r, pipe != nullptr), gpp_fsch(r));
     if (pipe && !p.pipe_chunks) return fail(c, FK_EINVAL, "gpp: pipelined staging needs the mixed path");
     cudaStream_t st = c.stream;
     int* igp = (int*)c.ws.take(p.bytesIgp);
@@ -1788,7 +1814,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
     }
     // prep variant: 0 = BGW-Kernels/gppKer.cpp, 1 = root gppKer.cpp, 2 = the Fortran source
     const int Q = (r.flags & FK_GPP_ROOT_QUIRKS) ? 1 : (r.flags & FK_GPP_PHYSICS) ? 2 : 0;
-    const int M = r.nb - r.nv;
+    const int M = r.nb - p.m0;  // contraction rows: bands m0 .. nb-1
     c.launches = 0;
     // the first prep pass also maps the columns, writes the epilogue weights and
     // the image's padding, and clears the reduction's counter
@@ -1803,6 +1829,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
             a.aqsm = r.aqsm; a.ldm = r.ldm; a.vcoul = r.vcoul;
             a.W = (p.mixed && M > 0) ? W : nullptr;
             a.M = M;
+            a.wm0 = p.m0;
             a.counter = counter;
             a.wf = wf;
             a.asx_neg = Q == 2;
@@ -1811,7 +1838,17 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
         return a;
     };
     auto launch_prep = [&](const PrepArgs& a, dim3 grid) {
-        if (p.mixed && a.est) {
+        if (p.mixed && p.fsch) {
+            // the flag bands' ssx sums only (their sch terms go through the contraction);
+            // fsch excludes the root file's variant (Q == 1)
+            if (a.est) {
+                if (Q == 2) prep_mixed_kernel<2, 64, true, false><<<grid, PREP_THREADS, 0, st>>>(a);
+                else prep_mixed_kernel<0, 64, true, false><<<grid, PREP_THREADS, 0, st>>>(a);
+            } else {
+                if (Q == 2) prep_mixed_kernel<2, 64, false, false><<<grid, PREP_THREADS, 0, st>>>(a);
+                else prep_mixed_kernel<0, 64, false, false><<<grid, PREP_THREADS, 0, st>>>(a);
+            }
+        } else if (p.mixed && a.est) {
             if (Q == 1) prep_mixed_kernel<1, 64, true><<<grid, PREP_THREADS, 0, st>>>(a);
             else if (Q == 2) prep_mixed_kernel<2, 64, true><<<grid, PREP_THREADS, 0, st>>>(a);
             else prep_mixed_kernel<0, 64, true><<<grid, PREP_THREADS, 0, st>>>(a);
@@ -1838,7 +1875,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
         for (int pass = 0; pass < p.passes; ++pass) launch_prep(prep_args(pass), dim3(p.nch, r.ng));
         if (p.mixed && M > 0) {
             ContractArgs a{};
-            a.A = r.aqsn; a.lda = r.nc; a.m0 = r.nv; a.M = M;
+            a.A = r.aqsn; a.lda = r.nc; a.m0 = p.m0; a.M = M;
             a.B = D; a.ldb = r.nc; a.bstride = 0; a.N = 3 * r.ng; a.K = r.nc;
             a.KS = p.KS; a.kchunk = p.kchunk; a.batches = 1; a.batch_plane = nullptr;
             a.aqsm = r.aqsm; a.ldm = r.ldm; a.vcoul = r.vcoul; a.igp = igp; a.acol = acol; a.wscale = 0.5; a.G = 3;
@@ -1872,7 +1909,7 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
     phase_mark(c, 2);
     if (M > 0 && !pipe) {
         ContractArgs a{};
-        a.A = r.aqsn; a.lda = r.nc; a.m0 = r.nv; a.M = M;
+        a.A = r.aqsn; a.lda = r.nc; a.m0 = p.m0; a.M = M;
         a.B = D; a.ldb = r.nc; a.bstride = 0; a.N = 3 * r.ng; a.K = r.nc;
         a.KS = p.KS; a.kchunk = p.kchunk; a.batches = 1; a.batch_plane = nullptr;
         a.aqsm = r.aqsm; a.ldm = r.ldm; a.vcoul = r.vcoul; a.igp = igp; a.acol = acol; a.wscale = 0.5; a.G = 3; a.P = P;
@@ -1936,6 +1973,8 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
     ra.counter = counter;  // the last block also writes the totals
     ra.out = r.out;
     ra.wf = wf;
+    ra.m0 = p.m0;
+    ra.fsch = p.fsch;
     rows_kernel<<<rows_blocks(r.nb, r.nv), ROWS_THREADS, 0, st>>>(ra);
     ++c.launches;
     if (est) {

@@ -928,69 +928,156 @@ __device__ __forceinline__ unsigned long long row_max_bits(const double2* row, i
     return mx;
 }
 
+// FF B image writer: the 16-byte swizzle chunk of each of the six sub-tiles
+// (-im, re, im of pieces h and l) for the 8 consecutive k-values k0.. of row n
+// (k0 % 8 == 0; values past K, if any, are zeros), scaled by s.
+template <int BN>
+__device__ __forceinline__ void bimg_chunk_f16(uint8_t* img_nt, int n, int k0, const double2 (&v)[8], float s) {
+    constexpr long STAGE = 6L * BN * 64;
+    uint32_t pk[4][4];  // piece (part + 2*level) x four fp16 pairs
+#pragma unroll
+    for (int j = 0; j < 8; j += 2) {
+        uint16_t h0, l0, h1, l1;
+        split_f16(f64_to_f32_bits(v[j].x) * s, h0, l0);
+        split_f16(f64_to_f32_bits(v[j + 1].x) * s, h1, l1);
+        pk[0][j / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        pk[2][j / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+        split_f16(f64_to_f32_bits(v[j].y) * s, h0, l0);
+        split_f16(f64_to_f32_bits(v[j + 1].y) * s, h1, l1);
+        pk[1][j / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        pk[3][j / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+    }
+    uint8_t* st = img_nt + (long)(k0 / BK) * STAGE;
+    const uint32_t off = tc::sw64_offset(n % BN, k0 % BK);  // 16-byte aligned: k0 % 8 == 0
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {  // piece level h, l: pk[2q] re, pk[2q+1] im
+        const uint32_t* re = pk[2 * q];
+        const uint32_t* im = pk[2 * q + 1];
+        *(uint4*)(st + (3 * q + 0) * BN * 64 + off) =
+            make_uint4(im[0] ^ 0x80008000u, im[1] ^ 0x80008000u, im[2] ^ 0x80008000u, im[3] ^ 0x80008000u);
+        *(uint4*)(st + (3 * q + 1) * BN * 64 + off) = make_uint4(re[0], re[1], re[2], re[3]);
+        *(uint4*)(st + (3 * q + 2) * BN * 64 + off) = make_uint4(im[0], im[1], im[2], im[3]);
+    }
+}
+__device__ __forceinline__ unsigned long long abs_bits2(double2 v) {
+    const unsigned long long a = (unsigned long long)__double_as_longlong(v.x) & 0x7fffffffffffffffull;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v.y) & 0x7fffffffffffffffull;
+    return max(a, b);
+}
+// Largest of the block's per-thread values (every thread gets it).
+__device__ __forceinline__ unsigned long long block_max_u64(unsigned long long mx) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    __shared__ unsigned long long wm[32];
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    mx = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mx = max(mx, wm[w]);
+    return mx;
+}
+
 // FP64 planes [plane][rows][K] -> the FF B images
 // [plane][nt][kstage][piece h, l][-im, re, im][BN][64 B], each row scaled by its
 // own 2^k (scale[plane][row] = 2^-k; a piece of -im is the piece of im with its
-// sign flipped).  One block of 256 threads per (row, plane): the row's largest
-// magnitude, then its pieces, each thread converting 8 consecutive k-values
-// (128 contiguous bytes in, one 16-byte swizzle chunk of each of the six
-// sub-tiles out; the swizzle permutes whole 16-byte chunks).  Grid (rows, planes).
-template <int BN>
-__global__ void __launch_bounds__(256) bimg_convert_kernel(const double2* src, long plane_stride, int rows, int K,
+// sign flipped).  One block of 512 threads per (row, plane), each thread holding
+// NCH chunks of 8 consecutive k-values (128 contiguous bytes) in registers: the
+// row's largest magnitude over the block, then the pieces of the held values,
+// one 16-byte swizzle chunk of each sub-tile per chunk (the swizzle permutes
+// whole 16-byte chunks).  Rows up to 4096 * NCH k-values; NCH = 0: any length,
+// the row read twice (its largest magnitude, then the pieces).  Grid (rows, planes).
+template <int BN, int NCH>
+__global__ void __launch_bounds__(512) bimg_convert_kernel(const double2* src, long plane_stride, int rows, int K,
                                                            const int* planes, int kstages, uint8_t* img,
                                                            float* scale) {
-    constexpr long STAGE = 6L * BN * 64;
+    constexpr int T = 512;
     const int n = blockIdx.x, b = blockIdx.y;
     const int f = planes ? planes[b] : b;
     const double2* row = src + (long)f * plane_stride + (long)n * K;
-    const int k2 = f16_row_shift(row_max_bits(row, K));
+    const int NT = (rows + BN - 1) / BN;
+    uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * (6L * BN * 64);
+    double2 v[NCH > 0 ? NCH : 1][8];
+    unsigned long long mx = 0;
+    auto load = [&](int k0, double2 (&w)[8]) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) w[j] = k0 + j < K ? row[k0 + j] : make_double2(0.0, 0.0);
+    };
+    if constexpr (NCH > 0) {
+#pragma unroll
+        for (int c = 0; c < NCH; ++c) {
+            const int k0 = 8 * (threadIdx.x + c * T);
+            if (k0 < K) {
+                load(k0, v[c]);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) mx = max(mx, abs_bits2(v[c][j]));
+            }
+        }
+    } else {
+        for (int k = threadIdx.x; k < K; k += T) mx = max(mx, abs_bits2(row[k]));
+    }
+    const int k2 = f16_row_shift(block_max_u64(mx));
+    const float s = pow2f(k2);
+    if (threadIdx.x == 0) scale[(long)b * rows + n] = pow2f(-k2);
+    if constexpr (NCH > 0) {
+#pragma unroll
+        for (int c = 0; c < NCH; ++c) {
+            const int k0 = 8 * (threadIdx.x + c * T);
+            if (k0 < K) bimg_chunk_f16<BN>(img_nt, n, k0, v[c], s);
+        }
+    } else {
+        for (int k0 = 8 * threadIdx.x; k0 < K; k0 += 8 * T) {
+            load(k0, v[0]);
+            bimg_chunk_f16<BN>(img_nt, n, k0, v[0], s);
+        }
+    }
+}
+// The same conversion with the row in shared memory: one thread copies the
+// whole row there with bulk copies (one request per 16 KB; no register staging,
+// so three 256-thread blocks per SM overlap their copies with the others'
+// conversion), then the block takes the row's largest magnitude and writes its
+// pieces.  Rows of at most FF_ROW_SMEM_K k-values (64 KB); the row must start on
+// a 16-byte boundary (double2 rows do).  A copy that does not land within
+// `wait_limit` cycles sets bit 0x200 of *err and the block writes nothing.
+constexpr int FF_ROW_SMEM_K = 4096;
+template <int BN>
+__global__ void __launch_bounds__(256) bimg_convert_smem_kernel(const double2* src, long plane_stride, int rows, int K,
+                                                                const int* planes, int kstages, uint8_t* img,
+                                                                float* scale, int* err, long long wait_limit) {
+    extern __shared__ __align__(16) uint8_t smem_row[];
+    double2* rowbuf = (double2*)smem_row;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int ok;
+    const int n = blockIdx.x, b = blockIdx.y;
+    const int f = planes ? planes[b] : b;
+    const double2* row = src + (long)f * plane_stride + (long)n * K;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        tc::fence_barrier_init();
+        const uint32_t bytes = (uint32_t)K * 16u;
+        tc::mbar_arrive_expect_tx(&bar, bytes);
+        for (uint32_t o = 0; o < bytes; o += 16384u)
+            tc::bulk_g2s(smem_row + o, (const uint8_t*)row + o, min(16384u, bytes - o), &bar);
+        // the block exits only after its copy has landed (the bound applies to a
+        // copy that never completes, which leaves the block's result unwritten)
+        ok = tc::mbar_wait(&bar, 0, wait_limit) ? 1 : 0;
+        if (!ok) {
+            atomicOr(err, 0x200);
+            tc::mbar_wait(&bar, 0, DRAIN_LIMIT);
+        }
+    }
+    __syncthreads();
+    if (!ok) return;
+    unsigned long long mx = 0;
+    for (int k = threadIdx.x; k < K; k += 256) mx = max(mx, abs_bits2(rowbuf[k]));
+    const int k2 = f16_row_shift(block_max_u64(mx));
     const float s = pow2f(k2);
     if (threadIdx.x == 0) scale[(long)b * rows + n] = pow2f(-k2);
     const int NT = (rows + BN - 1) / BN;
-    uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * STAGE;
-    for (int k0 = 8 * threadIdx.x; k0 < K; k0 += 8 * blockDim.x) {
-        if (k0 + 8 > K) {  // ragged end of the row: element by element
-            for (int k = k0; k < K; ++k) {
-                uint8_t* st = img_nt + (long)(k / BK) * STAGE;
-                const uint32_t off = tc::sw64_offset(n % BN, k % BK);
-                uint16_t rh, rl, ih, il;
-                split_f16(f64_to_f32_bits(row[k].x) * s, rh, rl);
-                split_f16(f64_to_f32_bits(row[k].y) * s, ih, il);
-                const uint16_t pr[2] = {rh, rl}, pi[2] = {ih, il};
+    uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * (6L * BN * 64);
+    for (int k0 = 8 * threadIdx.x; k0 < K; k0 += 8 * 256) {
+        double2 v[8];
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    *(uint16_t*)(st + (3 * q + 0) * BN * 64 + off) = (uint16_t)(pi[q] ^ 0x8000u);
-                    *(uint16_t*)(st + (3 * q + 1) * BN * 64 + off) = pr[q];
-                    *(uint16_t*)(st + (3 * q + 2) * BN * 64 + off) = pi[q];
-                }
-            }
-            break;
-        }
-        uint32_t pk[4][4];  // piece (part + 2*level) x four fp16 pairs
-#pragma unroll
-        for (int j = 0; j < 8; j += 2) {
-            const double2 v0 = row[k0 + j], v1 = row[k0 + j + 1];
-            uint16_t h0, l0, h1, l1;
-            split_f16(f64_to_f32_bits(v0.x) * s, h0, l0);
-            split_f16(f64_to_f32_bits(v1.x) * s, h1, l1);
-            pk[0][j / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-            pk[2][j / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
-            split_f16(f64_to_f32_bits(v0.y) * s, h0, l0);
-            split_f16(f64_to_f32_bits(v1.y) * s, h1, l1);
-            pk[1][j / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-            pk[3][j / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
-        }
-        uint8_t* st = img_nt + (long)(k0 / BK) * STAGE;
-        const uint32_t off = tc::sw64_offset(n % BN, k0 % BK);  // 16-byte aligned: k0 % 8 == 0
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {  // piece level h, l: pk[2q] re, pk[2q+1] im
-            const uint32_t* re = pk[2 * q];
-            const uint32_t* im = pk[2 * q + 1];
-            *(uint4*)(st + (3 * q + 0) * BN * 64 + off) =
-                make_uint4(im[0] ^ 0x80008000u, im[1] ^ 0x80008000u, im[2] ^ 0x80008000u, im[3] ^ 0x80008000u);
-            *(uint4*)(st + (3 * q + 1) * BN * 64 + off) = make_uint4(re[0], re[1], re[2], re[3]);
-            *(uint4*)(st + (3 * q + 2) * BN * 64 + off) = make_uint4(im[0], im[1], im[2], im[3]);
-        }
+        for (int j = 0; j < 8; ++j) v[j] = k0 + j < K ? rowbuf[k0 + j] : make_double2(0.0, 0.0);
+        bimg_chunk_f16<BN>(img_nt, n, k0, v, s);
     }
 }
 
