@@ -84,14 +84,15 @@ struct Cfg {
     // the negated imaginary parts serving the CTA pairs' complex accumulation.
     static constexpr bool IMG9 = WSMEM;
     static constexpr uint32_t B_BYTES = (IMG9 ? 3 * NPIECE : NSUB) * BN * 64;
-    // SL (FF on CTA pairs): one accumulator D = A_re x [B_re|B_im] + A_im x
-    // [-B_im|B_re] = [S_re | S_im], 2*BN columns, in four buffers; otherwise two
+    // SL (FF): one accumulator D = A_re x [B_re|B_im] + A_im x [-B_im|B_re] =
+    // [S_re | S_im], 2*BN columns, in four buffers; otherwise (GPP) two
     // accumulators X = A_re x [B_re|B_im], Y = A_im x [B_re|B_im] in two buffers.
-    static constexpr bool SL = WSMEM && PAIR;
-    // B in one CTA's stage: [B_re; B_im] of each piece (single CTA); for a CTA
-    // pair the even CTA's B_re (SL: [B_re; -B_im]) and the odd CTA's B_im (SL:
-    // [B_im; B_re]) of each piece
-    static constexpr uint32_t B_SMEM = (PAIR ? (SL ? 2 : 1) : 2) * NPIECE * BN * 64;
+    static constexpr bool SL = WSMEM;
+    // B in one CTA's stage, per piece: GPP single CTA [B_re; B_im], GPP pair the
+    // even CTA's B_re and the odd CTA's B_im; FF single CTA the image's three
+    // sub-tiles [-B_im; B_re; B_im] ([B_re; B_im] from the second, [-B_im; B_re]
+    // from the first), FF pair the even CTA's [B_re; -B_im], the odd CTA's [B_im; B_re]
+    static constexpr uint32_t B_SMEM = (SL ? (PAIR ? 2 : 3) : (PAIR ? 1 : 2)) * NPIECE * BN * 64;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_SMEM;
     static constexpr int NBUF = SL ? 4 : 2;
     // SL: the accumulator buffers are handed over in groups of two (consecutive
@@ -413,15 +414,20 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                             // or BN rows (pair without SL: its half [B_re] or [B_im])
                             auto ad = [&](int sub, int kk) { return dA + (uint64_t)((sub * BM * 64) >> 4) + 2 * kk; };
                             auto bd = [&](int piece, int kk) {
-                                return dB + (uint64_t)((piece * ((PAIR && !C::SL) ? 1 : 2) * BN * 64) >> 4) + 2 * kk;
+                                constexpr int SUBS = C::SL ? (PAIR ? 2 : 3) : (PAIR ? 1 : 2);  // sub-tiles per piece
+                                return dB + (uint64_t)((piece * SUBS * BN * 64) >> 4) + 2 * kk;
                             };
                             constexpr uint64_t B_HALF = (uint64_t)(BN * 64) >> 4;  // SL: the piece's second BN rows
                             auto mma2 = [&](int pa, int pb, int kk, uint32_t accumulate) {
                                 // X += A_re,pa x [B_re|B_im]_pb, Y += A_im,pa x [B_re|B_im]_pb; SL:
                                 // D += A_re,pa x [B_re|B_im]_pb + A_im,pa x [-B_im|B_re]_pb
-                                if constexpr (C::SL) {
+                                if constexpr (C::SL && PAIR) {
                                     tc::mma_bf16_pair(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
                                     tc::mma_bf16_pair(dX, ad(C::NPIECE + pa, kk), bd(pb, kk) + B_HALF, idp, 1u);
+                                } else if constexpr (C::SL) {
+                                    // [B_re; B_im] from the piece's second sub-tile, [-B_im; B_re] from its first
+                                    tc::mma_bf16(dX, ad(pa, kk), bd(pb, kk) + B_HALF, idp, accumulate);
+                                    tc::mma_bf16(dX, ad(C::NPIECE + pa, kk), bd(pb, kk), idp, 1u);
                                 } else if constexpr (PAIR) {
                                     tc::mma_bf16_pair(dX, ad(pa, kk), bd(pb, kk), idp, accumulate);
                                     tc::mma_bf16_pair(dY, ad(C::NPIECE + pa, kk), bd(pb, kk), idp, accumulate);
@@ -514,7 +520,11 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                             t.Bimg + (((long)plane * t.NT + nt) * t.kstages_total + kst) * (long)C::B_BYTES;
                         tc::mbar_arrive_expect_tx(&fullB[s], C::B_SMEM + (AIMG ? C::A_BYTES : 0u));
                         uint8_t* bdst = base + s * C::STAGE_BYTES + C::A_BYTES;
-                        if constexpr (C::SL) {
+                        if constexpr (C::SL && !PAIR) {
+                            // single CTA: all three sub-tiles -im, re, im of each piece, one copy
+                            for (int pc = 0; pc < C::NPIECE; ++pc)
+                                tc::bulk_g2s(bdst + (3 * pc) * BN * 64, src + (3 * pc) * BN * 64, 3 * BN * 64, &fullB[s]);
+                        } else if constexpr (C::SL) {
                             // image -im, re, im per piece: the even CTA takes [re; -im], the odd [im; re]
                             for (int pc = 0; pc < C::NPIECE; ++pc) {
                                 const int s0 = rank ? 2 : 1, s1 = rank ? 1 : 0;
@@ -522,11 +532,6 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                                 tc::bulk_g2s(bdst + (2 * pc + 1) * BN * 64, src + (3 * pc + s1) * BN * 64, BN * 64,
                                              &fullB[s]);
                             }
-                        } else if constexpr (C::IMG9) {
-                            // single CTA over the nine-sub-tile image: [re; im] of each piece, adjacent
-                            for (int pc = 0; pc < C::NPIECE; ++pc)
-                                tc::bulk_g2s(bdst + (2 * pc) * BN * 64, src + (3 * pc + 1) * BN * 64, 2 * BN * 64,
-                                             &fullB[s]);
                         } else if constexpr (PAIR) {
                             // the even CTA's B_re, the odd CTA's B_im of each piece (paired image layout:
                             // re h, im h, re m, im m, re l, im l), BN rows each
@@ -645,7 +650,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         else tc::mbar_arrive(&accEmpty[slot]);
                     }
                 };
-                if (EPI == EPI_FF && C::SL) {
+                if constexpr (EPI == EPI_FF) {
                     // the warp's 16 columns of D = [S_re | S_im] of each buffer (the real
                     // parts of both, added, then the imaginary parts: 48 registers of
                     // values live instead of 64), the buffers go back, then the weighted sums
@@ -678,37 +683,6 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         if (rs) {
                             gsum[1].x += t2.x;
                             gsum[1].y += t2.y;
-                        }
-                    }
-                    for (int gg = 0; gg < 2; ++gg) {
-                        ff_add(accx[gg], gsum[gg].x);
-                        ff_add(accy[gg], gsum[gg].y);
-                        gsum[gg] = make_float2(0.f, 0.f);
-                    }
-                } else if (EPI == EPI_FF) {
-                    // the warp's 16 columns in two halves of 8 (X = [A_re B_re | A_re B_im],
-                    // Y = [A_im B_re | A_im B_im]); the group's FP32 sums go to float-float once
-                    const int c0 = ej * 16;
-#pragma unroll
-                    for (int hh = 0; hh < 2; ++hh) {
-                        float xr[8], xi[8], yr[8], yi[8];
-                        tc::tmem_ld8(tl + c0 + 8 * hh, xr);
-                        tc::tmem_ld8(tl + BN + c0 + 8 * hh, xi);
-                        tc::tmem_ld8(tl + 2 * BN + c0 + 8 * hh, yr);
-                        tc::tmem_ld8(tl + 3 * BN + c0 + 8 * hh, yi);
-                        tc::tmem_ld_wait();
-                        if (hh == 1) release();
-#pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            const float2 sv = make_float2(xr[j] - yi[j], xi[j] + yr[j]);
-                            const float2 t2 = cmulf(wreg[8 * hh + j], sv);
-                            const float v = vreg[8 * hh + j];
-                            gsum[0].x = fmaf(v, t2.x, gsum[0].x);
-                            gsum[0].y = fmaf(v, t2.y, gsum[0].y);
-                            if (rs) {
-                                gsum[1].x += t2.x;
-                                gsum[1].y += t2.y;
-                            }
                         }
                     }
                     for (int gg = 0; gg < 2; ++gg) {
