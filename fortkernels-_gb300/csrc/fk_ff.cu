@@ -35,29 +35,35 @@ __global__ void ff_igp_kernel(int ng, int nc, const int* inv, const int* indinv,
 
 // Sum the (KS x NT) partial slots of each (batch, row, group) and scatter into
 // the per-plane tables RW/RS [nb][nf]; partial row i belongs to band order[i]
-// (or i).  One warp per (row, batch): lane l adds slots l, l+32, .. in order,
-// then a fixed shuffle tree adds the lanes (deterministic), so a row's slots
-// are loaded in a few round trips rather than one after another.
+// (or i).  One warp per (row, batch); lane 4g + c takes component c (RW re, RW
+// im, RS re, RS im) of slots g, g+8, .. in order, so that the four lanes of a
+// slot read its 32-byte (RW, RS) record as one sector, then three shuffle
+// levels add the eight slot groups (fixed order: deterministic).  GB300's FP64
+// pipe retires one warp instruction per 64 cycles per sub-partition: this takes
+// slots/8 + 3 FP64 adds per warp.
 __global__ void ff_rows_kernel(int nb, int nf, int batches, int slots_per_batch, const int* planes,
                                const double2* P, double2* RW, double2* RS, const int* order) {
     const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), b = blockIdx.y, lane = threadIdx.x & 31;
     if (i >= nb || b >= batches) return;  // warp-uniform
-    const double2* q = P + ((long)b * slots_per_batch * nb + i) * 2;
-    const int n = slots_per_batch > lane ? (slots_per_batch - lane + 31) / 32 : 0;
-    double2 s0 = ordered_sum(q + (long)lane * 2 * nb, 64L * nb, n);
-    double2 s1 = RS ? ordered_sum(q + 1 + (long)lane * 2 * nb, 64L * nb, n) : make_double2(0.0, 0.0);
+    const int g = lane >> 2, comp = lane & 3;
+    const double* q = (const double*)(P + ((long)b * slots_per_batch * nb + i) * 2) + comp;
+    const long sstride = 4L * nb;  // doubles per slot
+    const int ns = slots_per_batch;
+    double v = 0.0;
+    for (int s0 = g; s0 < ns; s0 += 64) {
+        double a[8];  // eight loads in flight; clamped indices, +0.0 past the end (exact)
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        s0.x = __dadd_rn(s0.x, __shfl_xor_sync(0xffffffffu, s0.x, off));
-        s0.y = __dadd_rn(s0.y, __shfl_xor_sync(0xffffffffu, s0.y, off));
-        s1.x = __dadd_rn(s1.x, __shfl_xor_sync(0xffffffffu, s1.x, off));
-        s1.y = __dadd_rn(s1.y, __shfl_xor_sync(0xffffffffu, s1.y, off));
+        for (int j = 0; j < 8; ++j) a[j] = q[(long)min(s0 + 8 * j, ns - 1) * sstride];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v = __dadd_rn(v, s0 + 8 * j < ns ? a[j] : 0.0);
     }
-    if (lane) return;
+#pragma unroll
+    for (int off = 4; off < 32; off <<= 1) v = __dadd_rn(v, __shfl_xor_sync(0xffffffffu, v, off));
+    if (lane >= 4) return;
     const int n1 = order ? order[i] : i;
     const int f = planes[b];
-    RW[(long)n1 * nf + f] = s0;
-    if (RS) RS[(long)n1 * nf + f] = s1;
+    if (comp < 2) ((double*)(RW + (long)n1 * nf + f))[comp] = v;
+    else if (RS) ((double*)(RS + (long)n1 * nf + f))[comp - 2] = v;
 }
 
 struct FactRow {
