@@ -73,10 +73,19 @@ def algorithmic(w):
         M, N, K = w["nb"] - w["nv"], 3 * w["ng"], w["nc"]
         return 8 * M * K + 4 * N * K, 2 * M * N * K
     if w["kind"] == "gpp":
-        M, N, K = w["nb"] - w["nv"], 3 * w["ng"], w["nc"]
+        # the mixed full sum contracts every band (the occupied bands' sch terms too);
+        # the half sum the bands n1 >= nvband, twice
+        M = w["nb"] - w["nv"] if w.get("half") else w["nb"]
+        N, K = 3 * w["ng"], w["nc"]
         n = 2 if w.get("half") else 1
         return n * (16 * M * K + 8 * N * K), n * 8 * M * N * K
     return 16 * w["nb"] * w["nc"] + 16 * w["nf"] * w["ng"] * w["nc"], 8 * w["nf"] * w["nb"] * w["ng"] * w["nc"]
+
+
+def piece_products(w):
+    """Tensor-core products per complex multiply-add of the mixed path: GPP's
+    BF16 hi/mid/lo pieces six, FF's FP16 hi/lo pieces three."""
+    return 3 if w["kind"] == "ff" else 6
 
 
 def roofline(w, prec, byts, flops, kms, launches, peaks):
@@ -86,22 +95,24 @@ def roofline(w, prec, byts, flops, kms, launches, peaks):
     the algorithmic work of those launches, so achieved = work / time is the
     launch-weighted average rate.  The bound is the higher floor: algorithmic
     bytes at the copy peak (GPP at small ngpown), or algorithmic flops, which
-    the BF16x3 emulation executes as 6 piece products each, at the bf16 peak
-    (FF; GPP at large ngpown).  A tensor-bound frac is algorithmic flops over
-    the bf16 peak, so 1/6 is the emulation's ceiling."""
+    the emulation executes as piece_products(w) products each (GPP 6, FF 3),
+    at the bf16 peak (FF; GPP at large ngpown).  A tensor-bound frac is
+    algorithmic flops over the bf16 peak, so 1/piece_products is the
+    emulation's ceiling."""
     t = kms * 1e-3 if kms and kms > 0 else None
     common = {"kernel": "contraction", "algorithmic_bytes": byts, "algorithmic_flops": flops,
               "traffic": measured_traffic(w) if prec == "mixed" else None,
               "launches_per_call": launches, "duration_ms": kms / launches if kms and launches else None}
     # the bound is whichever floor is higher: the algorithmic bytes at the copy peak, or the
-    # executed BF16 piece products (6 per complex MAC's worth of flops) at the bf16 peak
+    # executed piece products at the bf16 peak
+    npp = piece_products(w)
     hbm_floor = byts / (peaks.get("hbm_gbs", 6800.0) * 1e9)
-    tensor_floor = 6 * flops / (peaks.get("bf16_tflops", 1900.0) * 1e12)
+    tensor_floor = npp * flops / (peaks.get("bf16_tflops", 1900.0) * 1e12)
     if prec == "mixed" and tensor_floor > hbm_floor:
         peak = peaks.get("bf16_tflops", 1900.0)
         ach = flops / t / 1e12 if t else None
         return dict(common, bound="tensor", achieved=ach, peak=peak, unit="TFLOP/s", frac=ach / peak if ach else None,
-                    executed_bf16_tflops=6 * ach if ach else None,
+                    executed_tensor_tflops=npp * ach if ach else None, piece_products=npp,
                     peak_source="measured bf16_tflops (burst)" if "bf16_tflops" in peaks else "fallback")
     peak = peaks.get("hbm_gbs", 6800.0)
     ach = byts / t / 1e9 if t else None

@@ -21,9 +21,10 @@ def test_gpp_default_workload_is_hbm_bound(bench):
     w = dict(bench.WORKLOADS["gpp"], name="gpp")
     assert bench.terms(w) == 512 * 20 * 32768 * 3
     byts, flops = bench.algorithmic(w)
-    # aqsntemp rows n1 >= nvband once (16 B per complex) and the D image (8 B per complex)
-    assert byts == 16 * 510 * 32768 + 8 * 60 * 32768 == 283115520
-    assert flops == 8 * 510 * 60 * 32768
+    # every aqsntemp row once (16 B per complex; the occupied bands' sch terms go through
+    # the contraction too) and the D image (8 B per complex)
+    assert byts == 16 * 512 * 32768 + 8 * 60 * 32768 == 284164096
+    assert flops == 8 * 512 * 60 * 32768
     r = bench.roofline(w, "mixed", byts, flops, 0.070, 1, PEAKS)
     assert r["bound"] == "hbm" and r["unit"] == "GB/s" and r["peak"] == PEAKS["hbm_gbs"]
     assert r["achieved"] == pytest.approx(byts / 70e-6 / 1e9)
@@ -34,7 +35,9 @@ def test_gpp_default_workload_is_hbm_bound(bench):
 def test_half_sum_counts_both_contractions(bench):
     w = dict(bench.WORKLOADS["gpphalf"], name="gpphalf")
     full = dict(w, half=False)
-    assert bench.algorithmic(w) == tuple(2 * x for x in bench.algorithmic(full))
+    # the bands n1 >= nvband, once per A operand (aqsntemp, aqsmtemp)
+    M, N, K = 510, 60, 32768
+    assert bench.algorithmic(w) == (2 * (16 * M * K + 8 * N * K), 2 * 8 * M * N * K)
     # ig < igp for the baseline columns igp = i * ncouls / ngpown: about half the full sum
     assert 0.4 < bench.terms(w) / bench.terms(full) < 0.5
 
@@ -47,7 +50,8 @@ def test_ff_config_is_tensor_bound(bench):
     assert r["bound"] == "tensor" and r["unit"] == "TFLOP/s"
     assert r["duration_ms"] == pytest.approx(0.602)
     assert r["frac"] == pytest.approx(flops / 1.204e-3 / 1e12 / PEAKS["bf16_tflops"])
-    assert r["executed_bf16_tflops"] == pytest.approx(6 * r["achieved"])
+    assert r["piece_products"] == 3  # FF: FP16 hi/lo pieces
+    assert r["executed_tensor_tflops"] == pytest.approx(3 * r["achieved"])
 
 
 def test_fp64_precision_is_reported_against_hbm_and_without_traffic(bench):
