@@ -49,6 +49,28 @@ def test_ff_mixed_within_1e6(ctx, fk, orc, case):
     mixed_gate(res, ref, sc, TOLMX, keys=KEYS)
 
 
+@pytest.mark.parametrize("nc", [1001, 5003, 9001])
+def test_ff_mixed_row_scales_and_conversion_paths(ctx, fk, orc, nc):
+    """The FP16 pieces of the mixed FF path scale every row of aqsntemp and of
+    each epsilon plane by its own power of two: rows spread over twelve
+    (epsilon) and six (aqsntemp) decades, with a row of zeros in each, keep the
+    1e-6 gate.  ncouls 1001, 5003 and 9001 take the plane conversion's three
+    forms (a row through shared memory, in registers, read twice), each with a
+    ragged end."""
+    p = fk.inputs.ff_synthetic(40, 2, nc, 48, 4, 3, seed=nc)
+    rng = np.random.default_rng(nc)
+    for key in ("I_epsR_array", "I_epsA_array"):
+        e = p[key] * 10.0 ** rng.uniform(-6.0, 6.0, size=p[key].shape[:-1])[..., None]
+        e[:, 5, :] = 0.0
+        p[key] = np.ascontiguousarray(e)
+    a = p["aqsntemp"] * 10.0 ** rng.uniform(-3.0, 3.0, size=(p["aqsntemp"].shape[0], 1))
+    a[7, :] = 0.0
+    p["aqsntemp"] = np.ascontiguousarray(a)
+    f = fk.FK_FF_SCHDT_GEMM | fk.FK_FF_SPLIT_ACHD
+    res, ref = ctx.ff(p, "mixed", f), ctx.ff(p, "fp64", f)
+    mixed_gate(res, ref, ff_scales(p, orc), TOLMX, keys=KEYS)
+
+
 def test_ff_matches_reference_kernels_with_schdt(ctx, fk):
     z = np.load(os.path.join(GOLD, "ff_harness.npz"))
     p = {k: z[k] for k in z.files if not k.startswith("ref_")}
