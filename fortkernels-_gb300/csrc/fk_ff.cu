@@ -583,6 +583,13 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
                 const int sm = r.nc * 16;
                 cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, tcx::FF_ROW_SMEM_K * 16);
                 kc<<<gconv, 256, sm, st>>>(eps, a.bstride, r.ng, r.nc, pls, p.kstages, img, bsc, c.errword, c.wait_limit);
+            } else if (r.nc <= 2 * tcx::FF_ROW_SMEM_K && ((uintptr_t)eps & 15) == 0) {
+                // longer rows: half a row per CTA of a pair, the halves' maxima exchanged
+                auto kc = tcx::bimg_convert_pair_kernel<64>;
+                const int sm = ((r.nc + 15) / 16) * 8 * 16;
+                cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, tcx::FF_ROW_SMEM_K * 16);
+                kc<<<dim3(2 * r.ng, nb_), 256, sm, st>>>(eps, a.bstride, r.ng, r.nc, pls, p.kstages, img, bsc, c.errword,
+                                                         c.wait_limit);
             } else if (r.nc <= 4096)
                 tcx::bimg_convert_kernel<64, 1><<<gconv, 512, 0, st>>>(eps, a.bstride, r.ng, r.nc, pls, p.kstages, img, bsc);
             else if (r.nc <= 8192)

@@ -1055,6 +1055,71 @@ __global__ void __launch_bounds__(256) bimg_convert_smem_kernel(const double2* s
     }
 }
 
+// Rows of up to 2 * FF_ROW_SMEM_K k-values on CTA pairs: each CTA of the pair
+// copies its half of the row (a multiple of 8 k-values; at most 64 KB) into its
+// shared memory, takes the half's largest magnitude, and the two exchange them
+// through distributed shared memory, so that three CTAs per SM overlap their
+// copies with the others' conversion.  Both CTAs pass both cluster barriers on
+// every path (a copy that does not land within `wait_limit` cycles sets bit
+// 0x200 of *err, and that CTA writes nothing).  Grid (2 * rows, planes).
+template <int BN>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(256)
+    bimg_convert_pair_kernel(const double2* src, long plane_stride, int rows, int K, const int* planes, int kstages,
+                             uint8_t* img, float* scale, int* err, long long wait_limit) {
+    extern __shared__ __align__(16) uint8_t smem_row[];
+    double2* rowbuf = (double2*)smem_row;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ unsigned long long half_max;
+    __shared__ int ok;
+    const uint32_t rank = tc::cluster_rank();
+    const int n = blockIdx.x >> 1, b = blockIdx.y;
+    const int f = planes ? planes[b] : b;
+    const double2* row = src + (long)f * plane_stride + (long)n * K;
+    const int Kh = ((K + 15) / 16) * 8;  // the first half: a multiple of 8 k-values
+    const int k0 = rank ? Kh : 0, k1 = rank ? K : min(K, Kh), nk = max(0, k1 - k0);
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        tc::fence_barrier_init();
+        const uint32_t bytes = (uint32_t)nk * 16u;
+        int good = 1;
+        if (bytes) {
+            tc::mbar_arrive_expect_tx(&bar, bytes);
+            for (uint32_t o = 0; o < bytes; o += 16384u)
+                tc::bulk_g2s(smem_row + o, (const uint8_t*)(row + k0) + o, min(16384u, bytes - o), &bar);
+            good = tc::mbar_wait(&bar, 0, wait_limit) ? 1 : 0;
+            if (!good) {
+                atomicOr(err, 0x200);
+                tc::mbar_wait(&bar, 0, DRAIN_LIMIT);
+            }
+        }
+        ok = good;
+    }
+    __syncthreads();
+    unsigned long long mx = 0;
+    if (ok)
+        for (int k = threadIdx.x; k < nk; k += 256) mx = max(mx, abs_bits2(rowbuf[k]));
+    mx = block_max_u64(mx);
+    if (threadIdx.x == 0) half_max = mx;
+    tc::cluster_sync();  // both halves' maxima are in shared memory
+    uint32_t peer;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(peer) : "r"(tc::smem_u32(&half_max)), "r"(rank ^ 1u));
+    unsigned long long other;
+    asm volatile("ld.shared::cluster.u64 %0, [%1];" : "=l"(other) : "r"(peer) : "memory");
+    tc::cluster_sync();  // the peer's value was read before either CTA may exit
+    const int k2 = f16_row_shift(max(mx, other));
+    const float s = pow2f(k2);
+    if (rank == 0 && threadIdx.x == 0) scale[(long)b * rows + n] = pow2f(-k2);
+    if (!ok) return;
+    const int NT = (rows + BN - 1) / BN;
+    uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * (6L * BN * 64);
+    for (int j0 = 8 * threadIdx.x; j0 < nk; j0 += 8 * 256) {
+        double2 v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = j0 + j < nk ? rowbuf[j0 + j] : make_double2(0.0, 0.0);
+        bimg_chunk_f16<BN>(img_nt, n, k0 + j0, v, s);
+    }
+}
+
 // Zeros the image positions that no converter writes: rows past a tile's
 // valid rows and k-values past K.  Valid rows of tile nt: 3*min(gpp_cols,
 // cols - gpp_cols*nt) when gpp_cols > 0 (GPP: gpp_cols igp triples per tile),
