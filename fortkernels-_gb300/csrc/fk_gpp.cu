@@ -1231,7 +1231,10 @@ struct Plan {
     bool mixed;
     bool fsch;  // the occupied bands' sch sums through the contraction (its rows start at band 0)
     int m0;     // first band of the contraction: 0 with fsch, else nvband
-    size_t bytesD, bytesF, bytesP, bytesS, bytesRows, bytesIgp, bytesW;
+    // CTA pairs over four or more n-tiles: aqsntemp split into BF16 pieces once (an A
+    // image) instead of by the converter warps of every n-tile's units
+    bool apre;
+    size_t bytesD, bytesF, bytesP, bytesS, bytesRows, bytesIgp, bytesW, bytesAimg;
 };
 
 // fk_gpp's mixed path (not the half sum, not the root file's flag-band I_eps
@@ -1324,6 +1327,8 @@ Plan make_plan(const Ctx& c, const GppDev& r, int ks_override = 0, bool pipeline
             p.units = p.MT * p.NT * p.KS;
         }
         p.units = p.MT * p.NT * p.KS;
+        p.apre = pair && !pipelined && p.NT >= 4;
+        p.bytesAimg = p.apre ? (size_t)2 * p.MT * p.kstages * tcx::Cfg<64, false, true>::A_BYTES : 0;
     } else {
         p.MT = ceil_div(std::max(M, 1), d64::BM);
         p.NT = ceil_div(N, d64::BN);
@@ -1657,7 +1662,12 @@ size_t gpp_workspace(const Ctx& c, const GppDev& r, bool pipelined) {
     Plan p = make_plan(c, r, 0, pipelined, gpp_pair(r, pipelined), gpp_fsch(r));
     const size_t half = (r.flags & FK_GPP_HALF_SUM) ? p.bytesP + (size_t)r.ng * (4 + 3 * sizeof(double2)) + 768 : 0;
     const size_t wf = (size_t)r.nv * r.ng * 2 * sizeof(double2);
-    return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesRows + p.bytesIgp + p.bytesW + half + wf + 12 * 256;
+    // the error estimate's column magnitudes, row norms and band bounds (when on)
+    const size_t est = (c.est_on && p.mixed)
+                           ? (size_t)p.nch * r.ng * 18 * sizeof(float) + (size_t)r.nb * (sizeof(float2) + 6 * sizeof(double)) + 768
+                           : 0;
+    return p.bytesD + p.bytesF + p.bytesP + p.bytesS + p.bytesRows + p.bytesIgp + p.bytesW + p.bytesAimg + half + wf + est +
+           16 * 256;
 }
 
 int gpp_pipe_chunks(const Ctx& c, const GppDev& r) { return make_plan(c, r, 0, true, false, gpp_fsch(r)).pipe_chunks; }
@@ -1805,8 +1815,9 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
     float* estE = est ? (float*)c.ws.take((size_t)p.nch * r.ng * 18 * sizeof(float)) : nullptr;
     float2* estA = est ? (float2*)c.ws.take((size_t)r.nb * sizeof(float2)) : nullptr;
     double* estB = est ? (double*)c.ws.take((size_t)r.nb * 6 * sizeof(double)) : nullptr;
+    uint8_t* Aimg = p.bytesAimg ? (uint8_t*)c.ws.take(p.bytesAimg) : nullptr;
     if (!igp || !F || !rows || !counter || (p.bytesD && !D) || (p.bytesP && !P) || (p.bytesS && !S) ||
-        (p.bytesW && !W) || (r.nv > 0 && !wf) || (est && (!estE || !estA || !estB)))
+        (p.bytesW && !W) || (r.nv > 0 && !wf) || (est && (!estE || !estA || !estB)) || (p.bytesAimg && !Aimg))
         return fail(c, FK_ENOMEM, "workspace too small for GPP request");
     if (p.mixed && D) {
         cudaError_t e = cudaMemsetAsync(c.errword, 0, sizeof(int), st);  // bounded-wait status
@@ -1926,10 +1937,24 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
             if (tcx::encode_rows_map(&t.amap, r.aqsn, r.nc, r.nc, r.nb) != cudaSuccess)
                 return fail(c, FK_ECUDA, "gpp: cannot describe aqsntemp as a tensor map (needs a 16-byte aligned array)");
             if (gpp_pair(r, false)) {
-                auto k = tcx::tc_contract_pair_kernel<EPI_GPP, 64, false>;
+                auto k = p.apre ? tcx::tc_contract_pair_apre_kernel<EPI_GPP, 64>
+                                : tcx::tc_contract_pair_kernel<EPI_GPP, 64, false>;
                 constexpr size_t smem = tcx::Cfg<64, false, true>::SMEM;
-                static const int pairs = tcx::resident_pairs(k, smem, tcx::THREADS, c.sms / 2);
-                const int grid1 = 2 * std::min(p.units, pairs);
+                static const int pairs = tcx::resident_pairs(tcx::tc_contract_pair_kernel<EPI_GPP, 64, false>, smem,
+                                                             tcx::THREADS, c.sms / 2);
+                static const int pairs_apre = tcx::resident_pairs(tcx::tc_contract_pair_apre_kernel<EPI_GPP, 64>, smem,
+                                                                  tcx::THREADS, c.sms / 2);
+                const int grid1 = 2 * std::min(p.units, p.apre ? pairs_apre : pairs);
+                if (p.apre) {
+                    // aqsntemp rows m0 .. split once; an even number of 128-row tiles, rows past
+                    // number_bands and k-values past ncouls zero
+                    const int MTa = 2 * p.MT;
+                    tcx::img_pad_kernel<tcx::BM><<<dim3(p.kstages, MTa, 1), 256, 0, st>>>(Aimg, MTa, p.kstages, M, 0, r.nc);
+                    tcx::aimg_split3_kernel<<<dim3(ceil_div(r.nc, 256), M), 256, 0, st>>>(r.aqsn + (long)p.m0 * r.nc, M,
+                                                                                         r.nc, p.kstages, Aimg);
+                    c.launches += 2;
+                    t.Aimg = Aimg;
+                }
                 set_smem(k, smem);
                 kernel_begin(c);
                 k<<<grid1, tcx::THREADS, smem, st>>>(t);

@@ -111,7 +111,7 @@ struct TcArgs {
     CUtensorMap amap;     // GPP: A (FP64 complex rows) as a 2-D FP64 tensor, box 32 x BM (half a stage), zero fill
     ContractArgs c;       // shapes, partial buffer (same meaning as fk_gemm.cuh)
     const uint8_t* Bimg;  // pre-split B tiles: [plane][nt][kstage][NSUB][BN rows][64 B]
-    const uint8_t* Aimg;  // pre-split A tiles [mt][kstage][ASUB][BM rows][64 B] (AIMG kernels only)
+    const uint8_t* Aimg;  // pre-split A tiles [mt][kstage][ASUB][BM rows][64 B] (APRE kernels only)
     const float* ascale;  // FF: 2^-k of each A image row (the row was scaled by 2^k before its split)
     const float* bscale;  // FF: 2^-k of each B row, [batch][N]
     const float2* W1;     // epilogue weights, column-major [h][ldw] (GPP: 0.5 vcoul conj(aqsm); FF: vcoul conj(aqsm))
@@ -258,7 +258,11 @@ struct PlaneSeq {
     static constexpr bool kTable = false;
 };
 
-template <int EPI, int BN, bool AIMG, bool PAIR, class Src>
+// AIMG: the FF layout (16 epilogue warps over 16-column groups, no converter
+// warps); APRE: the A operand arrives as a pre-split image (bulk copies onto the
+// stage's B barrier) instead of FP64 rows split by the converter warps.  FF has
+// both; GPP on CTA pairs over many n-tiles has APRE alone (its converter warps idle).
+template <int EPI, int BN, bool AIMG, bool PAIR, class Src, bool APRE = AIMG>
 __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long long wait_limit) {
     using C = Cfg<BN, EPI == EPI_FF, PAIR>;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -288,7 +292,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
 
     if (tid == 0) {
         for (int s = 0; s < C::STAGES; ++s) {
-            tc::mbar_init(&fullA[s], AIMG ? 1 : NCONV);
+            tc::mbar_init(&fullA[s], APRE ? 1 : NCONV);
             tc::mbar_init(&fullB[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
@@ -357,7 +361,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                 for (int st = 0; st < nst; ++st, ++g) {
                     const int s = g % C::STAGES;
                     const uint32_t par = (g / C::STAGES) & 1;
-                    if ((!AIMG && !tc::mbar_wait(&fullA[s], par, wait_limit)) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
+                    if ((!APRE && !tc::mbar_wait(&fullA[s], par, wait_limit)) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
                         s_abort) {
                         fail(2);
                         ok = false;
@@ -396,8 +400,8 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         for (int st = st0; st < st1; ++st, ++g) {
                             const int s = g % C::STAGES;
                             const uint32_t par = (g / C::STAGES) & 1;
-                            // AIMG: the A image lands on fullB too (one barrier per stage)
-                            if ((!AIMG && !tc::mbar_wait(&fullA[s], par, wait_limit)) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
+                            // APRE: the A image lands on fullB too (one barrier per stage)
+                            if ((!APRE && !tc::mbar_wait(&fullA[s], par, wait_limit)) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
                                 (PAIR && !tc::mbar_wait_cluster(&peerFull[s], par, wait_limit))) {
                                 fail(2);
                                 ok = false;
@@ -467,7 +471,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
         }
     } else if (warp == 1) {
         // ------------------------------------------------ bulk copies
-        // lane 0: pre-split B (and, for AIMG, A) tiles into the operand stage;
+        // lane 0: pre-split B (and, for APRE, A) tiles into the operand stage;
         // all lanes (GPP): the next stage's FP64 A rows into the staging buffer.
         int g = 0;
         bool ok = true;
@@ -485,7 +489,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             krange(t, ks, k0, k1);
             const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
             const int plane = a.batch_plane ? a.batch_plane[batch] : batch;
-            if (Src::kTable && !AIMG && lane == 0) {
+            if (Src::kTable && !APRE && lane == 0) {
                 // the table was written by copies before the launch: make its
                 // tensor map visible to the tensor-memory-access unit
                 asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&t.amap) : "memory");
@@ -493,7 +497,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             for (int st = 0; st < nst; ++st, ++g) {
                 const int s = g % C::STAGES;
                 const long kst = (long)(k0 / BK) + st;
-                if (!AIMG) {
+                if (!APRE) {
                     // FP64 rows in two halves of BK/2 k-values, each into its own half of the
                     // staging buffer as soon as the converters have read that half of the last stage
                     for (int h = 0; h < 2 && ok; ++h) {
@@ -518,7 +522,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                     } else {
                         const uint8_t* src =
                             t.Bimg + (((long)plane * t.NT + nt) * t.kstages_total + kst) * (long)C::B_BYTES;
-                        tc::mbar_arrive_expect_tx(&fullB[s], C::B_SMEM + (AIMG ? C::A_BYTES : 0u));
+                        tc::mbar_arrive_expect_tx(&fullB[s], C::B_SMEM + (APRE ? C::A_BYTES : 0u));
                         uint8_t* bdst = base + s * C::STAGE_BYTES + C::A_BYTES;
                         if constexpr (C::SL && !PAIR) {
                             // single CTA: all three sub-tiles -im, re, im of each piece, one copy
@@ -540,7 +544,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         } else {
                             tc::bulk_g2s(base + s * C::STAGE_BYTES + C::A_BYTES, src, C::B_BYTES, &fullB[s]);
                         }
-                        if (AIMG) {
+                        if (APRE) {
                             const uint8_t* asrc = t.Aimg + ((long)mt * t.kstages_total + kst) * (long)C::A_BYTES;
                             tc::bulk_g2s(base + s * C::STAGE_BYTES, asrc, C::A_BYTES, &fullB[s]);
                         }
@@ -561,9 +565,9 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             for (int s = 0; s < C::STAGES; ++s)
                 if (last_st[s] >= 0) {
                     const uint32_t par = (uint32_t)(last_st[s] / C::STAGES) & 1u;
-                    drained = tc::mbar_wait(&fullB[s], par, DRAIN_LIMIT) && drained;  // AIMG: the A image too
+                    drained = tc::mbar_wait(&fullB[s], par, DRAIN_LIMIT) && drained;  // APRE: the A image too
                 }
-            if (!AIMG)
+            if (!APRE)
                 for (int h = 0; h < 2; ++h)
                     if (last_f[h] >= 0) drained = tc::mbar_wait(&fFull[h], (uint32_t)last_f[h] & 1u, DRAIN_LIMIT) && drained;
             if (!drained) fail(128);
@@ -733,7 +737,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
         // 512-byte read per instruction), release it so that the next stage's
         // half is copied while the other half is read, then split everything
         // into BF16 pieces and store it into the operand stage.
-        if (!AIMG) {
+        if (!APRE) {
             const int cw = warp < 4 ? warp - 2 : warp - 6;  // 0..7
             constexpr int RPW = BM / NCONV;                  // rows per converter warp
             int g = 0;
@@ -826,6 +830,14 @@ template <int EPI, int BN, bool AIMG>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(AIMG ? THREADS_FF : THREADS, 1)
     tc_contract_pair_kernel(const __grid_constant__ TcArgs t) {
     tc_contract_body<EPI, BN, AIMG, true>(OneReq{t}, t.err, t.wait_limit);
+}
+
+// GPP on CTA pairs with aqsntemp pre-split into an A image (over many n-tiles
+// the converter warps would split the same A rows again for every n-tile).
+template <int EPI, int BN>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
+    tc_contract_pair_apre_kernel(const __grid_constant__ TcArgs t) {
+    tc_contract_body<EPI, BN, false, true, OneReq, true>(OneReq{t}, t.err, t.wait_limit);
 }
 
 // The batches of a PlaneTab in one launch (single CTAs).
@@ -1170,6 +1182,18 @@ static __global__ void __launch_bounds__(256) aimg_convert_kernel(const double2*
         *(uint16_t*)(st + 2 * BM * 64 + off) = h;
         *(uint16_t*)(st + 3 * BM * 64 + off) = l;
     }
+}
+
+// GPP over many n-tiles: FP64 rows [rows][K] -> the BF16 A image
+// [mt][kstage][re h, m, l, im h, m, l][BM][64 B], exactly the pieces the
+// converter warps would make (the same FP32 rounding and split).  One thread per
+// element; grid (ceil(K / blockDim), rows).
+static __global__ void aimg_split3_kernel(const double2* src, int rows, int K, int kstages, uint8_t* img) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
+    if (k >= K || m >= rows) return;
+    const double2 v = src[(long)m * K + k];
+    uint8_t* tile = img + ((long)(m / BM) * kstages) * (long)(BM * NSUB * 64);
+    img_store<BM>(tile, m % BM, k, f64_to_f32_bits(v.x), f64_to_f32_bits(v.y));
 }
 
 // Host: how many CTA pairs of a pair kernel can be resident at once with
