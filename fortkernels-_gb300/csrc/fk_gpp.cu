@@ -1939,11 +1939,12 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
             if (gpp_pair(r, false)) {
                 auto k = p.apre ? tcx::tc_contract_pair_apre_kernel<EPI_GPP, 64>
                                 : tcx::tc_contract_pair_kernel<EPI_GPP, 64, false>;
-                constexpr size_t smem = tcx::Cfg<64, false, true>::SMEM;
-                static const int pairs = tcx::resident_pairs(tcx::tc_contract_pair_kernel<EPI_GPP, 64, false>, smem,
-                                                             tcx::THREADS, c.sms / 2);
-                static const int pairs_apre = tcx::resident_pairs(tcx::tc_contract_pair_apre_kernel<EPI_GPP, 64>, smem,
-                                                                  tcx::THREADS, c.sms / 2);
+                const size_t smem = p.apre ? tcx::Cfg<64, false, true, true>::SMEM : tcx::Cfg<64, false, true>::SMEM;
+                static const int pairs = tcx::resident_pairs(tcx::tc_contract_pair_kernel<EPI_GPP, 64, false>,
+                                                             tcx::Cfg<64, false, true>::SMEM, tcx::THREADS, c.sms / 2);
+                static const int pairs_apre =
+                    tcx::resident_pairs(tcx::tc_contract_pair_apre_kernel<EPI_GPP, 64>,
+                                        tcx::Cfg<64, false, true, true>::SMEM, tcx::THREADS, c.sms / 2);
                 const int grid1 = 2 * std::min(p.units, p.apre ? pairs_apre : pairs);
                 if (p.apre) {
                     // aqsntemp rows m0 .. split once; an even number of 128-row tiles, rows past

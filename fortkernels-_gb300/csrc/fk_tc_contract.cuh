@@ -60,7 +60,7 @@ constexpr long long WAIT_LIMIT = 4000000000LL;
 // keep the default bound whatever limit the launch passes.
 constexpr long long DRAIN_LIMIT = 4000000000LL;
 
-template <int BN, bool WSMEM = false, bool PAIR = false>
+template <int BN, bool WSMEM = false, bool PAIR = false, bool APRE = WSMEM>
 struct Cfg {
     static_assert(BN == 64, "the accumulator buffers fill the 512 TMEM columns at BN = 64");
     // Operand stages: FF three (its epilogue keeps the per-unit weights in
@@ -77,7 +77,8 @@ struct Cfg {
     static constexpr bool F16 = WSMEM;
     static constexpr int NPIECE = F16 ? 2 : NSPLIT;
     static constexpr int ASUB = 2 * NPIECE;  // A sub-tiles: the re pieces, then the im pieces
-    static constexpr int STAGES = WSMEM ? (F16 ? 4 : 3) : 2;
+    // (GPP with a pre-split A image: no FP64 staging, so three operand stages)
+    static constexpr int STAGES = WSMEM ? (F16 ? 4 : 3) : (APRE ? 3 : 2);
     static constexpr uint32_t A_BYTES = ASUB * BM * 64;
     // The pre-split B image, one k-stage of an n-tile: GPP six sub-tiles (re h,
     // im h, re m, im m, re l, im l); FF six (-im, re, im of each piece h, l),
@@ -103,7 +104,7 @@ struct Cfg {
     static constexpr uint32_t ACC_COLS = SL ? 2 * BN : 4 * BN;
     static constexpr uint32_t TMEM_COLS = NBUF * ACC_COLS;
     static constexpr uint32_t W_BYTES = 0u;
-    static constexpr uint32_t F64_BYTES = WSMEM ? 0u : (uint32_t)(BM * BK * sizeof(double2));
+    static constexpr uint32_t F64_BYTES = APRE ? 0u : (uint32_t)(BM * BK * sizeof(double2));
     static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + W_BYTES + F64_BYTES + 1024 + 256;
 };
 
@@ -264,7 +265,7 @@ struct PlaneSeq {
 // both; GPP on CTA pairs over many n-tiles has APRE alone (its converter warps idle).
 template <int EPI, int BN, bool AIMG, bool PAIR, class Src, bool APRE = AIMG>
 __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long long wait_limit) {
-    using C = Cfg<BN, EPI == EPI_FF, PAIR>;
+    using C = Cfg<BN, EPI == EPI_FF, PAIR, APRE>;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-aligned operand area
     uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
