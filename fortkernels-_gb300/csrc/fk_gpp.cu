@@ -2019,9 +2019,10 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
 
 // ========================================================== served steps
 // A served request (GppJob) keeps its plan, workspace and descriptors on the
-// host; a step runs the first-step work (index map, weights, prep), a range
-// of contraction units and the last-step reduction of up to STEP_MAX
-// requests with five table-driven kernels, replayed from one captured graph.
+// host; a step runs the first-step work (index map, weights, prep, and the A
+// image of requests over four or more n-tiles), a range of contraction units
+// and the last-step reduction of up to STEP_MAX requests with six table-driven
+// kernels, replayed from one captured graph.
 // A request's k-slices, partial slots and reduction order depend only on its
 // own shape and plan, never on which other requests share a step.
 namespace {
@@ -2030,6 +2031,11 @@ constexpr int STEP_MAX = tcx::TC_MAXREQ;
 
 struct StepReq {
     int nb, nv, nc, ng, M, compact, Q, passes;
+    // requests over four or more n-tiles: aqsntemp rows nvband .. split once into a
+    // BF16 A image (Aimg, kst k-stages per 128-row tile) in the request's first step
+    const double2* arows;
+    uint8_t* Aimg;
+    int MTa, kst;
     const int *inv, *indinv;
     int *igp, *acol;
     const double2* aqsm;
@@ -2049,6 +2055,7 @@ struct StepTable {
     long setup_start[STEP_MAX + 1];  // threads: ng (index map) + M*ng (weights) per first-step request
     int prep_start[STEP_MAX + 1];    // blocks: passes*nch*ng per first-step request
     long rows_start[STEP_MAX + 1];   // rows block tasks (rows_blocks) per last-step request
+    long aimg_start[STEP_MAX + 1];   // A image elements (padded) per first-step request (0 without one)
 };
 
 template <class T>
@@ -2080,6 +2087,23 @@ __global__ void step_setup_kernel(const StepTable* T) {
             if (g >= 0) w = tcx::weight_w1(q.aqsm[(long)(q.nv + m) * q.ldm + (q.compact ? h : g)], 0.5 * q.vcoul[g]);
             q.W[(long)h * q.M + m] = w;
         }
+    }
+}
+
+// First-step requests with an A image: aqsntemp rows nvband .. into the BF16
+// image (the converter warps' pieces), the positions past M rows or ncouls
+// k-values zero; one thread per element of the padded extent.
+__global__ void aimg_table_kernel(const StepTable* T) {
+    const long total = T->aimg_start[T->nfirst];
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int f = find_range(T->aimg_start, T->nfirst, t);
+        const StepReq& q = T->req[T->first[f]];
+        const long i = t - T->aimg_start[f];
+        const int KP = q.kst * tcx::BK;
+        const int m = (int)(i / KP), k = (int)(i % KP);
+        const double2 v = (m < q.M && k < q.nc) ? q.arows[(long)m * q.nc + k] : make_double2(0.0, 0.0);
+        uint8_t* tile = q.Aimg + ((long)(m / tcx::BM) * q.kst) * (long)(tcx::BM * tcx::NSUB * 64);
+        tcx::img_store<tcx::BM>(tile, m % tcx::BM, k, f64_to_f32_bits(v.x), f64_to_f32_bits(v.y));
     }
 }
 
@@ -2137,10 +2161,16 @@ struct GppStep {
     bool launched = false;
 };
 
+// A served request over four or more n-tiles gets an A image: without it the
+// converter warps of every n-tile's units would split the same A rows again.
+inline size_t job_aimg_bytes(const Plan& p) {
+    return (p.mixed && p.NT >= 4) ? (size_t)p.MT * p.kstages * tcx::Cfg<64>::A_BYTES : 0;
+}
+
 size_t gpp_job_bytes(const Ctx& c, const GppDev& r, int ks) {
     const Plan p = make_plan(c, r, ks);
-    return p.bytesD + p.bytesF + p.bytesP + p.bytesRows + p.bytesIgp + p.bytesW + (7 + (size_t)r.nb) * sizeof(double2) +
-           8 * 256;
+    return p.bytesD + p.bytesF + p.bytesP + p.bytesRows + p.bytesIgp + p.bytesW + job_aimg_bytes(p) +
+           (7 + (size_t)r.nb) * sizeof(double2) + 9 * 256;
 }
 
 int gpp_job_units(const GppJob* j) { return (j->r.nb - j->r.nv) > 0 ? j->p.units : 0; }
@@ -2175,7 +2205,10 @@ GppJob* gpp_job_create(Ctx& c, const GppDev& r0, int ks, void* ws, size_t bytes,
     double2* rows = (double2*)w.take(p.bytesRows);
     float2* W = p.bytesW ? (float2*)w.take(p.bytesW) : nullptr;
     double2* out = (double2*)w.take((7 + (size_t)r0.nb) * sizeof(double2));
-    if (!igp || !F || !rows || !out || (p.bytesD && !D) || (p.bytesP && !P) || (p.bytesW && !W)) {
+    const size_t aimg_bytes = job_aimg_bytes(p);
+    uint8_t* Aimg = aimg_bytes ? (uint8_t*)w.take(aimg_bytes) : nullptr;
+    if (!igp || !F || !rows || !out || (p.bytesD && !D) || (p.bytesP && !P) || (p.bytesW && !W) ||
+        (aimg_bytes && !Aimg)) {
         delete j;
         *st = FK_ENOMEM;
         return nullptr;
@@ -2193,6 +2226,10 @@ GppJob* gpp_job_create(Ctx& c, const GppDev& r0, int ks, void* ws, size_t bytes,
     q.rows = RowsArgs{r.nb, r.nv, r.ng, p.KS * p.NT, P, 0, nullptr, p.nch, F, r.ldm, r.aqsm, r.vcoul, igp, acol, rows};
     q.out = out;
     q.rows.out = out;  // the band rows write acht_n1_loc
+    q.arows = r.aqsn + (long)r.nv * r.nc;
+    q.Aimg = M > 0 ? Aimg : nullptr;
+    q.MTa = p.MT;
+    q.kst = p.kstages;
     if (M > 0) {
         ContractArgs a{};
         a.A = r.aqsn; a.lda = r.nc; a.m0 = r.nv; a.M = M;
@@ -2202,7 +2239,8 @@ GppJob* gpp_job_create(Ctx& c, const GppDev& r0, int ks, void* ws, size_t bytes,
         tcx::TcArgs& t = j->tc;
         t.c = a;
         t.Bimg = (const uint8_t*)D;
-        t.W1 = W; t.W2 = nullptr; t.ldw = M; t.gpp_cols = GPP_COLS; t.Aimg = nullptr; t.vcol = nullptr;
+        t.W1 = W; t.W2 = nullptr; t.ldw = M; t.gpp_cols = GPP_COLS; t.vcol = nullptr;
+        t.Aimg = q.Aimg;  // the table contraction reads a pre-split A image when the request has one
         t.kstages_total = p.kstages;
         t.MT = p.MT; t.NT = p.NT; t.units = p.units;
         t.err = c.errword;
@@ -2249,13 +2287,14 @@ GppStep* gpp_step_create(Ctx& c, fk_status* st) {
             cudaSuccess ||
         prep_per_sm < 1)
         prep_per_sm = 1;
-    // capture: table upload, error-word clear, the five kernels
+    // capture: table upload, error-word clear, the six kernels
     cudaStream_t str = c.stream;
     if (cudaStreamBeginCapture(str, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return bad(FK_ECUDA);
     cudaMemcpyAsync(s->dev, s->host, sizeof(StepTable), cudaMemcpyHostToDevice, str);
     cudaMemsetAsync(c.errword, 0, sizeof(int), str);
     step_setup_kernel<<<c.sms * 4, 256, 0, str>>>(s->dev);
     prep_table_kernel<64><<<c.sms * prep_per_sm, PREP_THREADS, 0, str>>>(s->dev);
+    aimg_table_kernel<<<c.sms * 4, 256, 0, str>>>(s->dev);
     tck<<<c.sms, tcx::THREADS, tcx::Cfg<64>::SMEM, str>>>(&s->dev->tc, c.errword, c.wait_limit);
     rows_table_kernel<<<c.sms * 4, ROWS_THREADS, 0, str>>>(s->dev);
     totals_table_kernel<<<STEP_MAX, ROWS_THREADS, 0, str>>>(s->dev);
@@ -2292,6 +2331,7 @@ fk_status gpp_step_launch(Ctx& c, GppStep* s, const GppStepItem* items, int n) {
     T.setup_start[0] = 0;
     T.prep_start[0] = 0;
     T.rows_start[0] = 0;
+    T.aimg_start[0] = 0;
     for (int i = 0; i < n; ++i) {
         const GppJob* j = items[i].job;
         T.req[i] = j->req;
@@ -2304,6 +2344,7 @@ fk_status gpp_step_launch(Ctx& c, GppStep* s, const GppStepItem* items, int n) {
             T.first[f] = i;
             T.setup_start[f + 1] = T.setup_start[f] + j->r.ng + (long)j->req.M * j->r.ng;
             T.prep_start[f + 1] = T.prep_start[f] + j->p.passes * j->p.nch * j->r.ng;
+            T.aimg_start[f + 1] = T.aimg_start[f] + (j->req.Aimg ? (long)j->req.MTa * tcx::BM * j->req.kst * tcx::BK : 0);
         }
         if (items[i].last) {
             const int l = T.nlast++;

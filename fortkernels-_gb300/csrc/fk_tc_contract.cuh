@@ -359,10 +359,11 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                 unit_coords(t, lu, mt, nt, ks, batch);
                 krange(t, ks, k0, k1);
                 const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
+                const bool ua = APRE || (Src::kTable && t.Aimg != nullptr);  // A pre-split: on fullB
                 for (int st = 0; st < nst; ++st, ++g) {
                     const int s = g % C::STAGES;
                     const uint32_t par = (g / C::STAGES) & 1;
-                    if ((!APRE && !tc::mbar_wait(&fullA[s], par, wait_limit)) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
+                    if ((!ua && !tc::mbar_wait(&fullA[s], par, wait_limit)) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
                         s_abort) {
                         fail(2);
                         ok = false;
@@ -385,6 +386,8 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                 krange(t, ks, k0, k1);
                 const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
                 const int CH = t.chunk_stages > 0 ? t.chunk_stages : 1;
+                // a served request may carry a pre-split A image (its stages' A lands on fullB)
+                const bool ua = APRE || (Src::kTable && t.Aimg != nullptr);
                 for (int sg0 = 0; sg0 < nst && ok; sg0 += C::GRP * CH, ++grp) {
                     // a group: up to GRP chunks of CH stages, each into its own buffer of the slot
                     const int slot = grp % C::NSLOT;
@@ -401,8 +404,8 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         for (int st = st0; st < st1; ++st, ++g) {
                             const int s = g % C::STAGES;
                             const uint32_t par = (g / C::STAGES) & 1;
-                            // APRE: the A image lands on fullB too (one barrier per stage)
-                            if ((!APRE && !tc::mbar_wait(&fullA[s], par, wait_limit)) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
+                            // pre-split A: the A image lands on fullB too (one barrier per stage)
+                            if ((!ua && !tc::mbar_wait(&fullA[s], par, wait_limit)) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
                                 (PAIR && !tc::mbar_wait_cluster(&peerFull[s], par, wait_limit))) {
                                 fail(2);
                                 ok = false;
@@ -472,9 +475,11 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
         }
     } else if (warp == 1) {
         // ------------------------------------------------ bulk copies
-        // lane 0: pre-split B (and, for APRE, A) tiles into the operand stage;
+        // lane 0: pre-split B (and, for a pre-split A, A) tiles into the operand stage;
         // all lanes (GPP): the next stage's FP64 A rows into the staging buffer.
-        int g = 0;
+        // g counts stage uses, gf the stage uses staged in FP64 (the staging
+        // halves' barriers complete once per such use)
+        int g = 0, gf = 0;
         bool ok = true;
         // the last copy issued into each stage / staging half (-1: none), so
         // that the CTA can wait for every copy it started before it exits
@@ -490,7 +495,8 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             krange(t, ks, k0, k1);
             const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
             const int plane = a.batch_plane ? a.batch_plane[batch] : batch;
-            if (Src::kTable && !APRE && lane == 0) {
+            const bool ua = APRE || (Src::kTable && t.Aimg != nullptr);
+            if (Src::kTable && !ua && lane == 0) {
                 // the table was written by copies before the launch: make its
                 // tensor map visible to the tensor-memory-access unit
                 asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&t.amap) : "memory");
@@ -498,11 +504,11 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             for (int st = 0; st < nst; ++st, ++g) {
                 const int s = g % C::STAGES;
                 const long kst = (long)(k0 / BK) + st;
-                if (!APRE) {
+                if (!ua) {
                     // FP64 rows in two halves of BK/2 k-values, each into its own half of the
                     // staging buffer as soon as the converters have read that half of the last stage
                     for (int h = 0; h < 2 && ok; ++h) {
-                        if (!tc::warp_all(tc::mbar_wait(&fEmpty[h], (g & 1) ^ 1, wait_limit) && !s_abort)) {
+                        if (!tc::warp_all(tc::mbar_wait(&fEmpty[h], (gf & 1) ^ 1, wait_limit) && !s_abort)) {
                             fail(64);
                             ok = false;
                             break;
@@ -511,10 +517,11 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                             tc::mbar_arrive_expect_tx(&fFull[h], C::F64_BYTES / 2);
                             tc::tma_load_2d(sF + h * (BM * BK / 2), &t.amap, 2 * (k0 + st * BK + h * (BK / 2)),
                                             a.m0 + mt * BM, &fFull[h]);
-                            last_f[h] = g;
+                            last_f[h] = gf;
                         }
                     }
                     if (!ok) break;
+                    ++gf;
                 }
                 if (lane == 0) {
                     if (!tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, wait_limit) || s_abort) {
@@ -523,7 +530,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                     } else {
                         const uint8_t* src =
                             t.Bimg + (((long)plane * t.NT + nt) * t.kstages_total + kst) * (long)C::B_BYTES;
-                        tc::mbar_arrive_expect_tx(&fullB[s], C::B_SMEM + (APRE ? C::A_BYTES : 0u));
+                        tc::mbar_arrive_expect_tx(&fullB[s], C::B_SMEM + (ua ? C::A_BYTES : 0u));
                         uint8_t* bdst = base + s * C::STAGE_BYTES + C::A_BYTES;
                         if constexpr (C::SL && !PAIR) {
                             // single CTA: all three sub-tiles -im, re, im of each piece, one copy
@@ -545,7 +552,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         } else {
                             tc::bulk_g2s(base + s * C::STAGE_BYTES + C::A_BYTES, src, C::B_BYTES, &fullB[s]);
                         }
-                        if (APRE) {
+                        if (ua) {
                             const uint8_t* asrc = t.Aimg + ((long)mt * t.kstages_total + kst) * (long)C::A_BYTES;
                             tc::bulk_g2s(base + s * C::STAGE_BYTES, asrc, C::A_BYTES, &fullB[s]);
                         }
@@ -566,7 +573,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             for (int s = 0; s < C::STAGES; ++s)
                 if (last_st[s] >= 0) {
                     const uint32_t par = (uint32_t)(last_st[s] / C::STAGES) & 1u;
-                    drained = tc::mbar_wait(&fullB[s], par, DRAIN_LIMIT) && drained;  // APRE: the A image too
+                    drained = tc::mbar_wait(&fullB[s], par, DRAIN_LIMIT) && drained;  // a pre-split A image too
                 }
             if (!APRE)
                 for (int h = 0; h < 2; ++h)
@@ -741,7 +748,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
         if (!APRE) {
             const int cw = warp < 4 ? warp - 2 : warp - 6;  // 0..7
             constexpr int RPW = BM / NCONV;                  // rows per converter warp
-            int g = 0;
+            int g = 0, gf = 0;  // stage uses, FP64-staged stage uses (as the copy warp counts them)
             bool ok = true;
             for (int u = pid; u < src.units() && ok; u += npairs) {
                 int lu;
@@ -751,9 +758,23 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                 unit_coords(t, lu, mt, nt, ks, batch);
                 krange(t, ks, k0, k1);
                 const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
+                const bool ua = Src::kTable && t.Aimg != nullptr;  // the request's A is pre-split
                 for (int st = 0; st < nst; ++st, ++g) {
                     const int s = g % C::STAGES;
-                    if (!tc::warp_all(tc::mbar_wait(&fFull[0], g & 1, wait_limit) && !s_abort)) {
+                    if (ua) {
+                        // the stage's A arrives by bulk copy: only complete this use's phase of
+                        // fullA (no data), after the stage is free, so that every use of a
+                        // stage completes one phase whichever way its A arrives
+                        if (!tc::warp_all(tc::mbar_wait(&empty[s], ((g / C::STAGES) & 1) ^ 1, wait_limit) && !s_abort)) {
+                            fail(32);
+                            ok = false;
+                            break;
+                        }
+                        __syncwarp();
+                        if (lane == 0) tc::mbar_arrive(&fullA[s]);
+                        continue;
+                    }
+                    if (!tc::warp_all(tc::mbar_wait(&fFull[0], gf & 1, wait_limit) && !s_abort)) {
                         fail(32);
                         ok = false;
                         break;
@@ -763,7 +784,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                     const int kk = lane & 15, rr = lane >> 4;
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
-                        if (h == 1 && !tc::warp_all(tc::mbar_wait(&fFull[1], g & 1, wait_limit) && !s_abort)) {
+                        if (h == 1 && !tc::warp_all(tc::mbar_wait(&fFull[1], gf & 1, wait_limit) && !s_abort)) {
                             fail(32);
                             ok = false;
                             break;
@@ -803,6 +824,7 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                     tc::fence_proxy_async_smem();
                     __syncwarp();
                     if (lane == 0) tc::mbar_arrive(&fullA[s]);
+                    ++gf;
                 }
             }
         }
