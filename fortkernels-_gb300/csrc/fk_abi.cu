@@ -631,8 +631,11 @@ fk_status gpp_call(fk_ctx_t c, int nb, int nv, int nc, int ng, const fk_c128* aq
     r.aqsm_compact = false;
     // Large host arrays of a mixed-precision call: stream eps, wtilde and aqsntemp in
     // k-chunks and compute each chunk as it lands (the host link is the bottleneck).
+    // Over four or more n-tiles (ngpown >= 64) the contraction on CTA pairs with a
+    // pre-split A image, after all inputs have landed, is faster than streaming
+    // single-CTA contractions that split the A rows again for every n-tile.
     if (precision == FK_MIXED && !(flags & FK_GPP_HALF_SUM) && !aqn.dev && !eps.dev && !wt.dev && nb > nv &&
-        band >= ((size_t)64 << 20))
+        band >= ((size_t)64 << 20) && ng < 64)
         return fk::gpp_host_pipelined(x, r, aqsmtemp, aqsntemp, I_eps_array, wtilde_array, vcoul, inv_igp_index,
                                       indinv, wx_array, achtemp, asxtemp, acht_n1_loc, achstemp);
     // Host aqsmtemp: the sum reads only its ngpown columns igp(my_igp)
