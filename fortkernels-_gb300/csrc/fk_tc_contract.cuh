@@ -83,8 +83,8 @@ struct Cfg {
     // The pre-split B image, one k-stage of an n-tile: GPP six sub-tiles (re h,
     // im h, re m, im m, re l, im l); FF six (-im, re, im of each piece h, l),
     // the negated imaginary parts serving the CTA pairs' complex accumulation.
-    static constexpr bool IMG9 = WSMEM;
-    static constexpr uint32_t B_BYTES = (IMG9 ? 3 * NPIECE : NSUB) * BN * 64;
+    static constexpr bool IMGN = WSMEM;  // images with the negated imaginary pieces
+    static constexpr uint32_t B_BYTES = (IMGN ? 3 * NPIECE : NSUB) * BN * 64;
     // SL (FF): one accumulator D = A_re x [B_re|B_im] + A_im x [-B_im|B_re] =
     // [S_re | S_im], 2*BN columns, in four buffers; otherwise (GPP) two
     // accumulators X = A_re x [B_re|B_im], Y = A_im x [B_re|B_im] in two buffers.
@@ -1158,8 +1158,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(256)
 // Zeros the image positions that no converter writes: rows past a tile's
 // valid rows and k-values past K.  Valid rows of tile nt: 3*min(gpp_cols,
 // cols - gpp_cols*nt) when gpp_cols > 0 (GPP: gpp_cols igp triples per tile),
-// else min(ROWS, cols - ROWS*nt).  NS sub-tiles per stage (six; nine for the
-// FF B images).  Grid (kstages, NT, planes).
+// else min(ROWS, cols - ROWS*nt).  NS sub-tiles per stage (six for the GPP
+// images and the FF B images, four for FF's A image).  Grid (kstages, NT, planes).
 template <int ROWS, int NS = NSUB>
 __global__ void img_pad_kernel(uint8_t* img, int NT, int kstages, int cols, int gpp_cols, int K) {
     const int kst = blockIdx.x, nt = blockIdx.y, pl = blockIdx.z;
