@@ -1949,11 +1949,10 @@ fk_status gpp_run(Ctx& c, const GppDev& r, const GppPipe* pipe) {
                 if (p.apre) {
                     // aqsntemp rows m0 .. split once; an even number of 128-row tiles, rows past
                     // number_bands and k-values past ncouls zero
-                    const int MTa = 2 * p.MT;
-                    tcx::img_pad_kernel<tcx::BM><<<dim3(p.kstages, MTa, 1), 256, 0, st>>>(Aimg, MTa, p.kstages, M, 0, r.nc);
-                    tcx::aimg_split3_kernel<<<dim3(ceil_div(r.nc, 256), M), 256, 0, st>>>(r.aqsn + (long)p.m0 * r.nc, M,
-                                                                                         r.nc, p.kstages, Aimg);
-                    c.launches += 2;
+                    const int MTa = 2 * p.MT;  // the conversion also writes the padding (zeros)
+                    tcx::aimg_split3_kernel<<<dim3(ceil_div(p.kstages * (tcx::BK / 8), 128), MTa * tcx::BM), 128, 0, st>>>(
+                        r.aqsn + (long)p.m0 * r.nc, M, r.nc, p.kstages, Aimg);
+                    c.launches += 1;
                     t.Aimg = Aimg;
                 }
                 set_smem(k, smem);
@@ -2092,18 +2091,21 @@ __global__ void step_setup_kernel(const StepTable* T) {
 
 // First-step requests with an A image: aqsntemp rows nvband .. into the BF16
 // image (the converter warps' pieces), the positions past M rows or ncouls
-// k-values zero; one thread per element of the padded extent.
+// k-values zero; one thread per 8 k-values of the padded extent (aimg_start
+// counts those chunks).
 __global__ void aimg_table_kernel(const StepTable* T) {
     const long total = T->aimg_start[T->nfirst];
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
         const int f = find_range(T->aimg_start, T->nfirst, t);
         const StepReq& q = T->req[T->first[f]];
         const long i = t - T->aimg_start[f];
-        const int KP = q.kst * tcx::BK;
-        const int m = (int)(i / KP), k = (int)(i % KP);
-        const double2 v = (m < q.M && k < q.nc) ? q.arows[(long)m * q.nc + k] : make_double2(0.0, 0.0);
-        uint8_t* tile = q.Aimg + ((long)(m / tcx::BM) * q.kst) * (long)(tcx::BM * tcx::NSUB * 64);
-        tcx::img_store<tcx::BM>(tile, m % tcx::BM, k, f64_to_f32_bits(v.x), f64_to_f32_bits(v.y));
+        const int CP = q.kst * (tcx::BK / 8);  // chunks per padded row
+        const int m = (int)(i / CP), k0 = 8 * (int)(i % CP);
+        double2 v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            v[j] = (m < q.M && k0 + j < q.nc) ? q.arows[(long)m * q.nc + k0 + j] : make_double2(0.0, 0.0);
+        tcx::aimg_chunk_split3(q.Aimg, q.kst, m, k0, v);
     }
 }
 
@@ -2344,7 +2346,8 @@ fk_status gpp_step_launch(Ctx& c, GppStep* s, const GppStepItem* items, int n) {
             T.first[f] = i;
             T.setup_start[f + 1] = T.setup_start[f] + j->r.ng + (long)j->req.M * j->r.ng;
             T.prep_start[f + 1] = T.prep_start[f] + j->p.passes * j->p.nch * j->r.ng;
-            T.aimg_start[f + 1] = T.aimg_start[f] + (j->req.Aimg ? (long)j->req.MTa * tcx::BM * j->req.kst * tcx::BK : 0);
+            T.aimg_start[f + 1] =
+                T.aimg_start[f] + (j->req.Aimg ? (long)j->req.MTa * tcx::BM * j->req.kst * (tcx::BK / 8) : 0);
         }
         if (items[i].last) {
             const int l = T.nlast++;

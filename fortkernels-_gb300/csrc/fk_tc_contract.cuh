@@ -1207,16 +1207,43 @@ static __global__ void __launch_bounds__(256) aimg_convert_kernel(const double2*
     }
 }
 
-// GPP over many n-tiles: FP64 rows [rows][K] -> the BF16 A image
-// [mt][kstage][re h, m, l, im h, m, l][BM][64 B], exactly the pieces the
-// converter warps would make (the same FP32 rounding and split).  One thread per
-// element; grid (ceil(K / blockDim), rows).
+// The BF16 A image [mt][kstage][re h, m, l, im h, m, l][BM][64 B] of 8
+// consecutive k-values k0.. (k0 % 8 == 0) of image row m: the pieces the
+// converter warps make (the same FP32 rounding and split), one 16-byte swizzle
+// chunk per sub-tile.
+__device__ __forceinline__ void aimg_chunk_split3(uint8_t* img, int kstages, int m, int k0, const double2 (&v)[8]) {
+    uint32_t pk[6][4];  // sub-tile (re h, m, l, im h, m, l) x four bf16 pairs
+#pragma unroll
+    for (int j = 0; j < 8; j += 2) {
+        uint16_t a0, b0, c0, a1, b1, c1;
+        split3(f64_to_f32_bits(v[j].x), a0, b0, c0);
+        split3(f64_to_f32_bits(v[j + 1].x), a1, b1, c1);
+        pk[0][j / 2] = (uint32_t)a0 | ((uint32_t)a1 << 16);
+        pk[1][j / 2] = (uint32_t)b0 | ((uint32_t)b1 << 16);
+        pk[2][j / 2] = (uint32_t)c0 | ((uint32_t)c1 << 16);
+        split3(f64_to_f32_bits(v[j].y), a0, b0, c0);
+        split3(f64_to_f32_bits(v[j + 1].y), a1, b1, c1);
+        pk[3][j / 2] = (uint32_t)a0 | ((uint32_t)a1 << 16);
+        pk[4][j / 2] = (uint32_t)b0 | ((uint32_t)b1 << 16);
+        pk[5][j / 2] = (uint32_t)c0 | ((uint32_t)c1 << 16);
+    }
+    uint8_t* st = img + ((long)(m / BM) * kstages + k0 / BK) * (long)(BM * NSUB * 64);
+    const uint32_t off = tc::sw64_offset(m % BM, k0 % BK);  // 16-byte aligned: k0 % 8 == 0
+#pragma unroll
+    for (int q = 0; q < NSUB; ++q) *(uint4*)(st + q * BM * 64 + off) = make_uint4(pk[q][0], pk[q][1], pk[q][2], pk[q][3]);
+}
+
+// GPP over many n-tiles: FP64 rows [rows][K] -> the BF16 A image, every
+// position of the padded extent (rows up to a whole number of 128-row tiles,
+// kstages * 32 k-values) written, zeros outside the rows and K.  One thread per
+// 8 k-values; grid (ceil(kstages * 4 / blockDim), padded rows).
 static __global__ void aimg_split3_kernel(const double2* src, int rows, int K, int kstages, uint8_t* img) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
-    if (k >= K || m >= rows) return;
-    const double2 v = src[(long)m * K + k];
-    uint8_t* tile = img + ((long)(m / BM) * kstages) * (long)(BM * NSUB * 64);
-    img_store<BM>(tile, m % BM, k, f64_to_f32_bits(v.x), f64_to_f32_bits(v.y));
+    const int k0 = 8 * (blockIdx.x * blockDim.x + threadIdx.x), m = blockIdx.y;
+    if (k0 >= kstages * BK) return;
+    double2 v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = (m < rows && k0 + j < K) ? src[(long)m * K + k0 + j] : make_double2(0.0, 0.0);
+    aimg_chunk_split3(img, kstages, m, k0, v);
 }
 
 // Host: how many CTA pairs of a pair kernel can be resident at once with
