@@ -258,7 +258,8 @@ fk_status fk_wait_error_status(int word, char* msg, size_t msg_len) {
                  {0x40, "copy warp waiting for a free staging half"},
                  {0x80, "copy warp waiting for its last copies"},
                  {0x100, "self-test wait"},
-                 {0x200, "plane conversion waiting for its row copy"}};
+                 {0x200, "plane conversion waiting for its row copy"},
+                 {0x400, "-B_im warp waiting for an operand stage"}};
     std::string m;
     if (word == 0) {
         m = "no device-side wait gave up";
@@ -271,7 +272,7 @@ fk_status fk_wait_error_status(int word, char* msg, size_t msg_len) {
             if (word & r.bit) {
                 m += std::string(known++ ? "; " : " ") + r.what;
             }
-        if (word & ~0x3FF) m += std::string(known ? "; " : " ") + "unknown bits";
+        if (word & ~0x7FF) m += std::string(known ? "; " : " ") + "unknown bits";
     }
     if (msg && msg_len) {
         std::strncpy(msg, m.c_str(), msg_len - 1);

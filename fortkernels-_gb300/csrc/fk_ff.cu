@@ -571,7 +571,7 @@ fk_status ff_run(Ctx& c, const FfDev& r, const FfPipe* pipe) {
             // pre-split B planes (FP16 hi/lo, rows scaled), then the tensor-core contraction
             const int NTb = ceil_div(r.ng, 64);
             if (tcx::img_needs_pad(64, r.ng, 0, r.nc)) {
-                tcx::img_pad_kernel<64, 6><<<dim3(p.kstages, NTb, nb_), 256, 0, st>>>(img, NTb, p.kstages, r.ng, 0, r.nc);
+                tcx::img_pad_kernel<64, tcx::FF_BSUB><<<dim3(p.kstages, NTb, nb_), 256, 0, st>>>(img, NTb, p.kstages, r.ng, 0, r.nc);
                 ++c.launches;
             }
             // rows up to 4096 k-values through shared memory (bulk copies: the planes

@@ -45,7 +45,7 @@ constexpr int BK = 32;            // complex k-values per stage (64 B of bf16 pe
 constexpr int NSPLIT = 3;         // bf16 pieces per real value
 constexpr int NSUB = 2 * NSPLIT;  // sub-tiles per operand: re h/m/l, im h/m/l
 constexpr int THREADS = 448;     // GPP: MMA, producer, 8 converter warps, 4 epilogue warps
-constexpr int THREADS_FF = 576;  // FF: MMA, producer, 16 epilogue warps
+constexpr int THREADS_FF = 608;  // FF: MMA, producer, 16 epilogue warps, the -B_im warp
 // FF (A operand pre-split, no converter work): the 16 warps 2..17 all drain
 // TMEM, four per lane quarter, each over one 16-column group with its own
 // weights in registers and its own partial-sum slot; GPP: warps 4..7, one per
@@ -81,10 +81,11 @@ struct Cfg {
     static constexpr int STAGES = WSMEM ? (F16 ? 4 : 3) : (APRE ? 3 : 2);
     static constexpr uint32_t A_BYTES = ASUB * BM * 64;
     // The pre-split B image, one k-stage of an n-tile: GPP six sub-tiles (re h,
-    // im h, re m, im m, re l, im l); FF six (-im, re, im of each piece h, l),
-    // the negated imaginary parts serving the CTA pairs' complex accumulation.
-    static constexpr bool IMGN = WSMEM;  // images with the negated imaginary pieces
-    static constexpr uint32_t B_BYTES = (IMGN ? 3 * NPIECE : NSUB) * BN * 64;
+    // im h, re m, im m, re l, im l); FF four (re, im of each piece h, l).  FF's
+    // one-accumulator layout also needs -B_im: the -B_im warp writes it into
+    // the stage after the copy lands (IMGN).
+    static constexpr bool IMGN = WSMEM;
+    static constexpr uint32_t B_BYTES = (IMGN ? 2 * NPIECE : NSUB) * BN * 64;
     // SL (FF): one accumulator D = A_re x [B_re|B_im] + A_im x [-B_im|B_re] =
     // [S_re | S_im], 2*BN columns, in four buffers; otherwise (GPP) two
     // accumulators X = A_re x [B_re|B_im], Y = A_im x [B_re|B_im] in two buffers.
@@ -95,6 +96,9 @@ struct Cfg {
     // from the first), FF pair the even CTA's [B_re; -B_im], the odd CTA's [B_im; B_re]
     static constexpr uint32_t B_SMEM = (SL ? (PAIR ? 2 : 3) : (PAIR ? 1 : 2)) * NPIECE * BN * 64;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_SMEM;
+    // B bytes the copies of one stage bring (FF single CTA: [re; im] of each
+    // piece, the -B_im warp writes the third sub-tile)
+    static constexpr uint32_t B_COPY = IMGN ? 2 * NPIECE * BN * 64 : B_SMEM;
     static constexpr int NBUF = SL ? 4 : 2;
     // SL: the accumulator buffers are handed over in groups of two (consecutive
     // chunks), one full and one empty barrier per group: the MMA issuer waits,
@@ -105,7 +109,7 @@ struct Cfg {
     static constexpr uint32_t TMEM_COLS = NBUF * ACC_COLS;
     static constexpr uint32_t W_BYTES = 0u;
     static constexpr uint32_t F64_BYTES = APRE ? 0u : (uint32_t)(BM * BK * sizeof(double2));
-    static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + W_BYTES + F64_BYTES + 1024 + 256;
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + W_BYTES + F64_BYTES + 1024 + 512;
 };
 
 struct TcArgs {
@@ -280,7 +284,8 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
     uint64_t* fFull = done + 1;    // [2] GPP: FP64 staging half filled (tx bytes)
     uint64_t* fEmpty = done + 3;   // [2] GPP: FP64 staging half read by all converter warps
     uint64_t* peerFull = done + 5; // [STAGES] PAIR, even CTA: the odd CTA's half of the stage has landed
-    uint32_t* tslot = (uint32_t*)(done + 5 + C::STAGES);
+    uint64_t* negFull = done + 5 + C::STAGES;  // [STAGES] FF: the stage's -B_im is written
+    uint32_t* tslot = (uint32_t*)(done + 5 + 2 * C::STAGES);
     __shared__ int s_abort_flag;
     volatile int& s_abort = s_abort_flag;
 
@@ -301,7 +306,10 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
             tc::mbar_init(&accFull[b], 1);
             tc::mbar_init(&accEmpty[b], PAIR ? 2 * EPI_WARPS : EPI_WARPS);  // both CTAs' epilogues drain
         }
-        for (int s = 0; s < C::STAGES; ++s) tc::mbar_init(&peerFull[s], 1);
+        for (int s = 0; s < C::STAGES; ++s) {
+            tc::mbar_init(&peerFull[s], 1);
+            tc::mbar_init(&negFull[s], 1);
+        }
         tc::mbar_init(done, 1);
         for (int h = 0; h < 2; ++h) {
             tc::mbar_init(&fFull[h], 1);
@@ -404,8 +412,10 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                         for (int st = st0; st < st1; ++st, ++g) {
                             const int s = g % C::STAGES;
                             const uint32_t par = (g / C::STAGES) & 1;
-                            // pre-split A: the A image lands on fullB too (one barrier per stage)
-                            if ((!ua && !tc::mbar_wait(&fullA[s], par, wait_limit)) || !tc::mbar_wait(&fullB[s], par, wait_limit) ||
+                            // pre-split A: the A image lands on fullB too (one barrier per stage);
+                            // FF: negFull follows fullB once the -B_im warp has written -B_im
+                            if ((!ua && !tc::mbar_wait(&fullA[s], par, wait_limit)) ||
+                                !tc::mbar_wait(C::IMGN ? &negFull[s] : &fullB[s], par, wait_limit) ||
                                 (PAIR && !tc::mbar_wait_cluster(&peerFull[s], par, wait_limit))) {
                                 fail(2);
                                 ok = false;
@@ -530,19 +540,25 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                     } else {
                         const uint8_t* src =
                             t.Bimg + (((long)plane * t.NT + nt) * t.kstages_total + kst) * (long)C::B_BYTES;
-                        tc::mbar_arrive_expect_tx(&fullB[s], C::B_SMEM + (ua ? C::A_BYTES : 0u));
+                        tc::mbar_arrive_expect_tx(&fullB[s], C::B_COPY + (ua ? C::A_BYTES : 0u));
                         uint8_t* bdst = base + s * C::STAGE_BYTES + C::A_BYTES;
                         if constexpr (C::SL && !PAIR) {
-                            // single CTA: all three sub-tiles -im, re, im of each piece, one copy
+                            // single CTA: [re; im] of each piece into sub-tiles 1, 2 of its three
+                            // (the -B_im warp writes -im into sub-tile 0)
                             for (int pc = 0; pc < C::NPIECE; ++pc)
-                                tc::bulk_g2s(bdst + (3 * pc) * BN * 64, src + (3 * pc) * BN * 64, 3 * BN * 64, &fullB[s]);
-                        } else if constexpr (C::SL) {
-                            // image -im, re, im per piece: the even CTA takes [re; -im], the odd [im; re]
-                            for (int pc = 0; pc < C::NPIECE; ++pc) {
-                                const int s0 = rank ? 2 : 1, s1 = rank ? 1 : 0;
-                                tc::bulk_g2s(bdst + (2 * pc) * BN * 64, src + (3 * pc + s0) * BN * 64, BN * 64, &fullB[s]);
-                                tc::bulk_g2s(bdst + (2 * pc + 1) * BN * 64, src + (3 * pc + s1) * BN * 64, BN * 64,
+                                tc::bulk_g2s(bdst + (3 * pc + 1) * BN * 64, src + (2 * pc) * BN * 64, 2 * BN * 64,
                                              &fullB[s]);
+                        } else if constexpr (C::SL) {
+                            // image re, im per piece: the even CTA takes [re; im] (its -B_im warp
+                            // negates im in place), the odd [im; re]
+                            for (int pc = 0; pc < C::NPIECE; ++pc) {
+                                if (rank == 0) {
+                                    tc::bulk_g2s(bdst + (2 * pc) * BN * 64, src + (2 * pc) * BN * 64, 2 * BN * 64, &fullB[s]);
+                                } else {
+                                    tc::bulk_g2s(bdst + (2 * pc) * BN * 64, src + (2 * pc + 1) * BN * 64, BN * 64, &fullB[s]);
+                                    tc::bulk_g2s(bdst + (2 * pc + 1) * BN * 64, src + (2 * pc) * BN * 64, BN * 64,
+                                                 &fullB[s]);
+                                }
                             }
                         } else if constexpr (PAIR) {
                             // the even CTA's B_re, the odd CTA's B_im of each piece (paired image layout:
@@ -579,6 +595,50 @@ __device__ __forceinline__ void tc_contract_body(Src src0, int* err, const long 
                 for (int h = 0; h < 2; ++h)
                     if (last_f[h] >= 0) drained = tc::mbar_wait(&fFull[h], (uint32_t)last_f[h] & 1u, DRAIN_LIMIT) && drained;
             if (!drained) fail(128);
+        }
+    } else if (C::IMGN && warp == THREADS_FF / 32 - 1) {
+        // ------------------------------------------------------- -B_im warp
+        // FF (the MMA-issuing CTA of a pair, or a single CTA): once a stage's
+        // copies have landed, write -im of each B piece (the FP16 sign bits
+        // flipped: the swizzle permutes whole 16-byte chunks, so no position
+        // moves), in place for a pair's even CTA, into sub-tile 0 for a single
+        // CTA; then fence toward the tensor cores' proxy and arrive on negFull.
+        if (!PAIR || rank == 0) {
+            int g = 0;
+            bool ok = true;
+            for (int u = pid; u < src.units() && ok; u += npairs) {
+                int lu;
+                const TcArgs& t = src.at(u, lu);
+                int mt, nt, ks, batch, k0, k1;
+                unit_coords(t, lu, mt, nt, ks, batch);
+                krange(t, ks, k0, k1);
+                const int nst = k1 > k0 ? (k1 - k0 + BK - 1) / BK : 0;
+                for (int st = 0; st < nst; ++st, ++g) {
+                    const int s = g % C::STAGES;
+                    if (!tc::warp_all(tc::mbar_wait(&fullB[s], (g / C::STAGES) & 1, wait_limit) && !s_abort)) {
+                        fail(0x400);
+                        ok = false;
+                        break;
+                    }
+                    uint8_t* bsm = base + s * C::STAGE_BYTES + C::A_BYTES;
+#pragma unroll
+                    for (int pc = 0; pc < C::NPIECE; ++pc) {
+                        const uint4* from = (const uint4*)(bsm + (PAIR ? 2 * pc + 1 : 3 * pc + 2) * BN * 64);
+                        uint4* to = (uint4*)(bsm + (PAIR ? 2 * pc + 1 : 3 * pc) * BN * 64);
+                        for (int i = lane; i < BN * 64 / 16; i += 32) {
+                            uint4 v = from[i];
+                            v.x ^= 0x80008000u;
+                            v.y ^= 0x80008000u;
+                            v.z ^= 0x80008000u;
+                            v.w ^= 0x80008000u;
+                            to[i] = v;
+                        }
+                    }
+                    tc::fence_proxy_async_smem();
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(&negFull[s]);
+                }
+            }
         }
     } else if ((warp >= 4 && warp < 8) || AIMG) {
         // ------------------------------------------------------- epilogue
@@ -937,12 +997,14 @@ __device__ __forceinline__ unsigned long long row_max_bits(const double2* row, i
     return mx;
 }
 
-// FF B image writer: the 16-byte swizzle chunk of each of the six sub-tiles
-// (-im, re, im of pieces h and l) for the 8 consecutive k-values k0.. of row n
-// (k0 % 8 == 0; values past K, if any, are zeros), scaled by s.
+// FF B images: four sub-tiles per k-stage (re, im of pieces h and l)
+constexpr int FF_BSUB = 4;
+// FF B image writer: the 16-byte swizzle chunk of each of the four sub-tiles
+// for the 8 consecutive k-values k0.. of row n (k0 % 8 == 0; values past K, if
+// any, are zeros), scaled by s.
 template <int BN>
 __device__ __forceinline__ void bimg_chunk_f16(uint8_t* img_nt, int n, int k0, const double2 (&v)[8], float s) {
-    constexpr long STAGE = 6L * BN * 64;
+    constexpr long STAGE = (long)FF_BSUB * BN * 64;
     uint32_t pk[4][4];  // piece (part + 2*level) x four fp16 pairs
 #pragma unroll
     for (int j = 0; j < 8; j += 2) {
@@ -959,14 +1021,8 @@ __device__ __forceinline__ void bimg_chunk_f16(uint8_t* img_nt, int n, int k0, c
     uint8_t* st = img_nt + (long)(k0 / BK) * STAGE;
     const uint32_t off = tc::sw64_offset(n % BN, k0 % BK);  // 16-byte aligned: k0 % 8 == 0
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {  // piece level h, l: pk[2q] re, pk[2q+1] im
-        const uint32_t* re = pk[2 * q];
-        const uint32_t* im = pk[2 * q + 1];
-        *(uint4*)(st + (3 * q + 0) * BN * 64 + off) =
-            make_uint4(im[0] ^ 0x80008000u, im[1] ^ 0x80008000u, im[2] ^ 0x80008000u, im[3] ^ 0x80008000u);
-        *(uint4*)(st + (3 * q + 1) * BN * 64 + off) = make_uint4(re[0], re[1], re[2], re[3]);
-        *(uint4*)(st + (3 * q + 2) * BN * 64 + off) = make_uint4(im[0], im[1], im[2], im[3]);
-    }
+    for (int q = 0; q < 4; ++q)  // sub-tiles re h, im h, re l, im l
+        *(uint4*)(st + q * BN * 64 + off) = make_uint4(pk[q][0], pk[q][1], pk[q][2], pk[q][3]);
 }
 __device__ __forceinline__ unsigned long long abs_bits2(double2 v) {
     const unsigned long long a = (unsigned long long)__double_as_longlong(v.x) & 0x7fffffffffffffffull;
@@ -986,9 +1042,8 @@ __device__ __forceinline__ unsigned long long block_max_u64(unsigned long long m
 }
 
 // FP64 planes [plane][rows][K] -> the FF B images
-// [plane][nt][kstage][piece h, l][-im, re, im][BN][64 B], each row scaled by its
-// own 2^k (scale[plane][row] = 2^-k; a piece of -im is the piece of im with its
-// sign flipped).  One block of 512 threads per (row, plane), each thread holding
+// [plane][nt][kstage][re h, im h, re l, im l][BN][64 B], each row scaled by its
+// own 2^k (scale[plane][row] = 2^-k).  One block of 512 threads per (row, plane), each thread holding
 // NCH chunks of 8 consecutive k-values (128 contiguous bytes) in registers: the
 // row's largest magnitude over the block, then the pieces of the held values,
 // one 16-byte swizzle chunk of each sub-tile per chunk (the swizzle permutes
@@ -1003,7 +1058,7 @@ __global__ void __launch_bounds__(512) bimg_convert_kernel(const double2* src, l
     const int f = planes ? planes[b] : b;
     const double2* row = src + (long)f * plane_stride + (long)n * K;
     const int NT = (rows + BN - 1) / BN;
-    uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * (6L * BN * 64);
+    uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * ((long)FF_BSUB * BN * 64);
     double2 v[NCH > 0 ? NCH : 1][8];
     unsigned long long mx = 0;
     auto load = [&](int k0, double2 (&w)[8]) {
@@ -1081,7 +1136,7 @@ __global__ void __launch_bounds__(256) bimg_convert_smem_kernel(const double2* s
     const float s = pow2f(k2);
     if (threadIdx.x == 0) scale[(long)b * rows + n] = pow2f(-k2);
     const int NT = (rows + BN - 1) / BN;
-    uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * (6L * BN * 64);
+    uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * ((long)FF_BSUB * BN * 64);
     for (int k0 = 8 * threadIdx.x; k0 < K; k0 += 8 * 256) {
         double2 v[8];
 #pragma unroll
@@ -1146,7 +1201,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(256)
     if (rank == 0 && threadIdx.x == 0) scale[(long)b * rows + n] = pow2f(-k2);
     if (!ok) return;
     const int NT = (rows + BN - 1) / BN;
-    uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * (6L * BN * 64);
+    uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * ((long)FF_BSUB * BN * 64);
     for (int j0 = 8 * threadIdx.x; j0 < nk; j0 += 8 * 256) {
         double2 v[8];
 #pragma unroll

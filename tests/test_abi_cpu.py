@@ -105,6 +105,8 @@ def test_wait_error_word_maps_to_timeout(fk):
     assert "self-test" in buf.value.decode()
     assert lib.fk_wait_error_status(0x200, buf, 512) == fk._native.FK_ETIMEOUT
     assert "plane conversion" in buf.value.decode() and "unknown" not in buf.value.decode()
+    assert lib.fk_wait_error_status(0x400, buf, 512) == fk._native.FK_ETIMEOUT
+    assert "-B_im" in buf.value.decode() and "unknown" not in buf.value.decode()
     assert lib.fk_wait_error_status(0x4000, buf, 512) == fk._native.FK_ETIMEOUT
     assert "unknown" in buf.value.decode()
     small = ctypes.create_string_buffer(8)
