@@ -33,24 +33,24 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    # BASELINE config 1: GPP at full mini-app size
+    # GPP at full mini-app size: 512 bands, 2 valence, ncouls 32768, ngpown 20
     "gpp": dict(kind="gpp", nb=512, nv=2, nc=32768, ng=20),
     # the reference's canonical run `gppKer 512 2 32768 20` (ngpown = 32768/20)
     "gpp1638": dict(kind="gpp", nb=512, nv=2, nc=32768, ng=1638),
-    # gppKerSeq.cpp's half sum (gppsum = 1) at the config-1 size; its inverted noflag mask keeps only
+    # gppKerSeq.cpp's half sum (gppsum = 1) at 512 x 2 x 32768 x 20; its inverted noflag mask keeps only
     # near-pole terms, which the uniform draw never produces, so wtilde comes from the branch-stress draw
     "gpphalf": dict(kind="gpp", nb=512, nv=2, nc=32768, ng=20, half=True, dist="branch"),
-    # gppKer_real.cpp's real-valued sum at the config-1 size; branch-stress wtilde so that the driver's
-    # carried noflag values (masked terms) occur
+    # gppKer_real.cpp's real-valued sum at 512 x 2 x 32768 x 20; branch-stress wtilde so that the
+    # reference program's carried noflag values (masked terms) occur
     "gppreal": dict(kind="gpp", nb=512, nv=2, nc=32768, ng=20, real=True, dist="branch"),
-    # BASELINE config 2: FF full-frequency contraction
+    # FF full-frequency contraction: 512 bands, ncouls 4096, ngpown 512, 15 frequencies
     "ff": dict(kind="ff", nb=512, nv=2, nc=4096, ng=512, nf=15, ne=10),
-    # BASELINE config 4: large FF contraction (I_epsR/I_epsA ~17 GB each, drawn on the GPU)
+    # large FF contraction: 2048 bands, ncouls 8192, ngpown 4096, 32 frequencies (I_epsR/I_epsA ~17 GB each, drawn on the GPU)
     "ff4": dict(kind="ff", nb=2048, nv=2, nc=8192, ng=4096, nf=32, ne=10, device_inputs=True),
     # the FF shape whose (band, frequency, evaluation frequency) epilogue dominates
     # (ffkernel.deslippe.best.f90's compute-bound example 8 2 1000 60 20000 30000)
     "ffsigma": dict(kind="ff", nb=8, nv=2, nc=1000, ng=60, nf=20000, ne=30000, device_inputs=True),
-    # BASELINE config 3: a served, uneven GPP request stream
+    # a served, uneven GPP request stream: 256 requests of 128-1024 bands, ncouls 2048-32768
     "serve": dict(kind="serve", requests=256, nb_choices=(128, 256, 512, 1024), nc_lo=2048, nc_hi=32768,
                   nc_levels=8, nv=2, load=0.8),
 }
@@ -296,9 +296,9 @@ def reference_gpp_binary(w, runs, warmup=1):
     built unmodified from its sources (oracle/Makefile, target ref), as its own
     chrono line reports them (the loop nest alone, :301,441-446), on all host
     cores: `gppKer_bgw nb nvband ncouls nodes_per_group`, nodes_per_group =
-    ncouls / ngpown so that the driver's ngpown (:175-176) is the workload's.
+    ncouls / ngpown so that the program's ngpown (:175-176) is the workload's.
     None when the binary was not built on this machine or the shape cannot be
-    expressed that way.  The driver fills its own constant inputs."""
+    expressed that way.  The program fills its own constant inputs."""
     if w["kind"] != "gpp" or w.get("half") or w.get("real") or not os.access(REF_GPP, os.X_OK):
         return None
     npg = w["nc"] // w["ng"]
@@ -382,7 +382,7 @@ def run_reference(a, w):
         }), flush=True)
         return
     if w.get("device_inputs"):
-        # config 4 is far too large for the host cores: a bounded sample of it
+        # the 2048 x 8192 x 4096 x 32 contraction is far too large for the host cores: a bounded sample of it
         # (8 bands, 2 frequency planes, full ncouls x ngpown) per step
         w = dict(w, nb=8, nf=2)
         p = fk.inputs.ff_synthetic(w["nb"], w["nv"], w["nc"], w["ng"], w["nf"], w["ne"], seed=2024)
@@ -549,7 +549,7 @@ def measure_ours(a, w, fk, world, rank, local, sub=False):
     kernel_launches = kt[-1][1]
     # end to end through the C ABI with pinned host buffers
     hp = dict(p)
-    # arrays drawn on the GPU (config 4) go through host memory like the others
+    # arrays drawn on the GPU (the large FF workload) go through host memory like the others
     keys_h = keys_c + [k for k, v in p.items() if type(v).__module__.startswith("torch")]
     for k in keys_h:
         hp[k] = (p[k].cpu() if k not in keys_c else torch.from_numpy(np.ascontiguousarray(p[k]))).pin_memory()
@@ -611,7 +611,7 @@ def measure_ours(a, w, fk, world, rank, local, sub=False):
 
 
 # The default line's sub-blocks: the metric's other workloads, each measured
-# after the headline (config 1) with a few steps.
+# after the headline (GPP 512 x 2 x 32768 x 20) with a few steps.
 SUB_BLOCKS = ("gpp1638", "ff", "serve", "ff4")
 
 

@@ -331,7 +331,7 @@ FK_DEV double2 half_sch(double wxt, double2 wt, double2 eps) {
     return on ? cmul(delw, eps) : make_double2(0.0, 0.0);
 }
 
-// ig takes part in column igp's noflag sum (the driver's 512-wide blocks)
+// ig takes part in column igp's noflag sum (the reference program's 512-wide blocks)
 FK_DEV bool half_member(int ig, int igp) { return ig < igp - 1 && (ig & 511) != 511; }
 
 // brk[my_igp] = the first ig < igp with |wtilde^2 * I_eps| < to1 (brk starts above
@@ -1366,7 +1366,7 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 //   sch_array[iw] = 0.5 * aqsm[n1][igp] * sum_g aqsn[n1][g] * E[my_igp][iw][g]
 // where E[iw][g] adds D(g, iw') once for every block sum of frequency iw that
 // found (g, iw') in scha[j].  The prep evaluates the mask and D; the carry
-// kernel replays the driver's sequence per (my_igp, j) and writes E.
+// kernel replays the reference program's sequence per (my_igp, j) and writes E.
 //
 // A real dot product is the real part of a complex one over half the length:
 // with a[k] = A[2k] + i A[2k+1] (the row of doubles read as complex pairs, in
@@ -1568,13 +1568,13 @@ struct RealCarryArgs {
     const int* igp;
     const double* Dv;
     const uint8_t* mask;
-    int carry;           // 1: the driver's stale scha; 0: a masked term contributes 0
+    int carry;           // 1: the reference program's stale scha; 0: a masked term contributes 0
     double* D64;         // FP64 operand rows [3*ng][2*K2] (pair form), or nullptr
     uint8_t* img;        // mixed: the pre-split B image, or nullptr
     int kstages;
 };
 
-// At block offset j the driver's block sums happen at times t = 3*b + iw
+// At block offset j the reference program's block sums happen at times t = 3*b + iw
 // (block b, frequency iw) for the blocks that reach j; the source of scha[j]
 // changes at the times whose mask bit is set.  A source (g, iw') set at t0 and
 // replaced at t1 adds D(g, iw') to E[iw][g] once for every t in [t0, t1) with

@@ -1323,7 +1323,7 @@ inline int resident_pairs(K kernel, size_t smem, int threads, int cap) {
 // Host: A (rows of complex FP64, row stride lda complex elements) as a 2-D FP64
 // tensor map for tma_load_2d: inner extent 2*K doubles, `rows` rows, box
 // BK doubles (half a stage) x BM rows, elements outside the extents read as zero.  The
-// encoder comes from the driver through the runtime, so the library links
+// encoder comes from the CUDA driver API through the runtime, so the library links
 // only the CUDA runtime.
 inline cudaError_t encode_rows_map(CUtensorMap* map, const double2* A, long lda, int K, int rows) {
     using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,

@@ -193,7 +193,7 @@ def ff_synthetic_device(number_bands: int, nvband: int, ncouls: int, ngpown: int
                         seed: int = 0, device: str = "cuda") -> dict:
     """ff_synthetic's distributions with the four large arrays (aqsmtemp,
     aqsntemp, I_epsR_array, I_epsA_array) drawn on the GPU as torch tensors
-    (BASELINE config 4 holds ~17 GB per epsilon array); the small arrays are
+    (2048 x 8192 x 4096 x 32 holds ~17 GB per epsilon array); the small arrays are
     numpy, as in ff_synthetic."""
     import torch
     gen = torch.Generator(device=device).manual_seed(seed)

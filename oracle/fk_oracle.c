@@ -431,7 +431,7 @@ int orc_gpp_real(int nb, int nv, int nc, int ng,
                     sch_array[iw] += 0.5 * scht;
                 }
             } else {
-                /* the driver's block loop, gppKer_real.cpp:341-383: scha persists
+                /* the reference program's block loop, gppKer_real.cpp:341-383: scha persists
                  * over blocks and frequencies of this (n1, my_igp) */
                 const int igblk = 512;
                 double scha[512];

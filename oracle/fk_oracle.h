@@ -71,7 +71,7 @@ int orc_gpp(int nb, int nv, int nc, int ng,
  * Real-valued GPP, gppKer_real.cpp:297-396: the loop nest of the GPP sum on
  * double arrays (aqsmtemp/aqsntemp [nb][ncouls], I_eps/wtilde [ngpown][ncouls]).
  * Occupied bands: flagOCC_solver (:124-153) over ssxt_scht_solver (:17-63).
- * Other bands: the driver's 512-wide blocks (:341-383), where a masked term
+ * Other bands: the reference program's 512-wide blocks (:341-383), where a masked term
  * leaves scha[ig] as it was (the value of the last unmasked term at that
  * block offset, for the same (n1, my_igp), or 0) and every block sum adds all
  * of scha[0 .. igend).  Outputs (real): achtemp[3], asxtemp[3],

@@ -47,7 +47,7 @@ def cx(z):
 
 
 def exact_constant_gpp(nb, nv, nc, npg):
-    """Closed form of achtemp for the drivers' constant inputs (every array
+    """Closed form of achtemp for the reference programs' constant inputs (every array
     0.5+0.5i, vcoul = 1, wx = {3,4,5}): all (n1, igp, ig) terms are equal and
     take the first branch, so achtemp[iw] = nb*ngpown*0.5*nc*t(iw) exactly
     (rational arithmetic)."""

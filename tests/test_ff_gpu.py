@@ -111,8 +111,8 @@ def test_ff_rejects_bad_arguments(ctx, fk):
     assert e.value.status == 1
 
 
-def test_ff_config4_full_size(ctx, fk):
-    """BASELINE config 4 (number_bands=2048, ncouls=8192, ngpown=4096, nFreq=32;
+def test_ff_2048x8192x4096x32_full_size(ctx, fk):
+    """The large FF workload (number_bands=2048, ncouls=8192, ngpown=4096, nFreq=32;
     I_epsR/I_epsA ~17 GB each, drawn on the GPU): the tensor-core path against
     the FP64 DMMA path, every output within 1e-6 relative."""
     import torch
@@ -181,7 +181,7 @@ def test_ff_host_planes_streamed(ctx, fk, orc, flags):
         np.testing.assert_array_equal(again[k], res[k])
 
 
-def test_ff_config2_full_size(ctx, fk, orc):
+def test_ff_512x4096x512x15_full_size(ctx, fk, orc):
     """The FF benchmark configuration at its stated size: 512 bands, ncouls
     4096, ngpown 512, 15 real frequencies on [0, 2] Ry, nfreqeval 10, epsilon
     re/im U[-0.5, 0.5] plus 1.0 on the G = G' diagonal, band energies U[-1, 1].

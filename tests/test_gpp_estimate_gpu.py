@@ -26,7 +26,7 @@ CASES = [
     (40, 3, 900, 9, "branch", "reference", "stress", "root", False),
     (33, 5, 1000, 13, "branch", "baseline", "negative", "physics", False),
     (512, 2, 8192, 16, "uniform", "baseline", "baseline", 0, True),      # host arrays: pipelined path
-    (512, 2, 32768, 20, "uniform", "baseline", "baseline", 0, True),     # benchmark config 1
+    (512, 2, 32768, 20, "uniform", "baseline", "baseline", 0, True),     # the benchmark workload
 ]
 
 

@@ -25,7 +25,7 @@ def check(res, ref, tol, keys=("achtemp", "asxtemp", "acht_n1_loc")):
 
 CASES = [
     # (nb, nv, nc, ng, dist, index, wx)
-    (512, 2, 2048, 64, "uniform", "baseline", "baseline"),   # benchmark config 0
+    (512, 2, 2048, 64, "uniform", "baseline", "baseline"),   # the reference's small CPU-runnable case
     (64, 2, 777, 7, "branch", "reference", "stress"),         # ragged, every branch
     (33, 5, 1000, 13, "branch", "baseline", "reference"),     # three flag passes
     (16, 0, 640, 9, "uniform", "reference", "reference"),     # no occupied bands

@@ -1,7 +1,7 @@
 """GPU parity tests of the half-sum GPP mode (FK_GPP_HALF_SUM, gppsum == 1 of
 gppKerSeq.cpp) through the C ABI against the oracle.
 
-For column igp the sum runs over ig below igp, in the driver's 512-wide
+For column igp the sum runs over ig below igp, in the reference program's 512-wide
 blocks (which skip ig = 511 mod 512 and add the diagonal ig = igp when igp is
 a multiple of 512), and each term carries its conjugate pair.  The cases put
 columns on both sides of those block edges.

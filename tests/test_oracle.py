@@ -30,7 +30,7 @@ def cx(v):
 def test_gpp_oracle_matches_bgw_driver(fk, orc, entry):
     p = fk.inputs.gpp_reference_init(*entry["args"])
     o = orc.gpp(p)
-    # the driver prints 15 significant digits and sums in a schedule-dependent order
+    # the reference program prints 15 significant digits and sums in a schedule-dependent order
     assert rel(o["achtemp"], cx(entry["achtemp"])) < 1e-13
 
 
@@ -158,7 +158,7 @@ def test_gpp_half_sum_oracle_matches_seq_driver(fk, orc, entry):
 
 def test_gpp_half_sum_oracle_vs_reference_solvers(orc):
     """Per-(n1, my_igp, iw) sch/ssx of gppKerSeq.cpp's own gppsum == 1
-    functions (flagOCC_solver, noflagOCC_solver and the driver's block loop) on
+    functions (flagOCC_solver, noflagOCC_solver and the reference program's block loop) on
     branch-stress inputs with igp on the 512-wide block edges.  The reference's
     std::complex division, abs and pow round differently from the oracle's
     textbook forms, hence 1e-13 rather than bit equality."""
@@ -179,7 +179,7 @@ def test_gpp_real_oracle_matches_real_driver(fk, orc, entry):
     p = fk.inputs.gpp_real_reference_init(*entry["args"])
     o = orc.gpp_real(p)
     assert rel(o["achtemp"], entry["achtemp_exact"]) < 1e-14
-    # the printed values carry the driver's own summation error (~1e-12)
+    # the printed values carry the reference program's own summation error (~1e-12)
     assert rel(o["achtemp"], entry["achtemp"]) < 1e-11
 
 

@@ -140,7 +140,7 @@ def test_autotuned_plan(fk, reqs, ref64):
         np.testing.assert_array_equal(mixed[2][k], alone[k])
 
 
-def test_served_config3_request_shapes(fk, ctx):
+def test_served_uneven_stream_request_shapes(fk, ctx):
     """The served stream's request shapes at their real sizes: every
     number_bands value of the stream (128, 256, 512, 1024) at both ends of
     its ncouls range (2048 and 32768), ngpown = ncouls / 64, nvband 2, the
