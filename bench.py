@@ -124,10 +124,10 @@ def roofline(w, prec, byts, flops, kms, launches, peaks):
 def make_inputs(fk, w, seed=2024):
     if w["kind"] == "gpp" and w.get("real"):
         return fk.inputs.gpp_real_synthetic(w["nb"], w["nv"], w["nc"], w["ng"], seed=seed, dist=w.get("dist", "uniform"),
-                                            index="baseline", wx="baseline")
+                                            index="even", wx="e10")
     if w["kind"] == "gpp":
         return fk.inputs.gpp_synthetic(w["nb"], w["nv"], w["nc"], w["ng"], seed=seed, dist=w.get("dist", "uniform"),
-                                       index="baseline", wx="baseline")
+                                       index="even", wx="e10")
     if w.get("device_inputs"):
         return fk.inputs.ff_synthetic_device(w["nb"], w["nv"], w["nc"], w["ng"], w["nf"], w["ne"], seed=seed)
     return fk.inputs.ff_synthetic(w["nb"], w["nv"], w["nc"], w["ng"], w["nf"], w["ne"], seed=seed)

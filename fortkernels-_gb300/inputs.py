@@ -66,7 +66,7 @@ def gpp_real_reference_init(number_bands: int, nvband: int, ncouls: int, nodes_p
 
 
 def gpp_real_synthetic(number_bands: int, nvband: int, ncouls: int, ngpown: int, seed: int = 0,
-                       dist: str = "uniform", index: str = "baseline", wx: str = "baseline") -> dict:
+                       dist: str = "uniform", index: str = "even", wx: str = "e10") -> dict:
     """Seeded inputs of the real-valued GPP: the real parts of gpp_synthetic's
     arrays (same options).  With dist="branch" wtilde lies around each
     frequency, so the noflag mask is false for many elements (the real driver
@@ -83,7 +83,7 @@ def _cu(rng, shape, lo=-0.5, hi=0.5):
 
 
 def gpp_synthetic(number_bands: int, nvband: int, ncouls: int, ngpown: int, seed: int = 0,
-                  dist: str = "uniform", index: str = "baseline", wx: str = "baseline") -> dict:
+                  dist: str = "uniform", index: str = "even", wx: str = "e10") -> dict:
     """Seeded GPP inputs.
 
     dist:  "uniform"   aqs*, I_eps re/im U[-0.5,0.5]; wtilde re U[0.5,2], im U[-0.05,0.05];
@@ -91,9 +91,9 @@ def gpp_synthetic(number_bands: int, nvband: int, ncouls: int, ngpown: int, seed
            "branch"    as uniform, but wtilde re is drawn around each wx so that
                        every branch of the GPP solver is taken (|wdiff|^2 near
                        0.25, |delw|^2 near 1e-6 and near 2.5e5)
-    index: "baseline"  inv_igp_index[i] = i*ncouls/ngpown
+    index: "even"      inv_igp_index[i] = i*ncouls/ngpown
            "reference" inv_igp_index[i] = (i+1)*ncouls/ngpown (clamped by the kernel)
-    wx:    "baseline"  e_lk-dw, e_lk, e_lk+dw with e_lk=10, dw=1
+    wx:    "e10"       e_lk-dw, e_lk, e_lk+dw with e_lk=10, dw=1
            "reference" e_lk - e_n1kq + dw*(iw-1) = {3,4,5}
            "stress"    {0.4, 3, 5}: a frequency below 0.5 makes the third branch
                        (neither sch nor ssx, |delw|^2 <= 1e-6) reachable
@@ -104,7 +104,7 @@ def gpp_synthetic(number_bands: int, nvband: int, ncouls: int, ngpown: int, seed
     aqsm = _cu(rng, (number_bands, ncouls))
     aqsn = _cu(rng, (number_bands, ncouls))
     eps = _cu(rng, (ngpown, ncouls))
-    wxa = {"baseline": np.array([9.0, 10.0, 11.0]), "reference": gpp_wx(),
+    wxa = {"e10": np.array([9.0, 10.0, 11.0]), "reference": gpp_wx(),
            "stress": np.array([0.4, 3.0, 5.0]), "negative": np.array([-1.2, -0.7, 1.1])}[wx]
     if dist == "uniform":
         wt = rng.uniform(0.5, 2.0, (ngpown, ncouls)) + 1j * rng.uniform(-0.05, 0.05, (ngpown, ncouls))
@@ -123,7 +123,7 @@ def gpp_synthetic(number_bands: int, nvband: int, ncouls: int, ngpown: int, seed
         wt[small] = (10.0 ** rng.uniform(-4, -1, small.sum())) * np.exp(1j * rng.uniform(0, 2 * np.pi, small.sum()))
     else:
         raise ValueError(dist)
-    if index == "baseline":
+    if index == "even":
         inv = np.array([i * ncouls // ngpown for i in range(ngpown)], np.int32)
         indinv = np.arange(ncouls, dtype=np.int32)
     else:

@@ -17,16 +17,16 @@ KEYS = ("achtemp", "asxtemp", "acht_n1_loc")
 
 CASES = [
     # (nb, nv, nc, ng, dist, index, wx, flags, useful)
-    (512, 2, 2048, 64, "uniform", "baseline", "baseline", 0, True),
+    (512, 2, 2048, 64, "uniform", "even", "e10", 0, True),
     (64, 2, 777, 7, "branch", "reference", "stress", 0, False),
-    (33, 5, 1000, 13, "branch", "baseline", "reference", 0, False),
+    (33, 5, 1000, 13, "branch", "even", "reference", 0, False),
     (16, 0, 640, 9, "uniform", "reference", "reference", 0, False),
     (12, 12, 300, 4, "branch", "reference", "stress", 0, False),
     (130, 2, 4099, 70, "branch", "reference", "stress", 0, False),
     (40, 3, 900, 9, "branch", "reference", "stress", "root", False),
-    (33, 5, 1000, 13, "branch", "baseline", "negative", "physics", False),
-    (512, 2, 8192, 16, "uniform", "baseline", "baseline", 0, True),      # host arrays: pipelined path
-    (512, 2, 32768, 20, "uniform", "baseline", "baseline", 0, True),     # the benchmark workload
+    (33, 5, 1000, 13, "branch", "even", "negative", "physics", False),
+    (512, 2, 8192, 16, "uniform", "even", "e10", 0, True),      # host arrays: pipelined path
+    (512, 2, 32768, 20, "uniform", "even", "e10", 0, True),     # the benchmark workload
 ]
 
 

@@ -25,12 +25,12 @@ def check(res, ref, tol, keys=("achtemp", "asxtemp", "acht_n1_loc")):
 
 CASES = [
     # (nb, nv, nc, ng, dist, index, wx)
-    (512, 2, 2048, 64, "uniform", "baseline", "baseline"),   # the reference's small CPU-runnable case
+    (512, 2, 2048, 64, "uniform", "even", "e10"),   # the reference's small CPU-runnable case
     (64, 2, 777, 7, "branch", "reference", "stress"),         # ragged, every branch
-    (33, 5, 1000, 13, "branch", "baseline", "reference"),     # three flag passes
+    (33, 5, 1000, 13, "branch", "even", "reference"),     # three flag passes
     (16, 0, 640, 9, "uniform", "reference", "reference"),     # no occupied bands
     (12, 12, 300, 4, "branch", "reference", "stress"),        # all bands occupied
-    (1, 1, 64, 1, "branch", "baseline", "stress"),            # smallest
+    (1, 1, 64, 1, "branch", "even", "stress"),            # smallest
     (130, 2, 4099, 70, "branch", "reference", "stress"),      # tile edges
 ]
 
@@ -266,10 +266,10 @@ def test_profiling_times_the_contraction_kernel(ctx, fk, prec):
 
 PHYS_CASES = [
     # (nb, nv, nc, ng, dist, index, wx)
-    (512, 2, 2048, 64, "uniform", "baseline", "baseline"),
+    (512, 2, 2048, 64, "uniform", "even", "e10"),
     (64, 2, 777, 7, "branch", "reference", "stress"),
-    (33, 5, 1000, 13, "branch", "baseline", "negative"),   # sexcut test of the Fortran source
-    (40, 2, 2048, 16, "uniform", "baseline", "negative"),
+    (33, 5, 1000, 13, "branch", "even", "negative"),   # sexcut test of the Fortran source
+    (40, 2, 2048, 16, "uniform", "even", "negative"),
 ]
 
 

@@ -28,7 +28,7 @@ EDGE_COLS = [0, 1, 2, 510, 511, 512, 513, 1023, 1024, 1025, 1535, 1536, 1537]
 
 
 def half_inputs(fk, nb, nv, nc, ng, seed, dist, wx):
-    p = fk.inputs.gpp_synthetic(nb, nv, nc, ng, seed=seed, dist=dist, index="baseline", wx=wx)
+    p = fk.inputs.gpp_synthetic(nb, nv, nc, ng, seed=seed, dist=dist, index="even", wx=wx)
     cols = [c for c in EDGE_COLS if c < nc] + [nc - 2, nc - 1, nc // 3]
     rng = np.random.default_rng(seed)
     extra = rng.integers(0, nc, size=max(0, ng - len(cols)))
@@ -40,7 +40,7 @@ def half_inputs(fk, nb, nv, nc, ng, seed, dist, wx):
 CASES = [
     # (nb, nv, nc, ng, dist, wx)
     (64, 2, 2048, 19, "branch", "stress"),      # every block edge up to 1537, every branch
-    (40, 5, 1600, 16, "uniform", "baseline"),   # three flag passes
+    (40, 5, 1600, 16, "uniform", "e10"),   # three flag passes
     (12, 12, 1100, 9, "branch", "reference"),   # all bands occupied
     (16, 0, 1030, 9, "branch", "stress"),       # no occupied bands
     (130, 2, 4099, 70, "uniform", "stress"),    # ragged tiles

@@ -28,12 +28,12 @@ KEYS = ("achtemp", "asxtemp", "acht_n1_loc")
 CASES = [
     # (nb, nv, nc, ng, dist, index, wx)
     (64, 2, 2048, 19, "branch", "reference", "stress"),   # every branch, carried values
-    (40, 5, 1600, 16, "uniform", "baseline", "baseline"), # three flag passes
+    (40, 5, 1600, 16, "uniform", "even", "e10"), # three flag passes
     (12, 12, 1100, 9, "branch", "reference", "stress"),   # all bands occupied
     (16, 0, 1031, 9, "branch", "reference", "stress"),    # odd ncouls, no occupied bands
-    (130, 2, 4099, 70, "branch", "baseline", "stress"),   # ragged tiles, odd ncouls
+    (130, 2, 4099, 70, "branch", "even", "stress"),   # ragged tiles, odd ncouls
     (1, 1, 64, 3, "branch", "reference", "stress"),       # smallest
-    (512, 2, 2048, 64, "uniform", "baseline", "baseline"),
+    (512, 2, 2048, 64, "uniform", "even", "e10"),
 ]
 
 
@@ -96,7 +96,7 @@ def test_real_matches_driver_prints(ctx, fk, entry):
 
 def test_real_benchmark_size(ctx, fk, orc):
     """512 x 2 x 32768 x 20: FP64 against the oracle, mixed against FP64."""
-    p = fk.inputs.gpp_real_synthetic(512, 2, 32768, 20, seed=88, dist="branch", wx="baseline")
+    p = fk.inputs.gpp_real_synthetic(512, 2, 32768, 20, seed=88, dist="branch", wx="e10")
     r64 = ctx.gpp_real(p, "fp64")
     # every host input is staged whole; the three outputs come back
     sent = sum(np.asarray(p[k]).nbytes for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array", "vcoul",

@@ -131,7 +131,7 @@ def test_compute_fact_quirks(orc):
 @pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(__file__), "..", "oracle", "_ref",
                                                     "ref_harness_gpp")), reason="reference harness not built")
 def test_gpp_oracle_bitexact_live_harness(fk, orc):
-    p = fk.inputs.gpp_synthetic(9, 4, 700, 6, seed=21, dist="branch", index="baseline", wx="reference")
+    p = fk.inputs.gpp_synthetic(9, 4, 700, 6, seed=21, dist="branch", index="even", wx="reference")
     o = orc.gpp(p, per_pair=True)
     igp = p["indinv"][p["inv_igp_index"]]
     h = orc.ref_gpp_pairs(p, igp)

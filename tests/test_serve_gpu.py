@@ -19,12 +19,12 @@ KEYS = ("achtemp", "asxtemp", "acht_n1_loc")
 # (nb, nv, nc, ng, dist, wx): uneven sizes, every branch, a request with no
 # contraction units (all bands occupied)
 REQS = [
-    (256, 2, 4096, 64, "uniform", "baseline"),
+    (256, 2, 4096, 64, "uniform", "e10"),
     (128, 2, 2048, 32, "branch", "stress"),
-    (512, 2, 8192, 128, "uniform", "baseline"),
+    (512, 2, 8192, 128, "uniform", "e10"),
     (96, 5, 3000, 47, "branch", "reference"),
     (12, 12, 300, 4, "branch", "stress"),
-    (1024, 2, 2048, 32, "uniform", "baseline"),
+    (1024, 2, 2048, 32, "uniform", "e10"),
 ]
 
 
@@ -107,7 +107,7 @@ def test_admission_is_gated_by_memory(fk, reqs, ref64):
         tickets = [srv.submit(d) for _ in range(6)]
         outs = [srv.wait(t)[0] for t in tickets]
         info = srv.stats()
-        big = make(fk, 9, (16, 2, 32768, 128, "uniform", "baseline"))  # its image alone is ~150 MB
+        big = make(fk, 9, (16, 2, 32768, 128, "uniform", "e10"))  # its image alone is ~150 MB
         with pytest.raises(fk.FKError) as e:
             srv.submit(big)
         assert e.value.status == fk._native.FK_ENOMEM

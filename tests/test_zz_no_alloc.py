@@ -39,7 +39,7 @@ def call_static(lib, d, nb, nv, nc, ng, flags, out, stream=0):
 
 CASES = [
     # (nb, nv, nc, ng, dist, wx, flags)
-    (512, 2, 32768, 20, "uniform", "baseline", 0),            # benchmark size
+    (512, 2, 32768, 20, "uniform", "e10", 0),            # benchmark size
     (130, 2, 4099, 70, "branch", "stress", 0),                # ragged tiles, every branch
     (33, 5, 1000, 13, "branch", "reference", 0x2),            # three flag passes, achstemp
     (64, 2, 777, 7, "branch", "stress", 0x1),                 # root-driver semantics
