@@ -5,7 +5,8 @@ nvband=2, ncouls=32768, ngpown=20 (synthetic inputs with the benchmark value
 distributions), mixed precision, with the FP64 path measured beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload gpp|gpp1638|ff] [--precision mixed|fp64]
+                  [--workload gpp|gpp1638|gpphalf|gppreal|ff|ff4|ffsigma|serve]
+                  [--precision mixed|fp64] [--no-cpu] [--headline-only]
 
 A step is one call of the hot path over one set of inputs.  `value` is the
 device throughput with inputs resident in HBM (CUDA events on the library's
@@ -13,8 +14,12 @@ stream); `e2e` repeats the step through the C ABI with pinned HOST buffers,
 so the host->device staging and the device->host read of the outputs are
 inside the timed region.  Under torchrun every rank runs its own replica
 (the path has no exchange step), and the slowest rank's time is used.
-`--impl reference` times the CPU restatement of the reference loop nest
-(oracle/, OpenMP on all host cores) on the same workload.
+`--impl reference` times the reference's own GPP program built from its
+sources (oracle/_ref) on all host cores where the workload can be expressed
+in its arguments, else the CPU restatement of the reference loop nest
+(oracle/, OpenMP on all host cores), on the same workload.  FF lines also
+carry the reference's own FF program's time (`reference_program`), which
+covers a subset of the call's outputs.
 """
 from __future__ import annotations
 
@@ -58,7 +63,7 @@ WORKLOADS = {
 
 def terms(w):
     if w["kind"] == "gpp" and w.get("half"):
-        # the (n1, igp, ig, iw) the half sum visits: ig < igp for the baseline columns igp = i*ncouls/ngpown
+        # the (n1, igp, ig, iw) the half sum visits: ig < igp for the evenly spread columns igp = i*ncouls/ngpown
         return w["nb"] * 3 * sum(i * w["nc"] // w["ng"] for i in range(w["ng"]))
     if w["kind"] == "gpp":
         return w["nb"] * w["ng"] * w["nc"] * 3
@@ -320,6 +325,46 @@ def reference_gpp_binary(w, runs, warmup=1):
     return {"times": times, "cores": cores, "args": [w["nb"], w["nv"], w["nc"], npg]}
 
 
+REF_FF = os.path.join(ROOT, "oracle", "_ref", "ffKernel")
+
+
+def reference_ff_binary(w, runs=2, warmup=1):
+    """Seconds per run of the reference's own FF driver, FFKer_cori/ffKernel.cpp
+    built unmodified from its sources (oracle/Makefile, target ref), as its own
+    "Total Kernel Time" line reports them (its four kernels, :478-513), on all
+    host cores: `ffKernel nb nvband ncouls ngpown nFreq nfreqeval`, its own
+    constant inputs.  That program has no band x G x G' contraction (its
+    schDt_matrix is filled with a constant, :386,422, and only read by
+    achDtemp_Kernel): it computes achsDtemp, asxDtemp,
+    achDtemp and achDtemp_cor, a subset of the workload's outputs, so its time
+    is reported beside the library's call, not as the workload's rate.  None
+    when the binary was not built on this machine, the run fails, or the shape
+    would hold more than 4 GB of epsilon planes in host memory."""
+    if w["kind"] != "ff" or not os.access(REF_FF, os.X_OK):
+        return None
+    if 2 * w["nf"] * w["ng"] * w["nc"] * 16 > 4e9 or w["ng"] > w["nc"]:
+        return None
+    cores = os.cpu_count() or 1
+    env = dict(os.environ, OMP_NUM_THREADS=str(cores))
+    args = [w["nb"], w["nv"], w["nc"], w["ng"], w["nf"], w["ne"]]
+    times = []
+    try:
+        for i in range(warmup + runs):
+            out = subprocess.run([REF_FF] + [str(x) for x in args], capture_output=True, text=True, env=env,
+                                 timeout=300)
+            t = [float(x.split("=")[1].split()[0]) for x in out.stdout.splitlines() if "Total Kernel Time" in x]
+            if out.returncode != 0 or not t:
+                return None
+            if i >= warmup:
+                times.append(t[0])
+    except (OSError, ValueError, IndexError, subprocess.TimeoutExpired):
+        return None
+    return {"kernel_s": statistics.mean(times), "runs": len(times), "cores": cores, "args": args,
+            "program": "FFKer_cori/ffKernel.cpp built unmodified (g++ -O3 -fopenmp), its constant inputs",
+            "computes": "achsDtemp, asxDtemp, achDtemp, achDtemp_cor, without the band x G x G' contraction "
+                        "that the library's call also performs (the program fills schDt_matrix with a constant)"}
+
+
 def run_reference(a, w):
     """The reference's own CPU implementation of the path on all host cores:
     its GPP driver when it was built here (reference_gpp_binary), else the CPU
@@ -577,6 +622,8 @@ def measure_ours(a, w, fk, world, rank, local, sub=False):
     ctx.close()
     del d, hp, outs, p
     torch.cuda.empty_cache()
+    # FF: the reference's own FF program on the host cores, beside the call (a subset of its outputs)
+    refprog = reference_ff_binary(w) if rank == 0 and world == 1 and not a.no_cpu else None
     if rank != 0:
         return None
     peaks = {}
@@ -607,6 +654,8 @@ def measure_ours(a, w, fk, world, rank, local, sub=False):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if refprog:
+        line["reference_program"] = dict(refprog, call_ms=ms)
     return line
 
 

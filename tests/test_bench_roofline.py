@@ -66,3 +66,18 @@ def test_fallback_peaks_are_named(bench):
     byts, flops = bench.algorithmic(w)
     r = bench.roofline(w, "mixed", byts, flops, 0.070, 1, {})
     assert r["peak_source"] == "fallback" and r["peak"] == 6800.0
+
+
+def test_reference_ff_program_timing(bench, monkeypatch):
+    """The reference's FF program is timed only for FF shapes whose epsilon planes
+    fit in 4 GB of host memory; where it was built here it reports its own kernel
+    time for a small shape."""
+    for name in ("gpp", "ff4", "ffsigma"):
+        assert bench.reference_ff_binary(dict(bench.WORKLOADS[name], name=name)) is None
+    if not os.access(bench.REF_FF, os.X_OK):
+        pytest.skip("the reference's FF program is not built on this machine")
+    monkeypatch.setattr(os, "cpu_count", lambda: 2)
+    w = dict(kind="ff", nb=16, nv=2, nc=256, ng=64, nf=4, ne=3)
+    r = bench.reference_ff_binary(w, runs=1, warmup=0)
+    assert r is not None and r["runs"] == 1 and r["cores"] == 2 and r["args"] == [16, 2, 256, 64, 4, 3]
+    assert 0 <= r["kernel_s"] < 60
