@@ -1024,6 +1024,34 @@ __device__ __forceinline__ void bimg_chunk_f16(uint8_t* img_nt, int n, int k0, c
     for (int q = 0; q < 4; ++q)  // sub-tiles re h, im h, re l, im l
         *(uint4*)(st + q * BN * 64 + off) = make_uint4(pk[q][0], pk[q][1], pk[q][2], pk[q][3]);
 }
+// Stage of a rotation of eight values: when `on`, w[i] takes w[(i - B) & 7].
+template <int B>
+__device__ __forceinline__ void rot8_stage(double2 (&w)[8], bool on) {
+    double2 t[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) t[i] = on ? w[(i - B) & 7] : w[i];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) w[i] = t[i];
+}
+// The values k0 .. k0+7 of a row held in shared memory (zeros at and past n).
+// A thread's eight values are 128 contiguous bytes, so the eight threads of a
+// quarter-warp read 128 bytes apart: read in order, every 16-byte load would
+// hit the same four banks (eight-way conflict).  Thread t reads element
+// (j + t) & 7 in step j instead, which puts the quarter-warp's eight loads on
+// eight different 16-byte bank groups, and rotates the values back (three
+// conditional stages by 1, 2 and 4 positions).
+__device__ __forceinline__ void smem_chunk8(const double2* rowbuf, int k0, int n, double2 (&v)[8]) {
+    const int r = threadIdx.x & 7;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int e = (j + r) & 7;
+        v[j] = k0 + e < n ? rowbuf[k0 + e] : make_double2(0.0, 0.0);
+    }
+    // v[j] holds element (j + r) & 7, so element i is v[(i - r) & 7]
+    rot8_stage<1>(v, (r & 1) != 0);
+    rot8_stage<2>(v, (r & 2) != 0);
+    rot8_stage<4>(v, (r & 4) != 0);
+}
 __device__ __forceinline__ unsigned long long abs_bits2(double2 v) {
     const unsigned long long a = (unsigned long long)__double_as_longlong(v.x) & 0x7fffffffffffffffull;
     const unsigned long long b = (unsigned long long)__double_as_longlong(v.y) & 0x7fffffffffffffffull;
@@ -1139,8 +1167,7 @@ __global__ void __launch_bounds__(256) bimg_convert_smem_kernel(const double2* s
     uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * ((long)FF_BSUB * BN * 64);
     for (int k0 = 8 * threadIdx.x; k0 < K; k0 += 8 * 256) {
         double2 v[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) v[j] = k0 + j < K ? rowbuf[k0 + j] : make_double2(0.0, 0.0);
+        smem_chunk8(rowbuf, k0, K, v);
         bimg_chunk_f16<BN>(img_nt, n, k0, v, s);
     }
 }
@@ -1204,8 +1231,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(256)
     uint8_t* img_nt = img + (((long)b * NT + n / BN) * kstages) * ((long)FF_BSUB * BN * 64);
     for (int j0 = 8 * threadIdx.x; j0 < nk; j0 += 8 * 256) {
         double2 v[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) v[j] = j0 + j < nk ? rowbuf[j0 + j] : make_double2(0.0, 0.0);
+        smem_chunk8(rowbuf, j0, nk, v);
         bimg_chunk_f16<BN>(img_nt, n, k0 + j0, v, s);
     }
 }
