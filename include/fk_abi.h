@@ -330,6 +330,9 @@ fk_status fk_server_wait(fk_server_t srv, unsigned long long ticket, double time
  * at once.  A request already admitted runs to completion: FK_EBUSY (wait for
  * it as usual).  FK_EINVAL for an unknown ticket. */
 fk_status fk_server_cancel(fk_server_t srv, unsigned long long ticket);
+/* The server's counters since it was created: requests submitted and
+ * completed, steps run, latency percentiles, throughput, requests per step
+ * and the peak of its memory budget in use (fk_server_info). */
 fk_status fk_server_stats(fk_server_t srv, fk_server_info* out);
 /* Autotunes the plan of one request shape (while the server is idle, else
  * FK_EBUSY): runs the shape with synthetic inputs through the server's steps
