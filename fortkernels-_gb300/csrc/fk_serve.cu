@@ -23,6 +23,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "fk_firstfit.h"
 #include "fk_internal.h"
 
 namespace fk {
@@ -46,68 +47,36 @@ struct DevScope {
     }
 };
 
-// First-fit allocator over one device block, coalescing on release.
+// First-fit allocator over one device block, coalescing on release (the
+// bookkeeping by offsets is FirstFit's).
 class Arena {
   public:
     ~Arena() {
         if (base_) cudaFree(base_);
     }
     bool init(size_t bytes) {
-        cap_ = round256(bytes);
-        if (cudaMalloc(&base_, cap_) != cudaSuccess) {
+        ff_.reset(bytes);
+        if (cudaMalloc(&base_, ff_.capacity()) != cudaSuccess) {
             cudaGetLastError();
             base_ = nullptr;
+            ff_.reset(0);
             return false;
         }
-        free_[0] = cap_;
         return true;
     }
     void* alloc(size_t bytes) {
-        bytes = round256(std::max<size_t>(bytes, 1));
-        for (auto it = free_.begin(); it != free_.end(); ++it) {
-            if (it->second < bytes) continue;
-            const size_t off = it->first, rest = it->second - bytes;
-            free_.erase(it);
-            if (rest) free_[off + bytes] = rest;
-            used_[off] = bytes;
-            in_use_ += bytes;
-            peak_ = std::max(peak_, in_use_);
-            return (char*)base_ + off;
-        }
-        return nullptr;
+        const size_t off = ff_.alloc(bytes);
+        return off == FirstFit::NONE ? nullptr : (char*)base_ + off;
     }
     void release(void* p) {
-        if (!p) return;
-        const size_t off = (size_t)((char*)p - (char*)base_);
-        auto u = used_.find(off);
-        if (u == used_.end()) return;
-        size_t size = u->second;
-        in_use_ -= size;
-        used_.erase(u);
-        size_t start = off;
-        auto next = free_.lower_bound(off);
-        if (next != free_.begin()) {
-            auto prev = std::prev(next);
-            if (prev->first + prev->second == off) {
-                start = prev->first;
-                size += prev->second;
-                free_.erase(prev);
-            }
-        }
-        next = free_.lower_bound(off);
-        if (next != free_.end() && next->first == off + u->second) {
-            size += next->second;
-            free_.erase(next);
-        }
-        free_[start] = size;
+        if (p) ff_.release((size_t)((char*)p - (char*)base_));
     }
-    size_t capacity() const { return cap_; }
-    size_t peak() const { return peak_; }
+    size_t capacity() const { return ff_.capacity(); }
+    size_t peak() const { return ff_.peak(); }
 
   private:
     void* base_ = nullptr;
-    size_t cap_ = 0, in_use_ = 0, peak_ = 0;
-    std::map<size_t, size_t> free_, used_;
+    FirstFit ff_;
 };
 
 struct Resident {
