@@ -300,29 +300,20 @@ fk_status fk_create(int device, fk_ctx_t* out) {
         return FK_ECUDA;
     }
     c->stream = c->own_stream;
-    if (cudaMalloc(&c->errword, 256) != cudaSuccess || cudaMemset(c->errword, 0, 256) != cudaSuccess) {
+    // from here on a failure releases everything created so far (fk_destroy
+    // skips the members that are still null)
+    auto undo = [c]() {
         cudaGetLastError();
-        cudaStreamDestroy(c->own_stream);
-        delete c;
-        return FK_ECUDA;
-    }
-    if (cudaEventCreateWithFlags(&c->pinned_ev, cudaEventDisableTiming) != cudaSuccess) {
+        fk_destroy(c);
         cudaGetLastError();
-        delete c;
         return FK_ECUDA;
-    }
+    };
+    if (cudaMalloc(&c->errword, 256) != cudaSuccess || cudaMemset(c->errword, 0, 256) != cudaSuccess) return undo();
+    if (cudaEventCreateWithFlags(&c->pinned_ev, cudaEventDisableTiming) != cudaSuccess) return undo();
     for (auto& e : c->ev)
-        if (cudaEventCreate(&e) != cudaSuccess) {
-            cudaGetLastError();
-            delete c;
-            return FK_ECUDA;
-        }
+        if (cudaEventCreate(&e) != cudaSuccess) return undo();
     for (auto& e : c->kev)
-        if (cudaEventCreate(&e) != cudaSuccess) {
-            cudaGetLastError();
-            delete c;
-            return FK_ECUDA;
-        }
+        if (cudaEventCreate(&e) != cudaSuccess) return undo();
     *out = c;
     return FK_OK;
 }
