@@ -426,11 +426,13 @@ namespace {
 
 // fk_gpp for large host arrays (mixed precision).  Everything crosses the host
 // link on one copy stream, in the order the GPU needs it: the small inputs
-// (packed into one pinned block), eps and wtilde, the igp columns of aqsmtemp
-// (gathered on the host while eps and wtilde are in flight), then aqsntemp in
-// row blocks.  The compute stream runs the prep once the first block (with the
-// flag bands) has landed and each block's contraction as soon as that block
-// has; the outputs come back through pinned memory in one copy.
+// (packed into one pinned block), eps and wtilde, the first row block of
+// aqsntemp (with the flag bands), the igp columns of aqsmtemp (gathered on the
+// host while that block is in flight: the gather's scattered reads take longer
+// than the eps and wtilde copies, and the link would otherwise wait for it),
+// then the other row blocks.  The compute stream runs the prep once the first
+// block and the columns have landed and each block's contraction as soon as
+// that block has; the outputs come back through pinned memory in one copy.
 fk_status gpp_host_pipelined(Ctx& x, GppDev r, const fk_c128* aqsmtemp, const fk_c128* aqsntemp,
                              const fk_c128* I_eps_array, const fk_c128* wtilde_array, const double* vcoul,
                              const int* inv_igp_index, const int* indinv, const double* wx_array, fk_c128* achtemp,
@@ -503,7 +505,10 @@ fk_status gpp_host_pipelined(Ctx& x, GppDev r, const fk_c128* aqsmtemp, const fk
         cudaMemcpyAsync(pipe.wt_d, wtilde_array, col, cudaMemcpyHostToDevice, cs) != cudaSuccess)
         return cuda_fail(x, cudaGetLastError(), "gpp: eps / wtilde");
     x.h2d_bytes += 2 * col;
-    // 3. aqsmtemp: its igp columns gathered on the host meanwhile (or the whole array)
+    // 3. the first row block of aqsntemp, then aqsmtemp: its igp columns gathered
+    // on the host while that block is in flight (or the whole array)
+    const int chunks = gpp_pipe_chunks(x, r);
+    if ((st = gpp_pipe_copy(x, r, &pipe, 0, 1)) != FK_OK) return st;
     if (compact) {
         std::vector<int> invh, indh;
         const int* ip = inv_igp_index;
@@ -547,8 +552,8 @@ fk_status gpp_host_pipelined(Ctx& x, GppDev r, const fk_c128* aqsmtemp, const fk
     }
     if (cudaEventRecord(x.pipe_ev[PIPE_READY], cs) != cudaSuccess)
         return cuda_fail(x, cudaGetLastError(), "gpp: pipeline");
-    // 4. aqsntemp in row blocks
-    if ((st = gpp_pipe_copy(x, r, &pipe, 0, gpp_pipe_chunks(x, r))) != FK_OK) return st;
+    // 4. the other row blocks of aqsntemp
+    if ((st = gpp_pipe_copy(x, r, &pipe, 1, chunks)) != FK_OK) return st;
     r.vcoul = sm[0].dev ? vcoul : (const double*)(small_d + sm[0].off);
     r.inv = sm[1].dev ? inv_igp_index : (const int*)(small_d + sm[1].off);
     r.indinv = sm[2].dev ? indinv : (const int*)(small_d + sm[2].off);
