@@ -257,6 +257,36 @@ def clock_sampler(index):
         return ClockSampler(index)
 
 
+def load_peaks():
+    """The measured HBM copy and bf16 peaks of this GPU type (MEASURED_PEAKS.json), or {}."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def serve_roofline(reqs, nv, seconds, steps, peaks):
+    """Roofline block of a served stream: the algorithmic work of every
+    request's contraction (bands nvband .. nb-1 against 3 * ngpown columns over
+    ncouls, ngpown = ncouls / 64; bytes: aqsntemp's rows once at 16 B and the
+    image at 8 B per complex, flops: 8 per complex multiply-add) over
+    `seconds`, the burst's wall time for `steps` steps.  That time holds every
+    kernel of the steps (index map, prep, A images, reductions) and the host's
+    gaps between steps, so `achieved` is a lower bound on the table
+    contraction's own rate."""
+    byts = flops = 0
+    for nb, nc in reqs:
+        M, N, K = nb - nv, 3 * (nc // 64), nc
+        byts += 16 * M * K + 8 * N * K
+        flops += 8 * M * N * K
+    r = roofline({"kind": "gpp", "name": "serve"}, "mixed", byts, flops, seconds * 1e3, max(1, steps), peaks)
+    r["kernel"] = "table contraction (the stream's steps)"
+    r["basis"] = ("algorithmic work of the stream's contractions over the burst's wall time (every kernel and "
+                  "host gap of its steps): a lower bound on the contraction's own rate")
+    return r
+
+
 def measured_traffic(w):
     """DRAM bytes per launch of the dominant kernel from a committed ncu
     capture summary (profiles/traffic.json), or None."""
@@ -628,12 +658,7 @@ def measure_ours(a, w, fk, world, rank, local, sub=False):
     refprog = reference_ff_binary(w) if rank == 0 and world == 1 and not a.no_cpu else None
     if rank != 0:
         return None
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except OSError:
-        pass
+    peaks = load_peaks()
     byts, flops = algorithmic(w)
     T = terms(w)
     line = {
@@ -797,6 +822,7 @@ def measure_serve(a, w, fk, sub=False):
         for t in [submit(128, nc) for nc in levels]:
             srv.wait(t)
     total = sum(terms_of(nb, nc) for nb, nc in reqs)
+    steps_before = srv.stats()["steps"]
     # burst: saturation throughput
     with clock_sampler(local) as clk:
         t0 = time.perf_counter()
@@ -805,7 +831,7 @@ def measure_serve(a, w, fk, sub=False):
             srv.wait(t)
         burst_s = time.perf_counter() - t0
     sat = total / burst_s
-    steps0 = srv.stats()["steps"]
+    steps0 = srv.stats()["steps"] - steps_before
     # Poisson arrivals at `load` x saturation
     rate = w["load"] * sat / (total / len(reqs))
     arrivals = np.cumsum(gaps / rate)
@@ -858,7 +884,7 @@ def measure_serve(a, w, fk, sub=False):
                        "steps_burst": steps0, "steps_total": info["steps"],
                        "mean_requests_per_step": info["mean_active"], "peak_active": info["peak_active"],
                        "hbm_peak_bytes": info["hbm_peak_bytes"], "autotuned_kslices": tuned},
-            "roofline": None,
+            "roofline": serve_roofline(reqs, w["nv"], burst_s, steps0, load_peaks()),
             "e2e": {"value": world * sat, "unit": "terms/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
                     "note": "requests through fk_server_submit/fk_server_wait; outputs returned to host"},
             "gpu_launches": 5 * info["steps"],

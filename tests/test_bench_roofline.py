@@ -81,3 +81,21 @@ def test_reference_ff_program_timing(bench, monkeypatch):
     r = bench.reference_ff_binary(w, runs=1, warmup=0)
     assert r is not None and r["runs"] == 1 and r["cores"] == 2 and r["args"] == [16, 2, 256, 64, 4, 3]
     assert 0 <= r["kernel_s"] < 60
+
+
+def test_served_stream_roofline(bench):
+    """The served stream's roofline: every request's contraction (bands nvband..nb-1
+    against 3*ngpown columns, ngpown = ncouls/64) over the burst's wall time."""
+    w = dict(bench.WORKLOADS["serve"], name="serve")
+    levels, reqs, _ = bench.serve_stream(w, seed=2024)
+    assert len(reqs) == 256 and all(nb in w["nb_choices"] and nc in levels for nb, nc in reqs)
+    byts = sum(16 * (nb - 2) * nc + 8 * 3 * (nc // 64) * nc for nb, nc in reqs)
+    flops = sum(8 * (nb - 2) * 3 * (nc // 64) * nc for nb, nc in reqs)
+    r = bench.serve_roofline(reqs, w["nv"], 0.125, 350, PEAKS)
+    assert r["algorithmic_bytes"] == byts and r["algorithmic_flops"] == flops
+    # large requests make the stream tensor-bound: six BF16 piece products per complex MAC
+    assert 6 * flops / (PEAKS["bf16_tflops"] * 1e12) > byts / (PEAKS["hbm_gbs"] * 1e9)
+    assert r["bound"] == "tensor" and r["unit"] == "TFLOP/s" and r["piece_products"] == 6
+    assert r["achieved"] == pytest.approx(flops / 0.125 / 1e12)
+    assert r["duration_ms"] == pytest.approx(125.0 / 350) and r["traffic"] is None
+    assert "lower bound" in r["basis"]
